@@ -1,0 +1,17 @@
+#!/bin/sh
+# Builds oracle/_ref/libgplsaco_ref.so from the reference's own CPU sources
+# (cpp/src/faco_cpu.cpp, cpp/src/program_cpu.cpp of LinHuanli/GPLSACO, read in
+# place, never copied) plus oracle/ref_shim.cpp.  Test infrastructure only.
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+if [ ! -f "$REF/cpp/src/faco_cpu.cpp" ]; then
+    echo "reference sources not found under $REF; oracle/_ref not built" >&2
+    exit 0
+fi
+mkdir -p "$HERE/_ref"
+g++ -std=c++17 -O2 -fPIC -shared -ffp-contract=off -I"$REF/cpp/include" \
+    "$REF/cpp/src/faco_cpu.cpp" "$REF/cpp/src/program_cpu.cpp" "$HERE/ref_shim.cpp" \
+    -o "$HERE/_ref/libgplsaco_ref.so"
+echo "built $HERE/_ref/libgplsaco_ref.so"

@@ -1,0 +1,616 @@
+/*
+ * faco_oracle.c -- CPU restatement of the GPLSACO Focused-ACO path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA engine, never linked
+ * into the shipped library.  Each function names the reference routine it
+ * follows (paths inside LinHuanli/GPLSACO).  Built with -ffp-contract=off so
+ * that every FP32/FP64 operation rounds exactly once, as on the GPU.
+ */
+#include "faco_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* Distances.  TSPLIB EUC_2D (python/gp_faco/distance.py:40-52):           */
+/* floor(sqrt(dx^2+dy^2)+0.5).  For |coords| < 2^26 the square sum is exact */
+/* in a double and sqrt is correctly rounded, so this is the exact integer */
+/* nearest to the true length (a half-integer is never a square root).    */
+/* ---------------------------------------------------------------------- */
+int32_t orc_euc2d(int64_t x0, int64_t y0, int64_t x1, int64_t y1) {
+    const int64_t dx = x0 - x1, dy = y0 - y1;
+    const double s = (double)(dx * dx + dy * dy);
+    return (int32_t)floor(sqrt(s) + 0.5);
+}
+
+int32_t orc_distance(const orc_dist_t* d, uint32_t a, uint32_t b) {
+    if (d->matrix) return d->matrix[(size_t)a * d->n + b];
+    return orc_euc2d(d->xy[2 * (size_t)a], d->xy[2 * (size_t)a + 1], d->xy[2 * (size_t)b],
+                     d->xy[2 * (size_t)b + 1]);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Tour primitives -- cpp/src/faco_cpu.cpp:47-146 (CpuTour).               */
+/* ---------------------------------------------------------------------- */
+static inline uint32_t succ(const orc_tour_t* t, uint32_t v) {
+    const uint32_t p = t->pos[v] + 1;
+    return t->order[p == t->n ? 0 : p];
+}
+static inline uint32_t pred(const orc_tour_t* t, uint32_t v) {
+    const uint32_t p = t->pos[v];
+    return t->order[p == 0 ? t->n - 1 : p - 1];
+}
+
+int64_t orc_tour_length(const uint32_t* order, uint32_t n, const orc_dist_t* d) {
+    int64_t sum = 0;
+    uint32_t previous = order[n - 1];
+    for (uint32_t i = 0; i < n; ++i) {
+        sum += orc_distance(d, previous, order[i]);
+        previous = order[i];
+    }
+    return sum;
+}
+
+int orc_tour_reset(orc_tour_t* t, const orc_dist_t* d) {
+    for (uint32_t i = 0; i < t->n; ++i) t->pos[i] = UINT32_MAX;
+    for (uint32_t i = 0; i < t->n; ++i) {
+        const uint32_t v = t->order[i];
+        if (v >= t->n || t->pos[v] != UINT32_MAX) return -1;
+        t->pos[v] = i;
+    }
+    t->cost = orc_tour_length(t->order, t->n, d);
+    return 0;
+}
+
+/* CpuTour::relocate (faco_cpu.cpp:82-112): move `node` right after `target`. */
+int orc_relocate(orc_tour_t* t, const orc_dist_t* d, uint32_t target, uint32_t node) {
+    if (succ(t, target) == node) return 0;
+    const uint32_t before = pred(t, node), after = succ(t, node), target_after = succ(t, target);
+    const uint32_t p = t->pos[node], tp = t->pos[target];
+    if (tp < p) {
+        for (uint32_t i = p; i > tp + 1; --i) t->order[i] = t->order[i - 1];
+        t->order[tp + 1] = node;
+    } else {
+        for (uint32_t i = p; i < tp; ++i) t->order[i] = t->order[i + 1];
+        t->order[tp] = node;
+    }
+    const uint32_t lo = p < tp ? p : tp, hi = p < tp ? tp : p;
+    for (uint32_t i = lo; i <= hi; ++i) t->pos[t->order[i]] = i;
+    t->cost += -(int64_t)orc_distance(d, before, node) - orc_distance(d, node, after) -
+               orc_distance(d, target, target_after) + orc_distance(d, before, after) +
+               orc_distance(d, target, node) + orc_distance(d, node, target_after);
+    return 1;
+}
+
+/* CpuTour::flip_without_cost (faco_cpu.cpp:114-135).  Positions first<last
+ * of the two endpoints; the shorter side is reversed, except that first==0
+ * always reverses [0,last) (the reference's wrap loop goes round once more
+ * and undoes the complement, leaving exactly that). */
+void orc_flip(orc_tour_t* t, uint32_t start, uint32_t end) {
+    uint32_t first = t->pos[start], last = t->pos[end];
+    if (first > last) { const uint32_t s = first; first = last; last = s; }
+    const uint32_t n = t->n, length = last - first;
+    const int straight = length <= n - length || first == 0;
+    const uint32_t count = straight ? length : n - length, begin = straight ? first : last;
+    for (uint32_t o = 0; o < count / 2; ++o) {
+        const uint32_t l = (begin + o) % n, r = (begin + count - 1 - o) % n;
+        const uint32_t a = t->order[l], b = t->order[r];
+        t->order[l] = b; t->order[r] = a;
+        t->pos[b] = l; t->pos[a] = r;
+    }
+}
+
+void orc_queue_push_absent(orc_queue_t* q, uint32_t v, uint64_t* pushed) {
+    if (q->queued[v]) return;
+    q->queued[v] = 1;
+    if (q->len < q->cap) q->items[q->len] = v;
+    else q->overflow = 1;
+    ++q->len;
+    if (pushed) ++*pushed;
+}
+
+/* CpuTour::checklist_two_opt (faco_cpu.cpp:148-217), the device variant's
+ * right-padding rule (cuda/faco_device.cuh:320) and integer gains. */
+void orc_checklist_two_opt(orc_tour_t* t, const orc_dist_t* d, const uint32_t* rows, uint32_t w,
+                           orc_queue_t* q, uint64_t cap, orc_ls_stats_t* st) {
+    int64_t accumulated = 0;
+    while (q->head < q->len && st->accepted_moves < t->n) {
+        if (st->move_evaluations >= cap) { st->evaluation_limit_reached = 1; break; }
+        const uint32_t a = q->items[q->head++];
+        q->queued[a] = 0;
+        const uint32_t an = succ(t, a), ap = pred(t, a);
+        ++st->processed_nodes;
+        const int64_t to_next = orc_distance(d, a, an), to_prev = orc_distance(d, ap, a);
+        int64_t best = -1;
+        uint32_t move[4] = {0, 0, 0, 0};
+        int interrupted = 0;
+        for (int kind = 0; kind < 2 && !interrupted; ++kind) {
+            const int64_t current = kind == 0 ? to_next : to_prev;
+            const uint32_t closing_end = kind == 0 ? an : ap;
+            for (uint32_t j = 0; j < w; ++j) {
+                const uint32_t b = rows[(size_t)a * w + j];
+                ++st->candidate_checks;
+                if (b >= t->n) break;
+                const int64_t ab = orc_distance(d, a, b);
+                if (!(current > ab)) break;
+                if (st->move_evaluations == cap) { interrupted = 1; break; }
+                ++st->move_evaluations;
+                const uint32_t nb = kind == 0 ? succ(t, b) : pred(t, b);
+                const int64_t other = orc_distance(d, b, nb);
+                const int64_t closing = orc_distance(d, closing_end, nb);
+                const int64_t gain = (nb == a || b == closing_end) ? 0 : current + other - ab - closing;
+                if (gain > best) {
+                    best = gain;
+                    if (kind == 0) { move[0] = an; move[1] = nb; move[2] = a; move[3] = b; }
+                    else { move[0] = a; move[1] = b; move[2] = ap; move[3] = nb; }
+                }
+            }
+        }
+        if (interrupted) { st->evaluation_limit_reached = 1; break; }
+        if (best > 0) {
+            orc_flip(t, move[0], move[1]);
+            for (int i = 0; i < 4; ++i) orc_queue_push_absent(q, move[i], &st->reactivations);
+            ++st->accepted_moves;
+            accumulated -= best;
+        }
+    }
+    t->cost += accumulated;
+}
+
+/* select_next (faco_cpu.cpp:247-294) with the device's visiting order
+ * (cuda/faco_choices.cuh:86-142): ordered FP64 prefix sums. */
+uint32_t orc_select_next(uint32_t current, const uint32_t* primary, const double* products, uint32_t k,
+                         const uint32_t* backup, uint32_t b, const uint8_t* visited,
+                         const orc_dist_t* d, double uniform, int* stage) {
+    uint32_t available = 0, last = UINT32_MAX;
+    double sum = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+        const uint32_t v = primary[j];
+        if (v < d->n && !visited[v]) { ++available; sum += products[j]; last = v; }
+    }
+    if (available) {
+        if (sum == 0) {
+            uint32_t target = (uint32_t)(uniform * available);
+            if (target >= available) target = available - 1;
+            for (uint32_t j = 0; j < k; ++j) {
+                const uint32_t v = primary[j];
+                if (v < d->n && !visited[v] && target-- == 0) { if (stage) *stage = ORC_ZERO_WEIGHT; return v; }
+            }
+        }
+        const double threshold = uniform * sum;
+        double prefix = 0;
+        for (uint32_t j = 0; j < k; ++j) {
+            const uint32_t v = primary[j];
+            if (v < d->n && !visited[v]) {
+                prefix += products[j];
+                if (threshold < prefix) { if (stage) *stage = ORC_PRIMARY; return v; }
+            }
+        }
+        if (stage) *stage = ORC_PRIMARY;
+        return last;
+    }
+    for (uint32_t j = 0; j < b; ++j) {
+        const uint32_t v = backup[j];
+        if (v < d->n && !visited[v]) { if (stage) *stage = ORC_BACKUP; return v; }
+    }
+    uint32_t chosen = current;
+    int64_t minimum = INT64_MAX;
+    for (uint32_t v = 0; v < d->n; ++v) {
+        if (visited[v]) continue;
+        const int64_t value = orc_distance(d, current, v);
+        if (value < minimum) { minimum = value; chosen = v; }
+    }
+    if (stage) *stage = chosen == current ? ORC_EXHAUSTED : ORC_GLOBAL;
+    return chosen;
+}
+
+/* One ant: FocusedConstruction (faco_cpu.cpp:219-245) then the checklist
+ * 2-opt on the construction's checklist (tests/cpp/test_fixed_faco.cpp:235-256). */
+int orc_ant(const uint32_t* parent, const orc_dist_t* d, const uint32_t* ls_rows, uint32_t w,
+            const orc_choices_t* ch, uint32_t mne_target, uint64_t max_evaluations,
+            uint32_t* construction_tour, uint32_t* tour, uint32_t* pos, uint32_t* checklist,
+            uint32_t* selected, orc_ant_info_t* info) {
+    const uint32_t n = d->n;
+    memset(info, 0, sizeof(*info));
+    uint32_t* ppos = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint8_t* visited = (uint8_t*)calloc(n, 1);
+    uint8_t* queued = (uint8_t*)calloc(n, 1);
+    const uint32_t cap = 8 * n + 8;
+    uint32_t* items = checklist ? checklist : (uint32_t*)malloc(sizeof(uint32_t) * cap);
+    double* row = (double*)malloc(sizeof(double) * (ch->k ? ch->k : 1));
+    if (!ppos || !visited || !queued || !items || !row) return -1;
+    for (uint32_t i = 0; i < n; ++i) ppos[parent[i]] = i;
+    memcpy(tour, parent, sizeof(uint32_t) * n);
+    orc_tour_t t = {n, tour, pos, 0};
+    orc_tour_reset(&t, d);
+    orc_queue_t q = {items, cap, 0, 0, queued, 0};
+    uint32_t current = ch->visit ? ch->visit[0] : ch->start;
+    info->start_node = current;
+    if (selected) selected[0] = current;
+    visited[current] = 1;
+    orc_cons_stats_t* cs = &info->cons;
+    while (cs->mne < mne_target && cs->steps + 1 < n) {
+        const uint32_t step = cs->steps + 1;
+        uint32_t chosen;
+        if (ch->visit) {
+            chosen = ch->visit[step];
+        } else {
+            const uint32_t* prow = ch->primary + (size_t)current * ch->k;
+            for (uint32_t j = 0; j < ch->k; ++j)
+                row[j] = ch->products64 ? ch->products64[(size_t)current * ch->k + j]
+                                        : (double)ch->products32[(size_t)current * ch->k + j];
+            chosen = orc_select_next(current, prow, row, ch->k, ch->backup + (size_t)current * ch->b, ch->b,
+                                     visited, d, ch->uniforms[step], NULL);
+        }
+        if (chosen >= n || visited[chosen]) { cs->legal_exhausted = 1; break; }
+        if (selected) selected[step] = chosen;
+        const uint32_t previous = pred(&t, chosen);
+        visited[chosen] = 1;
+        ++cs->steps;
+        if (orc_relocate(&t, d, current, chosen)) ++cs->nonidentity_relocations;
+        const uint32_t pp = ppos[current];
+        const uint32_t ps = parent[pp + 1 == n ? 0 : pp + 1], pq = parent[pp == 0 ? n - 1 : pp - 1];
+        if (ps != chosen && pq != chosen) {
+            ++cs->mne;
+            orc_queue_push_absent(&q, current, NULL);
+            orc_queue_push_absent(&q, chosen, NULL);
+            orc_queue_push_absent(&q, previous, NULL);
+        }
+        current = chosen;
+    }
+    if (construction_tour) memcpy(construction_tour, tour, sizeof(uint32_t) * n);
+    info->construction_cost = t.cost;
+    orc_checklist_two_opt(&t, d, ls_rows, w, &q, max_evaluations, &info->ls);
+    info->final_cost = t.cost;
+    info->checklist_len = q.len;
+    const int overflow = q.overflow;
+    free(ppos); free(visited); free(queued); free(row);
+    if (!checklist) free(items);
+    return overflow ? -2 : 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Trails -- candidate_trail_limits (faco_cpu.cpp:296-304), bounds()      */
+/* (cuda/colony_state.cuh:66-70), SparsePheromone evaporate/deposit       */
+/* (faco_cpu.cpp:322-343) and update_pheromone (colony_state.cuh:210-229). */
+/* ---------------------------------------------------------------------- */
+void orc_trail_limits(uint32_t width, double p_root, double retention, double cost, double* minimum,
+                      double* maximum) {
+    const double mx = 1.0 / (cost * (1.0 - retention));
+    const double mn = mx * (1.0 - p_root) / (((double)width - 1.0) * p_root);
+    *maximum = mx;
+    *minimum = mn < mx ? mn : mx;
+}
+
+static inline int parent_edge(const uint32_t* parent, const uint32_t* ppos, uint32_t n, uint32_t from,
+                              uint32_t to) {
+    const uint32_t p = ppos[from];
+    return parent[p + 1 == n ? 0 : p + 1] == to || parent[p == 0 ? n - 1 : p - 1] == to;
+}
+
+void orc_pheromone64(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
+                     double retention, double minimum, double maximum, double increment, double* trails,
+                     double* default_trail) {
+    uint32_t* ppos = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    for (uint32_t i = 0; i < n; ++i) ppos[parent[i]] = i;
+    for (uint32_t from = 0; from < n; ++from)
+        for (uint32_t j = 0; j < k; ++j) {
+            const size_t i = (size_t)from * k + j;
+            double v = trails[i] * retention;
+            v = v > minimum ? v : minimum;
+            if (primary[i] < n && parent_edge(parent, ppos, n, from, primary[i])) {
+                v = v + increment;
+                v = v < maximum ? v : maximum;
+            }
+            trails[i] = v;
+        }
+    const double dv = *default_trail * retention;
+    *default_trail = dv > minimum ? dv : minimum;
+    free(ppos);
+}
+
+void orc_pheromone32(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
+                     float retention, float minimum, float maximum, float increment, const float* eta,
+                     float* trails, float* products, float* default_trail) {
+    uint32_t* ppos = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    for (uint32_t i = 0; i < n; ++i) ppos[parent[i]] = i;
+    for (uint32_t from = 0; from < n; ++from)
+        for (uint32_t j = 0; j < k; ++j) {
+            const size_t i = (size_t)from * k + j;
+            float v = fmaxf(minimum, trails[i] * retention);
+            if (primary[i] < n && parent_edge(parent, ppos, n, from, primary[i])) v = fminf(maximum, v + increment);
+            trails[i] = v;
+            products[i] = v * eta[i];
+        }
+    *default_trail = fmaxf(minimum, *default_trail * retention);
+    free(ppos);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Random stream.  Philox4x32 with 10 rounds as published by Salmon,       */
+/* Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3"    */
+/* (SC'11).  The counter layout is this engine's own:                     */
+/*   (step, ant, batch, 0) construction uniform for step >= 1              */
+/*   (0, ant, batch, 1)    start node                                      */
+/*   (0, 0xffffffff, batch, 2) colony source draw (epoch vs iteration best)*/
+/* ---------------------------------------------------------------------- */
+void orc_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                    uint32_t out[4]) {
+    for (int round = 0; round < 10; ++round) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0; c1 = lo1; c2 = hi0 ^ c3 ^ k1; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static inline double u53(uint32_t hi, uint32_t lo) {
+    return (double)((((uint64_t)hi << 32) | lo) >> 11) * 0x1.0p-53;
+}
+
+double orc_uniform(uint64_t key, uint32_t batch, uint32_t ant, uint32_t step) {
+    uint32_t x[4];
+    orc_philox4x32(step, ant, batch, 0, (uint32_t)key, (uint32_t)(key >> 32), x);
+    return u53(x[0], x[1]);
+}
+
+uint32_t orc_start_node(uint64_t key, uint32_t batch, uint32_t ant, uint32_t n) {
+    uint32_t x[4];
+    orc_philox4x32(0, ant, batch, 1, (uint32_t)key, (uint32_t)(key >> 32), x);
+    return (uint32_t)(((uint64_t)x[0] * n) >> 32);
+}
+
+double orc_source_uniform(uint64_t key, uint32_t batch) {
+    uint32_t x[4];
+    orc_philox4x32(0, 0xffffffffu, batch, 2, (uint32_t)key, (uint32_t)(key >> 32), x);
+    return u53(x[0], x[1]);
+}
+
+/* SplitMix64 finaliser (Steele, Lea, Flood 2014) over seed and instance. */
+static uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+uint64_t orc_colony_key(uint64_t seed, uint64_t instance_key) { return mix64(seed ^ mix64(instance_key)); }
+
+/* ---------------------------------------------------------------------- */
+/* Preparation -- prepare_problem (cpp/src/prepared_problem.cpp:107-175)  */
+/* with EUC_2D integers: rows sorted by (distance, node id), NN tour from */
+/* node 0 (first strict minimum), checklist 2-opt over the whole tour,    */
+/* identity tour kept when it is no longer.                               */
+/* ---------------------------------------------------------------------- */
+typedef struct { int64_t d; uint32_t v; } orc_pair_t;
+static int pair_less(const void* x, const void* y) {
+    const orc_pair_t* a = (const orc_pair_t*)x; const orc_pair_t* b = (const orc_pair_t*)y;
+    if (a->d != b->d) return a->d < b->d ? -1 : 1;
+    return a->v < b->v ? -1 : (a->v > b->v);
+}
+
+int64_t orc_prepare(uint32_t n, const int32_t* xy, const orc_prep_cfg_t* cfg, uint32_t* primary,
+                    uint32_t* backup, uint32_t* ls, uint32_t* initial) {
+    const orc_dist_t d = {n, xy, NULL};
+    orc_pair_t* row = (orc_pair_t*)malloc(sizeof(orc_pair_t) * n);
+    for (uint32_t a = 0; a < n; ++a) {
+        uint32_t m = 0;
+        for (uint32_t b = 0; b < n; ++b) if (b != a) { row[m].d = orc_distance(&d, a, b); row[m].v = b; ++m; }
+        qsort(row, m, sizeof(orc_pair_t), pair_less);
+        for (uint32_t j = 0; j < cfg->k; ++j) primary[(size_t)a * cfg->k + j] = row[j].v;
+        for (uint32_t j = 0; j < cfg->b; ++j) backup[(size_t)a * cfg->b + j] = row[cfg->k + j].v;
+        for (uint32_t j = 0; j < cfg->w; ++j) ls[(size_t)a * cfg->w + j] = row[j].v;
+    }
+    free(row);
+    uint8_t* seen = (uint8_t*)calloc(n, 1);
+    uint32_t current = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        initial[i] = current; seen[current] = 1;
+        uint32_t next = n; int64_t shortest = INT64_MAX;
+        for (uint32_t b = 0; b < n; ++b) {
+            if (seen[b]) continue;
+            const int64_t v = orc_distance(&d, current, b);
+            if (v < shortest) { shortest = v; next = b; }
+        }
+        current = next;
+    }
+    uint32_t* pos = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    orc_tour_t t = {n, initial, pos, 0};
+    orc_tour_reset(&t, &d);
+    const uint32_t cap = 8 * n + 8;
+    uint32_t* items = (uint32_t*)malloc(sizeof(uint32_t) * cap);
+    memset(seen, 0, n);
+    orc_queue_t q = {items, cap, 0, 0, seen, 0};
+    for (uint32_t i = 0; i < n; ++i) orc_queue_push_absent(&q, initial[i], NULL);
+    orc_ls_stats_t st; memset(&st, 0, sizeof(st));
+    orc_checklist_two_opt(&t, &d, ls, cfg->w, &q, cfg->initial_ls_evaluation_limit, &st);
+    int64_t cost = orc_tour_length(initial, n, &d);
+    uint32_t* identity = items;  /* reuse */
+    for (uint32_t i = 0; i < n; ++i) identity[i] = i;
+    const int64_t cheap = orc_tour_length(identity, n, &d);
+    if (cheap <= cost) { memcpy(initial, identity, sizeof(uint32_t) * n); cost = cheap; }
+    free(items); free(pos); free(seen);
+    return cost;
+}
+
+/* ---------------------------------------------------------------------- */
+/* A whole colony in engine arithmetic: reset_colony + initialize_products */
+/* (colony_state.cuh:72-110), per batch every ant, reduce_and_select      */
+/* (:148-208) and the FP32 trail update.                                  */
+/* ---------------------------------------------------------------------- */
+int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const uint32_t* backup,
+                   const uint32_t* ls, const uint32_t* initial, int64_t initial_cost,
+                   const orc_run_cfg_t* c, uint64_t key, uint32_t iterations, uint32_t* global_tour,
+                   int64_t* global_cost_out, orc_iter_trace_t* trace, float* trails_out,
+                   float* products_out) {
+    const orc_dist_t d = {n, xy, NULL};
+    const uint32_t k = c->k, A = c->ants;
+    const size_t cells = (size_t)n * k;
+    float* eta = (float*)malloc(sizeof(float) * cells);
+    float* trails = (float*)malloc(sizeof(float) * cells);
+    float* products = (float*)malloc(sizeof(float) * cells);
+    uint32_t* parent = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint32_t* epoch = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint32_t* tours = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n * A);
+    orc_ant_info_t* infos = (orc_ant_info_t*)malloc(sizeof(orc_ant_info_t) * A);
+    if (!eta || !trails || !products || !parent || !epoch || !tours || !infos) return -1;
+    for (size_t i = 0; i < cells; ++i) {
+        const uint32_t to = primary[i];
+        const double dist = to < n ? (double)orc_distance(&d, (uint32_t)(i / k), to) : 0.0;
+        eta[i] = to >= n ? 0.0f : (float)(dist > 0 ? (c->beta == 1.0 ? 1.0 / dist : 1.0 / pow(dist, c->beta)) : 1.0);
+    }
+    const double p_root = pow(c->p_best, 1.0 / (double)k);
+    int64_t epoch_cost = initial_cost, global_cost = initial_cost;
+    double tmin, tmax;
+    orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
+    float dflt = (float)tmax;
+    for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * eta[i]; }
+    memcpy(parent, initial, sizeof(uint32_t) * n);
+    memcpy(epoch, initial, sizeof(uint32_t) * n);
+    memcpy(global_tour, initial, sizeof(uint32_t) * n);
+    int failed = 0;
+    for (uint32_t batch = 0; batch < iterations; ++batch) {
+#ifdef _OPENMP
+#pragma omp parallel num_threads(c->threads > 0 ? (int)c->threads : 1)
+#endif
+        {
+            uint32_t* ptour = (uint32_t*)malloc(sizeof(uint32_t) * n);
+            uint32_t* ppos = (uint32_t*)malloc(sizeof(uint32_t) * n);
+            double* uni = (double*)malloc(sizeof(double) * n);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+            for (int ant = 0; ant < (int)A; ++ant) {
+                for (uint32_t s = 1; s < n; ++s) uni[s] = orc_uniform(key, batch, (uint32_t)ant, s);
+                const orc_choices_t ch = {NULL, uni, orc_start_node(key, batch, (uint32_t)ant, n), primary,
+                                          products, NULL, k, backup, c->b};
+                if (orc_ant(parent, &d, ls, c->w, &ch, c->mne_target, c->ls_evaluation_limit, NULL, ptour, ppos,
+                            NULL, NULL, &infos[ant]) != 0)
+                    failed = 1;
+                memcpy(tours + (size_t)ant * n, ptour, sizeof(uint32_t) * n);
+            }
+            free(ptour); free(ppos); free(uni);
+        }
+        uint32_t best = 0;
+        uint64_t steps = 0, evals = 0;
+        for (uint32_t a = 0; a < A; ++a) {
+            steps += infos[a].cons.steps; evals += infos[a].ls.move_evaluations;
+            if (infos[a].final_cost < infos[best].final_cost) best = a;
+        }
+        const int64_t cost = infos[best].final_cost;
+        const uint32_t* best_tour = tours + (size_t)best * n;
+        if (cost < epoch_cost) { epoch_cost = cost; memcpy(epoch, best_tour, sizeof(uint32_t) * n); }
+        if (cost < global_cost) { global_cost = cost; memcpy(global_tour, best_tour, sizeof(uint32_t) * n); }
+        orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
+        const int from_epoch = orc_source_uniform(key, batch) < c->epoch_source_probability;
+        const int64_t parent_cost = from_epoch ? epoch_cost : cost;
+        memcpy(parent, from_epoch ? epoch : best_tour, sizeof(uint32_t) * n);
+        orc_pheromone32(n, k, primary, parent, (float)c->retention, (float)tmin, (float)tmax,
+                        (float)(1.0 / (double)parent_cost), eta, trails, products, &dflt);
+        if (trace) {
+            orc_iter_trace_t* r = &trace[batch];
+            r->iteration_best_cost = cost; r->global_cost = global_cost; r->parent_cost = parent_cost;
+            r->iteration_best = best; r->source_is_epoch = (uint32_t)from_epoch;
+            r->tau_min = (float)tmin; r->tau_max = (float)tmax;
+            r->construction_steps = steps; r->ls_evaluations = evals;
+        }
+    }
+    *global_cost_out = global_cost;
+    if (trails_out) memcpy(trails_out, trails, sizeof(float) * cells);
+    if (products_out) memcpy(products_out, products, sizeof(float) * cells);
+    free(eta); free(trails); free(products); free(parent); free(epoch); free(tours); free(infos);
+    return failed ? -2 : 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* GP scoring -- apply_operation (cpp/include/gp_faco/program_ops.hpp:13-30)*/
+/* and score_cpu (cpp/src/program_cpu.cpp:79-116).  Opcodes 0-8 are the  */
+/* reference IR; 9 (protected division) and 10 (if>0, three operands) are  */
+/* the extended grammar (numeric_spec_id 2).                               */
+/* ---------------------------------------------------------------------- */
+float orc_apply_operation(int opcode, float left, float right, float third) {
+    float r = 0.0f;
+    switch (opcode) {
+        case 2: r = left + right; break;
+        case 3: r = left - right; break;
+        case 4: r = left * right; break;
+        case 5: r = fminf(left, right); break;
+        case 6: r = fmaxf(left, right); break;
+        case 7: r = fabsf(left); break;
+        case 8: { const float q = 1.0f + right * right; r = left * (1.0f / sqrtf(q)); break; }
+        case 9: r = fabsf(right) < 1e-6f ? 1.0f : left / right; break;
+        case 10: r = left > 0.0f ? right : third; break;
+        default: break;
+    }
+    return fminf(8.0f, fmaxf(-8.0f, r));
+}
+
+static int arity_of(int op) { return op == 7 ? 1 : op == 10 ? 3 : 2; }
+
+int orc_validate_program(const orc_program_t* p) {
+    const int extended = p->numeric_spec_id == 2;
+    if (p->ir_version != 1 || (p->numeric_spec_id != 1 && !extended) ||
+        (p->feature_spec_id != 1 && p->feature_spec_id != 2) || p->length == 0 || p->length > 63 ||
+        p->constants_count > 63)
+        return -1;
+    for (int i = 0; i < p->constants_count; ++i)
+        if (!isfinite(p->constants[i]) || fabsf(p->constants[i]) > 2.0f) return -2;
+    int depth[64], top = 0;
+    const int max_op = extended ? 10 : 8, max_depth = extended ? 6 : 5, max_stack = extended ? 16 : 6;
+    for (int i = 0; i < p->length; ++i) {
+        const int op = p->opcode[i], operand = p->operand[i];
+        if (op == 0 || op == 1) {
+            if ((op == 0 && operand >= 12) || (op == 1 && operand >= p->constants_count)) return -3;
+            depth[top++] = 0;
+        } else if (op >= 2 && op <= max_op) {
+            const int a = arity_of(op);
+            if (operand != 0 || top < a) return -4;
+            int dmax = 0;
+            for (int j = top - a; j < top; ++j) dmax = depth[j] > dmax ? depth[j] : dmax;
+            top -= a;
+            if (dmax + 1 > max_depth) return -5;
+            depth[top++] = dmax + 1;
+        } else {
+            return -6;
+        }
+        if (top > max_stack) return -7;
+    }
+    return top == 1 ? 0 : -8;
+}
+
+void orc_score(const orc_program_t* p, uint32_t features_count, const float* features, const uint32_t* masks,
+               uint32_t colonies, float* scores, int32_t* actions) {
+    (void)features_count;
+    for (uint32_t c = 0; c < colonies; ++c) {
+        float maximum = -INFINITY;
+        for (int action = 0; action < 32; ++action) {
+            float stack[16] = {0};
+            int top = 0;
+            for (int i = 0; i < p->length; ++i) {
+                const int op = p->opcode[i];
+                if (op == 0) stack[top++] = features[((size_t)p->operand[i] * colonies + c) * 32 + action];
+                else if (op == 1) stack[top++] = p->constants[p->operand[i]];
+                else {
+                    const int a = arity_of(op);
+                    const float third = a == 3 ? stack[--top] : 0.0f;
+                    const float right = a >= 2 ? stack[--top] : 0.0f;
+                    const float left = stack[--top];
+                    stack[top++] = orc_apply_operation(op, left, right, third);
+                }
+            }
+            scores[(size_t)c * 32 + action] = stack[0];
+            if ((masks[c] >> action) & 1u) maximum = fmaxf(maximum, stack[0]);
+        }
+        actions[c] = 32;
+        for (int action = 0; action < 32; ++action)
+            if (((masks[c] >> action) & 1u) && maximum - scores[(size_t)c * 32 + action] <= 1e-6f) {
+                actions[c] = action;
+                break;
+            }
+    }
+}

@@ -1,0 +1,293 @@
+"""ctypes binding for the CPU oracle (oracle/faco_oracle.c) and, when it was
+built in this container, the reference-core shim (oracle/_ref).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py -- never by the gplsaco_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libfaco_oracle.so"
+REF_LIB = HERE / "_ref" / "libgplsaco_ref.so"
+
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with the host compiler (contractions off)."""
+    src = HERE / "faco_oracle.c"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime,
+                                                                (HERE / "faco_oracle.h").stat().st_mtime):
+        LIB.parent.mkdir(exist_ok=True)
+        tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+        subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                               str(src), "-o", str(tmp), "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+class DistT(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("xy", C.c_void_p), ("matrix", C.c_void_p)]
+
+
+class LsStats(C.Structure):
+    _fields_ = [("processed_nodes", C.c_uint64), ("candidate_checks", C.c_uint64),
+                ("move_evaluations", C.c_uint64), ("accepted_moves", C.c_uint64),
+                ("reactivations", C.c_uint64), ("evaluation_limit_reached", C.c_uint32)]
+
+
+class ConsStats(C.Structure):
+    _fields_ = [("mne", C.c_uint32), ("steps", C.c_uint32), ("nonidentity_relocations", C.c_uint32),
+                ("legal_exhausted", C.c_uint32)]
+
+
+class Choices(C.Structure):
+    _fields_ = [("visit", C.c_void_p), ("uniforms", C.c_void_p), ("start", C.c_uint32),
+                ("primary", C.c_void_p), ("products32", C.c_void_p), ("products64", C.c_void_p),
+                ("k", C.c_uint32), ("backup", C.c_void_p), ("b", C.c_uint32)]
+
+
+class AntInfo(C.Structure):
+    _fields_ = [("construction_cost", C.c_int64), ("final_cost", C.c_int64), ("cons", ConsStats),
+                ("ls", LsStats), ("start_node", C.c_uint32), ("checklist_len", C.c_uint32)]
+
+
+class PrepCfg(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("b", C.c_uint32), ("w", C.c_uint32),
+                ("initial_ls_evaluation_limit", C.c_uint64)]
+
+
+class RunCfg(C.Structure):
+    _fields_ = [("ants", C.c_uint32), ("k", C.c_uint32), ("b", C.c_uint32), ("w", C.c_uint32),
+                ("mne_target", C.c_uint32), ("beta", C.c_double), ("retention", C.c_double),
+                ("p_best", C.c_double), ("epoch_source_probability", C.c_double),
+                ("ls_evaluation_limit", C.c_uint64), ("threads", C.c_uint32)]
+
+
+class IterTrace(C.Structure):
+    _fields_ = [("iteration_best_cost", C.c_int64), ("global_cost", C.c_int64), ("parent_cost", C.c_int64),
+                ("iteration_best", C.c_uint32), ("source_is_epoch", C.c_uint32), ("tau_min", C.c_float),
+                ("tau_max", C.c_float), ("construction_steps", C.c_uint64), ("ls_evaluations", C.c_uint64)]
+
+
+class Program(C.Structure):
+    _fields_ = [("ir_version", C.c_uint16), ("numeric_spec_id", C.c_uint16), ("feature_spec_id", C.c_uint16),
+                ("length", C.c_uint16), ("constants_count", C.c_uint16), ("opcode", C.c_uint8 * 63),
+                ("operand", C.c_uint8 * 63), ("constants", C.c_float * 63)]
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        L = _lib
+        L.orc_euc2d.restype = C.c_int32
+        L.orc_euc2d.argtypes = [C.c_int64] * 4
+        L.orc_ant.restype = C.c_int
+        L.orc_ant.argtypes = [u32p, C.POINTER(DistT), u32p, C.c_uint32, C.POINTER(Choices), C.c_uint32,
+                              C.c_uint64, u32p, u32p, u32p, u32p, u32p, C.POINTER(AntInfo)]
+        L.orc_select_next.restype = C.c_uint32
+        L.orc_select_next.argtypes = [C.c_uint32, u32p, f64p, C.c_uint32, u32p, C.c_uint32, u8p,
+                                      C.POINTER(DistT), C.c_double, C.POINTER(C.c_int)]
+        L.orc_trail_limits.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_pheromone64.argtypes = [C.c_uint32, C.c_uint32, u32p, u32p, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, f64p, C.POINTER(C.c_double)]
+        L.orc_pheromone32.argtypes = [C.c_uint32, C.c_uint32, u32p, u32p, C.c_float, C.c_float, C.c_float,
+                                      C.c_float, f32p, f32p, f32p, C.POINTER(C.c_float)]
+        L.orc_philox4x32.argtypes = [C.c_uint32] * 6 + [u32p]
+        L.orc_uniform.restype = C.c_double
+        L.orc_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_start_node.restype = C.c_uint32
+        L.orc_start_node.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_source_uniform.restype = C.c_double
+        L.orc_source_uniform.argtypes = [C.c_uint64, C.c_uint32]
+        L.orc_colony_key.restype = C.c_uint64
+        L.orc_colony_key.argtypes = [C.c_uint64, C.c_uint64]
+        L.orc_prepare.restype = C.c_int64
+        L.orc_prepare.argtypes = [C.c_uint32, i32p, C.POINTER(PrepCfg), u32p, u32p, u32p, u32p]
+        L.orc_run_colony.restype = C.c_int
+        L.orc_run_colony.argtypes = [C.c_uint32, i32p, u32p, u32p, u32p, u32p, C.c_int64, C.POINTER(RunCfg),
+                                     C.c_uint64, C.c_uint32, u32p, C.POINTER(C.c_int64), C.c_void_p,
+                                     C.c_void_p, C.c_void_p]
+        L.orc_validate_program.restype = C.c_int
+        L.orc_validate_program.argtypes = [C.POINTER(Program)]
+        L.orc_score.argtypes = [C.POINTER(Program), C.c_uint32, f32p, u32p, C.c_uint32, f32p, i32p]
+        L.orc_apply_operation.restype = C.c_float
+        L.orc_apply_operation.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float]
+    return _lib
+
+
+def ref():
+    """The reference-core shim, or None when it was not built here."""
+    global _ref
+    if _ref is None and REF_LIB.exists():
+        R = C.CDLL(str(REF_LIB))
+        R.ref_ant.restype = C.c_int
+        R.ref_ant.argtypes = [C.c_uint32, f64p, u32p, C.c_uint32, u32p, u32p, C.c_uint32, C.c_uint64, u32p,
+                              C.POINTER(C.c_double), u32p, u32p, C.POINTER(C.c_double), u32p, C.c_uint32, u64p]
+        R.ref_select_next.restype = C.c_int
+        R.ref_select_next.argtypes = [C.c_uint32, f64p, C.c_uint32, u32p, f64p, C.c_uint32, u32p, C.c_uint32,
+                                      u8p, C.c_double, C.POINTER(C.c_uint32), C.POINTER(C.c_int)]
+        R.ref_trail_limits.restype = C.c_int
+        R.ref_trail_limits.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        R.ref_pheromone.restype = C.c_int
+        R.ref_pheromone.argtypes = [C.c_uint32, C.c_uint32, u32p, u32p, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_double, C.c_uint32, f64p, C.POINTER(C.c_double)]
+        R.ref_score.restype = C.c_int
+        R.ref_score.argtypes = [C.c_uint16, C.c_uint16, C.c_uint16, C.c_uint16, u8p, u8p, C.c_uint16, f32p,
+                                f32p, u32p, C.c_uint32, f32p, i32p]
+        _ref = R
+    return _ref
+
+
+# ---------------------------------------------------------------- helpers
+
+def euc2d_matrix(xy: np.ndarray) -> np.ndarray:
+    """Dense EUC_2D matrix (int32) -- floor(sqrt(dx^2+dy^2)+0.5)."""
+    xy = np.asarray(xy, dtype=np.int64)
+    d = xy[:, None, :] - xy[None, :, :]
+    s = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]).astype(np.float64)
+    return np.floor(np.sqrt(s) + 0.5).astype(np.int32)
+
+
+def dist_struct(n, xy=None, matrix=None):
+    keep = []
+    xy_ptr = mat_ptr = None
+    if xy is not None:
+        xy = np.ascontiguousarray(xy, dtype=np.int32); keep.append(xy); xy_ptr = xy.ctypes.data
+    if matrix is not None:
+        matrix = np.ascontiguousarray(matrix, dtype=np.int32); keep.append(matrix); mat_ptr = matrix.ctypes.data
+    return DistT(n, xy_ptr, mat_ptr), keep
+
+
+def distance_ordered(rows: np.ndarray, matrix: np.ndarray) -> np.ndarray:
+    """Stable sort of every candidate row by distance (DistanceOrderedCandidates)."""
+    rows = np.asarray(rows, dtype=np.uint32)
+    out = rows.copy()
+    for a in range(rows.shape[0]):
+        keys = matrix[a, rows[a]]
+        out[a] = rows[a][np.argsort(keys, kind="stable")]
+    return out
+
+
+def ant(parent, ls_rows, mne_target, cap, *, xy=None, matrix=None, visit=None, uniforms=None, start=0,
+        primary=None, products32=None, products64=None, backup=None):
+    """One focused construction + checklist 2-opt.  Returns a dict."""
+    parent = np.ascontiguousarray(parent, dtype=np.uint32)
+    n = parent.size
+    ls_rows = np.ascontiguousarray(ls_rows, dtype=np.uint32)
+    w = ls_rows.shape[1]
+    d, keep = dist_struct(n, xy, matrix)
+    arrays = {}
+
+    def ptr(name, a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt); arrays[name] = a
+        return a.ctypes.data
+
+    k = 0 if primary is None else np.asarray(primary).shape[1]
+    b = 0 if backup is None else np.asarray(backup).shape[1]
+    ch = Choices(ptr("visit", visit, np.uint32), ptr("uniforms", uniforms, np.float64), start,
+                 ptr("primary", primary, np.uint32), ptr("p32", products32, np.float32),
+                 ptr("p64", products64, np.float64), k, ptr("backup", backup, np.uint32), b)
+    cons_tour = np.zeros(n, np.uint32); tour = np.zeros(n, np.uint32); pos = np.zeros(n, np.uint32)
+    checklist = np.zeros(8 * n + 8, np.uint32); selected = np.zeros(n, np.uint32)
+    info = AntInfo()
+    rc = lib().orc_ant(parent, C.byref(d), ls_rows, w, C.byref(ch), mne_target, cap, cons_tour, tour, pos,
+                       checklist, selected, C.byref(info))
+    if rc != 0:
+        raise RuntimeError(f"oracle ant failed ({rc})")
+    steps = info.cons.steps
+    return dict(construction_tour=cons_tour, tour=tour, positions=pos,
+                checklist=checklist[:info.checklist_len].copy(), selected=selected[:steps + 1].copy(),
+                construction_cost=info.construction_cost, final_cost=info.final_cost,
+                mne=info.cons.mne, steps=steps, nonidentity=info.cons.nonidentity_relocations,
+                processed=info.ls.processed_nodes, checks=info.ls.candidate_checks,
+                evaluations=info.ls.move_evaluations, accepted=info.ls.accepted_moves,
+                reactivations=info.ls.reactivations, limit_reached=info.ls.evaluation_limit_reached,
+                start=info.start_node)
+
+
+def prepare(xy, k, b, w, initial_ls_limit=100000):
+    xy = np.ascontiguousarray(xy, dtype=np.int32)
+    n = xy.shape[0]
+    cfg = PrepCfg(k, b, w, initial_ls_limit)
+    primary = np.zeros((n, k), np.uint32); backup = np.zeros((n, max(b, 1)), np.uint32)
+    ls = np.zeros((n, w), np.uint32); initial = np.zeros(n, np.uint32)
+    cost = lib().orc_prepare(n, xy, C.byref(cfg), primary, backup, ls, initial)
+    return dict(primary=primary, backup=backup[:, :b].copy(), ls=ls, initial=initial, cost=int(cost))
+
+
+def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, retention=0.98, p_best=0.1,
+               epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True):
+    xy = np.ascontiguousarray(xy, dtype=np.int32)
+    n = xy.shape[0]
+    cfg = RunCfg(ants, k, b, w, mne, beta, retention, p_best, epoch_source_probability, ls_limit, threads)
+    tour = np.zeros(n, np.uint32)
+    cost = C.c_int64()
+    trace = (IterTrace * max(iterations, 1))() if want_trace else None
+    trails = np.zeros(n * k, np.float32); products = np.zeros(n * k, np.float32)
+    backup = np.ascontiguousarray(prep["backup"] if b else np.zeros((n, 1), np.uint32), dtype=np.uint32)
+    rc = lib().orc_run_colony(n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
+                              np.ascontiguousarray(prep["ls"], dtype=np.uint32),
+                              np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),
+                              key, iterations, tour, C.byref(cost),
+                              C.cast(trace, C.c_void_p) if trace is not None else None,
+                              trails.ctypes.data, products.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle colony run failed ({rc})")
+    rows = None
+    if trace is not None:
+        rows = [dict(iteration_best_cost=t.iteration_best_cost, global_cost=t.global_cost,
+                     parent_cost=t.parent_cost, iteration_best=t.iteration_best,
+                     source_is_epoch=t.source_is_epoch, tau_min=t.tau_min, tau_max=t.tau_max,
+                     construction_steps=t.construction_steps, ls_evaluations=t.ls_evaluations)
+                for t in trace[:iterations]]
+    return dict(tour=tour, cost=int(cost.value), trace=rows, trails=trails.reshape(n, k),
+                products=products.reshape(n, k))
+
+
+def program_struct(d: dict) -> Program:
+    p = Program()
+    p.ir_version = d["ir_version"]; p.numeric_spec_id = d["numeric_spec_id"]
+    p.feature_spec_id = d["feature_spec_id"]
+    ops, operands, bits = d["opcode"], d["operand"], d["constant_bits"]
+    p.length = len(ops); p.constants_count = len(bits)
+    for i, (o, a) in enumerate(zip(ops, operands)):
+        p.opcode[i] = o; p.operand[i] = a
+    consts = np.asarray(bits, dtype=np.uint32).view(np.float32)
+    for i, c in enumerate(consts):
+        p.constants[i] = float(c)
+    return p
+
+
+def score(program: dict, features: np.ndarray, masks: np.ndarray):
+    features = np.ascontiguousarray(features, dtype=np.float32)
+    masks = np.ascontiguousarray(masks, dtype=np.uint32)
+    colonies = masks.size
+    p = program_struct(program)
+    if lib().orc_validate_program(C.byref(p)) != 0:
+        raise ValueError("invalid program")
+    scores = np.zeros((colonies, 32), np.float32); actions = np.zeros(colonies, np.int32)
+    lib().orc_score(C.byref(p), features.shape[0], features, masks, colonies, scores, actions)
+    return scores, actions

@@ -1,0 +1,139 @@
+// ref_shim.cpp -- C entry points over the reference's own CPU FACO core.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled together with the unmodified reference
+// sources cpp/src/faco_cpu.cpp and cpp/src/program_cpu.cpp (LinHuanli/GPLSACO)
+// by oracle/build_ref.sh into oracle/_ref/libgplsaco_ref.so.  The tests use it
+// to pin the C restatement in oracle/faco_oracle.c to the reference's own code.
+// Each entry point composes the reference API the way its own tests do
+// (tests/cpp/test_cuda_faco.cpp:68-98, tests/cpp/test_fixed_faco.cpp:235-282,
+// tests/python/test_native_scoring.py:23-46).
+#include "gp_faco/faco_cpu.hpp"
+#include "gp_faco/program.hpp"
+
+#include <cstring>
+#include <exception>
+#include <vector>
+
+using gp_faco::Node;
+
+namespace {
+gp_faco::DistanceFunction matrix_distance(const double* m, Node n) {
+    return [m, n](Node a, Node b) { return m[static_cast<std::size_t>(a) * n + b]; };
+}
+gp_faco::CandidateRows rows_of(const std::uint32_t* flat, Node n, Node w) {
+    gp_faco::CandidateRows rows(n);
+    for (Node a = 0; a < n; ++a) rows[a].assign(flat + static_cast<std::size_t>(a) * w, flat + (a + 1ull) * w);
+    return rows;
+}
+}  // namespace
+
+extern "C" {
+
+// FocusedConstruction with an explicit visit order, then checklist_two_opt.
+// stats[0..9] = mne, steps, nonidentity, processed, checks, evaluations,
+// accepted, reactivations, limit_reached, checklist length.
+int ref_ant(std::uint32_t n, const double* matrix, const std::uint32_t* ls_rows, std::uint32_t w,
+            const std::uint32_t* parent, const std::uint32_t* visit, std::uint32_t mne_target,
+            std::uint64_t cap, std::uint32_t* construction_tour, double* construction_cost,
+            std::uint32_t* tour, std::uint32_t* positions, double* final_cost, std::uint32_t* checklist,
+            std::uint32_t checklist_capacity, std::uint64_t* stats) {
+    try {
+        const auto distance = matrix_distance(matrix, n);
+        gp_faco::DistanceOrderedCandidates candidates(rows_of(ls_rows, n, w), distance);
+        gp_faco::CpuTour reference(std::vector<Node>(parent, parent + n), distance);
+        gp_faco::FocusedConstruction cpu(reference, visit[0], mne_target);
+        Node next = 1;
+        while (!cpu.done()) cpu.step(visit[next++]);
+        std::memcpy(construction_tour, cpu.tour().order().data(), n * sizeof(Node));
+        *construction_cost = cpu.tour().cost();
+        const auto ls = cpu.tour().checklist_two_opt(candidates, cpu.checklist(), cap);
+        std::memcpy(tour, cpu.tour().order().data(), n * sizeof(Node));
+        std::memcpy(positions, cpu.tour().positions().data(), n * sizeof(Node));
+        *final_cost = cpu.tour().cost();
+        const auto& list = cpu.checklist();
+        if (list.size() > checklist_capacity) return -3;
+        std::memcpy(checklist, list.data(), list.size() * sizeof(Node));
+        const auto& cs = cpu.stats();
+        const std::uint64_t values[10] = {cs.mne, cs.steps, cs.nonidentity_relocations, ls.processed_nodes,
+            ls.candidate_checks, ls.move_evaluations, ls.accepted_moves, ls.reactivations,
+            ls.evaluation_limit_reached ? 1u : 0u, list.size()};
+        std::memcpy(stats, values, sizeof(values));
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// select_next over one row; returns the node, writes the stage code
+// (0 primary, 1 zero-weight, 2 backup, 3 global, 4 exhausted).
+int ref_select_next(std::uint32_t n, const double* matrix, std::uint32_t current, const std::uint32_t* primary,
+                    const double* products, std::uint32_t k, const std::uint32_t* backup, std::uint32_t b,
+                    const std::uint8_t* visited, double uniform, std::uint32_t* node, int* stage) {
+    try {
+        const auto s = gp_faco::select_next(current, std::vector<Node>(primary, primary + k),
+            std::vector<double>(products, products + k), std::vector<Node>(backup, backup + b),
+            std::vector<std::uint8_t>(visited, visited + n), matrix_distance(matrix, n), uniform);
+        *node = s.node;
+        *stage = static_cast<int>(s.stage);
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+int ref_trail_limits(std::uint32_t count, double p_best, double retention, double cost, double* minimum,
+                     double* maximum) {
+    try {
+        const auto limits = gp_faco::candidate_trail_limits(count, p_best, retention, cost);
+        *minimum = limits.minimum;
+        *maximum = limits.maximum;
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// SparsePheromone seeded with `trails` (all rows the given width), then
+// evaporate + symmetric deposit along every edge of `parent`
+// (tests/cpp/test_fixed_faco.cpp:277-281).  Writes the updated stored trails.
+int ref_pheromone(std::uint32_t n, std::uint32_t k, const std::uint32_t* primary, const std::uint32_t* parent,
+                  double initial, double retention, double minimum, double maximum, double increment,
+                  std::uint32_t rounds, double* trails_out, double* default_out) {
+    try {
+        gp_faco::SparsePheromone pheromone(rows_of(primary, n, k), initial, true);
+        for (std::uint32_t r = 0; r < rounds; ++r) {
+            pheromone.evaporate(retention, minimum);
+            for (Node i = 0; i < n; ++i) pheromone.deposit(parent[(i + n - 1) % n], parent[i], increment, maximum);
+        }
+        std::memcpy(trails_out, pheromone.stored().data(), sizeof(double) * n * k);
+        *default_out = pheromone.default_value();
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// score_cpu for a reference-IR program (features [12][colonies][32]).
+int ref_score(std::uint16_t ir_version, std::uint16_t numeric_spec_id, std::uint16_t feature_spec_id,
+              std::uint16_t length, const std::uint8_t* opcode, const std::uint8_t* operand,
+              std::uint16_t constants_count, const float* constants, const float* features,
+              const std::uint32_t* masks, std::uint32_t colonies, float* scores, std::int32_t* actions) {
+    try {
+        gp_faco::Program p;
+        p.ir_version = ir_version; p.numeric_spec_id = numeric_spec_id; p.feature_spec_id = feature_spec_id;
+        p.length = length; p.constants_count = constants_count;
+        if (length > 63 || constants_count > 63) return -2;
+        std::memcpy(p.opcode, opcode, length);
+        std::memcpy(p.operand, operand, length);
+        std::memcpy(p.constants, constants, constants_count * sizeof(float));
+        const auto out = gp_faco::score_cpu(p, std::vector<float>(features, features + 12ull * 32 * colonies),
+                                            std::vector<std::uint32_t>(masks, masks + colonies));
+        std::memcpy(scores, out.scores.data(), out.scores.size() * sizeof(float));
+        std::memcpy(actions, out.actions.data(), out.actions.size() * sizeof(std::int32_t));
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+}  // extern "C"
