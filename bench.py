@@ -1,0 +1,301 @@
+"""Benchmark: plain Focused-ACO ant-tours+LS per second at N=1000 on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one ACO iteration of the whole panel: every ant of every colony
+constructs a tour from its colony's parent and runs its local search, then
+each colony reduces, selects and updates its trails.  Workload: 16 instances
+of N=1000 integer coordinates uniform in [0,10^6]^2 x 16 seeds = 256 colonies,
+32 ants each, k=16, backup 64, LS width 20, MNE 8, 2-opt, retention 0.98.
+The data are synthetic (seeded), standing in for the reference's uniform
+TSP1000 rows.  With N>1 each rank runs its own panel (independent colonies,
+weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 1000
+INSTANCES = 16
+SEEDS_PER_INSTANCE = 16
+ANTS, K_PRIMARY, BACKUP, LS_WIDTH, MNE, RETENTION = 32, 16, 64, 20, 8, 0.98
+METRIC = "ant-tours+LS/sec (plain FACO, N=1000)"
+L2_BYTES = 129 * 2**20
+
+
+def instance_xy(i: int) -> np.ndarray:
+    rng = np.random.default_rng(1000 + i)
+    return rng.integers(0, 10**6 + 1, size=(N, 2)).astype(np.int32)
+
+
+def bytes_per_fe(n, k, ants, steps_per_fe, evals_per_fe, moved_per_fe) -> float:
+    """Algorithmic bytes per ant-tour+LS: parent read + tour write (8N),
+    candidate id + weight per construction step (8k each), 20 B per LS move
+    evaluation, 16 B per moved tour element, trail update amortised per ant."""
+    return 8 * n + 8 * k * steps_per_fe + 20 * evals_per_fe + 16 * moved_per_fe + 16 * n * k / ants
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [line for line in out.splitlines() if line.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "lines", []):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(seconds: float = 12.0, threads: int | None = None) -> dict:
+    """The oracle port (C, one colony per host thread) on a bounded sample of
+    the same workload: N=1000 colonies with 32 ants, run for ~`seconds`."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle
+    oracle.lib()
+    threads = threads or os.cpu_count() or 1
+    xy = instance_xy(0)
+    prep = oracle.prepare(xy, K_PRIMARY, BACKUP, LS_WIDTH)
+    iterations = 2
+
+    def colony(i):
+        key = oracle.lib().orc_colony_key(i, 1)
+        oracle.run_colony(xy, prep, ants=ANTS, k=K_PRIMARY, b=BACKUP, w=LS_WIDTH, mne=MNE, iterations=iterations,
+                          key=key, retention=RETENTION, threads=1, want_trace=False)
+        return ANTS * iterations
+
+    done = 0
+    start = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        seed = 0
+        while time.perf_counter() - start < seconds:
+            done += sum(pool.map(colony, range(seed, seed + threads)))
+            seed += threads
+    elapsed = time.perf_counter() - start
+    return {"value": done / elapsed, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
+            "sample": f"{done} ant-tours+LS of N=1000 colonies (32 ants, 2 iterations each from the prepared "
+                      f"initial tour), one colony per host thread, {elapsed:.1f} s"}
+
+
+def measured_peak():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        return json.loads(path.read_text())["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def run_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle
+    oracle.lib()
+    threads = os.cpu_count() or 1
+    xy = instance_xy(0)
+    prep = oracle.prepare(xy, K_PRIMARY, BACKUP, LS_WIDTH)
+
+    def colonies(iterations):
+        def one(i):
+            oracle.run_colony(xy, prep, ants=ANTS, k=K_PRIMARY, b=BACKUP, w=LS_WIDTH, mne=MNE,
+                              iterations=iterations, key=oracle.lib().orc_colony_key(i, 1), retention=RETENTION,
+                              threads=1, want_trace=False)
+        with ThreadPoolExecutor(max_workers=threads) as pool:
+            list(pool.map(one, range(threads)))
+
+    colonies(max(1, args.warmup // 3))
+    start = time.perf_counter()
+    colonies(args.steps)
+    elapsed = time.perf_counter() - start
+    fe = threads * ANTS * args.steps
+    value = fe / elapsed
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ant-tours+LS/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic",
+            "config": {"workload": f"plain FACO N=1000 uniform, {threads} colonies x 32 ants (one per host "
+                                   f"thread), k=16, MNE 8, 2-opt", "colonies": threads, "ants": ANTS, "n": N},
+            "cpu_baseline": {"value": value, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
+                             "sample": f"{threads} colonies x {args.steps} iterations"},
+            "e2e": {"value": value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank: int, world: int) -> None:
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    import gplsaco_gb300 as g
+
+    colonies = INSTANCES * SEEDS_PER_INSTANCE
+    settings = g.FixedFacoSettings(ants=ANTS, primary_width=K_PRIMARY, backup_width=BACKUP, ls_width=LS_WIDTH,
+                                   retention=RETENTION)
+    engine = g.FacoBatchEngine(N, colonies, settings, device=local)
+    t0 = time.perf_counter()
+    for i in range(INSTANCES):
+        engine.register_problem(1 + i, instance_xy(i).astype(np.float64))
+    registration_s = time.perf_counter() - t0
+    keys = np.repeat(np.arange(1, INSTANCES + 1, dtype=np.uint64), SEEDS_PER_INSTANCE)
+    seeds = (np.tile(np.arange(SEEDS_PER_INSTANCE, dtype=np.uint64), INSTANCES)
+             + np.uint64(1000 * rank))
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(engine.stream_ptr)
+
+    # ---- device throughput: inputs resident, L2 flushed before every step ----
+    engine.begin(keys, seeds, MNE)
+    engine.step(args.warmup)
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            engine.step(1)
+            b.record(stream)
+            b.synchronize()
+            step_ms.append(a.elapsed_time(b))
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    # per-kernel split of a few more steps (ant kernel = the dominant kernel)
+    kernel_steps = 3
+    ant_ms, upd_ms = engine.step_timed(kernel_steps)
+    totals = engine.finish()
+    iters = totals["completed_batches"]
+    fe_total = iters * colonies * ANTS
+    s_fe = totals["construction_steps"] / fe_total
+    e_fe = totals["ls_evaluations"] / fe_total
+    r_fe = totals["reversed_elements"] / fe_total
+    elapsed_ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    fe_timed = args.steps * colonies * ANTS * world
+    value = fe_timed / (elapsed_ms / 1e3)
+
+    # ---- end to end through the public API: host keys/seeds in, tours out ----
+    engine.evaluate_faco_evaluations(keys, seeds, ANTS * args.warmup, MNE)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = engine.evaluate_faco_evaluations(keys, seeds, ANTS * args.steps, MNE)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = args.steps * colonies * ANTS / e2e_s
+    h2d = keys.nbytes + seeds.nbytes
+    d2h = colonies * N * 4 + colonies * 8
+    assert all(len(it["tour"]) == N for it in res["items"])
+
+    # ---- roofline of the ant kernel (per launch = one step of all ants) ----
+    bfe = bytes_per_fe(N, K_PRIMARY, ANTS, s_fe, e_fe, r_fe)
+    ants_per_launch = colonies * ANTS
+    achieved = bfe * ants_per_launch / (ant_ms / kernel_steps / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    engine.close()
+    if rank != 0:
+        return
+    base = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "ant-tours+LS/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": {"workload": "plain FACO, N=1000 uniform int coords, 16 instances x 16 seeds = 256 colonies, "
+                               "32 ants, k=16, backup 64, LS width 20, MNE 8, 2-opt, retention 0.98",
+                   "colonies": colonies, "ants": ANTS, "n": N, "l2": "flushed before every timed step "
+                   "(258 MB write)", "registration_seconds": registration_s},
+        "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps,
+                "call": "FacoBatchEngine.evaluate_faco_evaluations (C ABI faco_evaluate), host keys/seeds in, "
+                        "host tours/costs out"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "ant_kernel<engine>", "peak_source": peak_kind,
+                     "bytes_per_fe": bfe, "per_fe": {"construction_steps": s_fe, "ls_evaluations": e_fe,
+                                                      "moved_elements": r_fe},
+                     "ant_kernel_ms": ant_ms / kernel_steps, "update_kernel_ms": upd_ms / kernel_steps},
+        "cpu_baseline": base,
+        "clocks": clocks.summary(),
+        "gpu_launches": 2 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_gb300(args, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,10 @@
+"""GB300-native Focused-ACO batch engine (drop-in for LinHuanli/GPLSACO's
+gp_faco_ext solve path).  All compute runs in the CUDA library built from
+gplsaco_gb300/csrc; importing this package does not load it until first use.
+"""
+from .engine import (FacoBatchEngine, FixedFacoSettings, ant_diagnostic, faco_ants, pheromone_step, program_to_c,
+                     score_cuda)
+from .session import GpuSession
+
+__all__ = ["FacoBatchEngine", "FixedFacoSettings", "GpuSession", "ant_diagnostic", "faco_ants", "pheromone_step",
+           "program_to_c", "score_cuda"]

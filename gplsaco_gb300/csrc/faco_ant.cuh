@@ -1,0 +1,251 @@
+// faco_ant.cuh -- one warp runs one ant: focused construction from the
+// colony's parent tour, then checklist local search.
+//
+// Semantics follow the reference's fused kernel construct_and_search
+// (cuda/faco_device.cuh:100-501) and its CPU restatement
+// (cpp/src/faco_cpu.cpp:82-294): relocation steps until the MNE target,
+// candidate-row roulette with backup and global fallbacks, then FIFO
+// checklist 2-opt with best-gain moves and the reference's tie, cap and
+// reversal rules.  The GB300 design differs throughout:
+//   - every per-ant scalar is warp-uniform and lives in registers of all 32
+//     lanes (no shared State struct, no lane-0 serial sections beyond the
+//     single store of a queue slot);
+//   - the tour, its inverse, the checklist ring and the visited/pending
+//     flags live in shared memory (16-bit nodes), coordinates are staged
+//     once per block for all its ants (same colony);
+//   - distances are exact EUC_2D integers computed on the fly, so gains and
+//     tour lengths are exact int64 and ties are decided by index only;
+//   - the roulette keeps the reference's ordered FP64 prefix sums (needed
+//     for bit-identical choices) but gathers weights with shuffles and
+//     selects with one ballot;
+//   - relocation shifts run as register-staged warp chunks, reversals as
+//     disjoint swap pairs, the best move by __reduce_max/min_sync.
+#pragma once
+
+#include "faco_common.cuh"
+
+namespace faco {
+
+enum AntMode : int {
+    kModeEngine = 0,    // Philox choices, colony parent (production path)
+    kModeVisits = 1,    // explicit visit orders (diagnostic)
+    kModeUniforms = 2,  // injected uniforms + given products (diagnostic)
+    kModePrepare = 3,   // no construction; LS over the whole tour (registration)
+};
+
+struct AntLaunch {
+    // instance (all ants of a block share one instance)
+    const InstanceView* instances;
+    // engine mode
+    const ColonyView* colonies;
+    ColonyState* states;
+    const uint2* work;            // per block: (colony, first ant)
+    std::uint32_t ants;           // ants per colony
+    std::uint32_t warps;          // warps per block
+    std::uint32_t n_max;          // smem layout size
+    unsigned long long ls_limit;
+    std::uint32_t ls_mode;
+    // diagnostic modes: tasks on instance 0
+    std::uint32_t tasks;
+    const node_t* task_tours;     // [tasks][n]
+    const node_t* task_pos;       // [tasks][n]
+    const long long* task_costs;  // [tasks]
+    const node_t* task_visits;    // [tasks][n]
+    const double* task_uniforms;  // [tasks][n]
+    const std::uint32_t* task_starts;
+    const std::uint32_t* task_targets;
+    const float* task_products;   // [n][k]
+    // diagnostic outputs (may be null)
+    node_t* out_construction;     // [tasks][n]
+    node_t* out_tours;            // [tasks][n]
+    node_t* out_pos;              // [tasks][n]
+    node_t* out_selected;         // [tasks][n]
+    std::uint32_t* out_checklist; // [tasks][checklist_cap]
+    std::uint32_t checklist_cap;
+    long long* out_costs;         // [tasks][2]
+    unsigned long long* out_counters;  // [tasks][10]
+    unsigned* error;
+};
+
+__device__ __forceinline__ int dist(const int2* xy, std::uint32_t a, std::uint32_t b) {
+    return euc2d(xy[a], xy[b]);
+}
+
+// Per-warp shared-memory workspace and checklist ring.
+struct AntSmem {
+    node_t* tour;
+    node_t* pos;
+    node_t* ring;
+    std::uint8_t* visited;
+    std::uint8_t* queued;
+};
+
+__host__ __device__ inline std::uint32_t ant_smem_bytes(std::uint32_t n) {
+    return (8u * n + 15u) & ~15u;
+}
+__host__ __device__ inline std::uint32_t block_smem_bytes(std::uint32_t n, std::uint32_t warps) {
+    return ((8u * n + 15u) & ~15u) + warps * ant_smem_bytes(n);
+}
+
+struct Checklist {
+    std::uint32_t head, tail, pending, pushed;  // ring indices and counters (warp-uniform)
+};
+
+// Appends v unless it is pending (reference append_if_absent,
+// cuda/faco_device.cuh:81-92).  Warp-uniform decision, lane 0 stores.
+__device__ __forceinline__ bool push_absent(const AntSmem& s, Checklist& q, std::uint32_t n, std::uint32_t v,
+                                            std::uint32_t lane, std::uint32_t* log, std::uint32_t log_cap) {
+    const bool absent = s.queued[v] == 0;
+    if (absent) {
+        if (lane == 0) {
+            s.queued[v] = 1;
+            s.ring[q.tail] = (node_t)v;
+            if (log && q.pushed < log_cap) log[q.pushed] = v;
+        }
+        q.tail = q.tail + 1 == n ? 0 : q.tail + 1;
+        ++q.pending;
+        ++q.pushed;
+    }
+    __syncwarp();
+    return absent;
+}
+
+struct AntResult {
+    long long construction_cost, final_cost;
+    std::uint32_t mne, steps, nonidentity;
+    unsigned long long processed, checks, evaluations, accepted, reactivations;
+    unsigned long long moved;  // tour elements rewritten by relocations and reversals
+    std::uint32_t limit_reached, checklist;
+};
+
+// Moves `node` right after `target` (CpuTour::relocate): shifts the closed
+// interval between their positions by one, register-staged per 32-element
+// chunk so that every read of a chunk precedes its writes.
+__device__ __forceinline__ void relocate_shift(const AntSmem& s, std::uint32_t lane, std::uint32_t tpos,
+                                               std::uint32_t npos, std::uint32_t node) {
+    if (tpos < npos) {
+        // new[tpos+1] = node, new[i] = old[i-1] for i in (tpos+1, npos]
+        for (int base = (int)npos; base >= (int)tpos + 1; base -= 32) {
+            const int i = base - (int)lane;
+            std::uint32_t v = 0;
+            const bool act = i >= (int)tpos + 1;
+            if (act) v = i == (int)tpos + 1 ? node : s.tour[i - 1];
+            __syncwarp();
+            if (act) { s.tour[i] = (node_t)v; s.pos[v] = (node_t)i; }
+            __syncwarp();
+        }
+    } else {
+        // new[i] = old[i+1] for i in [npos, tpos), new[tpos] = node
+        for (std::uint32_t base = npos; base <= tpos; base += 32) {
+            const std::uint32_t i = base + lane;
+            std::uint32_t v = 0;
+            const bool act = i <= tpos;
+            if (act) v = i == tpos ? node : s.tour[i + 1];
+            __syncwarp();
+            if (act) { s.tour[i] = (node_t)v; s.pos[v] = (node_t)i; }
+            __syncwarp();
+        }
+    }
+}
+
+// flip_without_cost (cpp/src/faco_cpu.cpp:114-135) as disjoint swap pairs.
+// Returns the number of elements in the reversed segment.
+__device__ __forceinline__ std::uint32_t flip(const AntSmem& s, std::uint32_t n, std::uint32_t lane,
+                                              std::uint32_t start, std::uint32_t end) {
+    std::uint32_t first = s.pos[start], last = s.pos[end];
+    if (first > last) { const std::uint32_t t = first; first = last; last = t; }
+    const std::uint32_t length = last - first;
+    const bool straight = length <= n - length || first == 0;
+    const std::uint32_t count = straight ? length : n - length, begin = straight ? first : last;
+    __syncwarp();
+    for (std::uint32_t o = lane; o < count / 2; o += 32) {
+        std::uint32_t l = begin + o, r = begin + count - 1 - o;
+        if (l >= n) l -= n;
+        if (r >= n) r -= n;
+        const node_t a = s.tour[l], b = s.tour[r];
+        s.tour[l] = b; s.tour[r] = a;
+        s.pos[b] = (node_t)l; s.pos[a] = (node_t)r;
+    }
+    __syncwarp();
+    return count;
+}
+
+// Checklist 2-opt, best gain per popped node, reference tie/cap rules
+// (cpp/src/faco_cpu.cpp:148-217; cuda/faco_device.cuh:295-478).
+__device__ __forceinline__ void checklist_two_opt(const AntSmem& s, const int2* xy, const InstanceView& in,
+                                                  std::uint32_t n, std::uint32_t lane, Checklist& q,
+                                                  unsigned long long cap, AntResult& r, long long& gain_sum,
+                                                  std::uint32_t* log, std::uint32_t log_cap) {
+    const std::uint32_t w = in.w;
+    while (q.pending > 0 && r.accepted < n) {
+        if (r.evaluations >= cap) { r.limit_reached = 1; break; }
+        const std::uint32_t a = s.ring[q.head];
+        q.head = q.head + 1 == n ? 0 : q.head + 1;
+        --q.pending;
+        __syncwarp();
+        if (lane == 0) s.queued[a] = 0;
+        const std::uint32_t pa = s.pos[a];
+        const std::uint32_t an = s.tour[pa + 1 == n ? 0 : pa + 1];
+        const std::uint32_t ap = s.tour[pa == 0 ? n - 1 : pa - 1];
+        ++r.processed;
+        const int2 pa_xy = xy[a];
+        const int cur0 = euc2d(pa_xy, xy[an]), cur1 = euc2d(xy[ap], pa_xy);
+        std::uint32_t b = n;
+        int ab = 0;
+        if (lane < w) {
+            b = in.ls[(size_t)a * w + lane];
+            ab = in.ls_dist[(size_t)a * w + lane];
+        }
+        // prefix of candidates that pass the distance test, per kind
+        const bool bad0 = lane < w && (b >= n || !(cur0 > ab));
+        const bool bad1 = lane < w && (b >= n || !(cur1 > ab));
+        const unsigned f0m = __ballot_sync(kFull, bad0), f1m = __ballot_sync(kFull, bad1);
+        const std::uint32_t f0 = f0m ? __ffs(f0m) - 1 : w, f1 = f1m ? __ffs(f1m) - 1 : w;
+        unsigned long long remaining = cap - r.evaluations;
+        const std::uint32_t used0 = remaining < f0 ? (std::uint32_t)remaining : f0;
+        r.evaluations += used0;
+        r.checks += used0 + (used0 < w ? 1 : 0);
+        if (used0 < f0) { r.limit_reached = 1; break; }
+        remaining = cap - r.evaluations;
+        const std::uint32_t used1 = remaining < f1 ? (std::uint32_t)remaining : f1;
+        r.evaluations += used1;
+        r.checks += used1 + (used1 < w ? 1 : 0);
+        if (used1 < f1) { r.limit_reached = 1; break; }
+        // gains
+        int g0 = INT_MIN, g1 = INT_MIN;
+        std::uint32_t nb0 = 0, nb1 = 0;
+        if (lane < used0 || lane < used1) {
+            const std::uint32_t pb = s.pos[b];
+            const int2 bxy = xy[b];
+            if (lane < used0) {
+                nb0 = s.tour[pb + 1 == n ? 0 : pb + 1];
+                g0 = (nb0 == a || b == an) ? 0 : cur0 + euc2d(bxy, xy[nb0]) - ab - euc2d(xy[an], xy[nb0]);
+            }
+            if (lane < used1) {
+                nb1 = s.tour[pb == 0 ? n - 1 : pb - 1];
+                g1 = (nb1 == a || b == ap) ? 0 : cur1 + euc2d(bxy, xy[nb1]) - ab - euc2d(xy[ap], xy[nb1]);
+            }
+        }
+        const int best = __reduce_max_sync(kFull, g0 > g1 ? g0 : g1);
+        if (best > 0) {
+            const std::uint32_t mine = g0 == best ? lane : g1 == best ? w + lane : 0xffu;
+            const std::uint32_t index = __reduce_min_sync(kFull, mine);
+            const std::uint32_t kind = index >= w, j = kind ? index - w : index;
+            const std::uint32_t bj = __shfl_sync(kFull, b, j);
+            const std::uint32_t nbj = __shfl_sync(kFull, kind ? nb1 : nb0, j);
+            std::uint32_t m0, m1, m2, m3;
+            if (kind == 0) { m0 = an; m1 = nbj; m2 = a; m3 = bj; }
+            else { m0 = a; m1 = bj; m2 = ap; m3 = nbj; }
+            r.moved += flip(s, n, lane, m0, m1);
+            r.reactivations += push_absent(s, q, n, m0, lane, log, log_cap);
+            r.reactivations += push_absent(s, q, n, m1, lane, log, log_cap);
+            r.reactivations += push_absent(s, q, n, m2, lane, log, log_cap);
+            r.reactivations += push_absent(s, q, n, m3, lane, log, log_cap);
+            ++r.accepted;
+            gain_sum -= best;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace faco

@@ -1,0 +1,124 @@
+// faco_common.cuh -- device types and primitives shared by the FACO kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace faco {
+
+using node_t = std::uint16_t;   // node ids on the device (n <= 65535)
+constexpr std::uint32_t kMaxNodes = 65535;
+constexpr std::uint32_t kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Device error word bits (the host turns a non-zero word into FACO_EDEVICE).
+enum DeviceError : unsigned {
+    kErrNone = 0,
+    kErrQueueOverflow = 1u << 0,
+    kErrBadChoice = 1u << 1,
+    kErrLoopCap = 1u << 2,
+    kErrShape = 1u << 3,
+};
+
+// TSPLIB EUC_2D: round(sqrt(dx^2+dy^2)) with halves up.  sqrt(s) is never a
+// half-integer for integer s, so the result is the unique m with
+// m*m - m < s <= m*m + m (m > 0) -- found from an FP32 estimate and at most
+// a few exact int64 corrections.  Equal to floor(sqrt((double)s) + 0.5) for
+// every |coordinate| < 2^26.
+__device__ __forceinline__ int euc2d(int2 p, int2 q) {
+    const long long dx = (long long)p.x - q.x, dy = (long long)p.y - q.y;
+    const long long s = dx * dx + dy * dy;
+    long long m = __float2ll_rn(sqrtf((float)s));
+    while (s > m * m + m) ++m;
+    while (m > 0 && s <= m * m - m) --m;
+    return (int)m;
+}
+
+// Philox4x32 with 10 rounds (Salmon, Moraes, Dror, Shaw, SC'11).
+struct uint4v { std::uint32_t x, y, z, w; };
+__device__ __forceinline__ uint4v philox4x32(std::uint32_t c0, std::uint32_t c1, std::uint32_t c2,
+                                             std::uint32_t c3, std::uint32_t k0, std::uint32_t k1) {
+#pragma unroll
+    for (int round = 0; round < 10; ++round) {
+        const std::uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const std::uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        c0 = hi1 ^ c1 ^ k0; c1 = lo1; c2 = hi0 ^ c3 ^ k1; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    return {c0, c1, c2, c3};
+}
+
+__device__ __forceinline__ double u53(std::uint32_t hi, std::uint32_t lo) {
+    return (double)(((((unsigned long long)hi) << 32) | lo) >> 11) * 0x1.0p-53;
+}
+
+// Counter layout: (step, ant, batch, tag).  tag 0 construction uniform,
+// 1 start node, 2 colony source draw (ant = 0xffffffff).
+__device__ __forceinline__ double step_uniform(unsigned long long key, std::uint32_t batch, std::uint32_t ant,
+                                               std::uint32_t step) {
+    const uint4v r = philox4x32(step, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+    return u53(r.x, r.y);
+}
+__device__ __forceinline__ std::uint32_t start_node(unsigned long long key, std::uint32_t batch,
+                                                    std::uint32_t ant, std::uint32_t n) {
+    const uint4v r = philox4x32(0, ant, batch, 1, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+    return (std::uint32_t)(((unsigned long long)r.x * n) >> 32);
+}
+__device__ __forceinline__ double source_uniform(unsigned long long key, std::uint32_t batch) {
+    const uint4v r = philox4x32(0, 0xffffffffu, batch, 2, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+    return u53(r.x, r.y);
+}
+
+// One registered instance resident on the device.
+struct InstanceView {
+    std::uint32_t n;
+    std::uint32_t k, b, w;         // primary / backup / LS widths (clipped to n)
+    const int2* xy;                // [n]
+    const node_t* primary;         // [n][k]
+    const node_t* backup;          // [n][b]
+    const node_t* ls;              // [n][w], distance ordered
+    const int* ls_dist;            // [n][w]
+    const float* eta;              // [n][k]
+    const node_t* initial;         // [n]
+    long long initial_cost;
+};
+
+// Per-colony mutable state (one per work item of an evaluation).
+struct ColonyState {
+    long long epoch_cost, global_cost, parent_cost;
+    long long iteration_best_cost;
+    float tau_min, tau_max, default_trail;
+    std::uint32_t iteration;       // completed batches
+    std::uint32_t iteration_best;
+    std::uint32_t source_is_epoch;
+    std::uint32_t mne_target;
+    std::int32_t action;
+    unsigned long long construction_steps, ls_evaluations, reversed_elements;
+};
+
+// Per-colony constant view.
+struct ColonyView {
+    std::uint32_t instance;        // index into the instance table
+    std::uint32_t n;
+    unsigned long long key;        // Philox key
+    float* trails;                 // [n][k]
+    float* products;               // [n][k]
+    node_t* parent;                // [n]
+    node_t* parent_pos;            // [n]
+    node_t* epoch;                 // [n]
+    node_t* global;                // [n]
+    node_t* ant_tours;             // [ants][n]
+    long long* ant_costs;          // [ants]
+    unsigned* ant_counts;          // [ants][3]: construction steps, LS evaluations, moved elements
+};
+
+struct TraceRow {
+    long long iteration_best_cost, global_cost, parent_cost;
+    std::uint32_t iteration_best, source_is_epoch;
+    float tau_min, tau_max;
+    std::uint32_t mne_target;
+    std::int32_t action;
+    unsigned long long construction_steps, ls_evaluations;
+};
+
+}  // namespace faco

@@ -1,0 +1,973 @@
+// faco_engine.cu -- the batch engine behind the C ABI (include/faco_gb300.h).
+//
+// Replaces the reference's FacoBatchEngine / FixedFacoGpu host drivers
+// (cuda/batch_engine.cu:78-1192, cuda/fixed_faco.cu:105-177) and the pybind11
+// boundary (cpp/src/bindings.cpp).  One engine owns one CUDA stream and all
+// device memory of its evaluations; instances are prepared once at
+// registration and stay resident.  The iteration loop -- ant kernel, fused
+// colony update -- is captured once per evaluation into a CUDA graph of
+// several iterations and replayed; the batch index lives on the device, so
+// replays need no parameter changes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/faco_gb300.h"
+#include "faco_host.h"
+#include "faco_kernels.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+// Iterations captured per CUDA graph (replayed until the budget is spent).
+constexpr std::uint32_t kGraphIterations = 16;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void require(bool ok, const std::string& message) {
+    if (!ok) throw Error(FACO_EINVAL, message);
+}
+void cuda_check(cudaError_t status, const char* what) {
+    if (status != cudaSuccess) throw Error(FACO_ECUDA, std::string(what) + ": " + cudaGetErrorString(status));
+}
+
+template <class F>
+int guarded(F&& body) {
+    try {
+        body();
+        return FACO_OK;
+    } catch (const Error& e) {
+        g_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_error = "host allocation failed";
+        return FACO_ENOMEM;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return FACO_EINVAL;
+    }
+}
+
+template <class T>
+class DeviceBuffer {
+public:
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(std::size_t count) { resize(count); }
+    ~DeviceBuffer() { release(); }
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), count_(o.count_) { o.ptr_ = nullptr; o.count_ = 0; }
+    void resize(std::size_t count) {
+        if (count <= count_ && ptr_) return;
+        release();
+        if (count) cuda_check(cudaMalloc(reinterpret_cast<void**>(&ptr_), count * sizeof(T)), "cudaMalloc");
+        count_ = count;
+    }
+    void upload(const T* host, std::size_t count, cudaStream_t s) {
+        resize(count);
+        if (count) cuda_check(cudaMemcpyAsync(ptr_, host, count * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+    }
+    void upload(const std::vector<T>& v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+    void download(T* host, std::size_t count, cudaStream_t s) const {
+        if (count) cuda_check(cudaMemcpyAsync(host, ptr_, count * sizeof(T), cudaMemcpyDeviceToHost, s), "download");
+    }
+    T* get() const { return ptr_; }
+    std::size_t size() const { return count_; }
+    std::size_t bytes() const { return count_ * sizeof(T); }
+
+private:
+    void release() {
+        if (ptr_) cudaFree(ptr_);
+        ptr_ = nullptr;
+        count_ = 0;
+    }
+    T* ptr_ = nullptr;
+    std::size_t count_ = 0;
+};
+
+std::uint64_t mix64(std::uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+using Clock = std::chrono::steady_clock;
+double seconds_since(Clock::time_point t) { return std::chrono::duration<double>(Clock::now() - t).count(); }
+
+std::vector<std::int32_t> integer_coordinates(const double* xy, std::uint32_t n) {
+    std::vector<std::int32_t> out(2ull * n);
+    for (std::size_t i = 0; i < 2ull * n; ++i) {
+        const double v = xy[i];
+        require(std::isfinite(v) && v == std::floor(v) && std::fabs(v) < 67108864.0,
+                "coordinates must be finite integers with |x| < 2^26 (EUC_2D)");
+        out[i] = static_cast<std::int32_t>(v);
+    }
+    return out;
+}
+
+// Warps (ants) per block: the largest that keeps the block's shared memory
+// within the opt-in limit and at least two blocks per SM when possible.
+std::uint32_t choose_warps(std::uint32_t n_max, std::uint32_t ants) {
+    constexpr std::uint32_t kSmemLimit = 227u * 1024u;
+    std::uint32_t best = 1;
+    for (std::uint32_t w = 1; w <= faco::kMaxWarpsPerBlock; w *= 2) {
+        if (faco::block_smem_bytes(n_max, w) <= kSmemLimit && w <= std::max(1u, ants)) best = w;
+    }
+    while (best > 1 && faco::block_smem_bytes(n_max, best) * 2 > kSmemLimit &&
+           faco::block_smem_bytes(n_max, best / 2) * 2 <= kSmemLimit)
+        best /= 2;
+    return std::min<std::uint32_t>(best, 4);
+}
+
+struct Instance {
+    std::uint64_t key = 0;
+    std::uint32_t n = 0, k = 0, b = 0, w = 0;
+    std::vector<std::int32_t> xy;
+    std::vector<std::uint32_t> initial;
+    std::vector<std::uint16_t> primary, backup, ls;
+    std::int64_t initial_cost = 0;
+    DeviceBuffer<int2> d_xy;
+    DeviceBuffer<faco::node_t> d_primary, d_backup, d_ls, d_initial;
+    DeviceBuffer<int> d_ls_dist;
+    DeviceBuffer<float> d_eta;
+    faco::InstanceView view() const {
+        return {n, k, b, w, d_xy.get(), d_primary.get(), d_backup.get(), d_ls.get(), d_ls_dist.get(), d_eta.get(),
+                d_initial.get(), static_cast<long long>(initial_cost)};
+    }
+};
+
+void launch_ants(int mode, const faco::AntLaunch& L, std::uint32_t blocks, std::uint32_t warps, cudaStream_t s) {
+    const std::uint32_t smem = faco::block_smem_bytes(L.n_max, warps);
+    cuda_check(faco::prepare_ant_kernel(mode, smem), "cudaFuncSetAttribute");
+    cuda_check(faco::launch_ant_kernel(mode, L, blocks, warps, smem, s), "ant kernel launch");
+}
+
+}  // namespace
+
+struct faco_engine {
+    faco_settings settings{};
+    std::uint32_t dimension = 0, capacity = 0, ants = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex busy;
+    std::map<std::uint64_t, std::unique_ptr<Instance>> instances;
+    std::vector<std::uint64_t> instance_order;  // device table index -> key
+    DeviceBuffer<faco::InstanceView> d_instances;
+    // evaluation buffers (grow-only)
+    DeviceBuffer<float> trails, products;
+    DeviceBuffer<faco::node_t> parent, parent_pos, epoch, global, ant_tours;
+    DeviceBuffer<long long> ant_costs;
+    DeviceBuffer<unsigned> ant_counts, error;
+    DeviceBuffer<faco::ColonyState> states;
+    DeviceBuffer<faco::ColonyView> colonies;
+    DeviceBuffer<uint2> work;
+    DeviceBuffer<faco::TraceRow> trace;
+    DeviceBuffer<faco::node_t> checkpoints;
+
+    // the evaluation in progress (begin .. finish)
+    struct EvalState {
+        bool active = false;
+        std::uint32_t count = 0, n_max = 0, warps = 0, blocks = 0, smem = 0, trace_cap = 0, done = 0;
+        std::size_t node_total = 0;
+        std::vector<std::uint32_t> sizes;
+        std::vector<std::uint64_t> keys;
+        faco::ColonyParams P{};
+        faco::AntLaunch L{};
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    } eval;
+
+    ~faco_engine() {
+        if (eval.exec) cudaGraphExecDestroy(eval.exec);
+        if (eval.graph) cudaGraphDestroy(eval.graph);
+        if (stream) {
+            cudaSetDevice(device);
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    std::uint32_t index_of(std::uint64_t key) const {
+        const auto it = std::find(instance_order.begin(), instance_order.end(), key);
+        return static_cast<std::uint32_t>(it - instance_order.begin());
+    }
+
+    void upload_instance_table() {
+        std::vector<faco::InstanceView> views;
+        for (const auto key : instance_order) views.push_back(instances.at(key)->view());
+        d_instances.upload(views, stream);
+    }
+
+    unsigned read_error() {
+        unsigned word = 0;
+        error.download(&word, 1, stream);
+        cuda_check(cudaStreamSynchronize(stream), "synchronize");
+        return word;
+    }
+    void reset_error() { cuda_check(cudaMemsetAsync(error.get(), 0, sizeof(unsigned), stream), "memset"); }
+};
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* faco_last_error(void) { return g_error.c_str(); }
+
+void faco_default_settings(faco_settings* s) {
+    if (!s) return;
+    std::memset(s, 0, sizeof(*s));
+    s->ants = 0;
+    s->primary_width = 16;
+    s->backup_width = 64;
+    s->ls_width = 20;
+    s->beta = 1.0;
+    s->retention = 0.5;
+    s->p_best = 0.1;
+    s->epoch_source_probability = 0.01;
+    s->ls_evaluation_limit = 100000;
+    s->initial_ls_evaluation_limit = 100000;
+    s->ls_mode = FACO_LS_TWO_OPT;
+}
+
+int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_settings* settings, int device,
+                       faco_engine** out) {
+    return guarded([&] {
+        require(out && settings, "null argument");
+        *out = nullptr;
+        const faco_settings& c = *settings;
+        require(dimension >= 3 && dimension <= 10000, "dimension must be in [3, 10000]");
+        require(colonies >= 1 && colonies <= 65536, "colonies must be in [1, 65536]");
+        require(c.ants <= 4096 && c.primary_width >= 2 && c.ls_width > 0 && std::isfinite(c.beta) && c.beta > 0 &&
+                    c.retention >= 0 && c.retention < 1 && c.p_best > 0 && c.p_best < 1 &&
+                    c.epoch_source_probability >= 0 && c.epoch_source_probability <= 1,
+                "invalid FACO settings");
+        require(c.primary_width <= 32 && c.ls_width <= 32, "primary and LS widths are limited to 32 (one warp)");
+        require(c.ls_mode == FACO_LS_TWO_OPT, "only the 2-opt local search is available in this build");
+        auto e = std::make_unique<faco_engine>();
+        e->settings = c;
+        e->dimension = dimension;
+        e->capacity = colonies;
+        e->device = device;
+        if (c.ants == 0) {
+            std::uint32_t groups = 1;
+            while (256ull * groups * groups < dimension) ++groups;
+            e->ants = 64 * groups;  // normalized_settings (prepared_problem.cpp:68-73)
+        } else {
+            e->ants = c.ants;
+        }
+        e->settings.ants = e->ants;
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        e->error.resize(1);
+        e->reset_error();
+        *out = e.release();
+    });
+}
+
+void faco_engine_destroy(faco_engine* engine) { delete engine; }
+
+int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* xy, uint32_t n,
+                          faco_registration* info) {
+    return guarded([&] {
+        require(e && xy, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        require(!e->eval.active, "cannot register while an evaluation is active");
+        require(n >= 3 && n <= e->dimension, "instance size must be in [3, dimension]");
+        require(e->instances.find(instance_key) == e->instances.end(), "instance key already registered");
+        cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+        const auto started = Clock::now();
+        auto inst = std::make_unique<Instance>();
+        inst->key = instance_key;
+        inst->n = n;
+        inst->xy = integer_coordinates(xy, n);
+        const faco_settings& c = e->settings;
+        inst->k = std::min(c.primary_width, n - 1);
+        inst->b = std::min(c.backup_width, n - 1 - inst->k);
+        inst->w = std::min(c.ls_width, n - 1);
+        // cheap solution: identity tour (make_cheap_problem, prepared_problem.cpp:90-105)
+        std::vector<std::uint32_t> identity(n);
+        for (std::uint32_t i = 0; i < n; ++i) identity[i] = i;
+        const std::int64_t cheap = faco::host_tour_length(inst->xy, identity.data(), n);
+        const double cheap_seconds = seconds_since(started);
+        std::vector<std::int32_t> ls_dist;
+        std::vector<float> eta;
+        faco::host_candidates(inst->xy, n, inst->k, inst->b, inst->w, inst->primary, inst->backup, inst->ls,
+                              ls_dist, eta, c.beta);
+        const auto nn = faco::host_nearest_neighbour_tour(inst->xy, n);
+        // device-resident instance
+        cudaStream_t s = e->stream;
+        inst->d_xy.upload(reinterpret_cast<const int2*>(inst->xy.data()), n, s);
+        inst->d_primary.upload(inst->primary, s);
+        inst->d_backup.resize(std::max<std::size_t>(inst->backup.size(), 1));
+        inst->d_backup.upload(inst->backup, s);
+        inst->d_ls.upload(inst->ls, s);
+        inst->d_ls_dist.upload(ls_dist, s);
+        inst->d_eta.upload(eta, s);
+        // initial checklist 2-opt over the NN tour on the GPU (prepared_problem.cpp:159-162)
+        std::vector<faco::node_t> tour16(nn.begin(), nn.end()), pos16(n);
+        for (std::uint32_t i = 0; i < n; ++i) pos16[nn[i]] = static_cast<faco::node_t>(i);
+        const long long nn_cost = faco::host_tour_length(inst->xy, nn.data(), n);
+        DeviceBuffer<faco::node_t> d_tour, d_pos, d_out;
+        DeviceBuffer<long long> d_cost, d_costs;
+        d_tour.upload(tour16, s);
+        d_pos.upload(pos16, s);
+        d_cost.upload(&nn_cost, 1, s);
+        d_out.resize(n);
+        d_costs.resize(2);
+        DeviceBuffer<faco::InstanceView> d_view;
+        inst->d_initial.resize(n);
+        const faco::InstanceView v = inst->view();
+        d_view.upload(&v, 1, s);
+        faco::AntLaunch L{};
+        L.instances = d_view.get();
+        L.warps = 1;
+        L.n_max = n;
+        L.ls_limit = c.initial_ls_evaluation_limit;
+        L.tasks = 1;
+        L.task_tours = d_tour.get();
+        L.task_pos = d_pos.get();
+        L.task_costs = d_cost.get();
+        L.out_tours = d_out.get();
+        L.out_costs = d_costs.get();
+        L.error = e->error.get();
+        e->reset_error();
+        launch_ants(faco::kModePrepare, L, 1, 1, s);
+        std::vector<faco::node_t> improved(n);
+        long long costs[2] = {0, 0};
+        d_out.download(improved.data(), n, s);
+        d_costs.download(costs, 2, s);
+        const unsigned err = e->read_error();
+        if (err) throw Error(FACO_EDEVICE, "device error word " + std::to_string(err) + " during registration");
+        inst->initial.assign(improved.begin(), improved.end());
+        inst->initial_cost = costs[1];
+        require(faco::host_tour_length(inst->xy, inst->initial.data(), n) == inst->initial_cost,
+                "initial tour length mismatch");
+        if (cheap <= inst->initial_cost) {
+            inst->initial = identity;
+            inst->initial_cost = cheap;
+        }
+        std::vector<faco::node_t> init16(inst->initial.begin(), inst->initial.end());
+        inst->d_initial.upload(init16, s);
+        cuda_check(cudaStreamSynchronize(s), "synchronize");
+        if (info) {
+            info->cheap_seconds = cheap_seconds;
+            info->preparation_seconds = seconds_since(started);
+            info->initial_cost = inst->initial_cost;
+            info->n = n;
+        }
+        e->instance_order.push_back(instance_key);
+        e->instances.emplace(instance_key, std::move(inst));
+        e->upload_instance_table();
+        cuda_check(cudaStreamSynchronize(s), "synchronize");
+    });
+}
+
+int faco_problem_rows(faco_engine* e, uint64_t key, uint32_t* initial, uint32_t* primary, uint32_t* backup,
+                      uint32_t* ls) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        const auto it = e->instances.find(key);
+        require(it != e->instances.end(), "instance not registered");
+        const Instance& in = *it->second;
+        if (initial) std::copy(in.initial.begin(), in.initial.end(), initial);
+        if (primary) std::copy(in.primary.begin(), in.primary.end(), primary);
+        if (backup) std::copy(in.backup.begin(), in.backup.end(), backup);
+        if (ls) std::copy(in.ls.begin(), in.ls.end(), ls);
+    });
+}
+
+}  // extern "C"
+
+// ---- evaluation: begin / step / finish ------------------------------------
+namespace {
+
+void destroy_graph(faco_engine* e) {
+    if (e->eval.exec) cudaGraphExecDestroy(e->eval.exec);
+    if (e->eval.graph) cudaGraphDestroy(e->eval.graph);
+    e->eval.exec = nullptr;
+    e->eval.graph = nullptr;
+}
+
+void enqueue_iteration(faco_engine* e, cudaStream_t st) {
+    auto& v = e->eval;
+    cuda_check(faco::launch_ant_kernel(faco::kModeEngine, v.L, v.blocks, v.warps, v.smem, st), "ant launch");
+    faco::colony_update_kernel<<<v.count, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
+                                                         v.P, v.trace_cap ? e->trace.get() : nullptr, v.count,
+                                                         v.trace_cap);
+    cuda_check(cudaGetLastError(), "update launch");
+}
+
+void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+                      uint32_t mne_target, uint32_t trace_iterations) {
+    require(e && keys && seeds, "null argument");
+    require(!e->eval.active, "an evaluation is already active on this engine");
+    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+    const std::uint32_t A = e->ants;
+    require(count >= 1 && count <= e->capacity, "task count must be in [1, colonies]");
+    require(mne_target > 0, "MNE target must be positive");
+    auto& v = e->eval;
+    v.sizes.assign(count, 0);
+    v.keys.assign(keys, keys + count);
+    std::vector<faco::ColonyView> views(count);
+    std::size_t tau_total = 0, node_total = 0, ant_total = 0;
+    std::uint32_t n_max = 3, k_common = 0;
+    for (std::uint32_t c = 0; c < count; ++c) {
+        const auto it = e->instances.find(keys[c]);
+        require(it != e->instances.end(), "task instance not registered");
+        const Instance& in = *it->second;
+        require(k_common == 0 || k_common == in.k, "instances of one evaluation must share the primary width");
+        k_common = in.k;
+        v.sizes[c] = in.n;
+        tau_total += static_cast<std::size_t>(in.n) * in.k;
+        node_total += in.n;
+        ant_total += static_cast<std::size_t>(A) * in.n;
+        n_max = std::max(n_max, in.n);
+    }
+    cudaStream_t s = e->stream;
+    e->trails.resize(tau_total);
+    e->products.resize(tau_total);
+    e->parent.resize(node_total);
+    e->parent_pos.resize(node_total);
+    e->epoch.resize(node_total);
+    e->global.resize(node_total);
+    e->ant_tours.resize(ant_total);
+    e->ant_costs.resize(static_cast<std::size_t>(A) * count);
+    e->ant_counts.resize(3ull * A * count);
+    e->states.resize(count);
+    std::size_t tau_off = 0, node_off = 0, ant_off = 0;
+    for (std::uint32_t c = 0; c < count; ++c) {
+        const Instance& in = *e->instances.at(keys[c]);
+        faco::ColonyView& cv = views[c];
+        cv.instance = e->index_of(keys[c]);
+        cv.n = in.n;
+        cv.key = mix64(seeds[c] ^ mix64(keys[c]));
+        cv.trails = e->trails.get() + tau_off;
+        cv.products = e->products.get() + tau_off;
+        cv.parent = e->parent.get() + node_off;
+        cv.parent_pos = e->parent_pos.get() + node_off;
+        cv.epoch = e->epoch.get() + node_off;
+        cv.global = e->global.get() + node_off;
+        cv.ant_tours = e->ant_tours.get() + ant_off;
+        cv.ant_costs = e->ant_costs.get() + static_cast<std::size_t>(c) * A;
+        cv.ant_counts = e->ant_counts.get() + 3ull * c * A;
+        tau_off += static_cast<std::size_t>(in.n) * in.k;
+        node_off += in.n;
+        ant_off += static_cast<std::size_t>(A) * in.n;
+    }
+    e->colonies.upload(views, s);
+    v.count = count;
+    v.node_total = node_total;
+    v.n_max = n_max;
+    v.warps = choose_warps(n_max, A);
+    // largest instances first so that the long ants start in the first wave
+    std::vector<std::uint32_t> order(count);
+    for (std::uint32_t c = 0; c < count; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](std::uint32_t x, std::uint32_t y) { return v.sizes[x] > v.sizes[y]; });
+    std::vector<uint2> jobs;
+    for (const std::uint32_t c : order)
+        for (std::uint32_t a = 0; a < A; a += v.warps) jobs.push_back(make_uint2(c, a));
+    e->work.upload(jobs, s);
+    v.blocks = static_cast<std::uint32_t>(jobs.size());
+    v.smem = faco::block_smem_bytes(n_max, v.warps);
+    v.trace_cap = trace_iterations;
+    if (trace_iterations) e->trace.resize(static_cast<std::size_t>(trace_iterations) * count);
+    v.P = faco::ColonyParams{};
+    v.P.ants = A;
+    v.P.mne_target = mne_target;
+    v.P.retention = e->settings.retention;
+    v.P.retention_f = static_cast<float>(e->settings.retention);
+    v.P.epoch_source_probability = e->settings.epoch_source_probability;
+    v.P.p_root = std::pow(e->settings.p_best, 1.0 / static_cast<double>(k_common));
+    v.L = faco::AntLaunch{};
+    v.L.instances = e->d_instances.get();
+    v.L.colonies = e->colonies.get();
+    v.L.states = e->states.get();
+    v.L.work = e->work.get();
+    v.L.ants = A;
+    v.L.warps = v.warps;
+    v.L.n_max = n_max;
+    v.L.ls_limit = e->settings.ls_evaluation_limit;
+    v.L.ls_mode = e->settings.ls_mode;
+    v.L.error = e->error.get();
+    e->reset_error();
+    cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, v.smem), "cudaFuncSetAttribute");
+    faco::colony_init_kernel<<<count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(), e->states.get(), v.P);
+    cuda_check(cudaGetLastError(), "init launch");
+    // one graph of kGraphIterations iterations, replayed; the batch index is device state
+    destroy_graph(e);
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    for (std::uint32_t i = 0; i < kGraphIterations; ++i) enqueue_iteration(e, s);
+    cuda_check(cudaStreamEndCapture(s, &v.graph), "end capture");
+    cuda_check(cudaGraphInstantiate(&v.exec, v.graph, 0), "graph instantiate");
+    v.done = 0;
+    v.active = true;
+}
+
+void step_evaluation(faco_engine* e, std::uint32_t iterations) {
+    auto& v = e->eval;
+    require(v.active, "no active evaluation");
+    std::uint32_t left = iterations;
+    while (left >= kGraphIterations) {
+        cuda_check(cudaGraphLaunch(v.exec, e->stream), "graph launch");
+        left -= kGraphIterations;
+    }
+    for (; left; --left) enqueue_iteration(e, e->stream);
+    v.done += iterations;
+}
+
+void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimension) {
+    auto& v = e->eval;
+    require(v.active, "no active evaluation");
+    v.active = false;
+    destroy_graph(e);
+    cudaStream_t s = e->stream;
+    cuda_check(cudaStreamSynchronize(s), "evaluation");
+    const unsigned err = e->read_error();
+    if (err) throw Error(FACO_EDEVICE, "device error word " + std::to_string(err));
+    if (!out) return;
+    std::vector<faco::node_t> global(v.node_total);
+    e->global.download(global.data(), v.node_total, s);
+    std::vector<faco::ColonyState> states(v.count);
+    e->states.download(states.data(), v.count, s);
+    if (out->trace && v.trace_cap) {
+        static_assert(sizeof(faco::TraceRow) == sizeof(faco_trace_row), "trace row layout");
+        e->trace.download(reinterpret_cast<faco::TraceRow*>(out->trace),
+                          static_cast<std::size_t>(std::min(v.trace_cap, v.done)) * v.count, s);
+    }
+    cuda_check(cudaStreamSynchronize(s), "download");
+    std::uint64_t steps = 0, evals = 0, reversed = 0;
+    std::size_t node_off = 0;
+    for (std::uint32_t c = 0; c < v.count; ++c) {
+        const std::uint32_t n = v.sizes[c];
+        if (out->tours)
+            for (std::uint32_t i = 0; i < dimension; ++i)
+                out->tours[static_cast<std::size_t>(c) * dimension + i] = i < n ? global[node_off + i] : UINT32_MAX;
+        if (out->costs) out->costs[c] = states[c].global_cost;
+        steps += states[c].construction_steps;
+        evals += states[c].ls_evaluations;
+        reversed += states[c].reversed_elements;
+        node_off += n;
+    }
+    out->completed_batches = v.done;
+    out->construction_steps = steps;
+    out->ls_evaluations = evals;
+    out->reversed_elements = reversed;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* faco_engine_stream(faco_engine* e) { return e ? static_cast<void*>(e->stream) : nullptr; }
+
+int faco_begin(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count, uint32_t mne_target,
+               uint32_t trace_iterations) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        begin_evaluation(e, keys, seeds, count, mne_target, trace_iterations);
+    });
+}
+
+int faco_step(faco_engine* e, uint32_t iterations) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        step_evaluation(e, iterations);
+    });
+}
+
+int faco_step_timed(faco_engine* e, uint32_t iterations, double* ant_ms, double* update_ms) {
+    return guarded([&] {
+        require(e && ant_ms && update_ms, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        cudaStream_t s = e->stream;
+        std::vector<cudaEvent_t> ev(3 * iterations);
+        for (auto& x : ev) cuda_check(cudaEventCreate(&x), "event");
+        for (std::uint32_t i = 0; i < iterations; ++i) {
+            cuda_check(cudaEventRecord(ev[3 * i], s), "event");
+            cuda_check(faco::launch_ant_kernel(faco::kModeEngine, v.L, v.blocks, v.warps, v.smem, s), "ant launch");
+            cuda_check(cudaEventRecord(ev[3 * i + 1], s), "event");
+            faco::colony_update_kernel<<<v.count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(),
+                                                               e->states.get(), v.P,
+                                                               v.trace_cap ? e->trace.get() : nullptr, v.count,
+                                                               v.trace_cap);
+            cuda_check(cudaGetLastError(), "update launch");
+            cuda_check(cudaEventRecord(ev[3 * i + 2], s), "event");
+        }
+        cuda_check(cudaStreamSynchronize(s), "timed step");
+        double a = 0, u = 0;
+        for (std::uint32_t i = 0; i < iterations; ++i) {
+            float x = 0, y = 0;
+            cuda_check(cudaEventElapsedTime(&x, ev[3 * i], ev[3 * i + 1]), "elapsed");
+            cuda_check(cudaEventElapsedTime(&y, ev[3 * i + 1], ev[3 * i + 2]), "elapsed");
+            a += x;
+            u += y;
+        }
+        for (auto& x : ev) cudaEventDestroy(x);
+        v.done += iterations;
+        *ant_ms = a;
+        *update_ms = u;
+    });
+}
+
+int faco_finish(faco_engine* e, faco_outputs* out) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        finish_evaluation(e, out, e->dimension);
+    });
+}
+
+int faco_evaluate(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+                  uint64_t evaluation_limit, uint32_t mne_target, const uint64_t* checkpoint_iterations,
+                  uint32_t n_checkpoints, faco_outputs* out) {
+    return guarded([&] {
+        require(e && keys && seeds && out, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "only one active evaluation per engine");
+        const auto started = Clock::now();
+        const std::uint32_t A = e->ants;
+        require(evaluation_limit % A == 0 && evaluation_limit / A <= UINT32_MAX,
+                "evaluation limit must be a whole number of ant batches");
+        const std::uint32_t T = static_cast<std::uint32_t>(evaluation_limit / A);
+        for (std::uint32_t i = 0; i < n_checkpoints; ++i) {
+            require(checkpoint_iterations[i] <= T, "checkpoint beyond the budget");
+            require(i == 0 || checkpoint_iterations[i] > checkpoint_iterations[i - 1],
+                    "checkpoints must be strictly increasing");
+        }
+        require(n_checkpoints == 0 || out->checkpoint_tours, "checkpoint output missing");
+        begin_evaluation(e, keys, seeds, count, mne_target, out->trace ? T : 0);
+        auto& v = e->eval;
+        try {
+            if (n_checkpoints) e->checkpoints.resize(static_cast<std::size_t>(n_checkpoints) * v.node_total);
+            cudaStream_t s = e->stream;
+            cudaEvent_t ev0, ev1;
+            cuda_check(cudaEventCreate(&ev0), "event");
+            cuda_check(cudaEventCreate(&ev1), "event");
+            std::uint32_t cp = 0;
+            auto checkpoint = [&]() {
+                while (cp < n_checkpoints && checkpoint_iterations[cp] == v.done) {
+                    cuda_check(cudaMemcpyAsync(e->checkpoints.get() + static_cast<std::size_t>(cp) * v.node_total,
+                                               e->global.get(), v.node_total * sizeof(faco::node_t),
+                                               cudaMemcpyDeviceToDevice, s),
+                               "checkpoint copy");
+                    ++cp;
+                }
+            };
+            cuda_check(cudaEventRecord(ev0, s), "event record");
+            checkpoint();
+            while (v.done < T) {
+                const std::uint32_t stop = cp < n_checkpoints ? static_cast<std::uint32_t>(checkpoint_iterations[cp]) : T;
+                step_evaluation(e, stop - v.done);
+                checkpoint();
+            }
+            cuda_check(cudaEventRecord(ev1, s), "event record");
+            cuda_check(cudaStreamSynchronize(s), "evaluation");
+            float ms = 0;
+            cuda_check(cudaEventElapsedTime(&ms, ev0, ev1), "event time");
+            cudaEventDestroy(ev0);
+            cudaEventDestroy(ev1);
+            std::vector<faco::node_t> cps;
+            if (n_checkpoints) {
+                cps.resize(static_cast<std::size_t>(n_checkpoints) * v.node_total);
+                e->checkpoints.download(cps.data(), cps.size(), s);
+            }
+            const std::vector<std::uint32_t> sizes = v.sizes;
+            const std::size_t node_total = v.node_total;
+            finish_evaluation(e, out, e->dimension);
+            const std::uint32_t D = e->dimension;
+            std::size_t node_off = 0;
+            for (std::uint32_t c = 0; c < count; ++c) {
+                for (std::uint32_t p = 0; p < n_checkpoints; ++p)
+                    for (std::uint32_t i = 0; i < D; ++i)
+                        out->checkpoint_tours[(static_cast<std::size_t>(p) * count + c) * D + i] =
+                            i < sizes[c] ? cps[static_cast<std::size_t>(p) * node_total + node_off + i] : UINT32_MAX;
+                node_off += sizes[c];
+            }
+            out->kernel_milliseconds = ms;
+            out->solve_seconds = seconds_since(started);
+        } catch (...) {
+            if (v.active) {
+                v.active = false;
+                destroy_graph(e);
+                cudaStreamSynchronize(e->stream);
+            }
+            throw;
+        }
+    });
+}
+
+
+int faco_validate_program(const faco_program* p) {
+    return guarded([&] {
+        require(p != nullptr, "null program");
+        const bool extended = p->numeric_spec_id == 2;
+        require(p->ir_version == 1 && (p->numeric_spec_id == 1 || extended) &&
+                    (p->feature_spec_id == 1 || p->feature_spec_id == 2) && p->length >= 1 && p->length <= 63 &&
+                    p->constants_count <= 63,
+                "unknown version or program size out of range");
+        for (int i = 0; i < p->constants_count; ++i)
+            require(std::isfinite(p->constants[i]) && std::fabs(p->constants[i]) <= 2.0f,
+                    "ERC must be finite and in [-2, 2]");
+        int depth[64], top = 0;
+        const int max_op = extended ? 10 : 8, max_depth = extended ? 6 : 5, max_stack = extended ? 16 : 6;
+        for (int i = 0; i < p->length; ++i) {
+            const int op = p->opcode[i], operand = p->operand[i];
+            if (op == 0 || op == 1) {
+                require(!((op == 0 && operand >= 12) || (op == 1 && operand >= p->constants_count)),
+                        "terminal index out of range");
+                depth[top++] = 0;
+            } else {
+                require(op >= 2 && op <= max_op, "unknown opcode");
+                const int arity = op == 7 ? 1 : op == 10 ? 3 : 2;
+                require(operand == 0 && top >= arity, "function operand non-zero or stack underflow");
+                int dmax = 0;
+                for (int j = top - arity; j < top; ++j) dmax = std::max(dmax, depth[j]);
+                top -= arity;
+                require(dmax + 1 <= max_depth, "tree too deep");
+                depth[top++] = dmax + 1;
+            }
+            require(top <= max_stack, "stack peak too high");
+        }
+        require(top == 1, "final stack is not a single value");
+    });
+}
+
+int faco_score(const faco_program* programs, uint32_t n_programs, const float* features, uint32_t features_count,
+               const uint32_t* masks, uint32_t colonies, float* scores, int32_t* actions) {
+    return guarded([&] {
+        require(programs && features && masks && scores && actions, "null argument");
+        require(n_programs >= 1 && colonies >= 1 && colonies % n_programs == 0,
+                "colonies must be a multiple of the program count");
+        require(features_count == 12, "features must be [12, colonies, 32]");
+        for (std::uint32_t i = 0; i < n_programs; ++i)
+            if (faco_validate_program(programs + i) != FACO_OK) throw Error(FACO_EINVAL, g_error);
+        const std::size_t nf = static_cast<std::size_t>(features_count) * colonies * 32;
+        for (std::size_t i = 0; i < nf; ++i)
+            require(std::isfinite(features[i]) && features[i] >= 0.0f && features[i] <= 1.0f,
+                    "features must be finite and in [0, 1]");
+        for (std::uint32_t c = 0; c < colonies; ++c) require(masks[c] != 0, "a colony has no legal action");
+        static_assert(sizeof(faco::Program) == sizeof(faco_program), "program layout");
+        DeviceBuffer<faco::Program> d_prog;
+        DeviceBuffer<float> d_feat, d_scores;
+        DeviceBuffer<std::uint32_t> d_masks;
+        DeviceBuffer<std::int32_t> d_actions;
+        cudaStream_t s = nullptr;
+        d_prog.upload(reinterpret_cast<const faco::Program*>(programs), n_programs, s);
+        d_feat.upload(features, nf, s);
+        d_masks.upload(masks, colonies, s);
+        d_scores.resize(static_cast<std::size_t>(colonies) * 32);
+        d_actions.resize(colonies);
+        const std::uint32_t blocks = (colonies * 32 + 127) / 128;
+        faco::score_kernel<<<blocks, 128, 0, s>>>(d_prog.get(), colonies / n_programs, d_feat.get(), d_masks.get(),
+                                                  d_scores.get(), d_actions.get(), colonies);
+        cuda_check(cudaGetLastError(), "score launch");
+        d_scores.download(scores, static_cast<std::size_t>(colonies) * 32, s);
+        d_actions.download(actions, colonies, s);
+        cuda_check(cudaStreamSynchronize(s), "score");
+    });
+}
+
+int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, uint32_t w, const uint32_t* tours,
+                        const uint32_t* visits, const double* uniforms, const uint32_t* starts,
+                        const uint32_t* primary, const float* products, uint32_t k, const uint32_t* backup,
+                        uint32_t b, const uint32_t* mne_targets, uint32_t tasks, uint64_t evaluation_limit,
+                        uint32_t ls_mode, faco_ant_outputs* out) {
+    return guarded([&] {
+        require(xy && ls_rows && tours && mne_targets && out, "null argument");
+        require(n >= 3 && n <= faco::kMaxNodes && tasks >= 1, "invalid sizes");
+        require(faco::block_smem_bytes(n, 1) <= 227u * 1024u, "instance too large for one warp-ant block");
+        require(w >= 1 && w <= 32 && w <= n - 1, "LS width must be in [1, min(32, n-1)]");
+        require(ls_mode == FACO_LS_TWO_OPT, "unsupported local-search mode");
+        require((visits != nullptr) != (uniforms != nullptr), "give exactly one of visits or uniforms");
+        if (uniforms) require(starts && primary && products && k >= 1 && k <= 32 && k <= n - 1, "roulette inputs missing");
+        std::vector<std::int32_t> hxy(xy, xy + 2ull * n);
+        for (auto v : hxy) require(std::abs(v) < (1 << 26), "coordinates must satisfy |x| < 2^26");
+        std::vector<std::uint16_t> ls;
+        std::vector<std::int32_t> ls_dist;
+        faco::host_distance_order(hxy, n, w, ls_rows, ls, ls_dist);
+        std::vector<std::uint16_t> prim16, back16;
+        if (uniforms) {
+            prim16.assign(primary, primary + static_cast<std::size_t>(n) * k);
+            for (auto v : prim16) require(v < n, "primary candidate out of range");
+            if (b) {
+                require(backup != nullptr, "backup rows missing");
+                back16.assign(backup, backup + static_cast<std::size_t>(n) * b);
+            }
+        }
+        std::vector<faco::node_t> t16(static_cast<std::size_t>(tasks) * n), p16(t16.size());
+        std::vector<long long> costs(tasks);
+        for (std::uint32_t t = 0; t < tasks; ++t) {
+            std::vector<std::uint8_t> seen(n, 0);
+            for (std::uint32_t i = 0; i < n; ++i) {
+                const std::uint32_t v = tours[static_cast<std::size_t>(t) * n + i];
+                require(v < n && !seen[v], "task tour is not a permutation");
+                seen[v] = 1;
+                t16[static_cast<std::size_t>(t) * n + i] = static_cast<faco::node_t>(v);
+                p16[static_cast<std::size_t>(t) * n + v] = static_cast<faco::node_t>(i);
+            }
+            costs[t] = faco::host_tour_length(hxy, tours + static_cast<std::size_t>(t) * n, n);
+            if (visits) {
+                std::fill(seen.begin(), seen.end(), 0);
+                for (std::uint32_t i = 0; i < n; ++i) {
+                    const std::uint32_t v = visits[static_cast<std::size_t>(t) * n + i];
+                    require(v < n && !seen[v], "visit order is not a permutation");
+                    seen[v] = 1;
+                }
+            } else {
+                require(starts[t] < n, "start node out of range");
+            }
+        }
+        cudaStream_t s = nullptr;
+        DeviceBuffer<int2> d_xy;
+        DeviceBuffer<faco::node_t> d_ls, d_prim, d_back, d_tours, d_pos, d_visits, d_cons, d_out, d_outpos, d_sel;
+        DeviceBuffer<int> d_lsd;
+        DeviceBuffer<long long> d_costs, d_outcosts;
+        DeviceBuffer<double> d_uni;
+        DeviceBuffer<std::uint32_t> d_starts, d_targets, d_check;
+        DeviceBuffer<float> d_products;
+        DeviceBuffer<unsigned long long> d_counters;
+        DeviceBuffer<unsigned> d_err(1);
+        DeviceBuffer<faco::InstanceView> d_view;
+        d_xy.upload(reinterpret_cast<const int2*>(hxy.data()), n, s);
+        d_ls.upload(ls, s);
+        d_lsd.upload(ls_dist, s);
+        faco::InstanceView v{n, uniforms ? k : 0, uniforms ? b : 0, w, d_xy.get(), nullptr, nullptr, d_ls.get(),
+                             d_lsd.get(), nullptr, nullptr, 0};
+        if (uniforms) {
+            d_prim.upload(prim16, s);
+            d_back.resize(std::max<std::size_t>(1, back16.size()));
+            d_back.upload(back16, s);
+            d_products.upload(products, static_cast<std::size_t>(n) * k, s);
+            v.primary = d_prim.get();
+            v.backup = d_back.get();
+            std::vector<std::uint16_t> v16;
+            d_uni.upload(uniforms, static_cast<std::size_t>(tasks) * n, s);
+            d_starts.upload(starts, tasks, s);
+        } else {
+            std::vector<faco::node_t> vis(visits, visits + static_cast<std::size_t>(tasks) * n);
+            d_visits.upload(vis, s);
+        }
+        d_view.upload(&v, 1, s);
+        d_tours.upload(t16, s);
+        d_pos.upload(p16, s);
+        d_costs.upload(costs, s);
+        d_targets.upload(mne_targets, tasks, s);
+        const std::size_t tn = static_cast<std::size_t>(tasks) * n;
+        d_cons.resize(tn); d_out.resize(tn); d_outpos.resize(tn); d_sel.resize(tn);
+        d_outcosts.resize(2ull * tasks);
+        d_counters.resize(10ull * tasks);
+        const std::uint32_t cap = out->checklists ? out->checklist_capacity : 0;
+        if (cap) d_check.resize(static_cast<std::size_t>(tasks) * cap);
+        cuda_check(cudaMemsetAsync(d_err.get(), 0, sizeof(unsigned), s), "memset");
+        cuda_check(cudaMemsetAsync(d_sel.get(), 0xff, tn * sizeof(faco::node_t), s), "memset");
+        faco::AntLaunch L{};
+        L.instances = d_view.get();
+        L.warps = choose_warps(n, tasks);
+        L.n_max = n;
+        L.ls_limit = evaluation_limit;
+        L.tasks = tasks;
+        L.task_tours = d_tours.get();
+        L.task_pos = d_pos.get();
+        L.task_costs = d_costs.get();
+        L.task_visits = d_visits.get();
+        L.task_uniforms = d_uni.get();
+        L.task_starts = d_starts.get();
+        L.task_targets = d_targets.get();
+        L.task_products = d_products.get();
+        L.out_construction = d_cons.get();
+        L.out_tours = d_out.get();
+        L.out_pos = d_outpos.get();
+        L.out_selected = d_sel.get();
+        L.out_checklist = cap ? d_check.get() : nullptr;
+        L.checklist_cap = cap;
+        L.out_costs = d_outcosts.get();
+        L.out_counters = d_counters.get();
+        L.error = d_err.get();
+        const std::uint32_t blocks = (tasks + L.warps - 1) / L.warps;
+        launch_ants(visits ? faco::kModeVisits : faco::kModeUniforms, L, blocks, L.warps, s);
+        std::vector<faco::node_t> h(tn);
+        auto widen = [&](const DeviceBuffer<faco::node_t>& d, std::uint32_t* dst) {
+            if (!dst) return;
+            d.download(h.data(), tn, s);
+            cuda_check(cudaStreamSynchronize(s), "download");
+            for (std::size_t i = 0; i < tn; ++i) dst[i] = h[i] == 0xffff ? UINT32_MAX : h[i];
+        };
+        widen(d_cons, out->construction_tours);
+        widen(d_out, out->tours);
+        widen(d_outpos, out->positions);
+        widen(d_sel, out->selected);
+        std::vector<long long> oc(2ull * tasks);
+        d_outcosts.download(oc.data(), oc.size(), s);
+        std::vector<unsigned long long> counters(10ull * tasks);
+        d_counters.download(counters.data(), counters.size(), s);
+        if (cap) d_check.download(out->checklists, static_cast<std::size_t>(tasks) * cap, s);
+        unsigned err = 0;
+        d_err.download(&err, 1, s);
+        cuda_check(cudaStreamSynchronize(s), "diagnostic");
+        for (std::uint32_t t = 0; t < tasks; ++t) {
+            if (out->construction_costs) out->construction_costs[t] = oc[2ull * t];
+            if (out->final_costs) out->final_costs[t] = oc[2ull * t + 1];
+        }
+        if (out->counters) std::copy(counters.begin(), counters.end(), out->counters);
+        if (err & ~static_cast<unsigned>(faco::kErrQueueOverflow))
+            throw Error(FACO_EDEVICE, "device error word " + std::to_string(err));
+        if (err) throw Error(FACO_EINVAL, "checklist capacity too small for the recorded pushes");
+    });
+}
+
+int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent, float retention,
+                        float minimum, float maximum, float increment, const float* eta, float* trails,
+                        float* products) {
+    return guarded([&] {
+        require(primary && parent && eta && trails && products && n >= 3 && k >= 1, "invalid arguments");
+        std::vector<std::uint32_t> pos(n, UINT32_MAX);
+        for (std::uint32_t i = 0; i < n; ++i) {
+            require(parent[i] < n && pos[parent[i]] == UINT32_MAX, "parent is not a permutation");
+            pos[parent[i]] = i;
+        }
+        cudaStream_t s = nullptr;
+        const std::size_t cells = static_cast<std::size_t>(n) * k;
+        DeviceBuffer<std::uint32_t> d_prim, d_par, d_pos;
+        DeviceBuffer<float> d_eta, d_tr, d_pr;
+        d_prim.upload(primary, cells, s);
+        d_par.upload(parent, n, s);
+        d_pos.upload(pos, s);
+        d_eta.upload(eta, cells, s);
+        d_tr.upload(trails, cells, s);
+        d_pr.resize(cells);
+        faco::pheromone_step_kernel<<<static_cast<unsigned>((cells + 255) / 256), 256, 0, s>>>(
+            n, k, d_prim.get(), d_par.get(), d_pos.get(), retention, minimum, maximum, increment, d_eta.get(),
+            d_tr.get(), d_pr.get());
+        cuda_check(cudaGetLastError(), "pheromone launch");
+        d_tr.download(trails, cells, s);
+        d_pr.download(products, cells, s);
+        cuda_check(cudaStreamSynchronize(s), "pheromone");
+    });
+}
+
+}  // extern "C"

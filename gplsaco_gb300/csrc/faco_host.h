@@ -1,0 +1,20 @@
+// faco_host.h -- host-side helpers of the engine (no CUDA types).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace faco {
+
+std::int32_t host_euc2d(std::int64_t x0, std::int64_t y0, std::int64_t x1, std::int64_t y1);
+std::int64_t host_tour_length(const std::vector<std::int32_t>& xy, const std::uint32_t* order, std::uint32_t n);
+void host_candidates(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t k, std::uint32_t b,
+                     std::uint32_t w, std::vector<std::uint16_t>& primary, std::vector<std::uint16_t>& backup,
+                     std::vector<std::uint16_t>& ls, std::vector<std::int32_t>& ls_dist, std::vector<float>& eta,
+                     double beta);
+std::vector<std::uint32_t> host_nearest_neighbour_tour(const std::vector<std::int32_t>& xy, std::uint32_t n);
+void host_distance_order(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t w,
+                         const std::uint32_t* rows, std::vector<std::uint16_t>& ls,
+                         std::vector<std::int32_t>& ls_dist);
+
+}  // namespace faco

@@ -1,0 +1,498 @@
+// faco_kernels.cu -- the FACO iteration kernels for sm_103a.
+//
+//   ant_kernel<mode>        construction + local search, one warp per ant
+//   colony_init_kernel      reset_colony + initialize_products
+//                           (cuda/colony_state.cuh:72-110)
+//   colony_update_kernel    reduce_and_select + update_pheromone fused, one
+//                           block per colony (cuda/colony_state.cuh:148-229)
+//   pheromone_step_kernel   the trail update alone (parity hook)
+//   score_kernel            GP controller scoring, warp per colony
+//                           (cuda/gp_score.cuh:64-102)
+#include <climits>
+
+#include "faco_ant.cuh"
+#include "faco_kernels.h"
+
+namespace faco {
+
+// ---------------------------------------------------------------------------
+// Ant kernel
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    std::uint32_t colony = 0, ant = 0, task = 0;
+    bool active;
+    if (MODE == kModeEngine) {
+        const uint2 job = L.work[blockIdx.x];
+        colony = job.x;
+        ant = job.y + warp;
+        active = ant < L.ants;
+    } else {
+        task = blockIdx.x * L.warps + warp;
+        ant = task;
+        active = task < L.tasks;
+    }
+    const InstanceView in = L.instances[MODE == kModeEngine ? L.colonies[colony].instance : 0];
+    const std::uint32_t n = in.n;
+    int2* xy = reinterpret_cast<int2*>(smem);
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) xy[i] = in.xy[i];
+    __syncthreads();
+    if (!active) return;
+
+    unsigned char* base = smem + ((8u * L.n_max + 15u) & ~15u) + warp * ant_smem_bytes(L.n_max);
+    const AntSmem s{reinterpret_cast<node_t*>(base), reinterpret_cast<node_t*>(base + 2 * L.n_max),
+                    reinterpret_cast<node_t*>(base + 4 * L.n_max), base + 6 * L.n_max, base + 7 * L.n_max};
+
+    const node_t* parent;
+    const node_t* parent_pos;
+    long long cost;
+    std::uint32_t target, batch = 0;
+    unsigned long long key = 0;
+    ColonyView cv{};
+    if (MODE == kModeEngine) {
+        cv = L.colonies[colony];
+        const ColonyState& st = L.states[colony];
+        parent = cv.parent;
+        parent_pos = cv.parent_pos;
+        cost = st.parent_cost;
+        target = st.mne_target;
+        batch = st.iteration;
+        key = cv.key;
+    } else {
+        parent = L.task_tours + (size_t)task * n;
+        parent_pos = L.task_pos + (size_t)task * n;
+        cost = L.task_costs[task];
+        target = MODE == kModePrepare ? 0 : L.task_targets[task];
+    }
+    for (std::uint32_t i = lane; i < n; i += 32) {
+        const std::uint32_t v = parent[i];
+        s.tour[i] = (node_t)v;
+        s.pos[v] = (node_t)i;
+        s.visited[i] = 0;
+        s.queued[i] = 0;
+    }
+    __syncwarp();
+
+    std::uint32_t* log = L.out_checklist ? L.out_checklist + (size_t)task * L.checklist_cap : nullptr;
+    const std::uint32_t log_cap = L.checklist_cap;
+    Checklist q{0, 0, 0, 0};
+    AntResult r{};
+
+    if (MODE == kModePrepare) {
+        // registration: every node pending, in tour order (prepared_problem.cpp:160-162)
+        for (std::uint32_t i = lane; i < n; i += 32) {
+            s.ring[i] = s.tour[i];
+            s.queued[i] = 1;
+            if (log && i < log_cap) log[i] = s.tour[i];
+        }
+        q.tail = 0;
+        q.pending = n;
+        q.pushed = n;
+        __syncwarp();
+    } else {
+        // ---------------- focused construction ----------------
+        std::uint32_t current;
+        if (MODE == kModeEngine) current = start_node(key, batch, ant, n);
+        else if (MODE == kModeVisits) current = L.task_visits[(size_t)task * n];
+        else current = L.task_starts[task];
+        if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n] = (node_t)current;
+        if (lane == 0) s.visited[current] = 1;
+        __syncwarp();
+        const float* products = MODE == kModeEngine ? cv.products : L.task_products;
+        const std::uint32_t k = in.k, b = in.b;
+        const unsigned long long loop_cap = 2ull * n + 2;
+        unsigned long long guard = 0;
+        while (r.mne < target && r.steps + 1 < n) {
+            if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
+            const std::uint32_t step = r.steps + 1;
+            std::uint32_t selected = n;
+            if (MODE == kModeVisits) {
+                selected = L.task_visits[(size_t)task * n + step];
+            } else {
+                const double u = MODE == kModeEngine ? step_uniform(key, batch, ant, step)
+                                                     : L.task_uniforms[(size_t)task * n + step];
+                std::uint32_t cand = n;
+                float p = 0.0f;
+                bool avail = false;
+                if (lane < k) {
+                    cand = in.primary[(size_t)current * k + lane];
+                    p = products[(size_t)current * k + lane];
+                    avail = cand < n && s.visited[cand] == 0;
+                }
+                const unsigned mask = __ballot_sync(kFull, avail);
+                if (mask) {
+                    // ordered FP64 sums, exactly the reference's left-to-right prefix
+                    double total = 0.0, mine = 0.0;
+                    for (unsigned m = mask; m; m &= m - 1) {
+                        const int j = __ffs(m) - 1;
+                        total += (double)__shfl_sync(kFull, p, j);
+                        if ((int)lane == j) mine = total;
+                    }
+                    int j;
+                    if (total > 0.0) {
+                        const double threshold = u * total;
+                        const unsigned hit = __ballot_sync(kFull, avail && threshold < mine);
+                        j = hit ? __ffs(hit) - 1 : 31 - __clz(mask);
+                    } else {
+                        const std::uint32_t count = __popc(mask);
+                        std::uint32_t t = (std::uint32_t)(u * count);
+                        if (t >= count) t = count - 1;
+                        unsigned m = mask;
+                        for (; t; --t) m &= m - 1;
+                        j = __ffs(m) - 1;
+                    }
+                    selected = __shfl_sync(kFull, cand, j);
+                } else {
+                    for (std::uint32_t base_j = 0; base_j < b && selected == n; base_j += 32) {
+                        const std::uint32_t jj = base_j + lane;
+                        std::uint32_t v = n;
+                        bool ok = false;
+                        if (jj < b) {
+                            v = in.backup[(size_t)current * b + jj];
+                            ok = v < n && s.visited[v] == 0;
+                        }
+                        const unsigned m = __ballot_sync(kFull, ok);
+                        if (m) selected = __shfl_sync(kFull, v, __ffs(m) - 1);
+                    }
+                    if (selected == n) {
+                        // global nearest unvisited, lowest id on ties
+                        unsigned long long bestkey = ~0ull;
+                        const int2 cxy = xy[current];
+                        for (std::uint32_t v = lane; v < n; v += 32) {
+                            if (s.visited[v]) continue;
+                            const unsigned long long kv =
+                                ((unsigned long long)(unsigned)euc2d(cxy, xy[v]) << 32) | v;
+                            bestkey = kv < bestkey ? kv : bestkey;
+                        }
+                        for (int o = 16; o; o >>= 1) {
+                            const unsigned long long other = __shfl_xor_sync(kFull, bestkey, o);
+                            bestkey = other < bestkey ? other : bestkey;
+                        }
+                        if (bestkey != ~0ull) selected = (std::uint32_t)(bestkey & 0xffffffffu);
+                    }
+                }
+            }
+            if (selected >= n || s.visited[selected]) {
+                // no legal choice (only an invalid explicit visit order can get here)
+                if (lane == 0) atomicOr(L.error, kErrBadChoice);
+                break;
+            }
+            if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n + step] = (node_t)selected;
+            const std::uint32_t npos = s.pos[selected], tpos = s.pos[current];
+            const std::uint32_t previous = s.tour[npos == 0 ? n - 1 : npos - 1];
+            const std::uint32_t after = s.tour[npos + 1 == n ? 0 : npos + 1];
+            const std::uint32_t target_after = s.tour[tpos + 1 == n ? 0 : tpos + 1];
+            const std::uint32_t pp = parent_pos[current];
+            const std::uint32_t ps = parent[pp + 1 == n ? 0 : pp + 1], pq = parent[pp == 0 ? n - 1 : pp - 1];
+            ++r.steps;
+            __syncwarp();
+            if (lane == 0) s.visited[selected] = 1;
+            if (target_after != selected) {
+                ++r.nonidentity;
+                // six-edge delta of CpuTour::relocate, one term per lane
+                int term = 0;
+                if (lane < 6) {
+                    // removed: (previous,selected) (selected,after) (current,target_after)
+                    // added:   (previous,after) (current,selected) (selected,target_after)
+                    const std::uint32_t e0 = lane == 0 || lane == 3 ? previous : lane == 2 || lane == 4 ? current
+                                                                                                        : selected;
+                    const std::uint32_t e1 = lane == 0 || lane == 4 ? selected : lane == 1 || lane == 3 ? after
+                                                                                                        : target_after;
+                    const int d = dist(xy, e0, e1);
+                    term = lane < 3 ? -d : d;
+                }
+                cost += __reduce_add_sync(kFull, term);
+                relocate_shift(s, lane, tpos, npos, selected);
+                r.moved += tpos < npos ? npos - tpos : tpos - npos + 1;
+            }
+            if (ps != selected && pq != selected) {
+                ++r.mne;
+                push_absent(s, q, n, current, lane, log, log_cap);
+                push_absent(s, q, n, selected, lane, log, log_cap);
+                push_absent(s, q, n, previous, lane, log, log_cap);
+            }
+            current = selected;
+            __syncwarp();
+        }
+        r.construction_cost = cost;
+        if (L.out_construction)
+            for (std::uint32_t i = lane; i < n; i += 32) L.out_construction[(size_t)task * n + i] = s.tour[i];
+        __syncwarp();
+    }
+    // ---------------- local search ----------------
+    long long gain_sum = 0;
+    checklist_two_opt(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
+    r.final_cost = cost + gain_sum;
+    r.checklist = q.pushed;
+    if (log && q.pushed > log_cap && lane == 0) atomicOr(L.error, kErrQueueOverflow);
+    __syncwarp();
+
+    if (MODE == kModeEngine) {
+        node_t* out = cv.ant_tours + (size_t)ant * n;
+        for (std::uint32_t i = lane; i < n; i += 32) out[i] = s.tour[i];
+        if (lane == 0) {
+            cv.ant_costs[ant] = r.final_cost;
+            cv.ant_counts[3 * ant] = r.steps;
+            cv.ant_counts[3 * ant + 1] = (unsigned)r.evaluations;
+            cv.ant_counts[3 * ant + 2] = (unsigned)r.moved;
+        }
+    } else {
+        if (L.out_tours)
+            for (std::uint32_t i = lane; i < n; i += 32) L.out_tours[(size_t)task * n + i] = s.tour[i];
+        if (L.out_pos)
+            for (std::uint32_t i = lane; i < n; i += 32) L.out_pos[(size_t)task * n + i] = s.pos[i];
+        if (lane == 0) {
+            if (L.out_costs) {
+                L.out_costs[2 * (size_t)task] = r.construction_cost;
+                L.out_costs[2 * (size_t)task + 1] = r.final_cost;
+            }
+            if (L.out_counters) {
+                unsigned long long* c = L.out_counters + 10 * (size_t)task;
+                c[0] = r.mne; c[1] = r.steps; c[2] = r.nonidentity; c[3] = r.processed; c[4] = r.checks;
+                c[5] = r.evaluations; c[6] = r.accepted; c[7] = r.reactivations; c[8] = r.limit_reached;
+                c[9] = r.checklist;
+            }
+        }
+    }
+}
+
+namespace {
+template <int MODE>
+cudaError_t prepare_mode(std::uint32_t smem) {
+    return cudaFuncSetAttribute(ant_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+}  // namespace
+
+cudaError_t prepare_ant_kernel(int mode, std::uint32_t smem) {
+    switch (mode) {
+        case kModeEngine: return prepare_mode<kModeEngine>(smem);
+        case kModeVisits: return prepare_mode<kModeVisits>(smem);
+        case kModeUniforms: return prepare_mode<kModeUniforms>(smem);
+        case kModePrepare: return prepare_mode<kModePrepare>(smem);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks, std::uint32_t warps,
+                              std::uint32_t smem, cudaStream_t stream) {
+    const dim3 grid(blocks), block(warps * 32);
+    switch (mode) {
+        case kModeEngine: ant_kernel<kModeEngine><<<grid, block, smem, stream>>>(L); break;
+        case kModeVisits: ant_kernel<kModeVisits><<<grid, block, smem, stream>>>(L); break;
+        case kModeUniforms: ant_kernel<kModeUniforms><<<grid, block, smem, stream>>>(L); break;
+        case kModePrepare: ant_kernel<kModePrepare><<<grid, block, smem, stream>>>(L); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Colony kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void trail_limits(long long cost, double retention, double p_root, std::uint32_t k,
+                                             float& tmin, float& tmax) {
+    const double mx = 1.0 / ((double)cost * (1.0 - retention));
+    double mn = mx * (1.0 - p_root) / (((double)k - 1.0) * p_root);
+    mn = mn < mx ? mn : mx;
+    tmax = (float)mx;
+    tmin = (float)mn;
+}
+
+__global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
+                                   ColonyParams P) {
+    const std::uint32_t c = blockIdx.x;
+    const ColonyView cv = colonies[c];
+    const InstanceView in = instances[cv.instance];
+    const std::uint32_t n = in.n, k = in.k;
+    __shared__ float s_tmax;
+    if (threadIdx.x == 0) {
+        ColonyState st{};
+        st.epoch_cost = st.global_cost = st.parent_cost = st.iteration_best_cost = in.initial_cost;
+        trail_limits(in.initial_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
+        st.default_trail = st.tau_max;
+        st.mne_target = P.mne_target;
+        st.action = -1;
+        states[c] = st;
+        s_tmax = st.tau_max;
+    }
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const node_t v = in.initial[i];
+        cv.parent[i] = cv.epoch[i] = cv.global[i] = v;
+        cv.parent_pos[v] = (node_t)i;
+    }
+    __syncthreads();
+    const float tmax = s_tmax;
+    for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
+        cv.trails[i] = tmax;
+        cv.products[i] = tmax * in.eta[i];
+    }
+}
+
+// Fused reduce_and_select + update_pheromone for one colony.
+__global__ void __launch_bounds__(512) colony_update_kernel(const InstanceView* instances,
+                                                            const ColonyView* colonies, ColonyState* states,
+                                                            ColonyParams P, TraceRow* trace,
+                                                            std::uint32_t colony_count, std::uint32_t trace_cap) {
+    const std::uint32_t c = blockIdx.x;
+    const ColonyView cv = colonies[c];
+    const InstanceView in = instances[cv.instance];
+    const std::uint32_t n = in.n, k = in.k, A = P.ants;
+    __shared__ unsigned long long s_key[32];
+    __shared__ unsigned long long s_steps[32], s_evals[32], s_moved[32];
+    __shared__ std::uint32_t s_best, s_improve_epoch, s_improve_global, s_from_epoch;
+    __shared__ float s_tmin, s_tmax, s_inc;
+
+    // iteration best: first strict minimum over ants (costs are >= 0)
+    unsigned long long best = ~0ull, steps = 0, evals = 0, moved = 0;
+    for (std::uint32_t a = threadIdx.x; a < A; a += blockDim.x) {
+        const unsigned long long key = ((unsigned long long)cv.ant_costs[a] << 16) | a;
+        best = key < best ? key : best;
+        steps += cv.ant_counts[3 * a];
+        evals += cv.ant_counts[3 * a + 1];
+        moved += cv.ant_counts[3 * a + 2];
+    }
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(kFull, best, o);
+        best = other < best ? other : best;
+        steps += __shfl_xor_sync(kFull, steps, o);
+        evals += __shfl_xor_sync(kFull, evals, o);
+        moved += __shfl_xor_sync(kFull, moved, o);
+    }
+    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    if (lane == 0) { s_key[warp] = best; s_steps[warp] = steps; s_evals[warp] = evals; s_moved[warp] = moved; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (std::uint32_t w = 1; w < warps; ++w) {
+            best = s_key[w] < best ? s_key[w] : best;
+            steps += s_steps[w];
+            evals += s_evals[w];
+            moved += s_moved[w];
+        }
+        ColonyState st = states[c];
+        const std::uint32_t ib = (std::uint32_t)(best & 0xffffu);
+        const long long cost = (long long)(best >> 16);
+        const bool ie = cost < st.epoch_cost, ig = cost < st.global_cost;
+        if (ie) st.epoch_cost = cost;
+        if (ig) st.global_cost = cost;
+        trail_limits(st.epoch_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
+        const bool from_epoch = source_uniform(cv.key, st.iteration) < P.epoch_source_probability;
+        st.parent_cost = from_epoch ? st.epoch_cost : cost;
+        st.iteration_best = ib;
+        st.iteration_best_cost = cost;
+        st.source_is_epoch = from_epoch;
+        st.construction_steps += steps;
+        st.ls_evaluations += evals;
+        st.reversed_elements += moved;
+        st.default_trail = fmaxf(st.tau_min, st.default_trail * P.retention_f);
+        if (trace && st.iteration < trace_cap) {
+            TraceRow& row = trace[(size_t)st.iteration * colony_count + c];
+            row.iteration_best_cost = cost;
+            row.global_cost = st.global_cost;
+            row.parent_cost = st.parent_cost;
+            row.iteration_best = ib;
+            row.source_is_epoch = from_epoch;
+            row.tau_min = st.tau_min;
+            row.tau_max = st.tau_max;
+            row.mne_target = st.mne_target;
+            row.action = st.action;
+            row.construction_steps = steps;
+            row.ls_evaluations = evals;
+        }
+        ++st.iteration;
+        states[c] = st;
+        s_best = ib; s_improve_epoch = ie; s_improve_global = ig; s_from_epoch = from_epoch;
+        s_tmin = st.tau_min; s_tmax = st.tau_max;
+        s_inc = (float)(1.0 / (double)st.parent_cost);
+    }
+    __syncthreads();
+    const node_t* best_tour = cv.ant_tours + (size_t)s_best * n;
+    const bool ie = s_improve_epoch, ig = s_improve_global, fe = s_from_epoch;
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const node_t v = best_tour[i];
+        if (ie) cv.epoch[i] = v;
+        if (ig) cv.global[i] = v;
+        const node_t src = fe ? cv.epoch[i] : v;
+        cv.parent[i] = src;
+        cv.parent_pos[src] = (node_t)i;
+    }
+    __syncthreads();
+    const float tmin = s_tmin, tmax = s_tmax, inc = s_inc, ret = P.retention_f;
+    for (std::uint32_t idx = threadIdx.x; idx < n * k; idx += blockDim.x) {
+        const std::uint32_t from = idx / k;
+        const std::uint32_t pp = cv.parent_pos[from];
+        const std::uint32_t to = in.primary[idx];
+        const std::uint32_t sn = cv.parent[pp + 1 == n ? 0 : pp + 1], pn = cv.parent[pp == 0 ? n - 1 : pp - 1];
+        float v = fmaxf(tmin, cv.trails[idx] * ret);
+        if (to == sn || to == pn) v = fminf(tmax, v + inc);
+        cv.trails[idx] = v;
+        cv.products[idx] = v * in.eta[idx];
+    }
+}
+
+__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const std::uint32_t* primary,
+                                      const std::uint32_t* parent, const std::uint32_t* parent_pos, float ret,
+                                      float tmin, float tmax, float inc, const float* eta, float* trails,
+                                      float* products) {
+    const std::uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * k) return;
+    const std::uint32_t from = idx / k, pp = parent_pos[from], to = primary[idx];
+    const std::uint32_t sn = parent[pp + 1 == n ? 0 : pp + 1], pn = parent[pp == 0 ? n - 1 : pp - 1];
+    float v = fmaxf(tmin, trails[idx] * ret);
+    if (to == sn || to == pn) v = fminf(tmax, v + inc);
+    trails[idx] = v;
+    products[idx] = v * eta[idx];
+}
+
+// ---------------------------------------------------------------------------
+// GP scoring: one warp per colony, lane = action (cuda/gp_score.cuh:64-102).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float apply_operation(int op, float l, float r, float t) {
+    float v = 0.0f;
+    switch (op) {
+        case 2: v = l + r; break;
+        case 3: v = l - r; break;
+        case 4: v = l * r; break;
+        case 5: v = fminf(l, r); break;
+        case 6: v = fmaxf(l, r); break;
+        case 7: v = fabsf(l); break;
+        case 8: { const float q = 1.0f + r * r; v = l * (1.0f / sqrtf(q)); break; }
+        case 9: v = fabsf(r) < 1e-6f ? 1.0f : l / r; break;
+        case 10: v = l > 0.0f ? r : t; break;
+        default: break;
+    }
+    return fminf(8.0f, fmaxf(-8.0f, v));
+}
+
+__global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
+                             const std::uint32_t* masks, float* scores, std::int32_t* actions,
+                             std::uint32_t colonies) {
+    const std::uint32_t colony = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (colony >= colonies) return;
+    const Program& p = programs[colony / replicas];
+    float stack[16];
+    int top = 0;
+    for (int i = 0; i < p.length; ++i) {
+        const int op = p.opcode[i];
+        if (op == 0) stack[top++] = features[((size_t)p.operand[i] * colonies + colony) * 32 + lane];
+        else if (op == 1) stack[top++] = p.constants[p.operand[i]];
+        else {
+            const int arity = op == 7 ? 1 : op == 10 ? 3 : 2;
+            const float t = arity == 3 ? stack[--top] : 0.0f;
+            const float r = arity >= 2 ? stack[--top] : 0.0f;
+            const float l = stack[--top];
+            stack[top++] = apply_operation(op, l, r, t);
+        }
+    }
+    const float value = stack[0];
+    scores[(size_t)colony * 32 + lane] = value;
+    const bool legal = (masks[colony] >> lane) & 1u;
+    float maximum = legal ? value : -INFINITY;
+    for (int o = 16; o; o >>= 1) maximum = fmaxf(maximum, __shfl_xor_sync(kFull, maximum, o));
+    const std::uint32_t mine = legal && maximum - value <= 1e-6f ? lane : 32u;
+    const std::uint32_t chosen = __reduce_min_sync(kFull, mine);
+    if (lane == 0) actions[colony] = (std::int32_t)chosen;
+}
+
+}  // namespace faco

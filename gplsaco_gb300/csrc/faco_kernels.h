@@ -1,0 +1,48 @@
+// faco_kernels.h -- kernel declarations shared by faco_kernels.cu and the
+// host engine.
+#pragma once
+
+#include <cstdint>
+
+#include "faco_ant.cuh"
+
+namespace faco {
+
+constexpr std::uint32_t kMaxWarpsPerBlock = 8;
+
+// Device mirror of faco_program (include/faco_gb300.h).
+struct Program {
+    std::uint16_t ir_version, numeric_spec_id, feature_spec_id, length, constants_count;
+    std::uint8_t opcode[63];
+    std::uint8_t operand[63];
+    float constants[63];
+};
+
+struct ColonyParams {
+    std::uint32_t ants;
+    std::uint32_t mne_target;
+    double retention;
+    float retention_f;
+    double p_root;                   // p_best^(1/k), computed once on the host
+    double epoch_source_probability;
+};
+
+// Host-side launchers (the kernels are defined in faco_kernels.cu).
+cudaError_t prepare_ant_kernel(int mode, std::uint32_t smem_bytes);
+cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks, std::uint32_t warps,
+                              std::uint32_t smem_bytes, cudaStream_t stream);
+
+__global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
+                                   ColonyParams P);
+__global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,
+                                     ColonyState* states, ColonyParams P, TraceRow* trace,
+                                     std::uint32_t colony_count, std::uint32_t trace_cap);
+__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const std::uint32_t* primary,
+                                      const std::uint32_t* parent, const std::uint32_t* parent_pos, float ret,
+                                      float tmin, float tmax, float inc, const float* eta, float* trails,
+                                      float* products);
+__global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
+                             const std::uint32_t* masks, float* scores, std::int32_t* actions,
+                             std::uint32_t colonies);
+
+}  // namespace faco

@@ -1,0 +1,120 @@
+// faco_prepare.cpp -- host part of instance registration.
+//
+// Follows prepare_problem (cpp/src/prepared_problem.cpp:107-175) with TSPLIB
+// EUC_2D integer lengths: per node the nearest candidates by (distance,
+// node id) -- primary row, backup row, LS row -- and a nearest-neighbour tour
+// from node 0.  The initial checklist 2-opt over that tour runs on the GPU
+// with the engine's own local-search kernel (faco_engine.cu).
+#include "faco_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+namespace faco {
+
+std::int32_t host_euc2d(std::int64_t x0, std::int64_t y0, std::int64_t x1, std::int64_t y1) {
+    const std::int64_t dx = x0 - x1, dy = y0 - y1;
+    return static_cast<std::int32_t>(std::floor(std::sqrt(static_cast<double>(dx * dx + dy * dy)) + 0.5));
+}
+
+std::int64_t host_tour_length(const std::vector<std::int32_t>& xy, const std::uint32_t* order, std::uint32_t n) {
+    std::int64_t sum = 0;
+    std::uint32_t prev = order[n - 1];
+    for (std::uint32_t i = 0; i < n; ++i) {
+        const std::uint32_t v = order[i];
+        sum += host_euc2d(xy[2 * prev], xy[2 * prev + 1], xy[2 * v], xy[2 * v + 1]);
+        prev = v;
+    }
+    return sum;
+}
+
+void host_candidates(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t k, std::uint32_t b,
+                     std::uint32_t w, std::vector<std::uint16_t>& primary, std::vector<std::uint16_t>& backup,
+                     std::vector<std::uint16_t>& ls, std::vector<std::int32_t>& ls_dist, std::vector<float>& eta,
+                     double beta) {
+    primary.assign(static_cast<std::size_t>(n) * k, 0);
+    backup.assign(static_cast<std::size_t>(n) * b, 0);
+    ls.assign(static_cast<std::size_t>(n) * w, 0);
+    ls_dist.assign(static_cast<std::size_t>(n) * w, 0);
+    eta.assign(static_cast<std::size_t>(n) * k, 0.0f);
+    const std::uint32_t needed = std::max(k + b, w);
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const unsigned threads = n >= 2000 ? hw : 1;
+    auto work = [&](unsigned t) {
+        std::vector<std::pair<std::int32_t, std::uint32_t>> row;
+        row.reserve(n);
+        for (std::uint32_t a = t; a < n; a += threads) {
+            row.clear();
+            for (std::uint32_t v = 0; v < n; ++v)
+                if (v != a) row.emplace_back(host_euc2d(xy[2 * a], xy[2 * a + 1], xy[2 * v], xy[2 * v + 1]), v);
+            std::partial_sort(row.begin(), row.begin() + needed, row.end());
+            for (std::uint32_t j = 0; j < k; ++j) {
+                primary[static_cast<std::size_t>(a) * k + j] = static_cast<std::uint16_t>(row[j].second);
+                const double d = row[j].first;
+                eta[static_cast<std::size_t>(a) * k + j] =
+                    static_cast<float>(d > 0 ? (beta == 1.0 ? 1.0 / d : 1.0 / std::pow(d, beta)) : 1.0);
+            }
+            for (std::uint32_t j = 0; j < b; ++j)
+                backup[static_cast<std::size_t>(a) * b + j] = static_cast<std::uint16_t>(row[k + j].second);
+            for (std::uint32_t j = 0; j < w; ++j) {
+                ls[static_cast<std::size_t>(a) * w + j] = static_cast<std::uint16_t>(row[j].second);
+                ls_dist[static_cast<std::size_t>(a) * w + j] = row[j].first;
+            }
+        }
+    };
+    if (threads == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < threads; ++t) pool.emplace_back(work, t);
+        for (auto& th : pool) th.join();
+    }
+}
+
+std::vector<std::uint32_t> host_nearest_neighbour_tour(const std::vector<std::int32_t>& xy, std::uint32_t n) {
+    std::vector<std::uint32_t> tour;
+    tour.reserve(n);
+    std::vector<std::uint8_t> seen(n, 0);
+    std::uint32_t current = 0;
+    for (std::uint32_t i = 0; i < n; ++i) {
+        tour.push_back(current);
+        seen[current] = 1;
+        std::uint32_t next = n;
+        std::int32_t shortest = INT32_MAX;
+        for (std::uint32_t v = 0; v < n; ++v) {
+            if (seen[v]) continue;
+            const std::int32_t d = host_euc2d(xy[2 * current], xy[2 * current + 1], xy[2 * v], xy[2 * v + 1]);
+            if (d < shortest) { shortest = d; next = v; }
+        }
+        current = next;
+    }
+    return tour;
+}
+
+// DistanceOrderedCandidates (cpp/src/faco_cpu.cpp:32-45): stable sort of a
+// given row by distance, keeping the input order of ties.
+void host_distance_order(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t w,
+                         const std::uint32_t* rows, std::vector<std::uint16_t>& ls,
+                         std::vector<std::int32_t>& ls_dist) {
+    ls.assign(static_cast<std::size_t>(n) * w, 0);
+    ls_dist.assign(static_cast<std::size_t>(n) * w, 0);
+    std::vector<std::pair<std::int32_t, std::uint32_t>> row(w);
+    for (std::uint32_t a = 0; a < n; ++a) {
+        for (std::uint32_t j = 0; j < w; ++j) {
+            const std::uint32_t v = rows[static_cast<std::size_t>(a) * w + j];
+            if (v >= n || v == a) throw std::invalid_argument("LS candidate out of range or self loop");
+            row[j] = {host_euc2d(xy[2 * a], xy[2 * a + 1], xy[2 * v], xy[2 * v + 1]), v};
+        }
+        std::stable_sort(row.begin(), row.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+        for (std::uint32_t j = 0; j < w; ++j) {
+            ls[static_cast<std::size_t>(a) * w + j] = static_cast<std::uint16_t>(row[j].second);
+            ls_dist[static_cast<std::size_t>(a) * w + j] = row[j].first;
+        }
+    }
+}
+
+}  // namespace faco

@@ -1,0 +1,345 @@
+"""Reference-facing host API, mirroring the pybind11 module gp_faco_ext of
+LinHuanli/GPLSACO (cpp/src/bindings.cpp:500-1046): FixedFacoSettings,
+FacoBatchEngine (register_problem, evaluate_faco_evaluations), score_cuda, with
+the same argument meaning, result dictionary keys and error behaviour
+(ValueError for invalid input, RuntimeError for CUDA failures).  Everything
+runs through the C ABI of the CUDA library; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import struct
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+
+
+def _exact_int(value, name: str, lo: int = 0, hi: int = 2**64 - 1) -> int:
+    # JSON bools are ints in Python; the reference rejects them (bindings.cpp:131-145)
+    if type(value) is not int:
+        raise ValueError(f"{name} must be an int (not bool/float)")
+    if not lo <= value <= hi:
+        raise ValueError(f"{name} out of range")
+    return value
+
+
+@dataclass
+class FixedFacoSettings:
+    """FixedFacoSettings (cpp/include/gp_faco/fixed_faco_gpu.hpp:10-21)."""
+    ants: int = 0
+    primary_width: int = 16
+    backup_width: int = 64
+    ls_width: int = 20
+    beta: float = 1.0
+    retention: float = 0.5
+    p_best: float = 0.1
+    epoch_source_probability: float = 0.01
+    ls_evaluation_limit: int = 100000
+    initial_ls_evaluation_limit: int = 100000
+    ls_mode: int = _lib.FACO_LS_TWO_OPT
+
+    def to_c(self) -> _lib.Settings:
+        s = _lib.Settings()
+        for name in ("ants", "primary_width", "backup_width", "ls_width", "ls_evaluation_limit",
+                     "initial_ls_evaluation_limit", "ls_mode"):
+            setattr(s, name, _exact_int(getattr(self, name), name))
+        for name in ("beta", "retention", "p_best", "epoch_source_probability"):
+            value = getattr(self, name)
+            if type(value) not in (int, float) or not math.isfinite(value):
+                raise ValueError(f"{name} must be a finite number")
+            setattr(s, name, float(value))
+        return s
+
+
+def faco_ants(dimension: int) -> int:
+    """64 * ceil(sqrt(n)/16) ants (python/gp_faco/worker.py:30-34)."""
+    if type(dimension) is not int or dimension < 3:
+        raise ValueError("TSP size must be an int >= 3")
+    return 64 * (math.isqrt(dimension - 1) // 16 + 1)
+
+
+def _u64_array(a, name: str) -> np.ndarray:
+    if not isinstance(a, np.ndarray) or a.dtype != np.uint64 or a.ndim != 1 or not a.flags.c_contiguous:
+        raise ValueError(f"{name} must be a contiguous 1-D uint64 array")
+    return a
+
+
+class FacoBatchEngine:
+    """FacoBatchEngine(dimension, colonies, settings) (bindings.cpp:558-573).
+
+    `dimension` is the largest instance size accepted; instances of different
+    sizes may share an evaluation.  One evaluation at a time per engine.
+    """
+
+    def __init__(self, dimension, colonies, settings: FixedFacoSettings, constraint_mode="unrestricted",
+                 population_size=1, device: int = 0):
+        _exact_int(dimension, "dimension")
+        _exact_int(colonies, "colonies")
+        _exact_int(population_size, "population_size")
+        if constraint_mode != "unrestricted":
+            raise ValueError("only the unrestricted candidate graph is supported")
+        if population_size != 1:
+            raise ValueError("population engines are created with population_size=1 and a replicated panel")
+        self._L = _lib.load()
+        self._handle = C.c_void_p()
+        _lib.check(self._L.faco_engine_create(dimension, colonies, C.byref(settings.to_c()), device,
+                                              C.byref(self._handle)))
+        self.dimension, self.colonies = dimension, colonies
+        self.settings = settings
+        self.ants = settings.ants or faco_ants(dimension)
+        self._sizes: dict[int, int] = {}
+        self._lock = threading.Lock()
+
+    def close(self) -> None:
+        if self._handle:
+            self._L.faco_engine_destroy(self._handle)
+            self._handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def register_problem(self, instance_key, coordinates) -> dict:
+        """register_problem(instance_key, coordinates f64[n,2]) (bindings.cpp:623-638)."""
+        key = _exact_int(instance_key, "instance_key")
+        if (not isinstance(coordinates, np.ndarray) or coordinates.dtype != np.float64 or coordinates.ndim != 2
+                or coordinates.shape[1] != 2 or not coordinates.flags.c_contiguous):
+            raise ValueError("coordinates must be a C-contiguous float64 [n, 2] array")
+        info = _lib.Registration()
+        _lib.check(self._L.faco_register_problem(self._handle, key, coordinates.ctypes.data, coordinates.shape[0],
+                                                 C.byref(info)))
+        self._sizes[key] = coordinates.shape[0]
+        return {"cheap_seconds": info.cheap_seconds, "preparation_seconds": info.preparation_seconds,
+                "initial_cost": int(info.initial_cost)}
+
+    def problem_rows(self, instance_key) -> dict:
+        n = self._sizes[instance_key]
+        s = self.settings
+        k = min(s.primary_width, n - 1)
+        b = min(s.backup_width, n - 1 - k)
+        w = min(s.ls_width, n - 1)
+        out = dict(initial_tour=np.zeros(n, np.uint32), primary=np.zeros((n, k), np.uint32),
+                   backup=np.zeros((n, max(b, 1)), np.uint32), ls=np.zeros((n, w), np.uint32))
+        _lib.check(self._L.faco_problem_rows(self._handle, instance_key, *(out[x].ctypes.data for x in
+                                                                          ("initial_tour", "primary", "backup",
+                                                                           "ls"))))
+        out["backup"] = out["backup"][:, :b]
+        return out
+
+    def evaluate_faco_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, mne=8,
+                                  preparation_mode="cached", *, checkpoint_iterations=(), profile_events_only=False,
+                                  trace=False) -> dict:
+        """evaluate_faco_evaluations (bindings.cpp:701-720): plain FACO with a
+        constant MNE target, budget in ant-tour evaluations per colony."""
+        keys = _u64_array(instance_keys, "instance_keys")
+        seeds = _u64_array(seeds, "seeds")
+        if keys.size != seeds.size:
+            raise ValueError("instance_keys and seeds differ in length")
+        limit = _exact_int(evaluation_limit_per_colony, "evaluation_limit_per_colony")
+        mne = _exact_int(mne, "mne", 1, 2**32 - 1)
+        if preparation_mode not in ("cached", "cached_charged"):
+            raise ValueError("unknown preparation mode")
+        if type(profile_events_only) is not bool or type(trace) is not bool:
+            raise ValueError("flags must be bool")
+        cps = np.asarray([_exact_int(c, "checkpoint") for c in checkpoint_iterations], dtype=np.uint64)
+        count = keys.size
+        D = self.dimension
+        iterations = limit // self.ants if self.ants else 0
+        tours = np.zeros((count, D), np.uint32)
+        costs = np.zeros(count, np.int64)
+        trace_rows = np.zeros((iterations, count), _lib.TRACE_DTYPE) if trace else None
+        cp_tours = np.zeros((cps.size, count, D), np.uint32) if cps.size else None
+        out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), _lib.ptr(cp_tours))
+        if not self._lock.acquire(blocking=False):
+            raise RuntimeError("only one active evaluation per engine")
+        try:
+            _lib.check(self._L.faco_evaluate(self._handle, keys.ctypes.data, seeds.ctypes.data, count, limit, mne,
+                                             _lib.ptr(cps) if cps.size else None, cps.size, C.byref(out)))
+        finally:
+            self._lock.release()
+        items = []
+        for c in range(count):
+            n = self._sizes[int(keys[c])]
+            items.append({"has_incumbent": True, "tour": tours[c, :n].tolist(), "cost": int(costs[c]),
+                          "completed_seconds": out.solve_seconds})
+        result = {
+            "items": items,
+            "budget_seconds": None,
+            "budget_kind": "search_tour_evaluations",
+            "evaluation_limit_per_colony": limit,
+            "completed_tour_evaluations_per_colony": int(out.completed_batches) * self.ants,
+            "total_tour_evaluations": int(out.completed_batches) * self.ants * count,
+            "completed_batches": int(out.completed_batches),
+            "completed_construction_steps": int(out.construction_steps),
+            "completed_ls_evaluations": int(out.ls_evaluations),
+            "production_kernel_milliseconds": {"iteration_loop": out.kernel_milliseconds},
+            "elapsed_seconds": out.solve_seconds,
+            "actual_seconds": out.solve_seconds,
+            "preparation_mode": preparation_mode,
+        }
+        if cps.size:
+            result["checkpoints"] = [
+                {"iterations": int(cps[i]),
+                 "tours": [cp_tours[i, c, :self._sizes[int(keys[c])]].tolist() for c in range(count)]}
+                for i in range(cps.size)]
+        if trace:
+            result["trace"] = trace_rows
+        return result
+
+
+    # ---- stepwise evaluation (caller-driven ant batches) -------------------
+    def begin(self, instance_keys, seeds, mne=8, *, trace_iterations: int = 0) -> None:
+        keys = _u64_array(instance_keys, "instance_keys")
+        seeds = _u64_array(seeds, "seeds")
+        if keys.size != seeds.size:
+            raise ValueError("instance_keys and seeds differ in length")
+        _exact_int(mne, "mne", 1, 2**32 - 1)
+        _exact_int(trace_iterations, "trace_iterations", 0, 2**32 - 1)
+        _lib.check(self._L.faco_begin(self._handle, keys.ctypes.data, seeds.ctypes.data, keys.size, mne,
+                                      trace_iterations))
+        self._active = (keys.copy(), trace_iterations, 0)
+
+    def step(self, iterations: int) -> None:
+        """Enqueues `iterations` ant batches on the engine stream (asynchronous)."""
+        _exact_int(iterations, "iterations", 0, 2**32 - 1)
+        _lib.check(self._L.faco_step(self._handle, iterations))
+        keys, cap, done = self._active
+        self._active = (keys, cap, done + iterations)
+
+    def step_timed(self, iterations: int) -> tuple[float, float]:
+        """Runs ant batches with a CUDA event around every kernel; returns the
+        summed device milliseconds (ant kernel, colony update)."""
+        _exact_int(iterations, "iterations", 0, 2**32 - 1)
+        ant_ms, update_ms = C.c_double(), C.c_double()
+        _lib.check(self._L.faco_step_timed(self._handle, iterations, C.byref(ant_ms), C.byref(update_ms)))
+        keys, cap, done = self._active
+        self._active = (keys, cap, done + iterations)
+        return ant_ms.value, update_ms.value
+
+    def finish(self) -> dict:
+        keys, cap, done = self._active
+        count, D = keys.size, self.dimension
+        tours = np.zeros((count, D), np.uint32)
+        costs = np.zeros(count, np.int64)
+        trace_rows = np.zeros((min(cap, done), count), _lib.TRACE_DTYPE) if cap else None
+        out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), None)
+        self._active = None
+        _lib.check(self._L.faco_finish(self._handle, C.byref(out)))
+        return {"tours": [tours[c, :self._sizes[int(keys[c])]] for c in range(count)], "costs": costs,
+                "completed_batches": int(out.completed_batches),
+                "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
+                "reversed_elements": int(out.reversed_elements), "trace": trace_rows}
+
+    @property
+    def stream_ptr(self) -> int:
+        """The engine's cudaStream_t as an integer (torch.cuda.ExternalStream)."""
+        return int(self._L.faco_engine_stream(self._handle) or 0)
+
+
+def program_to_c(program: dict) -> _lib.Program:
+    """read_program (bindings.cpp:22-56): strict IR dict -> Program struct."""
+    if not isinstance(program, dict):
+        raise ValueError("program must be a dict")
+    if len(program) != 6 and not (len(program) == 7 and "program_id" in program):
+        raise ValueError("wrong number of IR fields")
+    p = _lib.Program()
+    for name in ("ir_version", "numeric_spec_id", "feature_spec_id"):
+        setattr(p, name, _exact_int(program[name], name, 0, 0xFFFF))
+    ops, operands, bits = program["opcode"], program["operand"], program["constant_bits"]
+    for seq in (ops, operands, bits):
+        for v in seq:
+            if type(v) is not int:
+                raise ValueError("opcodes, operands and bit patterns must be ints")
+    if not 1 <= len(ops) <= 63 or len(operands) != len(ops) or len(bits) > 63:
+        raise ValueError("IR array sizes out of range")
+    p.length, p.constants_count = len(ops), len(bits)
+    for i, (o, a) in enumerate(zip(ops, operands)):
+        if not (0 <= o <= 255 and 0 <= a <= 255):
+            raise ValueError("opcode/operand out of uint8 range")
+        p.opcode[i], p.operand[i] = o, a
+    for i, b in enumerate(bits):
+        if not 0 <= b <= 0xFFFFFFFF:
+            raise ValueError("constant bits out of uint32 range")
+        p.constants[i] = struct.unpack("<f", struct.pack("<I", b))[0]
+    _lib.check(_lib.load().faco_validate_program(C.byref(p)))
+    return p
+
+
+def score_cuda(programs, features, masks) -> dict:
+    """score_cuda(program, features f32[12,C,32], masks u32[C]) (bindings.cpp:
+    504-506,1007-1009).  `programs` may be one IR dict or a list of them (the
+    colonies are split evenly between programs)."""
+    if isinstance(programs, dict):
+        programs = [programs]
+    if (not isinstance(features, np.ndarray) or features.dtype != np.float32 or features.ndim != 3
+            or features.shape[0] != 12 or features.shape[2] != 32 or not features.flags.c_contiguous):
+        raise ValueError("features must be C-contiguous float32 [12, colonies, 32]")
+    if (not isinstance(masks, np.ndarray) or masks.dtype != np.uint32 or masks.ndim != 1
+            or masks.shape[0] != features.shape[1] or not masks.flags.c_contiguous):
+        raise ValueError("masks must be C-contiguous uint32 [colonies]")
+    arr = (_lib.Program * len(programs))(*[program_to_c(p) for p in programs])
+    colonies = masks.shape[0]
+    scores = np.zeros((colonies, 32), np.float32)
+    actions = np.zeros(colonies, np.int32)
+    _lib.check(_lib.load().faco_score(C.cast(arr, C.c_void_p), len(programs), features.ctypes.data, 12,
+                                      masks.ctypes.data, colonies, scores.ctypes.data, actions.ctypes.data))
+    return {"scores": scores, "actions": actions}
+
+
+def ant_diagnostic(xy, ls_rows, tours, mne_targets, evaluation_limit, *, visits=None, uniforms=None, starts=None,
+                   primary=None, products=None, backup=None, checklist_capacity=None) -> dict:
+    """cuda_faco_diagnostic (cpp/include/gp_faco/faco_cuda_diagnostic.hpp:36-39):
+    explicit-choice (visits) or injected-uniform construction + local search,
+    one warp-ant per task."""
+    xy = np.ascontiguousarray(xy, dtype=np.int32)
+    n = xy.shape[0]
+    ls_rows = np.ascontiguousarray(ls_rows, dtype=np.uint32)
+    tours = np.ascontiguousarray(tours, dtype=np.uint32).reshape(-1, n)
+    tasks = tours.shape[0]
+    targets = np.ascontiguousarray(mne_targets, dtype=np.uint32)
+    cap = checklist_capacity or 8 * n + 8
+    outs = dict(construction_tours=np.zeros((tasks, n), np.uint32), tours=np.zeros((tasks, n), np.uint32),
+                positions=np.zeros((tasks, n), np.uint32), selected=np.zeros((tasks, n), np.uint32),
+                checklists=np.zeros((tasks, cap), np.uint32), construction_costs=np.zeros(tasks, np.int64),
+                final_costs=np.zeros(tasks, np.int64), counters=np.zeros((tasks, 10), np.uint64))
+    o = _lib.AntOutputs(outs["construction_tours"].ctypes.data, outs["tours"].ctypes.data,
+                        outs["positions"].ctypes.data, outs["selected"].ctypes.data, outs["checklists"].ctypes.data,
+                        cap, outs["construction_costs"].ctypes.data, outs["final_costs"].ctypes.data,
+                        outs["counters"].ctypes.data)
+    keep = []
+
+    def arr(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    k = 0 if primary is None else np.asarray(primary).shape[1]
+    b = 0 if backup is None else np.asarray(backup).shape[1]
+    _lib.check(_lib.load().faco_ant_diagnostic(
+        xy.ctypes.data, n, ls_rows.ctypes.data, ls_rows.shape[1], tours.ctypes.data, arr(visits, np.uint32),
+        arr(uniforms, np.float64), arr(starts, np.uint32), arr(primary, np.uint32), arr(products, np.float32), k,
+        arr(backup, np.uint32) if b else None, b, targets.ctypes.data, tasks, evaluation_limit,
+        _lib.FACO_LS_TWO_OPT, C.byref(o)))
+    return outs
+
+
+def pheromone_step(primary, parent, trails, eta, *, retention, minimum, maximum, increment):
+    """One MMAS evaporate/deposit step on FP32 trails (cuda/colony_state.cuh:210-229)."""
+    primary = np.ascontiguousarray(primary, dtype=np.uint32)
+    n, k = primary.shape
+    parent = np.ascontiguousarray(parent, dtype=np.uint32)
+    trails = np.array(trails, dtype=np.float32, order="C", copy=True).reshape(n, k)
+    eta = np.ascontiguousarray(eta, dtype=np.float32).reshape(n, k)
+    products = np.zeros((n, k), np.float32)
+    _lib.check(_lib.load().faco_pheromone_step(n, k, primary.ctypes.data, parent.ctypes.data, retention, minimum,
+                                               maximum, increment, eta.ctypes.data, trails.ctypes.data,
+                                               products.ctypes.data))
+    return trails, products

@@ -1,0 +1,197 @@
+/*
+ * faco_gb300.h -- C ABI of the GB300 Focused-ACO batch engine.
+ *
+ * Plain pointers and sizes only.  Every call returns FACO_OK (0) or a
+ * negative status; faco_last_error() then holds a message for the calling
+ * thread.  No call aborts, traps or throws across the boundary.
+ *
+ * Each entry point replaces one interface of LinHuanli/GPLSACO's pybind11
+ * module gp_faco_ext (cpp/src/bindings.cpp); the file:line it replaces is
+ * given beside it.  Host buffers are copied in before a call returns.
+ */
+#ifndef FACO_GB300_H
+#define FACO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FACO_OK 0
+#define FACO_EINVAL (-1)   /* invalid argument: ValueError in the reference        */
+#define FACO_ECUDA (-2)    /* CUDA runtime error: RuntimeError in the reference    */
+#define FACO_EBUSY (-3)    /* a second evaluation on one engine (try_lock failure) */
+#define FACO_EDEVICE (-4)  /* a kernel raised its device error word                */
+#define FACO_ENOMEM (-5)
+
+/* Local-search variants. */
+#define FACO_LS_TWO_OPT 0       /* checklist 2-opt, best gain per node (reference) */
+#define FACO_LS_TWO_OPT_OR_OPT 1 /* 2-opt + Or-opt (segments <= 3), first improvement */
+
+/* FixedFacoSettings (cpp/include/gp_faco/fixed_faco_gpu.hpp:10-21;
+ * bindings.cpp:508-519).  ants == 0 selects 64*ceil(sqrt(n)/16). */
+typedef struct faco_settings {
+    uint32_t ants;
+    uint32_t primary_width;
+    uint32_t backup_width;
+    uint32_t ls_width;
+    double beta;
+    double retention;
+    double p_best;
+    double epoch_source_probability;
+    uint64_t ls_evaluation_limit;
+    uint64_t initial_ls_evaluation_limit;
+    uint32_t ls_mode; /* FACO_LS_* */
+    uint32_t reserved;
+} faco_settings;
+
+void faco_default_settings(faco_settings* s);
+
+/* Returns the message of the last failed call on this thread. */
+const char* faco_last_error(void);
+
+typedef struct faco_engine faco_engine;
+
+/* FacoBatchEngine(dimension, colonies, settings) (bindings.cpp:558-573).
+ * `dimension` is the largest instance size the engine accepts; instances of
+ * different sizes up to it may share one evaluation (uneven batching).
+ * `colonies` is the capacity of one evaluation; `device` the CUDA ordinal. */
+int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_settings* settings, int device,
+                       faco_engine** engine);
+void faco_engine_destroy(faco_engine* engine);
+
+typedef struct faco_registration {
+    double cheap_seconds;
+    double preparation_seconds;
+    int64_t initial_cost;
+    uint32_t n;
+    uint32_t reserved;
+} faco_registration;
+
+/* register_problem(instance_key, coordinates f64[n,2]) (bindings.cpp:623-638).
+ * Coordinates must be finite integers with |x| < 2^26 (TSPLIB EUC_2D). */
+int faco_register_problem(faco_engine* engine, uint64_t instance_key, const double* xy, uint32_t n,
+                          faco_registration* info);
+
+/* Initial tour and candidate rows of a registered instance (u32 [n], [n][k],
+ * [n][b], [n][w]; any pointer may be NULL). */
+int faco_problem_rows(faco_engine* engine, uint64_t instance_key, uint32_t* initial_tour, uint32_t* primary,
+                      uint32_t* backup, uint32_t* ls);
+
+/* Per-iteration colony trace row. */
+typedef struct faco_trace_row {
+    int64_t iteration_best_cost;
+    int64_t global_cost;
+    int64_t parent_cost;
+    uint32_t iteration_best;
+    uint32_t source_is_epoch;
+    float tau_min;
+    float tau_max;
+    uint32_t mne_target;
+    int32_t action;
+    uint64_t construction_steps;
+    uint64_t ls_evaluations;
+} faco_trace_row;
+
+typedef struct faco_outputs {
+    uint32_t* tours;          /* [count][dimension] global-best tours (u32)       */
+    int64_t* costs;           /* [count] integer EUC_2D lengths                   */
+    faco_trace_row* trace;    /* [iterations][count], may be NULL                 */
+    uint32_t* checkpoint_tours; /* [n_checkpoints][count][dimension], may be NULL */
+    uint64_t completed_batches;
+    uint64_t construction_steps;
+    uint64_t ls_evaluations;
+    uint64_t reversed_elements; /* tour elements moved by relocations/reversals */
+    double kernel_milliseconds; /* device time of the iteration loop             */
+    double solve_seconds;
+} faco_outputs;
+
+/* evaluate_faco_evaluations(keys, seeds, evaluation_limit_per_colony, mne,
+ * checkpoint_iterations=...) (bindings.cpp:701-720; engine
+ * cuda/batch_engine.cu:362-365, loop :875-1135).  Plain FACO with a constant
+ * MNE target.  The budget must be a whole number of ant batches; instance
+ * keys may name instances of different sizes (uneven batching). */
+int faco_evaluate(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds, uint32_t count,
+                  uint64_t evaluation_limit_per_colony, uint32_t mne_target, const uint64_t* checkpoint_iterations,
+                  uint32_t n_checkpoints, faco_outputs* out);
+
+/* The same evaluation in explicit steps (the reference's per-batch loop,
+ * cuda/batch_engine.cu:875-1135, driven by the caller): faco_begin uploads the
+ * panel and resets every colony; faco_step enqueues `iterations` ant batches
+ * on the engine's stream (asynchronous); faco_step_timed runs them with a CUDA
+ * event around every kernel and returns the summed device milliseconds of
+ * the ant kernel and of the colony update (synchronous); faco_finish waits
+ * and fills tours, costs, counters and up to trace_iterations trace rows. */
+int faco_begin(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds, uint32_t count,
+               uint32_t mne_target, uint32_t trace_iterations);
+int faco_step(faco_engine* engine, uint32_t iterations);
+int faco_step_timed(faco_engine* engine, uint32_t iterations, double* ant_milliseconds,
+                    double* update_milliseconds);
+int faco_finish(faco_engine* engine, faco_outputs* out);
+/* The engine's cudaStream_t (for events recorded by the caller). */
+void* faco_engine_stream(faco_engine* engine);
+
+/* ---- GP programs -------------------------------------------------------- */
+/* Program (cpp/include/gp_faco/program.hpp:10-19). numeric_spec_id 1 is the
+ * reference IR (opcodes 0-8, depth <= 5); 2 adds protected division (9) and
+ * if>0 (10, three operands), depth <= 6. */
+typedef struct faco_program {
+    uint16_t ir_version;
+    uint16_t numeric_spec_id;
+    uint16_t feature_spec_id;
+    uint16_t length;
+    uint16_t constants_count;
+    uint8_t opcode[63];
+    uint8_t operand[63];
+    float constants[63];
+} faco_program;
+
+int faco_validate_program(const faco_program* program);
+
+/* score_cuda(program, features f32[F,C,32], masks u32[C]) (bindings.cpp:
+ * 504-506,1007-1009; kernel cuda/gp_score.cuh:64-102).  `programs` holds
+ * n_programs programs; colony c uses programs[c / (colonies / n_programs)].
+ * Host buffers. */
+int faco_score(const faco_program* programs, uint32_t n_programs, const float* features, uint32_t features_count,
+               const uint32_t* masks, uint32_t colonies, float* scores, int32_t* actions);
+
+/* ---- diagnostics (parity hooks) ---------------------------------------- */
+/* cuda_faco_diagnostic (cpp/include/gp_faco/faco_cuda_diagnostic.hpp:36-39,
+ * cuda/faco_operations.cu:60-134): one warp-ant per task runs focused
+ * construction from tours[t] then checklist LS.  Choices come from visit
+ * orders (visits != NULL, [tasks][n]) or from a roulette over `products`
+ * ([n][k] FP32) driven by injected uniforms ([tasks][n], step s uses [s]) with
+ * starts[t] as the first node.  ls_rows [n][w] in any order (the engine
+ * builds the distance-ordered view).  Outputs (u32/i64) may be NULL. */
+typedef struct faco_ant_outputs {
+    uint32_t* construction_tours; /* [tasks][n]                                 */
+    uint32_t* tours;              /* [tasks][n]                                 */
+    uint32_t* positions;          /* [tasks][n]                                 */
+    uint32_t* selected;           /* [tasks][n] node chosen at each step        */
+    uint32_t* checklists;         /* [tasks][checklist_capacity]                */
+    uint32_t checklist_capacity;
+    int64_t* construction_costs;  /* [tasks]                                    */
+    int64_t* final_costs;         /* [tasks]                                    */
+    uint64_t* counters;           /* [tasks][10]: mne, steps, nonidentity,
+                                     processed, checks, evaluations, accepted,
+                                     reactivations, limit_reached, checklist   */
+} faco_ant_outputs;
+
+int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, uint32_t w, const uint32_t* tours,
+                        const uint32_t* visits, const double* uniforms, const uint32_t* starts,
+                        const uint32_t* primary, const float* products, uint32_t k, const uint32_t* backup,
+                        uint32_t b, const uint32_t* mne_targets, uint32_t tasks, uint64_t evaluation_limit,
+                        uint32_t ls_mode, faco_ant_outputs* out);
+
+/* One MMAS evaporate/deposit step (cuda/colony_state.cuh:210-229) on FP32
+ * trails [n][k] along `parent`; refreshes products = trails * eta. */
+int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent, float retention,
+                        float minimum, float maximum, float increment, const float* eta, float* trails,
+                        float* products);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

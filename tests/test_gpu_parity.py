@@ -1,0 +1,261 @@
+"""CUDA engine vs the CPU oracle, through the C ABI.  Integer/index work is
+compared bit-for-bit; FP32 trails against the FP64 reference arithmetic
+within 1e-6 relative."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tests import _cases, _programs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api(engine_lib):
+    import gplsaco_gb300 as g
+    return g
+
+
+def _oracle_ant_case(oracle, xy, ordered, tour, target, cap, **kw):
+    return oracle.ant(tour, ordered, int(target), cap, xy=xy, **kw)
+
+
+def _compare_ant(gpu, t, ref, ctx):
+    assert np.array_equal(gpu["construction_tours"][t], ref["construction_tour"]), ctx
+    assert gpu["construction_costs"][t] == ref["construction_cost"], ctx
+    assert np.array_equal(gpu["tours"][t], ref["tour"]), ctx
+    assert np.array_equal(gpu["positions"][t], ref["positions"]), ctx
+    c = gpu["counters"][t]
+    got = tuple(int(x) for x in c)
+    want = (ref["mne"], ref["steps"], ref["nonidentity"], ref["processed"], ref["checks"], ref["evaluations"],
+            ref["accepted"], ref["reactivations"], ref["limit_reached"], len(ref["checklist"]))
+    assert got == want, ctx
+    assert np.array_equal(gpu["checklists"][t][:len(ref["checklist"])], ref["checklist"]), ctx
+    assert gpu["final_costs"][t] == ref["final_cost"], ctx
+
+
+@pytest.mark.parametrize("n", _cases.N_GRID)
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_explicit_choice_construction_and_ls(api, oracle, n, metric):
+    """Identical construction tour, LS tour, positions, checklist order and
+    work counters for explicit visit orders (tests/cpp/test_cuda_faco.cpp:31-104)."""
+    xy = _cases.coordinates(n, metric, seed=83741 + n + metric * 1117)
+    matrix = oracle.euc2d_matrix(xy)
+    width = min(20, n - 1)
+    rows = _cases.ls_rows(matrix, width, reverse=metric == 0)
+    ordered = oracle.distance_ordered(rows, matrix)
+    ants = 16
+    tours, visits, targets = _cases.ant_tasks(n, ants, seed=n * 31 + metric)
+    for cap in _cases.CAPS:
+        gpu = api.ant_diagnostic(xy, rows, tours, targets, cap, visits=visits)
+        for t in range(ants):
+            ref = _oracle_ant_case(oracle, xy, ordered, tours[t], targets[t], cap, visit=visits[t])
+            _compare_ant(gpu, t, ref, f"n={n} metric={metric} cap={cap} ant={t}")
+            assert oracle.lib().orc_euc2d(0, 0, 3, 4) == 5
+
+
+def test_identity_two_opt_golden(api):
+    """A 3-node cycle has no real 2-opt move (tests/cpp/test_cuda_faco.cpp:106-125)."""
+    xy = np.array([[0, 0], [25, 0], [10, 27]], np.int32)
+    rows = np.array([[1, 2], [2, 0], [1, 0]], np.uint32)
+    ident = np.arange(3, dtype=np.uint32)
+    gpu = api.ant_diagnostic(xy, rows, ident[None], [2], 1000, visits=ident[None])
+    assert int(gpu["counters"][0][6]) == 0
+    assert np.array_equal(gpu["tours"][0], ident)
+
+
+@pytest.mark.parametrize("n,k,b", [(7, 2, 1), (17, 16, 0), (100, 16, 64), (100, 2, 1), (500, 16, 64),
+                                   (1000, 16, 64), (1000, 2, 1)])
+def test_injected_uniform_roulette(api, oracle, n, k, b):
+    """Given a stream of uniforms, construction picks bit-identical nodes,
+    including zero-weight, backup and global fallbacks (tests/cpp/test_fixed_faco.cpp:236-249)."""
+    rng = np.random.default_rng(4703 + n + k)
+    xy = _cases.uniform_instance(n, seed=n + 8999)
+    b = min(b, n - 1 - k)
+    prep = oracle.prepare(xy, k, b, min(20, n - 1))
+    products = rng.random((n, k), dtype=np.float32) * np.float32(1e-3)
+    products[rng.random((n, k)) < 0.1] = 0.0
+    products[rng.random(n) < 0.05] = 0.0          # whole rows of zero weight
+    ants = 16
+    tours = np.stack([rng.permutation(n) for _ in range(ants)]).astype(np.uint32)
+    uniforms = rng.random((ants, n))
+    starts = rng.integers(0, n, ants).astype(np.uint32)
+    targets = np.full(ants, 16, np.uint32)
+    gpu = api.ant_diagnostic(xy, prep["ls"], tours, targets, 5000, uniforms=uniforms, starts=starts,
+                             primary=prep["primary"], products=products, backup=prep["backup"] if b else None)
+    for t in range(ants):
+        ref = oracle.ant(tours[t], prep["ls"], 16, 5000, xy=xy, uniforms=uniforms[t], start=int(starts[t]),
+                         primary=prep["primary"], products32=products, backup=prep["backup"] if b else None)
+        steps = ref["steps"]
+        assert np.array_equal(gpu["selected"][t][:steps + 1], ref["selected"]), f"n={n} ant={t}"
+        _compare_ant(gpu, t, ref, f"n={n} k={k} b={b} ant={t}")
+
+
+def test_pheromone_step(api, oracle):
+    rng = np.random.default_rng(11)
+    n, k = 1000, 16
+    xy = _cases.uniform_instance(n, seed=3)
+    prep = oracle.prepare(xy, k, 0, 20)
+    primary = prep["primary"]
+    eta = (1.0 / np.maximum(1, oracle.euc2d_matrix(xy)[np.arange(n)[:, None], primary])).astype(np.float32)
+    for retention in (0.25, 0.5, 0.98):
+        tmin, tmax = np.float32(1e-7), np.float32(2e-6)
+        trails = rng.uniform(float(tmin), float(tmax), (n, k)).astype(np.float32)
+        parent = rng.permutation(n).astype(np.uint32)
+        inc = np.float32(1.0 / 7.3e7)
+        got_t, got_p = api.pheromone_step(primary, parent, trails, eta, retention=float(np.float32(retention)),
+                                          minimum=float(tmin), maximum=float(tmax), increment=float(inc))
+        ref_t = trails.reshape(-1).copy(); ref_p = np.zeros(n * k, np.float32); d = C.c_float(tmax)
+        oracle.lib().orc_pheromone32(n, k, primary, parent, np.float32(retention), tmin, tmax, inc,
+                                     eta.reshape(-1), ref_t, ref_p, C.byref(d))
+        assert np.array_equal(got_t.reshape(-1), ref_t) and np.array_equal(got_p.reshape(-1), ref_p)
+        # FP32 engine trails vs FP64 reference arithmetic: 1e-6 relative
+        t64 = trails.astype(np.float64).reshape(-1); d64 = C.c_double(float(tmax))
+        oracle.lib().orc_pheromone64(n, k, primary, parent, retention, float(tmin), float(tmax), float(inc), t64,
+                                     C.byref(d64))
+        assert np.max(np.abs(got_t.reshape(-1) - t64) / t64) <= 1e-6
+
+
+def test_scores_reference_and_extended(api, oracle):
+    rng = np.random.default_rng(6677)
+    features = rng.random((12, 7, 32), dtype=np.float32)
+    masks = rng.integers(1, 0xFFFFFFFF, size=7, dtype=np.uint32)
+    masks[:3] = [1, 1 << 31, 0xFFFFFFFF]
+    for extended in (False, True):
+        for _ in range(128):
+            program = _programs.random_program(rng, extended=extended)
+            got = api.score_cuda(program, features, masks)
+            ref_scores, ref_actions = oracle.score(program, features, masks)
+            assert np.array_equal(got["scores"], ref_scores)
+            assert np.array_equal(got["actions"], ref_actions)
+    zeros = np.zeros((12, 3, 32), np.float32)
+    program = dict(ir_version=1, numeric_spec_id=1, feature_spec_id=1, opcode=[0], operand=[4], constant_bits=[])
+    got = api.score_cuda(program, zeros, np.array([0xFFFFFFFF, 1 << 31, 1 << 7], np.uint32))
+    assert got["actions"].tolist() == [0, 31, 7]
+
+
+def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000):
+    return api.FixedFacoSettings(ants=ants, primary_width=k, backup_width=b, ls_width=w, retention=retention,
+                                 epoch_source_probability=epoch, ls_evaluation_limit=ls_limit)
+
+
+@pytest.mark.parametrize("n,ants,iterations,variant", [(7, 4, 8, 0), (17, 8, 8, 1), (100, 32, 20, 2),
+                                                       (500, 16, 6, 3), (1000, 32, 4, 0)])
+def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant):
+    """Whole plain-FACO runs: registration rows and initial tour, every
+    iteration's best/global/parent costs and trail bounds, the final global
+    tour and the FP32 trails agree bit-for-bit with the oracle."""
+    k = 2 if variant % 2 else 16
+    b = 1 if variant % 2 else 64
+    retention = (0.25, 0.5, 0.75, 0.98)[variant]
+    epoch = (0.0, 0.01, 1.0, 0.3)[variant]
+    xy = _cases.uniform_instance(n, seed=4703 + n)
+    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000)
+    engine = api.FacoBatchEngine(n, 3, settings)
+    info = engine.register_problem(n + 8999, xy.astype(np.float64))
+    kk, bb, ww = min(k, n - 1), min(b, n - 1 - min(k, n - 1)), min(20, n - 1)
+    prep = oracle.prepare(xy, kk, bb, ww)
+    rows = engine.problem_rows(n + 8999)
+    assert np.array_equal(rows["primary"], prep["primary"]) and np.array_equal(rows["backup"], prep["backup"])
+    assert np.array_equal(rows["ls"], prep["ls"]) and np.array_equal(rows["initial_tour"], prep["initial"])
+    assert info["initial_cost"] == prep["cost"]
+    seeds = np.array([17, 29, 17], np.uint64)
+    keys = np.full(3, n + 8999, np.uint64)
+    res = engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8, trace=True)
+    assert res["completed_tour_evaluations_per_colony"] == ants * iterations
+    for c in range(3):
+        key = oracle.lib().orc_colony_key(int(seeds[c]), n + 8999)
+        ref = oracle.run_colony(xy, prep, ants=ants, k=kk, b=bb, w=ww, mne=8, iterations=iterations, key=key,
+                                retention=retention, epoch_source_probability=epoch, ls_limit=5000)
+        assert res["items"][c]["cost"] == ref["cost"]
+        assert res["items"][c]["tour"] == ref["tour"].tolist()
+        for it in range(iterations):
+            row, want = res["trace"][it, c], ref["trace"][it]
+            for field in ("iteration_best_cost", "global_cost", "parent_cost", "iteration_best", "source_is_epoch",
+                          "construction_steps", "ls_evaluations"):
+                assert int(row[field]) == int(want[field]), (c, it, field)
+            assert row["tau_min"] == np.float32(want["tau_min"]) and row["tau_max"] == np.float32(want["tau_max"])
+    # same seed, same instance -> same result (colonies 0 and 2)
+    assert res["items"][0]["tour"] == res["items"][2]["tour"]
+    engine.close()
+
+
+def test_uneven_batch_matches_independent_runs(api, oracle):
+    """Instances of different sizes share one evaluation; each colony equals
+    its own oracle run (tests/cpp/test_batch_engine.cpp:39-88)."""
+    sizes = [200, 537, 1000, 311]
+    ants, iterations = 16, 5
+    settings = _settings(api, ants)
+    engine = api.FacoBatchEngine(1000, 8, settings)
+    preps = {}
+    for i, n in enumerate(sizes):
+        xy = _cases.uniform_instance(n, seed=100 + i)
+        engine.register_problem(1000 + i, xy.astype(np.float64))
+        preps[1000 + i] = (xy, oracle.prepare(xy, 16, 64, 20))
+    keys = np.array([1003, 1000, 1002, 1001, 1002], np.uint64)
+    seeds = np.array([5, 6, 7, 8, 9], np.uint64)
+    res = engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8)
+    for c in range(keys.size):
+        xy, prep = preps[int(keys[c])]
+        key = oracle.lib().orc_colony_key(int(seeds[c]), int(keys[c]))
+        ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations, key=key)
+        assert res["items"][c]["cost"] == ref["cost"], c
+        assert res["items"][c]["tour"] == ref["tour"].tolist(), c
+    engine.close()
+
+
+def test_full_size_invariants(api, oracle):
+    """N=1000, 64 colonies x 32 ants: every global tour is a permutation whose
+    recomputed EUC_2D length equals the reported one; global costs never
+    increase; FE accounting is ants x iterations; checkpoints are prefixes."""
+    n, colonies, ants, iterations = 1000, 64, 32, 12
+    engine = api.FacoBatchEngine(n, colonies, _settings(api, ants))
+    xys = []
+    for i in range(4):
+        xy = _cases.uniform_instance(n, seed=1 + i)
+        xys.append(xy)
+        engine.register_problem(i + 1, xy.astype(np.float64))
+    keys = np.array([1 + (c % 4) for c in range(colonies)], np.uint64)
+    seeds = np.arange(colonies, dtype=np.uint64)
+    res = engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8, checkpoint_iterations=[0, 5, 12],
+                                           trace=True)
+    assert res["total_tour_evaluations"] == colonies * ants * iterations
+    for c in range(colonies):
+        tour = np.array(res["items"][c]["tour"], np.uint32)
+        assert np.array_equal(np.sort(tour), np.arange(n))
+        m = xys[c % 4]
+        length = int(np.sum(oracle.euc2d_matrix(m)[tour, np.roll(tour, -1)]))
+        assert length == res["items"][c]["cost"]
+        g = res["trace"]["global_cost"][:, c]
+        assert np.all(np.diff(g) <= 0)
+    assert res["checkpoints"][-1]["tours"] == [item["tour"] for item in res["items"]]
+    engine.close()
+
+
+def test_invalid_inputs_raise_before_search(api):
+    """Strict inputs (tests/python/test_fixed_faco_gpu.py:39-68, test_batch_engine.py:62-79)."""
+    engine = api.FacoBatchEngine(50, 2, _settings(api, 8))
+    xy = _cases.uniform_instance(50, seed=1).astype(np.float64)
+    with pytest.raises(ValueError):
+        engine.register_problem(1, xy.astype(np.float32))
+    with pytest.raises(ValueError):
+        engine.register_problem(True, xy)
+    bad = xy.copy(); bad[0, 0] = np.nan
+    with pytest.raises(ValueError):
+        engine.register_problem(1, bad)
+    bad = xy.copy(); bad[0, 0] = 0.5
+    with pytest.raises(ValueError):
+        engine.register_problem(1, bad)
+    engine.register_problem(1, xy)
+    keys = np.array([1, 1], np.uint64); seeds = np.array([1, 2], np.uint64)
+    with pytest.raises(ValueError):
+        engine.evaluate_faco_evaluations(keys, seeds, 7, 8)          # not whole ant batches
+    with pytest.raises(ValueError):
+        engine.evaluate_faco_evaluations(keys.astype(np.int64), seeds, 8, 8)
+    with pytest.raises(ValueError):
+        engine.evaluate_faco_evaluations(np.array([1, 9], np.uint64), seeds, 8, 8)  # unregistered
+    zero = engine.evaluate_faco_evaluations(keys, seeds, 0, 8)
+    rows = engine.problem_rows(1)
+    assert zero["items"][0]["tour"] == rows["initial_tour"].tolist()
+    engine.close()
