@@ -18,7 +18,6 @@ import json
 import os
 import subprocess
 import sys
-import threading
 import time
 from pathlib import Path
 
@@ -31,6 +30,8 @@ N = 1000
 INSTANCES = 16
 SEEDS_PER_INSTANCE = 16
 ANTS, K_PRIMARY, BACKUP, LS_WIDTH, MNE, RETENTION = 32, 16, 64, 20, 8, 0.98
+PRECONDITION = 100   # untimed iterations before the timed steps (steady-state trails)
+CPU_COLONIES_PER_THREAD = 6
 METRIC = "ant-tours+LS/sec (plain FACO, N=1000)"
 L2_BYTES = 129 * 2**20
 
@@ -97,35 +98,37 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(seconds: float = 12.0, threads: int | None = None) -> dict:
-    """The oracle port (C, one colony per host thread) on a bounded sample of
-    the same workload: N=1000 colonies with 32 ants, run for ~`seconds`."""
+def cpu_colonies(threads: int, colonies: int, iterations: int) -> float:
+    """Runs `colonies` N=1000 colonies of `iterations` iterations each with the
+    oracle port (C), one colony per host thread; returns elapsed seconds."""
     from concurrent.futures import ThreadPoolExecutor
 
     from oracle import oracle
     oracle.lib()
-    threads = threads or os.cpu_count() or 1
     xy = instance_xy(0)
     prep = oracle.prepare(xy, K_PRIMARY, BACKUP, LS_WIDTH)
-    iterations = 2
 
-    def colony(i):
-        key = oracle.lib().orc_colony_key(i, 1)
+    def one(i):
         oracle.run_colony(xy, prep, ants=ANTS, k=K_PRIMARY, b=BACKUP, w=LS_WIDTH, mne=MNE, iterations=iterations,
-                          key=key, retention=RETENTION, threads=1, want_trace=False)
-        return ANTS * iterations
+                          key=oracle.lib().orc_colony_key(i, 1), retention=RETENTION, threads=1, want_trace=False)
 
-    done = 0
     start = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as pool:
-        seed = 0
-        while time.perf_counter() - start < seconds:
-            done += sum(pool.map(colony, range(seed, seed + threads)))
-            seed += threads
-    elapsed = time.perf_counter() - start
-    return {"value": done / elapsed, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
-            "sample": f"{done} ant-tours+LS of N=1000 colonies (32 ants, 2 iterations each from the prepared "
-                      f"initial tour), one colony per host thread, {elapsed:.1f} s"}
+        list(pool.map(one, range(colonies)))
+    return time.perf_counter() - start
+
+
+def cpu_baseline(iterations: int) -> dict:
+    """The oracle port on a bounded sample of the same workload: one N=1000
+    colony of 32 ants per host thread, `iterations` iterations from the
+    prepared initial tour (the span of the e2e measurement)."""
+    threads = os.cpu_count() or 1
+    colonies = CPU_COLONIES_PER_THREAD * threads
+    elapsed = cpu_colonies(threads, colonies, iterations)
+    fe = colonies * ANTS * iterations
+    return {"value": fe / elapsed, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
+            "sample": f"{colonies} N=1000 colonies x 32 ants x {iterations} iterations ({fe} ant-tours+LS) "
+                      f"from the prepared initial tour, one colony per host thread, {elapsed:.1f} s"}
 
 
 def measured_peak():
@@ -136,38 +139,28 @@ def measured_peak():
 
 
 def run_reference(args, rank: int) -> None:
+    """The CPU implementation of the path (the oracle port; the reference's own
+    C++ core cannot be built on this host) on all host threads: one colony per
+    thread, PRECONDITION + steps iterations each, like the e2e measurement."""
     if rank != 0:
         return
-    from concurrent.futures import ThreadPoolExecutor
-
-    from oracle import oracle
-    oracle.lib()
     threads = os.cpu_count() or 1
-    xy = instance_xy(0)
-    prep = oracle.prepare(xy, K_PRIMARY, BACKUP, LS_WIDTH)
-
-    def colonies(iterations):
-        def one(i):
-            oracle.run_colony(xy, prep, ants=ANTS, k=K_PRIMARY, b=BACKUP, w=LS_WIDTH, mne=MNE,
-                              iterations=iterations, key=oracle.lib().orc_colony_key(i, 1), retention=RETENTION,
-                              threads=1, want_trace=False)
-        with ThreadPoolExecutor(max_workers=threads) as pool:
-            list(pool.map(one, range(threads)))
-
-    colonies(max(1, args.warmup // 3))
-    start = time.perf_counter()
-    colonies(args.steps)
-    elapsed = time.perf_counter() - start
-    fe = threads * ANTS * args.steps
+    iterations = PRECONDITION + args.steps
+    colonies = CPU_COLONIES_PER_THREAD * threads
+    cpu_colonies(threads, threads, max(1, args.warmup))
+    elapsed = cpu_colonies(threads, colonies, iterations)
+    fe = colonies * ANTS * iterations
     value = fe / elapsed
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ant-tours+LS/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / iterations,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
             "data": "synthetic",
-            "config": {"workload": f"plain FACO N=1000 uniform, {threads} colonies x 32 ants (one per host "
-                                   f"thread), k=16, MNE 8, 2-opt", "colonies": threads, "ants": ANTS, "n": N},
+            "config": {"workload": f"plain FACO N=1000 uniform, {colonies} colonies x 32 ants ({threads} host "
+                                   f"threads, one colony each at a time), k=16, backup 64, LS width 20, MNE 8, "
+                                   f"2-opt, retention 0.98, {iterations} iterations from the initial tour",
+                       "colonies": colonies, "ants": ANTS, "n": N},
             "cpu_baseline": {"value": value, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
-                             "sample": f"{threads} colonies x {args.steps} iterations"},
+                             "sample": f"{colonies} colonies x {iterations} iterations"},
             "e2e": {"value": value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -194,8 +187,10 @@ def run_gb300(args, rank: int, world: int) -> None:
     stream = torch.cuda.ExternalStream(engine.stream_ptr)
 
     # ---- device throughput: inputs resident, L2 flushed before every step ----
+    # the panel first runs PRECONDITION iterations so that the timed steps see
+    # converged trails (construction steps per tour grow as they converge)
     engine.begin(keys, seeds, MNE)
-    engine.step(args.warmup)
+    engine.step(PRECONDITION + args.warmup)
     torch.cuda.synchronize()
     step_ms = []
     with ClockSampler(local) as clocks:
@@ -231,13 +226,15 @@ def run_gb300(args, rank: int, world: int) -> None:
     fe_timed = args.steps * colonies * ANTS * world
     value = fe_timed / (elapsed_ms / 1e3)
 
-    # ---- end to end through the public API: host keys/seeds in, tours out ----
+    # ---- end to end through the public API: host keys/seeds in, tours out;
+    # one solve call of PRECONDITION + steps iterations from the initial tours ----
+    e2e_iters = PRECONDITION + args.steps
     engine.evaluate_faco_evaluations(keys, seeds, ANTS * args.warmup, MNE)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = engine.evaluate_faco_evaluations(keys, seeds, ANTS * args.steps, MNE)
+    res = engine.evaluate_faco_evaluations(keys, seeds, ANTS * e2e_iters, MNE)
     e2e_s = time.perf_counter() - t0
-    e2e_value = args.steps * colonies * ANTS / e2e_s
+    e2e_value = e2e_iters * colonies * ANTS / e2e_s
     h2d = keys.nbytes + seeds.nbytes
     d2h = colonies * N * 4 + colonies * 8
     assert all(len(it["tour"]) == N for it in res["items"])
@@ -250,7 +247,7 @@ def run_gb300(args, rank: int, world: int) -> None:
     engine.close()
     if rank != 0:
         return
-    base = cpu_baseline(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    base = cpu_baseline(PRECONDITION + 4) if args.cpu_baseline else None
     line = {
         "metric": METRIC, "value": value, "unit": "ant-tours+LS/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -258,9 +255,10 @@ def run_gb300(args, rank: int, world: int) -> None:
         "config": {"workload": "plain FACO, N=1000 uniform int coords, 16 instances x 16 seeds = 256 colonies, "
                                "32 ants, k=16, backup 64, LS width 20, MNE 8, 2-opt, retention 0.98",
                    "colonies": colonies, "ants": ANTS, "n": N, "l2": "flushed before every timed step "
-                   "(258 MB write)", "registration_seconds": registration_s},
-        "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d / args.steps,
-                "d2h_bytes_per_step": d2h / args.steps,
+                   "(258 MB write)", "timed_iterations_start_at": PRECONDITION + args.warmup,
+                   "registration_seconds": registration_s},
+        "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d / e2e_iters,
+                "d2h_bytes_per_step": d2h / e2e_iters, "iterations": e2e_iters,
                 "call": "FacoBatchEngine.evaluate_faco_evaluations (C ABI faco_evaluate), host keys/seeds in, "
                         "host tours/costs out"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -281,7 +279,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

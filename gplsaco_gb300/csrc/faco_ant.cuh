@@ -9,18 +9,23 @@
 // reversal rules.  The GB300 design differs throughout:
 //   - every per-ant scalar is warp-uniform and lives in registers of all 32
 //     lanes (no shared State struct, no lane-0 serial sections beyond the
-//     single store of a queue slot);
-//   - the tour, its inverse, the checklist ring and the visited/pending
-//     flags live in shared memory (16-bit nodes), coordinates are staged
-//     once per block for all its ants (same colony);
+//     single store of a queue slot or flag word);
+//   - the tour, its inverse and the checklist ring live in shared memory as
+//     16-bit nodes, the visited/pending flags as bitsets; coordinates are
+//     staged once per block for all its ants (one colony per block);
 //   - distances are exact EUC_2D integers computed on the fly, so gains and
 //     tour lengths are exact int64 and ties are decided by index only;
-//   - the roulette keeps the reference's ordered FP64 prefix sums (needed
-//     for bit-identical choices) but gathers weights with shuffles and
-//     selects with one ballot;
+//   - the roulette decides from an FP32 warp scan whenever a proven error
+//     margin allows and otherwise recomputes the reference's ordered FP64
+//     prefix sums, so the choice is always the FP64 one (GB300 runs FP64 at
+//     a small fraction of its FP32 rate);
 //   - relocation shifts run as register-staged warp chunks, reversals as
-//     disjoint swap pairs, the best move by __reduce_max/min_sync.
+//     disjoint swap pairs, the best move by __reduce_max/min_sync, and the
+//     LS rows of the next pending node are fetched while the current one is
+//     evaluated.
 #pragma once
+
+#include <climits>
 
 #include "faco_common.cuh"
 
@@ -47,14 +52,14 @@ struct AntLaunch {
     std::uint32_t ls_mode;
     // diagnostic modes: tasks on instance 0
     std::uint32_t tasks;
-    const node_t* task_tours;     // [tasks][n]
-    const node_t* task_pos;       // [tasks][n]
-    const long long* task_costs;  // [tasks]
-    const node_t* task_visits;    // [tasks][n]
-    const double* task_uniforms;  // [tasks][n]
+    const node_t* task_tours;        // [tasks][n]
+    const std::uint32_t* task_nbr;   // [tasks][n] parent successor | predecessor << 16
+    const long long* task_costs;     // [tasks]
+    const node_t* task_visits;       // [tasks][n]
+    const double* task_uniforms;     // [tasks][n]
     const std::uint32_t* task_starts;
     const std::uint32_t* task_targets;
-    const float* task_products;   // [n][k]
+    const float* task_products;      // [n][k]
     // diagnostic outputs (may be null)
     node_t* out_construction;     // [tasks][n]
     node_t* out_tours;            // [tasks][n]
@@ -67,24 +72,33 @@ struct AntLaunch {
     unsigned* error;
 };
 
-__device__ __forceinline__ int dist(const int2* xy, std::uint32_t a, std::uint32_t b) {
-    return euc2d(xy[a], xy[b]);
+__host__ __device__ inline std::uint32_t pad8(std::uint32_t n) { return (n + 7u) & ~7u; }
+
+// Per-warp shared-memory workspace: tour, inverse, checklist ring (16-bit),
+// visited and pending bitsets.
+__host__ __device__ inline std::uint32_t ant_smem_bytes(std::uint32_t n) {
+    return (6u * pad8(n) + 8u * ((n + 31u) / 32u) + 15u) & ~15u;
+}
+__host__ __device__ inline std::uint32_t block_smem_bytes(std::uint32_t n, std::uint32_t warps) {
+    return ((8u * n + 15u) & ~15u) + warps * ant_smem_bytes(n);
 }
 
-// Per-warp shared-memory workspace and checklist ring.
 struct AntSmem {
     node_t* tour;
     node_t* pos;
     node_t* ring;
-    std::uint8_t* visited;
-    std::uint8_t* queued;
+    std::uint32_t* visited;
+    std::uint32_t* queued;
+    __device__ static AntSmem at(unsigned char* base, std::uint32_t n_max) {
+        const std::uint32_t np = pad8(n_max), words = (n_max + 31u) / 32u;
+        return {reinterpret_cast<node_t*>(base), reinterpret_cast<node_t*>(base + 2 * np),
+                reinterpret_cast<node_t*>(base + 4 * np), reinterpret_cast<std::uint32_t*>(base + 6 * np),
+                reinterpret_cast<std::uint32_t*>(base + 6 * np) + words};
+    }
 };
 
-__host__ __device__ inline std::uint32_t ant_smem_bytes(std::uint32_t n) {
-    return (8u * n + 15u) & ~15u;
-}
-__host__ __device__ inline std::uint32_t block_smem_bytes(std::uint32_t n, std::uint32_t warps) {
-    return ((8u * n + 15u) & ~15u) + warps * ant_smem_bytes(n);
+__device__ __forceinline__ bool test_bit(const std::uint32_t* bits, std::uint32_t v) {
+    return (bits[v >> 5] >> (v & 31u)) & 1u;
 }
 
 struct Checklist {
@@ -95,10 +109,10 @@ struct Checklist {
 // cuda/faco_device.cuh:81-92).  Warp-uniform decision, lane 0 stores.
 __device__ __forceinline__ bool push_absent(const AntSmem& s, Checklist& q, std::uint32_t n, std::uint32_t v,
                                             std::uint32_t lane, std::uint32_t* log, std::uint32_t log_cap) {
-    const bool absent = s.queued[v] == 0;
+    const bool absent = !test_bit(s.queued, v);
     if (absent) {
         if (lane == 0) {
-            s.queued[v] = 1;
+            s.queued[v >> 5] |= 1u << (v & 31u);
             s.ring[q.tail] = (node_t)v;
             if (log && q.pushed < log_cap) log[q.pushed] = v;
         }
@@ -108,6 +122,16 @@ __device__ __forceinline__ bool push_absent(const AntSmem& s, Checklist& q, std:
     }
     __syncwarp();
     return absent;
+}
+
+__device__ __forceinline__ std::uint32_t pop(const AntSmem& s, Checklist& q, std::uint32_t n,
+                                             std::uint32_t lane) {
+    const std::uint32_t a = s.ring[q.head];
+    q.head = q.head + 1 == n ? 0 : q.head + 1;
+    --q.pending;
+    __syncwarp();
+    if (lane == 0) s.queued[a >> 5] &= ~(1u << (a & 31u));
+    return a;
 }
 
 struct AntResult {
@@ -170,6 +194,33 @@ __device__ __forceinline__ std::uint32_t flip(const AntSmem& s, std::uint32_t n,
     return count;
 }
 
+// LS row of one node: candidate id and its cached distance, one per lane.
+struct LsRow {
+    std::uint32_t node, b;
+    int ab;
+};
+__device__ __forceinline__ LsRow load_row(const InstanceView& in, std::uint32_t a, std::uint32_t lane) {
+    LsRow r{a, in.n, 0};
+    if (lane < in.w) {
+        r.b = __ldg(in.ls + (size_t)a * in.w + lane);
+        r.ab = __ldg(in.ls_dist + (size_t)a * in.w + lane);
+    }
+    return r;
+}
+
+// Pops the next pending node and returns its LS row, taking the prefetched
+// row when it belongs to that node; then prefetches the row of the node now
+// at the head (it cannot change before it is popped).
+__device__ __forceinline__ LsRow pop_with_row(const AntSmem& s, Checklist& q, std::uint32_t n,
+                                              std::uint32_t lane, const InstanceView& in, LsRow& next) {
+    const std::uint32_t a = pop(s, q, n, lane);
+    LsRow row = next.node == a ? next : load_row(in, a, lane);
+    row.node = a;
+    next.node = n;
+    if (q.pending > 0) next = load_row(in, s.ring[q.head], lane);
+    return row;
+}
+
 // Checklist 2-opt, best gain per popped node, reference tie/cap rules
 // (cpp/src/faco_cpu.cpp:148-217; cuda/faco_device.cuh:295-478).
 __device__ __forceinline__ void checklist_two_opt(const AntSmem& s, const int2* xy, const InstanceView& in,
@@ -177,25 +228,18 @@ __device__ __forceinline__ void checklist_two_opt(const AntSmem& s, const int2* 
                                                   unsigned long long cap, AntResult& r, long long& gain_sum,
                                                   std::uint32_t* log, std::uint32_t log_cap) {
     const std::uint32_t w = in.w;
+    LsRow next{n, n, 0};
     while (q.pending > 0 && r.accepted < n) {
         if (r.evaluations >= cap) { r.limit_reached = 1; break; }
-        const std::uint32_t a = s.ring[q.head];
-        q.head = q.head + 1 == n ? 0 : q.head + 1;
-        --q.pending;
-        __syncwarp();
-        if (lane == 0) s.queued[a] = 0;
+        const LsRow row = pop_with_row(s, q, n, lane, in, next);
+        const std::uint32_t a = row.node, b = row.b;
+        const int ab = row.ab;
         const std::uint32_t pa = s.pos[a];
         const std::uint32_t an = s.tour[pa + 1 == n ? 0 : pa + 1];
         const std::uint32_t ap = s.tour[pa == 0 ? n - 1 : pa - 1];
         ++r.processed;
         const int2 pa_xy = xy[a];
         const int cur0 = euc2d(pa_xy, xy[an]), cur1 = euc2d(xy[ap], pa_xy);
-        std::uint32_t b = n;
-        int ab = 0;
-        if (lane < w) {
-            b = in.ls[(size_t)a * w + lane];
-            ab = in.ls_dist[(size_t)a * w + lane];
-        }
         // prefix of candidates that pass the distance test, per kind
         const bool bad0 = lane < w && (b >= n || !(cur0 > ab));
         const bool bad1 = lane < w && (b >= n || !(cur1 > ab));
@@ -244,6 +288,145 @@ __device__ __forceinline__ void checklist_two_opt(const AntSmem& s, const int2* 
             ++r.accepted;
             gain_sum -= best;
         }
+        __syncwarp();
+    }
+}
+
+// Checklist local search with first-improvement 2-opt then Or-opt (segments
+// of 1-3 nodes starting at the popped node).  The reference has no Or-opt;
+// the move order, pruning and counting rules are this engine's own (stated in
+// full beside the CPU restatement).  Every lane evaluates one candidate; the
+// first improving move in scan order is found with one ballot.
+__device__ __forceinline__ void checklist_ls_first(const AntSmem& s, const int2* xy, const InstanceView& in,
+                                                   std::uint32_t n, std::uint32_t lane, Checklist& q,
+                                                   unsigned long long cap, AntResult& r, long long& gain_sum,
+                                                   std::uint32_t* log, std::uint32_t log_cap) {
+    const std::uint32_t w = in.w;
+    LsRow next{n, n, 0};
+    while (q.pending > 0 && r.accepted < n) {
+        if (r.evaluations >= cap) { r.limit_reached = 1; break; }
+        const LsRow row = pop_with_row(s, q, n, lane, in, next);
+        const std::uint32_t a = row.node, c = row.b;
+        const int ac = row.ab;
+        const std::uint32_t pa = s.pos[a];
+        const std::uint32_t an = s.tour[pa + 1 == n ? 0 : pa + 1];
+        const std::uint32_t ap = s.tour[pa == 0 ? n - 1 : pa - 1];
+        ++r.processed;
+        const int2 a_xy = xy[a];
+        const int cur0 = euc2d(a_xy, xy[an]), cur1 = euc2d(xy[ap], a_xy);
+        const bool valid = lane < w && c < n;
+        std::uint32_t pc = 0, c_next = 0, c_prev = 0;
+        int2 c_xy = make_int2(0, 0);
+        if (valid) {
+            pc = s.pos[c];
+            c_next = s.tour[pc + 1 == n ? 0 : pc + 1];
+            c_prev = s.tour[pc == 0 ? n - 1 : pc - 1];
+            c_xy = xy[c];
+        }
+        bool interrupted = false, found = false;
+        // ---- 2-opt, first improvement in (kind, j) order
+        for (std::uint32_t kind = 0; kind < 2 && !found && !interrupted; ++kind) {
+            const int cur = kind == 0 ? cur0 : cur1;
+            const std::uint32_t closing_end = kind == 0 ? an : ap;
+            const unsigned badm = __ballot_sync(kFull, lane < w && (!valid || !(cur > ac)));
+            const std::uint32_t f = badm ? __ffs(badm) - 1 : w;
+            const unsigned long long remaining = cap - r.evaluations;
+            const std::uint32_t used = remaining < f ? (std::uint32_t)remaining : f;
+            int g = INT_MIN;
+            const std::uint32_t nb = kind == 0 ? c_next : c_prev;
+            if (lane < used)
+                g = (nb == a || c == closing_end) ? 0 : cur + euc2d(c_xy, xy[nb]) - ac - euc2d(xy[closing_end], xy[nb]);
+            const unsigned improving = __ballot_sync(kFull, lane < used && g > 0);
+            if (improving) {
+                const std::uint32_t j = __ffs(improving) - 1;
+                r.evaluations += j + 1;
+                r.checks += j + 1;
+                const int gain = __shfl_sync(kFull, g, j);
+                const std::uint32_t bj = __shfl_sync(kFull, c, j), nbj = __shfl_sync(kFull, nb, j);
+                std::uint32_t m0, m1, m2, m3;
+                if (kind == 0) { m0 = an; m1 = nbj; m2 = a; m3 = bj; }
+                else { m0 = a; m1 = bj; m2 = ap; m3 = nbj; }
+                r.moved += flip(s, n, lane, m0, m1);
+                r.reactivations += push_absent(s, q, n, m0, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, m1, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, m2, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, m3, lane, log, log_cap);
+                ++r.accepted;
+                gain_sum -= gain;
+                found = true;
+            } else {
+                r.evaluations += used;
+                r.checks += used + (used < w ? 1 : 0);
+                if (used < f) interrupted = true;
+            }
+        }
+        if (interrupted) { r.limit_reached = 1; break; }
+        if (found) {
+            __syncwarp();
+            continue;
+        }
+        // ---- Or-opt: segment a.. of L nodes, first improvement in (L, j, variant) order
+        std::uint32_t seg0 = a, seg1 = n, seg2 = n;
+        const int d_pa = cur1;
+        for (std::uint32_t L = 1; L <= 3 && !found && !interrupted; ++L) {
+            if (n < L + 3) break;
+            if (L == 2) seg1 = an;
+            if (L == 3) { const std::uint32_t p1 = s.pos[seg1]; seg2 = s.tour[p1 + 1 == n ? 0 : p1 + 1]; }
+            const std::uint32_t e = L == 1 ? seg0 : L == 2 ? seg1 : seg2;
+            const std::uint32_t pe = s.pos[e];
+            const std::uint32_t qn = s.tour[pe + 1 == n ? 0 : pe + 1];
+            const int2 e_xy = xy[e];
+            const int G = d_pa + euc2d(e_xy, xy[qn]) - euc2d(xy[ap], xy[qn]);
+            const unsigned badm = __ballot_sync(kFull, lane < w && (!valid || !(G > ac)));
+            const std::uint32_t f = badm ? __ffs(badm) - 1 : w;
+            const unsigned long long remaining = cap - r.evaluations;
+            const std::uint32_t used = remaining < f ? (std::uint32_t)remaining : f;
+            int g1 = INT_MIN, g2 = INT_MIN;
+            if (lane < used) {
+                const bool inside = c == seg0 || c == seg1 || c == seg2;
+                if (!inside) {
+                    if (!(c_next == seg0 || c_next == seg1 || c_next == seg2))
+                        g1 = G + euc2d(c_xy, xy[c_next]) - ac - euc2d(e_xy, xy[c_next]);
+                    if (!(c_prev == seg0 || c_prev == seg1 || c_prev == seg2))
+                        g2 = G + euc2d(xy[c_prev], c_xy) - euc2d(xy[c_prev], e_xy) - ac;
+                }
+            }
+            const unsigned improving = __ballot_sync(kFull, lane < used && (g1 > 0 || g2 > 0));
+            if (improving) {
+                const std::uint32_t j = __ffs(improving) - 1;
+                r.evaluations += j + 1;
+                r.checks += j + 1;
+                const int g1j = __shfl_sync(kFull, g1, j), g2j = __shfl_sync(kFull, g2, j);
+                const std::uint32_t cj = __shfl_sync(kFull, c, j);
+                const std::uint32_t c2 = __shfl_sync(kFull, c_next, j), c0 = __shfl_sync(kFull, c_prev, j);
+                const bool first_variant = g1j > 0;
+                // (i) c, a .. e, c2: relocate a after c, then each next node after the last moved
+                // (ii) c0, e .. a, c: relocate e after c0, then each previous node
+                std::uint32_t target = first_variant ? cj : c0;
+                for (std::uint32_t t = 0; t < L; ++t) {
+                    const std::uint32_t idx = first_variant ? t : L - 1 - t;
+                    const std::uint32_t node = idx == 0 ? seg0 : idx == 1 ? seg1 : seg2;
+                    const std::uint32_t tp = s.pos[target], np = s.pos[node];
+                    relocate_shift(s, lane, tp, np, node);
+                    r.moved += tp < np ? np - tp : tp - np + 1;
+                    target = node;
+                }
+                r.reactivations += push_absent(s, q, n, ap, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, a, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, e, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, qn, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, first_variant ? cj : c0, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, first_variant ? c2 : cj, lane, log, log_cap);
+                ++r.accepted;
+                gain_sum -= first_variant ? g1j : g2j;
+                found = true;
+            } else {
+                r.evaluations += used;
+                r.checks += used + (used < w ? 1 : 0);
+                if (used < f) interrupted = true;
+            }
+        }
+        if (interrupted) { r.limit_reached = 1; break; }
         __syncwarp();
     }
 }

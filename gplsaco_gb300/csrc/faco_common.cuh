@@ -103,11 +103,12 @@ struct ColonyView {
     unsigned long long key;        // Philox key
     float* trails;                 // [n][k]
     float* products;               // [n][k]
-    node_t* parent;                // [n]
-    node_t* parent_pos;            // [n]
+    node_t* parent;                // [n_pad] (16-byte aligned)
+    std::uint32_t* parent_nbr;     // [n]: parent successor | predecessor << 16
     node_t* epoch;                 // [n]
     node_t* global;                // [n]
-    node_t* ant_tours;             // [ants][n]
+    node_t* ant_tours;             // [ants][n_pad] (16-byte aligned rows)
+    std::uint32_t n_pad;           // row stride of ant_tours (n rounded up to 8)
     long long* ant_costs;          // [ants]
     unsigned* ant_counts;          // [ants][3]: construction steps, LS evaluations, moved elements
 };

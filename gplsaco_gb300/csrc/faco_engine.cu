@@ -150,6 +150,14 @@ struct Instance {
     }
 };
 
+// Packed parent neighbours: successor | predecessor << 16, indexed by node.
+std::vector<std::uint32_t> parent_neighbours(const std::uint32_t* tour, std::uint32_t n) {
+    std::vector<std::uint32_t> nbr(n);
+    for (std::uint32_t i = 0; i < n; ++i)
+        nbr[tour[i]] = tour[i + 1 == n ? 0 : i + 1] | (tour[i == 0 ? n - 1 : i - 1] << 16);
+    return nbr;
+}
+
 void launch_ants(int mode, const faco::AntLaunch& L, std::uint32_t blocks, std::uint32_t warps, cudaStream_t s) {
     const std::uint32_t smem = faco::block_smem_bytes(L.n_max, warps);
     cuda_check(faco::prepare_ant_kernel(mode, smem), "cudaFuncSetAttribute");
@@ -169,7 +177,8 @@ struct faco_engine {
     DeviceBuffer<faco::InstanceView> d_instances;
     // evaluation buffers (grow-only)
     DeviceBuffer<float> trails, products;
-    DeviceBuffer<faco::node_t> parent, parent_pos, epoch, global, ant_tours;
+    DeviceBuffer<faco::node_t> parent, epoch, global, ant_tours;
+    DeviceBuffer<std::uint32_t> parent_nbr;
     DeviceBuffer<long long> ant_costs;
     DeviceBuffer<unsigned> ant_counts, error;
     DeviceBuffer<faco::ColonyState> states;
@@ -257,7 +266,7 @@ int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_setting
                     c.epoch_source_probability >= 0 && c.epoch_source_probability <= 1,
                 "invalid FACO settings");
         require(c.primary_width <= 32 && c.ls_width <= 32, "primary and LS widths are limited to 32 (one warp)");
-        require(c.ls_mode == FACO_LS_TWO_OPT, "only the 2-opt local search is available in this build");
+        require(c.ls_mode == FACO_LS_TWO_OPT || c.ls_mode == FACO_LS_TWO_OPT_OR_OPT, "unknown local-search mode");
         auto e = std::make_unique<faco_engine>();
         e->settings = c;
         e->dimension = dimension;
@@ -320,13 +329,13 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         inst->d_ls_dist.upload(ls_dist, s);
         inst->d_eta.upload(eta, s);
         // initial checklist 2-opt over the NN tour on the GPU (prepared_problem.cpp:159-162)
-        std::vector<faco::node_t> tour16(nn.begin(), nn.end()), pos16(n);
-        for (std::uint32_t i = 0; i < n; ++i) pos16[nn[i]] = static_cast<faco::node_t>(i);
+        std::vector<faco::node_t> tour16(nn.begin(), nn.end());
         const long long nn_cost = faco::host_tour_length(inst->xy, nn.data(), n);
-        DeviceBuffer<faco::node_t> d_tour, d_pos, d_out;
+        DeviceBuffer<faco::node_t> d_tour, d_out;
+        DeviceBuffer<std::uint32_t> d_nbr;
         DeviceBuffer<long long> d_cost, d_costs;
         d_tour.upload(tour16, s);
-        d_pos.upload(pos16, s);
+        d_nbr.upload(parent_neighbours(nn.data(), n), s);
         d_cost.upload(&nn_cost, 1, s);
         d_out.resize(n);
         d_costs.resize(2);
@@ -341,7 +350,7 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         L.ls_limit = c.initial_ls_evaluation_limit;
         L.tasks = 1;
         L.task_tours = d_tour.get();
-        L.task_pos = d_pos.get();
+        L.task_nbr = d_nbr.get();
         L.task_costs = d_cost.get();
         L.out_tours = d_out.get();
         L.out_costs = d_costs.get();
@@ -434,16 +443,18 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         require(k_common == 0 || k_common == in.k, "instances of one evaluation must share the primary width");
         k_common = in.k;
         v.sizes[c] = in.n;
-        tau_total += static_cast<std::size_t>(in.n) * in.k;
-        node_total += in.n;
-        ant_total += static_cast<std::size_t>(A) * in.n;
+        tau_total += (static_cast<std::size_t>(in.n) * in.k + 3) & ~std::size_t{3};
+        node_total += faco::pad8(in.n);
+        ant_total += static_cast<std::size_t>(A) * faco::pad8(in.n);
         n_max = std::max(n_max, in.n);
     }
     cudaStream_t s = e->stream;
+    // HBM layout: per colony, trails and products [n][k] (16-byte aligned),
+    // node arrays padded to 8 nodes so that every row starts 16-byte aligned
     e->trails.resize(tau_total);
     e->products.resize(tau_total);
     e->parent.resize(node_total);
-    e->parent_pos.resize(node_total);
+    e->parent_nbr.resize(node_total);
     e->epoch.resize(node_total);
     e->global.resize(node_total);
     e->ant_tours.resize(ant_total);
@@ -456,19 +467,20 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         faco::ColonyView& cv = views[c];
         cv.instance = e->index_of(keys[c]);
         cv.n = in.n;
+        cv.n_pad = faco::pad8(in.n);
         cv.key = mix64(seeds[c] ^ mix64(keys[c]));
         cv.trails = e->trails.get() + tau_off;
         cv.products = e->products.get() + tau_off;
         cv.parent = e->parent.get() + node_off;
-        cv.parent_pos = e->parent_pos.get() + node_off;
+        cv.parent_nbr = e->parent_nbr.get() + node_off;
         cv.epoch = e->epoch.get() + node_off;
         cv.global = e->global.get() + node_off;
         cv.ant_tours = e->ant_tours.get() + ant_off;
         cv.ant_costs = e->ant_costs.get() + static_cast<std::size_t>(c) * A;
         cv.ant_counts = e->ant_counts.get() + 3ull * c * A;
-        tau_off += static_cast<std::size_t>(in.n) * in.k;
-        node_off += in.n;
-        ant_off += static_cast<std::size_t>(A) * in.n;
+        tau_off += (static_cast<std::size_t>(in.n) * in.k + 3) & ~std::size_t{3};
+        node_off += cv.n_pad;
+        ant_off += static_cast<std::size_t>(A) * cv.n_pad;
     }
     e->colonies.upload(views, s);
     v.count = count;
@@ -563,7 +575,7 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
         steps += states[c].construction_steps;
         evals += states[c].ls_evaluations;
         reversed += states[c].reversed_elements;
-        node_off += n;
+        node_off += faco::pad8(n);
     }
     out->completed_batches = v.done;
     out->construction_steps = steps;
@@ -706,7 +718,7 @@ int faco_evaluate(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, u
                     for (std::uint32_t i = 0; i < D; ++i)
                         out->checkpoint_tours[(static_cast<std::size_t>(p) * count + c) * D + i] =
                             i < sizes[c] ? cps[static_cast<std::size_t>(p) * node_total + node_off + i] : UINT32_MAX;
-                node_off += sizes[c];
+                node_off += faco::pad8(sizes[c]);
             }
             out->kernel_milliseconds = ms;
             out->solve_seconds = seconds_since(started);
@@ -802,7 +814,7 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
         require(n >= 3 && n <= faco::kMaxNodes && tasks >= 1, "invalid sizes");
         require(faco::block_smem_bytes(n, 1) <= 227u * 1024u, "instance too large for one warp-ant block");
         require(w >= 1 && w <= 32 && w <= n - 1, "LS width must be in [1, min(32, n-1)]");
-        require(ls_mode == FACO_LS_TWO_OPT, "unsupported local-search mode");
+        require(ls_mode == FACO_LS_TWO_OPT || ls_mode == FACO_LS_TWO_OPT_OR_OPT, "unknown local-search mode");
         require((visits != nullptr) != (uniforms != nullptr), "give exactly one of visits or uniforms");
         if (uniforms) require(starts && primary && products && k >= 1 && k <= 32 && k <= n - 1, "roulette inputs missing");
         std::vector<std::int32_t> hxy(xy, xy + 2ull * n);
@@ -819,7 +831,8 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
                 back16.assign(backup, backup + static_cast<std::size_t>(n) * b);
             }
         }
-        std::vector<faco::node_t> t16(static_cast<std::size_t>(tasks) * n), p16(t16.size());
+        std::vector<faco::node_t> t16(static_cast<std::size_t>(tasks) * n);
+        std::vector<std::uint32_t> nbr(t16.size());
         std::vector<long long> costs(tasks);
         for (std::uint32_t t = 0; t < tasks; ++t) {
             std::vector<std::uint8_t> seen(n, 0);
@@ -828,8 +841,9 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
                 require(v < n && !seen[v], "task tour is not a permutation");
                 seen[v] = 1;
                 t16[static_cast<std::size_t>(t) * n + i] = static_cast<faco::node_t>(v);
-                p16[static_cast<std::size_t>(t) * n + v] = static_cast<faco::node_t>(i);
             }
+            const auto tn = parent_neighbours(tours + static_cast<std::size_t>(t) * n, n);
+            std::copy(tn.begin(), tn.end(), nbr.begin() + static_cast<std::size_t>(t) * n);
             costs[t] = faco::host_tour_length(hxy, tours + static_cast<std::size_t>(t) * n, n);
             if (visits) {
                 std::fill(seen.begin(), seen.end(), 0);
@@ -844,11 +858,11 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
         }
         cudaStream_t s = nullptr;
         DeviceBuffer<int2> d_xy;
-        DeviceBuffer<faco::node_t> d_ls, d_prim, d_back, d_tours, d_pos, d_visits, d_cons, d_out, d_outpos, d_sel;
+        DeviceBuffer<faco::node_t> d_ls, d_prim, d_back, d_tours, d_visits, d_cons, d_out, d_outpos, d_sel;
         DeviceBuffer<int> d_lsd;
         DeviceBuffer<long long> d_costs, d_outcosts;
         DeviceBuffer<double> d_uni;
-        DeviceBuffer<std::uint32_t> d_starts, d_targets, d_check;
+        DeviceBuffer<std::uint32_t> d_starts, d_targets, d_check, d_nbr;
         DeviceBuffer<float> d_products;
         DeviceBuffer<unsigned long long> d_counters;
         DeviceBuffer<unsigned> d_err(1);
@@ -865,7 +879,6 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
             d_products.upload(products, static_cast<std::size_t>(n) * k, s);
             v.primary = d_prim.get();
             v.backup = d_back.get();
-            std::vector<std::uint16_t> v16;
             d_uni.upload(uniforms, static_cast<std::size_t>(tasks) * n, s);
             d_starts.upload(starts, tasks, s);
         } else {
@@ -874,7 +887,7 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
         }
         d_view.upload(&v, 1, s);
         d_tours.upload(t16, s);
-        d_pos.upload(p16, s);
+        d_nbr.upload(nbr, s);
         d_costs.upload(costs, s);
         d_targets.upload(mne_targets, tasks, s);
         const std::size_t tn = static_cast<std::size_t>(tasks) * n;
@@ -890,9 +903,10 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
         L.warps = choose_warps(n, tasks);
         L.n_max = n;
         L.ls_limit = evaluation_limit;
+        L.ls_mode = ls_mode;
         L.tasks = tasks;
         L.task_tours = d_tours.get();
-        L.task_pos = d_pos.get();
+        L.task_nbr = d_nbr.get();
         L.task_costs = d_costs.get();
         L.task_visits = d_visits.get();
         L.task_uniforms = d_uni.get();
@@ -944,25 +958,31 @@ int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const u
                         float minimum, float maximum, float increment, const float* eta, float* trails,
                         float* products) {
     return guarded([&] {
-        require(primary && parent && eta && trails && products && n >= 3 && k >= 1, "invalid arguments");
-        std::vector<std::uint32_t> pos(n, UINT32_MAX);
+        require(primary && parent && eta && trails && products && n >= 3 && n <= faco::kMaxNodes && k >= 1,
+                "invalid arguments");
+        std::vector<std::uint8_t> seen(n, 0);
         for (std::uint32_t i = 0; i < n; ++i) {
-            require(parent[i] < n && pos[parent[i]] == UINT32_MAX, "parent is not a permutation");
-            pos[parent[i]] = i;
+            require(parent[i] < n && !seen[parent[i]], "parent is not a permutation");
+            seen[parent[i]] = 1;
         }
         cudaStream_t s = nullptr;
         const std::size_t cells = static_cast<std::size_t>(n) * k;
-        DeviceBuffer<std::uint32_t> d_prim, d_par, d_pos;
+        std::vector<faco::node_t> prim16(cells);
+        for (std::size_t i = 0; i < cells; ++i) {
+            require(primary[i] < n, "primary candidate out of range");
+            prim16[i] = static_cast<faco::node_t>(primary[i]);
+        }
+        DeviceBuffer<faco::node_t> d_prim;
+        DeviceBuffer<std::uint32_t> d_nbr;
         DeviceBuffer<float> d_eta, d_tr, d_pr;
-        d_prim.upload(primary, cells, s);
-        d_par.upload(parent, n, s);
-        d_pos.upload(pos, s);
+        d_prim.upload(prim16, s);
+        d_nbr.upload(parent_neighbours(parent, n), s);
         d_eta.upload(eta, cells, s);
         d_tr.upload(trails, cells, s);
         d_pr.resize(cells);
-        faco::pheromone_step_kernel<<<static_cast<unsigned>((cells + 255) / 256), 256, 0, s>>>(
-            n, k, d_prim.get(), d_par.get(), d_pos.get(), retention, minimum, maximum, increment, d_eta.get(),
-            d_tr.get(), d_pr.get());
+        faco::pheromone_step_kernel<<<static_cast<unsigned>((cells + 1023) / 1024), 256, 0, s>>>(
+            n, k, d_prim.get(), d_nbr.get(), retention, minimum, maximum, increment, d_eta.get(), d_tr.get(),
+            d_pr.get());
         cuda_check(cudaGetLastError(), "pheromone launch");
         d_tr.download(trails, cells, s);
         d_pr.download(products, cells, s);

@@ -18,6 +18,32 @@ namespace faco {
 // ---------------------------------------------------------------------------
 // Ant kernel
 // ---------------------------------------------------------------------------
+// Copies a parent tour into the warp's shared tour/inverse.  Engine parents
+// are 16-byte aligned with padded rows, so lanes move 8 nodes per load.
+__device__ __forceinline__ void load_parent(const AntSmem& s, const node_t* parent, std::uint32_t n,
+                                            std::uint32_t lane, bool aligned) {
+    if (aligned) {
+        const uint4* src = reinterpret_cast<const uint4*>(parent);
+        uint4* dst = reinterpret_cast<uint4*>(s.tour);
+        for (std::uint32_t c = lane; c * 8 < n; c += 32) {
+            const uint4 v = __ldg(src + c);
+            dst[c] = v;
+            const std::uint32_t words[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const std::uint32_t i = c * 8 + t;
+                if (i < n) s.pos[(words[t >> 1] >> (16 * (t & 1))) & 0xffffu] = (node_t)i;
+            }
+        }
+    } else {
+        for (std::uint32_t i = lane; i < n; i += 32) {
+            const std::uint32_t v = parent[i];
+            s.tour[i] = (node_t)v;
+            s.pos[v] = (node_t)i;
+        }
+    }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -41,12 +67,9 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
     __syncthreads();
     if (!active) return;
 
-    unsigned char* base = smem + ((8u * L.n_max + 15u) & ~15u) + warp * ant_smem_bytes(L.n_max);
-    const AntSmem s{reinterpret_cast<node_t*>(base), reinterpret_cast<node_t*>(base + 2 * L.n_max),
-                    reinterpret_cast<node_t*>(base + 4 * L.n_max), base + 6 * L.n_max, base + 7 * L.n_max};
-
+    const AntSmem s = AntSmem::at(smem + ((8u * L.n_max + 15u) & ~15u) + warp * ant_smem_bytes(L.n_max), L.n_max);
     const node_t* parent;
-    const node_t* parent_pos;
+    const std::uint32_t* parent_nbr;
     long long cost;
     std::uint32_t target, batch = 0;
     unsigned long long key = 0;
@@ -55,23 +78,22 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
         cv = L.colonies[colony];
         const ColonyState& st = L.states[colony];
         parent = cv.parent;
-        parent_pos = cv.parent_pos;
+        parent_nbr = cv.parent_nbr;
         cost = st.parent_cost;
         target = st.mne_target;
         batch = st.iteration;
         key = cv.key;
     } else {
         parent = L.task_tours + (size_t)task * n;
-        parent_pos = L.task_pos + (size_t)task * n;
+        parent_nbr = L.task_nbr + (size_t)task * n;
         cost = L.task_costs[task];
         target = MODE == kModePrepare ? 0 : L.task_targets[task];
     }
-    for (std::uint32_t i = lane; i < n; i += 32) {
-        const std::uint32_t v = parent[i];
-        s.tour[i] = (node_t)v;
-        s.pos[v] = (node_t)i;
+    load_parent(s, parent, n, lane, MODE == kModeEngine);
+    const std::uint32_t words = (n + 31) / 32;
+    for (std::uint32_t i = lane; i < words; i += 32) {
         s.visited[i] = 0;
-        s.queued[i] = 0;
+        s.queued[i] = MODE == kModePrepare ? ~0u : 0u;
     }
     __syncwarp();
 
@@ -84,7 +106,6 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
         // registration: every node pending, in tour order (prepared_problem.cpp:160-162)
         for (std::uint32_t i = lane; i < n; i += 32) {
             s.ring[i] = s.tour[i];
-            s.queued[i] = 1;
             if (log && i < log_cap) log[i] = s.tour[i];
         }
         q.tail = 0;
@@ -98,7 +119,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
         else if (MODE == kModeVisits) current = L.task_visits[(size_t)task * n];
         else current = L.task_starts[task];
         if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n] = (node_t)current;
-        if (lane == 0) s.visited[current] = 1;
+        if (lane == 0) s.visited[current >> 5] |= 1u << (current & 31u);
         __syncwarp();
         const float* products = MODE == kModeEngine ? cv.products : L.task_products;
         const std::uint32_t k = in.k, b = in.b;
@@ -107,41 +128,75 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
         while (r.mne < target && r.steps + 1 < n) {
             if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
             const std::uint32_t step = r.steps + 1;
+            // loads that depend only on `current`, issued first
+            const std::uint32_t pnbr = __ldg(parent_nbr + current);
+            std::uint32_t cand = n;
+            float p = 0.0f;
+            if (MODE != kModeVisits && lane < k) {
+                cand = __ldg(in.primary + (size_t)current * k + lane);
+                p = __ldg(products + (size_t)current * k + lane);
+            }
             std::uint32_t selected = n;
             if (MODE == kModeVisits) {
                 selected = L.task_visits[(size_t)task * n + step];
             } else {
-                const double u = MODE == kModeEngine ? step_uniform(key, batch, ant, step)
-                                                     : L.task_uniforms[(size_t)task * n + step];
-                std::uint32_t cand = n;
-                float p = 0.0f;
-                bool avail = false;
-                if (lane < k) {
-                    cand = in.primary[(size_t)current * k + lane];
-                    p = products[(size_t)current * k + lane];
-                    avail = cand < n && s.visited[cand] == 0;
+                std::uint32_t rhi = 0, rlo = 0;
+                double u_given = 0.0;
+                float uf;
+                if (MODE == kModeEngine) {
+                    const uint4v rb = philox4x32(step, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+                    rhi = rb.x;
+                    rlo = rb.y;
+                    uf = __uint2float_rn(rhi) * 0x1p-32f;
+                } else {
+                    u_given = L.task_uniforms[(size_t)task * n + step];
+                    uf = (float)u_given;
                 }
+                const bool avail = cand < n && !test_bit(s.visited, cand);
                 const unsigned mask = __ballot_sync(kFull, avail);
                 if (mask) {
-                    // ordered FP64 sums, exactly the reference's left-to-right prefix
-                    double total = 0.0, mine = 0.0;
-                    for (unsigned m = mask; m; m &= m - 1) {
-                        const int j = __ffs(m) - 1;
-                        total += (double)__shfl_sync(kFull, p, j);
-                        if ((int)lane == j) mine = total;
+                    // FP32 inclusive scan of the available weights.  Each prefix is
+                    // within 5 roundings (< 3.1e-7 relative) of the exact prefix, the
+                    // threshold u*total within 4.3e-7; a choice is taken only when the
+                    // first candidate not certainly below the threshold is certainly
+                    // above it by delta = total * 2^-19 (> 1.9e-6), which the FP64
+                    // ordered sums of the reference then decide identically.
+                    const float pv = avail ? p : 0.0f;
+                    float scan = pv;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const float t = __shfl_up_sync(kFull, scan, o);
+                        if ((int)lane >= o) scan += t;
                     }
-                    int j;
-                    if (total > 0.0) {
-                        const double threshold = u * total;
-                        const unsigned hit = __ballot_sync(kFull, avail && threshold < mine);
-                        j = hit ? __ffs(hit) - 1 : 31 - __clz(mask);
-                    } else {
-                        const std::uint32_t count = __popc(mask);
-                        std::uint32_t t = (std::uint32_t)(u * count);
-                        if (t >= count) t = count - 1;
-                        unsigned m = mask;
-                        for (; t; --t) m &= m - 1;
-                        j = __ffs(m) - 1;
+                    const float tot = __shfl_sync(kFull, scan, 31);
+                    int j = -1;
+                    if (tot >= 0x1p-100f) {
+                        const float thr = uf * tot, delta = tot * 0x1p-19f, diff = scan - thr;
+                        const unsigned yes = __ballot_sync(kFull, avail && diff > delta);
+                        const unsigned maybe = __ballot_sync(kFull, avail && diff >= -delta);
+                        if (maybe != 0u && (maybe & (0u - maybe)) == (yes & (0u - yes))) j = __ffs(yes) - 1;
+                    }
+                    if (j < 0) {
+                        // exact path: ordered FP64 prefix sums (faco_cpu.cpp:254-279)
+                        const double u = MODE == kModeEngine ? u53(rhi, rlo) : u_given;
+                        double total = 0.0, mine = 0.0;
+                        for (unsigned m = mask; m; m &= m - 1) {
+                            const int jj = __ffs(m) - 1;
+                            total += (double)__shfl_sync(kFull, p, jj);
+                            if ((int)lane == jj) mine = total;
+                        }
+                        if (total > 0.0) {
+                            const double threshold = u * total;
+                            const unsigned hit = __ballot_sync(kFull, avail && threshold < mine);
+                            j = hit ? __ffs(hit) - 1 : 31 - __clz(mask);
+                        } else {
+                            const std::uint32_t count = __popc(mask);
+                            std::uint32_t t = (std::uint32_t)(u * count);
+                            if (t >= count) t = count - 1;
+                            unsigned m = mask;
+                            for (; t; --t) m &= m - 1;
+                            j = __ffs(m) - 1;
+                        }
                     }
                     selected = __shfl_sync(kFull, cand, j);
                 } else {
@@ -150,8 +205,8 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
                         std::uint32_t v = n;
                         bool ok = false;
                         if (jj < b) {
-                            v = in.backup[(size_t)current * b + jj];
-                            ok = v < n && s.visited[v] == 0;
+                            v = __ldg(in.backup + (size_t)current * b + jj);
+                            ok = v < n && !test_bit(s.visited, v);
                         }
                         const unsigned m = __ballot_sync(kFull, ok);
                         if (m) selected = __shfl_sync(kFull, v, __ffs(m) - 1);
@@ -161,7 +216,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
                         unsigned long long bestkey = ~0ull;
                         const int2 cxy = xy[current];
                         for (std::uint32_t v = lane; v < n; v += 32) {
-                            if (s.visited[v]) continue;
+                            if (test_bit(s.visited, v)) continue;
                             const unsigned long long kv =
                                 ((unsigned long long)(unsigned)euc2d(cxy, xy[v]) << 32) | v;
                             bestkey = kv < bestkey ? kv : bestkey;
@@ -174,7 +229,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
                     }
                 }
             }
-            if (selected >= n || s.visited[selected]) {
+            if (selected >= n || test_bit(s.visited, selected)) {
                 // no legal choice (only an invalid explicit visit order can get here)
                 if (lane == 0) atomicOr(L.error, kErrBadChoice);
                 break;
@@ -184,11 +239,9 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
             const std::uint32_t previous = s.tour[npos == 0 ? n - 1 : npos - 1];
             const std::uint32_t after = s.tour[npos + 1 == n ? 0 : npos + 1];
             const std::uint32_t target_after = s.tour[tpos + 1 == n ? 0 : tpos + 1];
-            const std::uint32_t pp = parent_pos[current];
-            const std::uint32_t ps = parent[pp + 1 == n ? 0 : pp + 1], pq = parent[pp == 0 ? n - 1 : pp - 1];
             ++r.steps;
             __syncwarp();
-            if (lane == 0) s.visited[selected] = 1;
+            if (lane == 0) s.visited[selected >> 5] |= 1u << (selected & 31u);
             if (target_after != selected) {
                 ++r.nonidentity;
                 // six-edge delta of CpuTour::relocate, one term per lane
@@ -200,14 +253,14 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
                                                                                                         : selected;
                     const std::uint32_t e1 = lane == 0 || lane == 4 ? selected : lane == 1 || lane == 3 ? after
                                                                                                         : target_after;
-                    const int d = dist(xy, e0, e1);
+                    const int d = euc2d(xy[e0], xy[e1]);
                     term = lane < 3 ? -d : d;
                 }
                 cost += __reduce_add_sync(kFull, term);
                 relocate_shift(s, lane, tpos, npos, selected);
                 r.moved += tpos < npos ? npos - tpos : tpos - npos + 1;
             }
-            if (ps != selected && pq != selected) {
+            if ((pnbr & 0xffffu) != selected && (pnbr >> 16) != selected) {
                 ++r.mne;
                 push_absent(s, q, n, current, lane, log, log_cap);
                 push_absent(s, q, n, selected, lane, log, log_cap);
@@ -223,15 +276,17 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLa
     }
     // ---------------- local search ----------------
     long long gain_sum = 0;
-    checklist_two_opt(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
+    if (L.ls_mode == 1) checklist_ls_first(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
+    else checklist_two_opt(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
     r.final_cost = cost + gain_sum;
     r.checklist = q.pushed;
     if (log && q.pushed > log_cap && lane == 0) atomicOr(L.error, kErrQueueOverflow);
     __syncwarp();
 
     if (MODE == kModeEngine) {
-        node_t* out = cv.ant_tours + (size_t)ant * n;
-        for (std::uint32_t i = lane; i < n; i += 32) out[i] = s.tour[i];
+        uint4* out = reinterpret_cast<uint4*>(cv.ant_tours + (size_t)ant * cv.n_pad);
+        const uint4* src = reinterpret_cast<const uint4*>(s.tour);
+        for (std::uint32_t c = lane; c * 8 < n; c += 32) out[c] = src[c];
         if (lane == 0) {
             cv.ant_costs[ant] = r.final_cost;
             cv.ant_counts[3 * ant] = r.steps;
@@ -320,13 +375,55 @@ __global__ void colony_init_kernel(const InstanceView* instances, const ColonyVi
     for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         const node_t v = in.initial[i];
         cv.parent[i] = cv.epoch[i] = cv.global[i] = v;
-        cv.parent_pos[v] = (node_t)i;
+        cv.parent_nbr[v] = (std::uint32_t)in.initial[i + 1 == n ? 0 : i + 1] |
+                           ((std::uint32_t)in.initial[i == 0 ? n - 1 : i - 1] << 16);
     }
     __syncthreads();
     const float tmax = s_tmax;
     for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
         cv.trails[i] = tmax;
         cv.products[i] = tmax * in.eta[i];
+    }
+}
+
+// MMAS evaporate/deposit on FP32 trails (cuda/colony_state.cuh:210-229):
+// tau <- max(tau_min, tau * retention); a directed candidate entry (from, to)
+// on the parent tour also gains min(tau_max, tau + 1/parent_cost); products
+// are refreshed as tau * eta.  The parent-edge test reads the packed parent
+// neighbours of `from`.  Threads stride over entries, four at a time when the
+// row width allows 16-byte accesses.
+__device__ __forceinline__ float trail_value(float tau, std::uint32_t to, std::uint32_t nb, float ret, float tmin,
+                                             float tmax, float inc) {
+    float v = fmaxf(tmin, tau * ret);
+    if (to == (nb & 0xffffu) || to == (nb >> 16)) v = fminf(tmax, v + inc);
+    return v;
+}
+
+__device__ __forceinline__ void trail_update(std::uint32_t n, std::uint32_t k, const node_t* primary,
+                                             const std::uint32_t* nbr, float ret, float tmin, float tmax, float inc,
+                                             const float* eta, float* trails, float* products, std::uint32_t first,
+                                             std::uint32_t stride) {
+    const std::uint32_t cells = n * k;
+    if ((k & 3u) == 0) {
+        for (std::uint32_t q = first; q * 4 < cells; q += stride) {
+            const std::uint32_t idx = q * 4, nb = nbr[idx / k];
+            const float4 t = *reinterpret_cast<const float4*>(trails + idx);
+            const float4 e = *reinterpret_cast<const float4*>(eta + idx);
+            const uint2 pr = *reinterpret_cast<const uint2*>(primary + idx);
+            float4 v;
+            v.x = trail_value(t.x, pr.x & 0xffffu, nb, ret, tmin, tmax, inc);
+            v.y = trail_value(t.y, pr.x >> 16, nb, ret, tmin, tmax, inc);
+            v.z = trail_value(t.z, pr.y & 0xffffu, nb, ret, tmin, tmax, inc);
+            v.w = trail_value(t.w, pr.y >> 16, nb, ret, tmin, tmax, inc);
+            *reinterpret_cast<float4*>(trails + idx) = v;
+            *reinterpret_cast<float4*>(products + idx) = make_float4(v.x * e.x, v.y * e.y, v.z * e.z, v.w * e.w);
+        }
+    } else {
+        for (std::uint32_t idx = first; idx < cells; idx += stride) {
+            const float v = trail_value(trails[idx], primary[idx], nbr[idx / k], ret, tmin, tmax, inc);
+            trails[idx] = v;
+            products[idx] = v * eta[idx];
+        }
     }
 }
 
@@ -407,42 +504,28 @@ __global__ void __launch_bounds__(512) colony_update_kernel(const InstanceView* 
         s_inc = (float)(1.0 / (double)st.parent_cost);
     }
     __syncthreads();
-    const node_t* best_tour = cv.ant_tours + (size_t)s_best * n;
+    const node_t* best_tour = cv.ant_tours + (size_t)s_best * cv.n_pad;
     const bool ie = s_improve_epoch, ig = s_improve_global, fe = s_from_epoch;
     for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         const node_t v = best_tour[i];
         if (ie) cv.epoch[i] = v;
         if (ig) cv.global[i] = v;
-        const node_t src = fe ? cv.epoch[i] : v;
-        cv.parent[i] = src;
-        cv.parent_pos[src] = (node_t)i;
+        cv.parent[i] = fe ? cv.epoch[i] : v;
     }
     __syncthreads();
-    const float tmin = s_tmin, tmax = s_tmax, inc = s_inc, ret = P.retention_f;
-    for (std::uint32_t idx = threadIdx.x; idx < n * k; idx += blockDim.x) {
-        const std::uint32_t from = idx / k;
-        const std::uint32_t pp = cv.parent_pos[from];
-        const std::uint32_t to = in.primary[idx];
-        const std::uint32_t sn = cv.parent[pp + 1 == n ? 0 : pp + 1], pn = cv.parent[pp == 0 ? n - 1 : pp - 1];
-        float v = fmaxf(tmin, cv.trails[idx] * ret);
-        if (to == sn || to == pn) v = fminf(tmax, v + inc);
-        cv.trails[idx] = v;
-        cv.products[idx] = v * in.eta[idx];
-    }
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
+                                      ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
+    __syncthreads();
+    trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, in.eta, cv.trails,
+                 cv.products, threadIdx.x, blockDim.x);
 }
 
-__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const std::uint32_t* primary,
-                                      const std::uint32_t* parent, const std::uint32_t* parent_pos, float ret,
-                                      float tmin, float tmax, float inc, const float* eta, float* trails,
-                                      float* products) {
-    const std::uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * k) return;
-    const std::uint32_t from = idx / k, pp = parent_pos[from], to = primary[idx];
-    const std::uint32_t sn = parent[pp + 1 == n ? 0 : pp + 1], pn = parent[pp == 0 ? n - 1 : pp - 1];
-    float v = fmaxf(tmin, trails[idx] * ret);
-    if (to == sn || to == pn) v = fminf(tmax, v + inc);
-    trails[idx] = v;
-    products[idx] = v * eta[idx];
+__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
+                                      const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
+                                      const float* eta, float* trails, float* products) {
+    trail_update(n, k, primary, parent_nbr, ret, tmin, tmax, inc, eta, trails, products,
+                 blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ---------------------------------------------------------------------------

@@ -37,10 +37,9 @@ __global__ void colony_init_kernel(const InstanceView* instances, const ColonyVi
 __global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,
                                      ColonyState* states, ColonyParams P, TraceRow* trace,
                                      std::uint32_t colony_count, std::uint32_t trace_cap);
-__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const std::uint32_t* primary,
-                                      const std::uint32_t* parent, const std::uint32_t* parent_pos, float ret,
-                                      float tmin, float tmax, float inc, const float* eta, float* trails,
-                                      float* products);
+__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
+                                      const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
+                                      const float* eta, float* trails, float* products);
 __global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
                              const std::uint32_t* masks, float* scores, std::int32_t* actions,
                              std::uint32_t colonies);

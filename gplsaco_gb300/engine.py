@@ -293,7 +293,8 @@ def score_cuda(programs, features, masks) -> dict:
 
 
 def ant_diagnostic(xy, ls_rows, tours, mne_targets, evaluation_limit, *, visits=None, uniforms=None, starts=None,
-                   primary=None, products=None, backup=None, checklist_capacity=None) -> dict:
+                   primary=None, products=None, backup=None, checklist_capacity=None,
+                   ls_mode: int = _lib.FACO_LS_TWO_OPT) -> dict:
     """cuda_faco_diagnostic (cpp/include/gp_faco/faco_cuda_diagnostic.hpp:36-39):
     explicit-choice (visits) or injected-uniform construction + local search,
     one warp-ant per task."""
@@ -327,7 +328,7 @@ def ant_diagnostic(xy, ls_rows, tours, mne_targets, evaluation_limit, *, visits=
         xy.ctypes.data, n, ls_rows.ctypes.data, ls_rows.shape[1], tours.ctypes.data, arr(visits, np.uint32),
         arr(uniforms, np.float64), arr(starts, np.uint32), arr(primary, np.uint32), arr(products, np.float32), k,
         arr(backup, np.uint32) if b else None, b, targets.ctypes.data, tasks, evaluation_limit,
-        _lib.FACO_LS_TWO_OPT, C.byref(o)))
+        _exact_int(ls_mode, "ls_mode", 0, 1), C.byref(o)))
     return outs
 
 

@@ -161,6 +161,128 @@ void orc_checklist_two_opt(orc_tour_t* t, const orc_dist_t* d, const uint32_t* r
     t->cost += accumulated;
 }
 
+/* Relocation without the cost update (used to apply Or-opt moves). */
+static void relocate_order(orc_tour_t* t, uint32_t target, uint32_t node) {
+    const uint32_t p = t->pos[node], tp = t->pos[target];
+    if (tp < p) {
+        for (uint32_t i = p; i > tp + 1; --i) t->order[i] = t->order[i - 1];
+        t->order[tp + 1] = node;
+    } else {
+        for (uint32_t i = p; i < tp; ++i) t->order[i] = t->order[i + 1];
+        t->order[tp] = node;
+    }
+    const uint32_t lo = p < tp ? p : tp, hi = p < tp ? tp : p;
+    for (uint32_t i = lo; i <= hi; ++i) t->pos[t->order[i]] = i;
+}
+
+/* Checklist local search with first-improvement 2-opt and Or-opt.  The
+ * reference has no Or-opt (its LS is the best-gain 2-opt above); this is the
+ * engine's own variant, defined here:
+ *  - a popped node a first scans 2-opt moves in the same (kind, j) order and
+ *    with the same pruning and cap rules as the best-gain search, applying
+ *    the FIRST move with positive gain;
+ *  - if none, Or-opt: for L = 1, 2, 3 (n >= L + 3) the segment a..e of L
+ *    nodes following a in tour order, p = pred(a), q = succ(e), removal gain
+ *    G = d(p,a) + d(e,q) - d(p,q); candidates c of a's LS row while
+ *    d(a,c) < G, each counted as one move evaluation, c outside the segment;
+ *    (i) insert between c and c2 = succ(c) as c,a..e,c2 (c2 outside the
+ *    segment), gain G + d(c,c2) - d(c,a) - d(e,c2); then (ii) insert between
+ *    c0 = pred(c) and c as c0,e..a,c (c0 outside), gain G + d(c0,c) -
+ *    d(c0,e) - d(a,c); the first positive gain in (L, j, variant) order is
+ *    applied by successive relocations (c<-a<-...<-e, or c0<-e<-...<-a) and
+ *    p, a, e, q and the two insertion neighbours are queued. */
+void orc_checklist_ls_first(orc_tour_t* t, const orc_dist_t* d, const uint32_t* rows, uint32_t w,
+                            orc_queue_t* q, uint64_t cap, orc_ls_stats_t* st) {
+    int64_t accumulated = 0;
+    const uint32_t n = t->n;
+    while (q->head < q->len && st->accepted_moves < n) {
+        if (st->move_evaluations >= cap) { st->evaluation_limit_reached = 1; break; }
+        const uint32_t a = q->items[q->head++];
+        q->queued[a] = 0;
+        const uint32_t an = succ(t, a), ap = pred(t, a);
+        ++st->processed_nodes;
+        int interrupted = 0, found = 0;
+        int64_t gain = 0;
+        uint32_t move[6] = {0, 0, 0, 0, 0, 0};
+        for (int kind = 0; kind < 2 && !interrupted && !found; ++kind) {
+            const int64_t current = kind == 0 ? orc_distance(d, a, an) : orc_distance(d, ap, a);
+            const uint32_t closing_end = kind == 0 ? an : ap;
+            for (uint32_t j = 0; j < w; ++j) {
+                const uint32_t b = rows[(size_t)a * w + j];
+                ++st->candidate_checks;
+                if (b >= n) break;
+                const int64_t ab = orc_distance(d, a, b);
+                if (!(current > ab)) break;
+                if (st->move_evaluations == cap) { interrupted = 1; break; }
+                ++st->move_evaluations;
+                const uint32_t nb = kind == 0 ? succ(t, b) : pred(t, b);
+                const int64_t g = (nb == a || b == closing_end)
+                    ? 0 : current + orc_distance(d, b, nb) - ab - orc_distance(d, closing_end, nb);
+                if (g > 0) {
+                    gain = g; found = 1;
+                    if (kind == 0) { move[0] = an; move[1] = nb; move[2] = a; move[3] = b; }
+                    else { move[0] = a; move[1] = b; move[2] = ap; move[3] = nb; }
+                    break;
+                }
+            }
+        }
+        if (interrupted) { st->evaluation_limit_reached = 1; break; }
+        if (found) {
+            orc_flip(t, move[0], move[1]);
+            for (int i = 0; i < 4; ++i) orc_queue_push_absent(q, move[i], &st->reactivations);
+            ++st->accepted_moves;
+            accumulated -= gain;
+            continue;
+        }
+        uint32_t seg[3] = {a, 0, 0}, variant = 0, L = 0, cj = 0, cn = 0;
+        for (uint32_t len = 1; len <= 3 && !found && !interrupted; ++len) {
+            if (n < len + 3) break;
+            if (len > 1) seg[len - 1] = succ(t, seg[len - 2]);
+            const uint32_t e = seg[len - 1], qn = succ(t, e);
+            const int64_t G = orc_distance(d, ap, a) + orc_distance(d, e, qn) - orc_distance(d, ap, qn);
+            for (uint32_t j = 0; j < w; ++j) {
+                const uint32_t c = rows[(size_t)a * w + j];
+                ++st->candidate_checks;
+                if (c >= n) break;
+                const int64_t ac = orc_distance(d, a, c);
+                if (!(G > ac)) break;
+                if (st->move_evaluations == cap) { interrupted = 1; break; }
+                ++st->move_evaluations;
+                int inside = 0;
+                for (uint32_t i = 0; i < len; ++i) inside |= seg[i] == c;
+                if (inside) continue;
+                const uint32_t c2 = succ(t, c), c0 = pred(t, c);
+                int c2_in = 0, c0_in = 0;
+                for (uint32_t i = 0; i < len; ++i) { c2_in |= seg[i] == c2; c0_in |= seg[i] == c0; }
+                if (!c2_in) {
+                    const int64_t g = G + orc_distance(d, c, c2) - ac - orc_distance(d, e, c2);
+                    if (g > 0) { gain = g; found = 1; variant = 1; L = len; cj = c; cn = c2; break; }
+                }
+                if (!c0_in) {
+                    const int64_t g = G + orc_distance(d, c0, c) - orc_distance(d, c0, e) - ac;
+                    if (g > 0) { gain = g; found = 1; variant = 2; L = len; cj = c; cn = c0; break; }
+                }
+            }
+        }
+        if (interrupted) { st->evaluation_limit_reached = 1; break; }
+        if (found) {
+            const uint32_t e = seg[L - 1], qn = succ(t, e);
+            if (variant == 1) {
+                relocate_order(t, cj, seg[0]);
+                for (uint32_t i = 1; i < L; ++i) relocate_order(t, seg[i - 1], seg[i]);
+            } else {
+                relocate_order(t, cn, e);
+                for (uint32_t i = L - 1; i > 0; --i) relocate_order(t, seg[i], seg[i - 1]);
+            }
+            const uint32_t order6[6] = {ap, a, e, qn, variant == 1 ? cj : cn, variant == 1 ? cn : cj};
+            for (int i = 0; i < 6; ++i) orc_queue_push_absent(q, order6[i], &st->reactivations);
+            ++st->accepted_moves;
+            accumulated -= gain;
+        }
+    }
+    t->cost += accumulated;
+}
+
 /* select_next (faco_cpu.cpp:247-294) with the device's visiting order
  * (cuda/faco_choices.cuh:86-142): ordered FP64 prefix sums. */
 uint32_t orc_select_next(uint32_t current, const uint32_t* primary, const double* products, uint32_t k,
@@ -211,7 +333,7 @@ uint32_t orc_select_next(uint32_t current, const uint32_t* primary, const double
 /* One ant: FocusedConstruction (faco_cpu.cpp:219-245) then the checklist
  * 2-opt on the construction's checklist (tests/cpp/test_fixed_faco.cpp:235-256). */
 int orc_ant(const uint32_t* parent, const orc_dist_t* d, const uint32_t* ls_rows, uint32_t w,
-            const orc_choices_t* ch, uint32_t mne_target, uint64_t max_evaluations,
+            const orc_choices_t* ch, uint32_t mne_target, uint64_t max_evaluations, uint32_t ls_mode,
             uint32_t* construction_tour, uint32_t* tour, uint32_t* pos, uint32_t* checklist,
             uint32_t* selected, orc_ant_info_t* info) {
     const uint32_t n = d->n;
@@ -264,7 +386,8 @@ int orc_ant(const uint32_t* parent, const orc_dist_t* d, const uint32_t* ls_rows
     }
     if (construction_tour) memcpy(construction_tour, tour, sizeof(uint32_t) * n);
     info->construction_cost = t.cost;
-    orc_checklist_two_opt(&t, d, ls_rows, w, &q, max_evaluations, &info->ls);
+    if (ls_mode == 1) orc_checklist_ls_first(&t, d, ls_rows, w, &q, max_evaluations, &info->ls);
+    else orc_checklist_two_opt(&t, d, ls_rows, w, &q, max_evaluations, &info->ls);
     info->final_cost = t.cost;
     info->checklist_len = q.len;
     const int overflow = q.overflow;
@@ -489,7 +612,8 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                 for (uint32_t s = 1; s < n; ++s) uni[s] = orc_uniform(key, batch, (uint32_t)ant, s);
                 const orc_choices_t ch = {NULL, uni, orc_start_node(key, batch, (uint32_t)ant, n), primary,
                                           products, NULL, k, backup, c->b};
-                if (orc_ant(parent, &d, ls, c->w, &ch, c->mne_target, c->ls_evaluation_limit, NULL, ptour, ppos,
+                if (orc_ant(parent, &d, ls, c->w, &ch, c->mne_target, c->ls_evaluation_limit, c->ls_mode, NULL,
+                            ptour, ppos,
                             NULL, NULL, &infos[ant]) != 0)
                     failed = 1;
                 memcpy(tours + (size_t)ant * n, ptour, sizeof(uint32_t) * n);

@@ -68,6 +68,9 @@ typedef struct {
  * >= n are right padding. */
 void orc_checklist_two_opt(orc_tour_t* t, const orc_dist_t* d, const uint32_t* rows, uint32_t w,
                            orc_queue_t* q, uint64_t max_evaluations, orc_ls_stats_t* st);
+/* First-improvement 2-opt + Or-opt (segments of 1-3 nodes); see the .c file. */
+void orc_checklist_ls_first(orc_tour_t* t, const orc_dist_t* d, const uint32_t* rows, uint32_t w,
+                            orc_queue_t* q, uint64_t max_evaluations, orc_ls_stats_t* st);
 
 typedef struct {
     uint32_t mne, steps, nonidentity_relocations, legal_exhausted;
@@ -105,7 +108,7 @@ typedef struct {
 /* construction_tour, tour, pos: [n]; checklist: capacity 8n+8 (may be NULL);
  * selected (optional, [n]): node chosen at each step, [0] = start. */
 int orc_ant(const uint32_t* parent, const orc_dist_t* d, const uint32_t* ls_rows, uint32_t w,
-            const orc_choices_t* ch, uint32_t mne_target, uint64_t max_evaluations,
+            const orc_choices_t* ch, uint32_t mne_target, uint64_t max_evaluations, uint32_t ls_mode,
             uint32_t* construction_tour, uint32_t* tour, uint32_t* pos, uint32_t* checklist,
             uint32_t* selected, orc_ant_info_t* info);
 
@@ -148,6 +151,7 @@ typedef struct {
     double beta, retention, p_best, epoch_source_probability;
     uint64_t ls_evaluation_limit;
     uint32_t threads;        /* OpenMP threads over ants (1 = serial)       */
+    uint32_t ls_mode;        /* 0 best-gain 2-opt, 1 first-improvement 2-opt + Or-opt */
 } orc_run_cfg_t;
 
 typedef struct {

@@ -74,7 +74,7 @@ class RunCfg(C.Structure):
     _fields_ = [("ants", C.c_uint32), ("k", C.c_uint32), ("b", C.c_uint32), ("w", C.c_uint32),
                 ("mne_target", C.c_uint32), ("beta", C.c_double), ("retention", C.c_double),
                 ("p_best", C.c_double), ("epoch_source_probability", C.c_double),
-                ("ls_evaluation_limit", C.c_uint64), ("threads", C.c_uint32)]
+                ("ls_evaluation_limit", C.c_uint64), ("threads", C.c_uint32), ("ls_mode", C.c_uint32)]
 
 
 class IterTrace(C.Structure):
@@ -102,7 +102,7 @@ def lib():
         L.orc_euc2d.argtypes = [C.c_int64] * 4
         L.orc_ant.restype = C.c_int
         L.orc_ant.argtypes = [u32p, C.POINTER(DistT), u32p, C.c_uint32, C.POINTER(Choices), C.c_uint32,
-                              C.c_uint64, u32p, u32p, u32p, u32p, u32p, C.POINTER(AntInfo)]
+                              C.c_uint64, C.c_uint32, u32p, u32p, u32p, u32p, u32p, C.POINTER(AntInfo)]
         L.orc_select_next.restype = C.c_uint32
         L.orc_select_next.argtypes = [C.c_uint32, u32p, f64p, C.c_uint32, u32p, C.c_uint32, u8p,
                                       C.POINTER(DistT), C.c_double, C.POINTER(C.c_int)]
@@ -190,7 +190,7 @@ def distance_ordered(rows: np.ndarray, matrix: np.ndarray) -> np.ndarray:
 
 
 def ant(parent, ls_rows, mne_target, cap, *, xy=None, matrix=None, visit=None, uniforms=None, start=0,
-        primary=None, products32=None, products64=None, backup=None):
+        primary=None, products32=None, products64=None, backup=None, ls_mode=0):
     """One focused construction + checklist 2-opt.  Returns a dict."""
     parent = np.ascontiguousarray(parent, dtype=np.uint32)
     n = parent.size
@@ -213,7 +213,7 @@ def ant(parent, ls_rows, mne_target, cap, *, xy=None, matrix=None, visit=None, u
     cons_tour = np.zeros(n, np.uint32); tour = np.zeros(n, np.uint32); pos = np.zeros(n, np.uint32)
     checklist = np.zeros(8 * n + 8, np.uint32); selected = np.zeros(n, np.uint32)
     info = AntInfo()
-    rc = lib().orc_ant(parent, C.byref(d), ls_rows, w, C.byref(ch), mne_target, cap, cons_tour, tour, pos,
+    rc = lib().orc_ant(parent, C.byref(d), ls_rows, w, C.byref(ch), mne_target, cap, ls_mode, cons_tour, tour, pos,
                        checklist, selected, C.byref(info))
     if rc != 0:
         raise RuntimeError(f"oracle ant failed ({rc})")
@@ -239,10 +239,10 @@ def prepare(xy, k, b, w, initial_ls_limit=100000):
 
 
 def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, retention=0.98, p_best=0.1,
-               epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True):
+               epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True, ls_mode=0):
     xy = np.ascontiguousarray(xy, dtype=np.int32)
     n = xy.shape[0]
-    cfg = RunCfg(ants, k, b, w, mne, beta, retention, p_best, epoch_source_probability, ls_limit, threads)
+    cfg = RunCfg(ants, k, b, w, mne, beta, retention, p_best, epoch_source_probability, ls_limit, threads, ls_mode)
     tour = np.zeros(n, np.uint32)
     cost = C.c_int64()
     trace = (IterTrace * max(iterations, 1))() if want_trace else None

@@ -37,9 +37,12 @@ def _compare_ant(gpu, t, ref, ctx):
 
 @pytest.mark.parametrize("n", _cases.N_GRID)
 @pytest.mark.parametrize("metric", [0, 1, 2])
-def test_explicit_choice_construction_and_ls(api, oracle, n, metric):
+@pytest.mark.parametrize("ls_mode", [0, 1])
+def test_explicit_choice_construction_and_ls(api, oracle, n, metric, ls_mode):
     """Identical construction tour, LS tour, positions, checklist order and
-    work counters for explicit visit orders (tests/cpp/test_cuda_faco.cpp:31-104)."""
+    work counters for explicit visit orders (tests/cpp/test_cuda_faco.cpp:31-104);
+    ls_mode 0 is the reference's best-gain 2-opt, 1 the 2-opt + Or-opt
+    first-improvement variant."""
     xy = _cases.coordinates(n, metric, seed=83741 + n + metric * 1117)
     matrix = oracle.euc2d_matrix(xy)
     width = min(20, n - 1)
@@ -48,11 +51,11 @@ def test_explicit_choice_construction_and_ls(api, oracle, n, metric):
     ants = 16
     tours, visits, targets = _cases.ant_tasks(n, ants, seed=n * 31 + metric)
     for cap in _cases.CAPS:
-        gpu = api.ant_diagnostic(xy, rows, tours, targets, cap, visits=visits)
+        gpu = api.ant_diagnostic(xy, rows, tours, targets, cap, visits=visits, ls_mode=ls_mode)
         for t in range(ants):
-            ref = _oracle_ant_case(oracle, xy, ordered, tours[t], targets[t], cap, visit=visits[t])
-            _compare_ant(gpu, t, ref, f"n={n} metric={metric} cap={cap} ant={t}")
-            assert oracle.lib().orc_euc2d(0, 0, 3, 4) == 5
+            ref = _oracle_ant_case(oracle, xy, ordered, tours[t], targets[t], cap, visit=visits[t],
+                                   ls_mode=ls_mode)
+            _compare_ant(gpu, t, ref, f"n={n} metric={metric} cap={cap} ant={t} ls_mode={ls_mode}")
 
 
 def test_identity_two_opt_golden(api):
@@ -135,14 +138,15 @@ def test_scores_reference_and_extended(api, oracle):
     assert got["actions"].tolist() == [0, 31, 7]
 
 
-def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000):
+def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000, ls_mode=0):
     return api.FixedFacoSettings(ants=ants, primary_width=k, backup_width=b, ls_width=w, retention=retention,
-                                 epoch_source_probability=epoch, ls_evaluation_limit=ls_limit)
+                                 epoch_source_probability=epoch, ls_evaluation_limit=ls_limit, ls_mode=ls_mode)
 
 
-@pytest.mark.parametrize("n,ants,iterations,variant", [(7, 4, 8, 0), (17, 8, 8, 1), (100, 32, 20, 2),
-                                                       (500, 16, 6, 3), (1000, 32, 4, 0)])
-def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant):
+@pytest.mark.parametrize("n,ants,iterations,variant,ls_mode", [
+    (7, 4, 8, 0, 0), (17, 8, 8, 1, 0), (100, 32, 20, 2, 0), (500, 16, 6, 3, 0), (1000, 32, 4, 0, 0),
+    (17, 8, 8, 1, 1), (100, 32, 20, 2, 1), (1000, 32, 4, 0, 1)])
+def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode):
     """Whole plain-FACO runs: registration rows and initial tour, every
     iteration's best/global/parent costs and trail bounds, the final global
     tour and the FP32 trails agree bit-for-bit with the oracle."""
@@ -151,7 +155,7 @@ def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant):
     retention = (0.25, 0.5, 0.75, 0.98)[variant]
     epoch = (0.0, 0.01, 1.0, 0.3)[variant]
     xy = _cases.uniform_instance(n, seed=4703 + n)
-    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000)
+    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000, ls_mode)
     engine = api.FacoBatchEngine(n, 3, settings)
     info = engine.register_problem(n + 8999, xy.astype(np.float64))
     kk, bb, ww = min(k, n - 1), min(b, n - 1 - min(k, n - 1)), min(20, n - 1)
@@ -167,7 +171,8 @@ def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant):
     for c in range(3):
         key = oracle.lib().orc_colony_key(int(seeds[c]), n + 8999)
         ref = oracle.run_colony(xy, prep, ants=ants, k=kk, b=bb, w=ww, mne=8, iterations=iterations, key=key,
-                                retention=retention, epoch_source_probability=epoch, ls_limit=5000)
+                                retention=retention, epoch_source_probability=epoch, ls_limit=5000,
+                                ls_mode=ls_mode)
         assert res["items"][c]["cost"] == ref["cost"]
         assert res["items"][c]["tour"] == ref["tour"].tolist()
         for it in range(iterations):
