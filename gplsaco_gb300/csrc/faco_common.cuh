@@ -25,13 +25,16 @@ enum DeviceError : unsigned {
 // m*m - m < s <= m*m + m (m > 0) -- found from an FP32 estimate and at most
 // a few exact int64 corrections.  Equal to floor(sqrt((double)s) + 0.5) for
 // every |coordinate| < 2^26.
+// The estimate comes from 32-bit dx, dy in FP32 (GB300 runs 64-bit
+// integer/float conversions on its narrow FP64 pipe, so none are used).
 __device__ __forceinline__ int euc2d(int2 p, int2 q) {
-    const long long dx = (long long)p.x - q.x, dy = (long long)p.y - q.y;
-    const long long s = dx * dx + dy * dy;
-    long long m = __float2ll_rn(sqrtf((float)s));
-    while (s > m * m + m) ++m;
-    while (m > 0 && s <= m * m - m) --m;
-    return (int)m;
+    const int dx = p.x - q.x, dy = p.y - q.y;  // |dx|, |dy| < 2^27
+    const float fx = (float)dx, fy = (float)dy;
+    int m = __float2int_rn(sqrtf(fx * fx + fy * fy));
+    const long long s = (long long)dx * dx + (long long)dy * dy;
+    while (s > (long long)m * m + m) ++m;
+    while (m > 0 && s <= (long long)m * m - m) --m;
+    return m;
 }
 
 // Philox4x32 with 10 rounds (Salmon, Moraes, Dror, Shaw, SC'11).

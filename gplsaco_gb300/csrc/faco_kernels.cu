@@ -45,7 +45,7 @@ __device__ __forceinline__ void load_parent(const AntSmem& s, const node_t* pare
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) ant_kernel(const AntLaunch L) {
+__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_kernel(const AntLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     std::uint32_t colony = 0, ant = 0, task = 0;

@@ -8,7 +8,10 @@
 
 namespace faco {
 
-constexpr std::uint32_t kMaxWarpsPerBlock = 8;
+// Ants (warps) per block of the ant kernel, and the resident blocks per SM the
+// register budget is sized for (6 x 4 warps x 85 registers fills the file).
+constexpr std::uint32_t kMaxWarpsPerBlock = 4;
+constexpr std::uint32_t kAntBlocksPerSM = 6;
 
 // Device mirror of faco_program (include/faco_gb300.h).
 struct Program {
