@@ -26,7 +26,7 @@ EXPORTED = (
     "faco_default_settings", "faco_last_error", "faco_engine_create", "faco_engine_destroy",
     "faco_register_problem", "faco_problem_rows", "faco_evaluate", "faco_validate_program", "faco_score",
     "faco_ant_diagnostic", "faco_pheromone_step", "faco_begin", "faco_step", "faco_step_timed", "faco_finish",
-    "faco_engine_stream",
+    "faco_engine_stream", "faco_evaluate_programs",
 )
 
 
@@ -117,6 +117,8 @@ def load():
                                       C.c_uint32, vp, C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(AntOutputs)]
     L.faco_pheromone_step.argtypes = [C.c_uint32, C.c_uint32, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float,
                                       vp, vp, vp]
+    L.faco_evaluate_programs.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint64, vp, C.c_uint32, C.c_uint32,
+                                         C.c_uint32, vp, C.c_uint32, C.POINTER(Outputs)]
     L.faco_begin.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32]
     L.faco_step.argtypes = [vp, C.c_uint32]
     L.faco_step_timed.argtypes = [vp, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]

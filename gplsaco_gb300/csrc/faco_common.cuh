@@ -84,7 +84,30 @@ struct InstanceView {
     const float* eta;              // [n][k]
     const node_t* initial;         // [n]
     long long initial_cost;
+    const node_t* region_list;     // nodes grouped by quadrant of the bounding box
+    std::uint32_t region_offsets[5];
 };
+
+// GP program (postfix IR; device mirror of faco_program).
+struct Program {
+    std::uint16_t ir_version, numeric_spec_id, feature_spec_id, length, constants_count;
+    std::uint8_t opcode[63];
+    std::uint8_t operand[63];
+    float constants[63];
+};
+
+// Start node from a start region (quadrant) when one is set and non-empty,
+// else uniform over all nodes; the same Philox draw either way.
+__device__ __forceinline__ std::uint32_t region_start(unsigned long long key, std::uint32_t batch,
+                                                      std::uint32_t ant, const InstanceView* in,
+                                                      std::uint32_t region) {
+    const uint4v r = philox4x32(0, ant, batch, 1, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+    if (region < 4) {
+        const std::uint32_t lo = in->region_offsets[region], size = in->region_offsets[region + 1] - lo;
+        if (size) return in->region_list[lo + (std::uint32_t)(((unsigned long long)r.x * size) >> 32)];
+    }
+    return (std::uint32_t)(((unsigned long long)r.x * in->n) >> 32);
+}
 
 // Per-colony mutable state (one per work item of an evaluation).
 struct ColonyState {
@@ -97,6 +120,9 @@ struct ColonyState {
     std::uint32_t mne_target;
     std::int32_t action;
     unsigned long long construction_steps, ls_evaluations, reversed_elements;
+    // controller state (GP-controlled evaluations)
+    std::uint32_t region;          // start region of the next iteration (4 = all nodes)
+    std::uint32_t restarts, last_improvement, last_restart;
 };
 
 // Per-colony constant view.
@@ -112,8 +138,11 @@ struct ColonyView {
     node_t* global;                // [n]
     node_t* ant_tours;             // [ants][n_pad] (16-byte aligned rows)
     std::uint32_t n_pad;           // row stride of ant_tours (n rounded up to 8)
-    long long* ant_costs;          // [ants]
+    long long* ant_costs;          // [ants] final (after LS)
+    long long* ant_ccosts;         // [ants] after construction
     unsigned* ant_counts;          // [ants][3]: construction steps, LS evaluations, moved elements
+    const Program* program;        // GP controller of this colony (null: plain FACO)
+    std::uint32_t action_mask;     // legal actions
 };
 
 struct TraceRow {

@@ -144,9 +144,14 @@ struct Instance {
     DeviceBuffer<faco::node_t> d_primary, d_backup, d_ls, d_initial;
     DeviceBuffer<int> d_ls_dist;
     DeviceBuffer<float> d_eta;
+    DeviceBuffer<faco::node_t> d_regions;
+    std::uint32_t region_offsets[5] = {0, 0, 0, 0, 0};
     faco::InstanceView view() const {
-        return {n, k, b, w, d_xy.get(), d_primary.get(), d_backup.get(), d_ls.get(), d_ls_dist.get(), d_eta.get(),
-                d_initial.get(), static_cast<long long>(initial_cost)};
+        faco::InstanceView v{n, k, b, w, d_xy.get(), d_primary.get(), d_backup.get(), d_ls.get(), d_ls_dist.get(),
+                             d_eta.get(), d_initial.get(), static_cast<long long>(initial_cost), d_regions.get(),
+                             {0, 0, 0, 0, 0}};
+        for (int r = 0; r < 5; ++r) v.region_offsets[r] = region_offsets[r];
+        return v;
     }
 };
 
@@ -179,7 +184,8 @@ struct faco_engine {
     DeviceBuffer<float> trails, products;
     DeviceBuffer<faco::node_t> parent, epoch, global, ant_tours;
     DeviceBuffer<std::uint32_t> parent_nbr;
-    DeviceBuffer<long long> ant_costs;
+    DeviceBuffer<long long> ant_costs, ant_ccosts;
+    DeviceBuffer<faco::Program> programs;
     DeviceBuffer<unsigned> ant_counts, error;
     DeviceBuffer<faco::ColonyState> states;
     DeviceBuffer<faco::ColonyView> colonies;
@@ -328,6 +334,9 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         inst->d_ls.upload(inst->ls, s);
         inst->d_ls_dist.upload(ls_dist, s);
         inst->d_eta.upload(eta, s);
+        std::vector<std::uint16_t> regions;
+        faco::host_regions(inst->xy, n, inst->region_offsets, regions);
+        inst->d_regions.upload(regions, s);
         // initial checklist 2-opt over the NN tour on the GPU (prepared_problem.cpp:159-162)
         std::vector<faco::node_t> tour16(nn.begin(), nn.end());
         const long long nn_cost = faco::host_tour_length(inst->xy, nn.data(), n);
@@ -422,8 +431,16 @@ void enqueue_iteration(faco_engine* e, cudaStream_t st) {
     cuda_check(cudaGetLastError(), "update launch");
 }
 
+// Controller programs of a GP-controlled evaluation (null: plain FACO).
+struct Control {
+    const faco_program* programs = nullptr;
+    std::uint32_t n_programs = 0;
+    std::uint32_t action_mask = 0xFFFFFFFFu;
+    std::uint32_t total_iterations = 1;
+};
+
 void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
-                      uint32_t mne_target, uint32_t trace_iterations) {
+                      uint32_t mne_target, uint32_t trace_iterations, const Control& control = Control{}) {
     require(e && keys && seeds, "null argument");
     require(!e->eval.active, "an evaluation is already active on this engine");
     cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
@@ -459,6 +476,20 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     e->global.resize(node_total);
     e->ant_tours.resize(ant_total);
     e->ant_costs.resize(static_cast<std::size_t>(A) * count);
+    e->ant_ccosts.resize(static_cast<std::size_t>(A) * count);
+    std::uint32_t replicas = 1;
+    if (control.programs) {
+        require(control.n_programs >= 1 && count % control.n_programs == 0,
+                "colonies must be a whole number of replicas per program");
+        require(control.action_mask != 0, "the action mask leaves no legal action");
+        for (std::uint32_t i = 0; i < control.n_programs; ++i) {
+            if (faco_validate_program(control.programs + i) != FACO_OK) throw Error(FACO_EINVAL, g_error);
+            require(control.programs[i].feature_spec_id == 3, "controllers use feature spec 3");
+        }
+        replicas = count / control.n_programs;
+        static_assert(sizeof(faco::Program) == sizeof(faco_program), "program layout");
+        e->programs.upload(reinterpret_cast<const faco::Program*>(control.programs), control.n_programs, e->stream);
+    }
     e->ant_counts.resize(3ull * A * count);
     e->states.resize(count);
     std::size_t tau_off = 0, node_off = 0, ant_off = 0;
@@ -477,6 +508,9 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         cv.global = e->global.get() + node_off;
         cv.ant_tours = e->ant_tours.get() + ant_off;
         cv.ant_costs = e->ant_costs.get() + static_cast<std::size_t>(c) * A;
+        cv.ant_ccosts = e->ant_ccosts.get() + static_cast<std::size_t>(c) * A;
+        cv.program = control.programs ? e->programs.get() + c / replicas : nullptr;
+        cv.action_mask = control.action_mask;
         cv.ant_counts = e->ant_counts.get() + 3ull * c * A;
         tau_off += (static_cast<std::size_t>(in.n) * in.k + 3) & ~std::size_t{3};
         node_off += cv.n_pad;
@@ -506,6 +540,9 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.P.retention = e->settings.retention;
     v.P.retention_f = static_cast<float>(e->settings.retention);
     v.P.epoch_source_probability = e->settings.epoch_source_probability;
+    v.P.controlled = control.programs != nullptr;
+    v.P.total_iterations = std::max<std::uint32_t>(1, control.total_iterations);
+    v.P.log2k = faco::host_log2(static_cast<float>(k_common));
     v.P.p_root = std::pow(e->settings.p_best, 1.0 / static_cast<double>(k_common));
     v.L = faco::AntLaunch{};
     v.L.instances = e->d_instances.get();
@@ -654,9 +691,12 @@ int faco_finish(faco_engine* e, faco_outputs* out) {
     });
 }
 
-int faco_evaluate(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+}  // extern "C"
+
+namespace {
+int evaluate_impl(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
                   uint64_t evaluation_limit, uint32_t mne_target, const uint64_t* checkpoint_iterations,
-                  uint32_t n_checkpoints, faco_outputs* out) {
+                  uint32_t n_checkpoints, faco_outputs* out, Control control) {
     return guarded([&] {
         require(e && keys && seeds && out, "null argument");
         std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
@@ -672,7 +712,8 @@ int faco_evaluate(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, u
                     "checkpoints must be strictly increasing");
         }
         require(n_checkpoints == 0 || out->checkpoint_tours, "checkpoint output missing");
-        begin_evaluation(e, keys, seeds, count, mne_target, out->trace ? T : 0);
+        control.total_iterations = T;
+        begin_evaluation(e, keys, seeds, count, mne_target, out->trace ? T : 0, control);
         auto& v = e->eval;
         try {
             if (n_checkpoints) e->checkpoints.resize(static_cast<std::size_t>(n_checkpoints) * v.node_total);
@@ -734,12 +775,39 @@ int faco_evaluate(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, u
 }
 
 
+}  // namespace
+
+extern "C" {
+
+int faco_evaluate(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+                  uint64_t evaluation_limit, uint32_t mne_target, const uint64_t* checkpoint_iterations,
+                  uint32_t n_checkpoints, faco_outputs* out) {
+    return evaluate_impl(e, keys, seeds, count, evaluation_limit, mne_target, checkpoint_iterations, n_checkpoints,
+                         out, Control{});
+}
+
+int faco_evaluate_programs(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+                           uint64_t evaluation_limit, const faco_program* programs, uint32_t n_programs,
+                           uint32_t action_mask, uint32_t initial_mne, const uint64_t* checkpoint_iterations,
+                           uint32_t n_checkpoints, faco_outputs* out) {
+    if (!programs || n_programs == 0) {
+        g_error = "controller programs missing";
+        return FACO_EINVAL;
+    }
+    Control control;
+    control.programs = programs;
+    control.n_programs = n_programs;
+    control.action_mask = action_mask;
+    return evaluate_impl(e, keys, seeds, count, evaluation_limit, initial_mne, checkpoint_iterations, n_checkpoints,
+                         out, control);
+}
+
 int faco_validate_program(const faco_program* p) {
     return guarded([&] {
         require(p != nullptr, "null program");
         const bool extended = p->numeric_spec_id == 2;
         require(p->ir_version == 1 && (p->numeric_spec_id == 1 || extended) &&
-                    (p->feature_spec_id == 1 || p->feature_spec_id == 2) && p->length >= 1 && p->length <= 63 &&
+                    p->feature_spec_id >= 1 && p->feature_spec_id <= 3 && p->length >= 1 && p->length <= 63 &&
                     p->constants_count <= 63,
                 "unknown version or program size out of range");
         for (int i = 0; i < p->constants_count; ++i)

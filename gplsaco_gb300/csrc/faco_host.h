@@ -6,6 +6,9 @@
 
 namespace faco {
 
+float host_log2(float x);
+void host_regions(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t offsets[5],
+                  std::vector<std::uint16_t>& list);
 std::int32_t host_euc2d(std::int64_t x0, std::int64_t y0, std::int64_t x1, std::int64_t y1);
 std::int64_t host_tour_length(const std::vector<std::int32_t>& xy, const std::uint32_t* order, std::uint32_t n);
 void host_candidates(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t k, std::uint32_t b,

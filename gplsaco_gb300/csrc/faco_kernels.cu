@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         ant = task;
         active = task < L.tasks;
     }
-    const InstanceView in = L.instances[MODE == kModeEngine ? L.colonies[colony].instance : 0];
+    const InstanceView* in_ptr = L.instances + (MODE == kModeEngine ? L.colonies[colony].instance : 0);
+    const InstanceView in = *in_ptr;
     const std::uint32_t n = in.n;
     int2* xy = reinterpret_cast<int2*>(smem);
     for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) xy[i] = in.xy[i];
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
     const node_t* parent;
     const std::uint32_t* parent_nbr;
     long long cost;
-    std::uint32_t target, batch = 0;
+    std::uint32_t target, batch = 0, region = 4;
     unsigned long long key = 0;
     ColonyView cv{};
     if (MODE == kModeEngine) {
@@ -82,6 +83,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         cost = st.parent_cost;
         target = st.mne_target;
         batch = st.iteration;
+        region = st.region;
         key = cv.key;
     } else {
         parent = L.task_tours + (size_t)task * n;
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
     } else {
         // ---------------- focused construction ----------------
         std::uint32_t current;
-        if (MODE == kModeEngine) current = start_node(key, batch, ant, n);
+        if (MODE == kModeEngine) current = region_start(key, batch, ant, in_ptr, region);
         else if (MODE == kModeVisits) current = L.task_visits[(size_t)task * n];
         else current = L.task_starts[task];
         if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n] = (node_t)current;
@@ -289,6 +291,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         for (std::uint32_t c = lane; c * 8 < n; c += 32) out[c] = src[c];
         if (lane == 0) {
             cv.ant_costs[ant] = r.final_cost;
+            cv.ant_ccosts[ant] = r.construction_cost;
             cv.ant_counts[3 * ant] = r.steps;
             cv.ant_counts[3 * ant + 1] = (unsigned)r.evaluations;
             cv.ant_counts[3 * ant + 2] = (unsigned)r.moved;
@@ -369,6 +372,7 @@ __global__ void colony_init_kernel(const InstanceView* instances, const ColonyVi
         st.default_trail = st.tau_max;
         st.mne_target = P.mne_target;
         st.action = -1;
+        st.region = 4;
         states[c] = st;
         s_tmax = st.tau_max;
     }
@@ -427,110 +431,39 @@ __device__ __forceinline__ void trail_update(std::uint32_t n, std::uint32_t k, c
     }
 }
 
-// Fused reduce_and_select + update_pheromone for one colony.
-__global__ void __launch_bounds__(512) colony_update_kernel(const InstanceView* instances,
-                                                            const ColonyView* colonies, ColonyState* states,
-                                                            ColonyParams P, TraceRow* trace,
-                                                            std::uint32_t colony_count, std::uint32_t trace_cap) {
-    const std::uint32_t c = blockIdx.x;
-    const ColonyView cv = colonies[c];
-    const InstanceView in = instances[cv.instance];
-    const std::uint32_t n = in.n, k = in.k, A = P.ants;
-    __shared__ unsigned long long s_key[32];
-    __shared__ unsigned long long s_steps[32], s_evals[32], s_moved[32];
-    __shared__ std::uint32_t s_best, s_improve_epoch, s_improve_global, s_from_epoch;
-    __shared__ float s_tmin, s_tmax, s_inc;
-
-    // iteration best: first strict minimum over ants (costs are >= 0)
-    unsigned long long best = ~0ull, steps = 0, evals = 0, moved = 0;
-    for (std::uint32_t a = threadIdx.x; a < A; a += blockDim.x) {
-        const unsigned long long key = ((unsigned long long)cv.ant_costs[a] << 16) | a;
-        best = key < best ? key : best;
-        steps += cv.ant_counts[3 * a];
-        evals += cv.ant_counts[3 * a + 1];
-        moved += cv.ant_counts[3 * a + 2];
-    }
-    for (int o = 16; o; o >>= 1) {
-        const unsigned long long other = __shfl_xor_sync(kFull, best, o);
-        best = other < best ? other : best;
-        steps += __shfl_xor_sync(kFull, steps, o);
-        evals += __shfl_xor_sync(kFull, evals, o);
-        moved += __shfl_xor_sync(kFull, moved, o);
-    }
-    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-    if (lane == 0) { s_key[warp] = best; s_steps[warp] = steps; s_evals[warp] = evals; s_moved[warp] = moved; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (std::uint32_t w = 1; w < warps; ++w) {
-            best = s_key[w] < best ? s_key[w] : best;
-            steps += s_steps[w];
-            evals += s_evals[w];
-            moved += s_moved[w];
-        }
-        ColonyState st = states[c];
-        const std::uint32_t ib = (std::uint32_t)(best & 0xffffu);
-        const long long cost = (long long)(best >> 16);
-        const bool ie = cost < st.epoch_cost, ig = cost < st.global_cost;
-        if (ie) st.epoch_cost = cost;
-        if (ig) st.global_cost = cost;
-        trail_limits(st.epoch_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
-        const bool from_epoch = source_uniform(cv.key, st.iteration) < P.epoch_source_probability;
-        st.parent_cost = from_epoch ? st.epoch_cost : cost;
-        st.iteration_best = ib;
-        st.iteration_best_cost = cost;
-        st.source_is_epoch = from_epoch;
-        st.construction_steps += steps;
-        st.ls_evaluations += evals;
-        st.reversed_elements += moved;
-        st.default_trail = fmaxf(st.tau_min, st.default_trail * P.retention_f);
-        if (trace && st.iteration < trace_cap) {
-            TraceRow& row = trace[(size_t)st.iteration * colony_count + c];
-            row.iteration_best_cost = cost;
-            row.global_cost = st.global_cost;
-            row.parent_cost = st.parent_cost;
-            row.iteration_best = ib;
-            row.source_is_epoch = from_epoch;
-            row.tau_min = st.tau_min;
-            row.tau_max = st.tau_max;
-            row.mne_target = st.mne_target;
-            row.action = st.action;
-            row.construction_steps = steps;
-            row.ls_evaluations = evals;
-        }
-        ++st.iteration;
-        states[c] = st;
-        s_best = ib; s_improve_epoch = ie; s_improve_global = ig; s_from_epoch = from_epoch;
-        s_tmin = st.tau_min; s_tmax = st.tau_max;
-        s_inc = (float)(1.0 / (double)st.parent_cost);
-    }
-    __syncthreads();
-    const node_t* best_tour = cv.ant_tours + (size_t)s_best * cv.n_pad;
-    const bool ie = s_improve_epoch, ig = s_improve_global, fe = s_from_epoch;
-    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const node_t v = best_tour[i];
-        if (ie) cv.epoch[i] = v;
-        if (ig) cv.global[i] = v;
-        cv.parent[i] = fe ? cv.epoch[i] : v;
-    }
-    __syncthreads();
-    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-        cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
-                                      ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
-    __syncthreads();
-    trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, in.eta, cv.trails,
-                 cv.products, threadIdx.x, blockDim.x);
+// ---------------------------------------------------------------------------
+// GP controller pieces (the engine's feature spec 3; the same arithmetic is
+// restated on the CPU beside the oracle colony run).
+// ---------------------------------------------------------------------------
+// log2 from the exponent and the atanh series of the mantissa,
+// m in [sqrt(2)/2, sqrt(2)): log2 m = (2/ln 2) (t + t^3/3 + t^5/5 + t^7/7),
+// t = (m-1)/(m+1).  Single-rounding FP32 operations only, so that the CPU
+// computes identical bits.
+__device__ __forceinline__ float own_log2(float x) {
+    const std::uint32_t bits = __float_as_uint(x);
+    int e = (int)((bits >> 23) & 255u) - 127;
+    float m = __uint_as_float((bits & 0x7FFFFFu) | 0x3F800000u);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    const float t = (m - 1.0f) / (m + 1.0f), t2 = t * t;
+    const float s = t * (1.0f + t2 * (0x1.555556p-2f + t2 * (0x1.99999ap-3f + t2 * 0x1.24924ap-3f)));
+    return (float)e + s * 0x1.715476p+1f;
 }
 
-__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
-                                      const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
-                                      const float* eta, float* trails, float* products) {
-    trail_update(n, k, primary, parent_nbr, ret, tmin, tmax, inc, eta, trails, products,
-                 blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+// Normalised Shannon entropy of one trail row, in units of 2^-20.
+__device__ __forceinline__ std::uint32_t row_entropy_q(const float* tau, std::uint32_t k, float log2k) {
+    float sum = 0.0f;
+    for (std::uint32_t j = 0; j < k; ++j) sum = sum + tau[j];
+    if (!(sum > 0.0f)) return 0;
+    float h = 0.0f;
+    for (std::uint32_t j = 0; j < k; ++j) {
+        const float p = tau[j] / sum;
+        if (p > 0.0f) h = h - p * own_log2(p);
+    }
+    float hn = h / log2k;
+    hn = hn < 0.0f ? 0.0f : hn > 1.0f ? 1.0f : hn;
+    return (std::uint32_t)(hn * 1048576.0f + 0.5f);
 }
 
-// ---------------------------------------------------------------------------
-// GP scoring: one warp per colony, lane = action (cuda/gp_score.cuh:64-102).
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ float apply_operation(int op, float l, float r, float t) {
     float v = 0.0f;
     switch (op) {
@@ -548,17 +481,14 @@ __device__ __forceinline__ float apply_operation(int op, float l, float r, float
     return fminf(8.0f, fmaxf(-8.0f, v));
 }
 
-__global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
-                             const std::uint32_t* masks, float* scores, std::int32_t* actions,
-                             std::uint32_t colonies) {
-    const std::uint32_t colony = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (colony >= colonies) return;
-    const Program& p = programs[colony / replicas];
+// Postfix interpreter (cuda/gp_score.cuh:64-102); feature(i) supplies terminal i.
+template <class Feature>
+__device__ __forceinline__ float eval_program(const Program& p, Feature feature) {
     float stack[16];
     int top = 0;
     for (int i = 0; i < p.length; ++i) {
         const int op = p.opcode[i];
-        if (op == 0) stack[top++] = features[((size_t)p.operand[i] * colonies + colony) * 32 + lane];
+        if (op == 0) stack[top++] = feature(p.operand[i]);
         else if (op == 1) stack[top++] = p.constants[p.operand[i]];
         else {
             const int arity = op == 7 ? 1 : op == 10 ? 3 : 2;
@@ -568,13 +498,213 @@ __global__ void score_kernel(const Program* programs, std::uint32_t replicas, co
             stack[top++] = apply_operation(op, l, r, t);
         }
     }
-    const float value = stack[0];
-    scores[(size_t)colony * 32 + lane] = value;
-    const bool legal = (masks[colony] >> lane) & 1u;
+    return stack[0];
+}
+
+// First maximum within 1e-6 among legal lanes (score_cpu rule); 32 if none.
+__device__ __forceinline__ std::uint32_t choose_action(float value, bool legal, std::uint32_t lane) {
     float maximum = legal ? value : -INFINITY;
     for (int o = 16; o; o >>= 1) maximum = fmaxf(maximum, __shfl_xor_sync(kFull, maximum, o));
-    const std::uint32_t mine = legal && maximum - value <= 1e-6f ? lane : 32u;
-    const std::uint32_t chosen = __reduce_min_sync(kFull, mine);
+    return __reduce_min_sync(kFull, legal && maximum - value <= 1e-6f ? lane : 32u);
+}
+
+__device__ __forceinline__ float clamp01(double v) { return (float)(v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v); }
+
+// Fused reduce_and_select + update_pheromone for one colony, then (GP-controlled
+// evaluations) the controller decision for the next iteration.
+__global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* instances,
+                                                            const ColonyView* colonies, ColonyState* states,
+                                                            ColonyParams P, TraceRow* trace,
+                                                            std::uint32_t colony_count, std::uint32_t trace_cap) {
+    const std::uint32_t c = blockIdx.x;
+    const ColonyView cv = colonies[c];
+    const InstanceView in = instances[cv.instance];
+    const std::uint32_t n = in.n, k = in.k, A = P.ants;
+    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    __shared__ unsigned long long s_red[6][8];
+    __shared__ ColonyState s_st;
+    __shared__ std::uint32_t s_best, s_improve_epoch, s_improve_global, s_from_epoch, s_restart;
+    __shared__ float s_tmin, s_tmax, s_inc, s_feat[7];
+    __shared__ long long s_sum_final, s_sum_cons, s_best_cost;
+    __shared__ unsigned long long s_steps, s_evals;
+    __shared__ std::uint32_t s_used_mne;
+
+    // iteration best: first strict minimum over ants (costs are >= 0); work counters
+    unsigned long long best = ~0ull, steps = 0, evals = 0, moved = 0, sum_final = 0, sum_cons = 0;
+    for (std::uint32_t a = threadIdx.x; a < A; a += blockDim.x) {
+        const unsigned long long key = ((unsigned long long)cv.ant_costs[a] << 16) | a;
+        best = key < best ? key : best;
+        steps += cv.ant_counts[3 * a];
+        evals += cv.ant_counts[3 * a + 1];
+        moved += cv.ant_counts[3 * a + 2];
+        sum_final += (unsigned long long)cv.ant_costs[a];
+        sum_cons += (unsigned long long)cv.ant_ccosts[a];
+    }
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(kFull, best, o);
+        best = other < best ? other : best;
+        steps += __shfl_xor_sync(kFull, steps, o);
+        evals += __shfl_xor_sync(kFull, evals, o);
+        moved += __shfl_xor_sync(kFull, moved, o);
+        sum_final += __shfl_xor_sync(kFull, sum_final, o);
+        sum_cons += __shfl_xor_sync(kFull, sum_cons, o);
+    }
+    if (lane == 0) {
+        s_red[0][warp] = best; s_red[1][warp] = steps; s_red[2][warp] = evals;
+        s_red[3][warp] = moved; s_red[4][warp] = sum_final; s_red[5][warp] = sum_cons;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (std::uint32_t w = 1; w < warps; ++w) {
+            best = s_red[0][w] < best ? s_red[0][w] : best;
+            steps += s_red[1][w]; evals += s_red[2][w]; moved += s_red[3][w];
+            sum_final += s_red[4][w]; sum_cons += s_red[5][w];
+        }
+        ColonyState st = states[c];
+        const std::uint32_t ib = (std::uint32_t)(best & 0xffffu);
+        const long long cost = (long long)(best >> 16);
+        const bool ie = cost < st.epoch_cost, ig = cost < st.global_cost;
+        if (ie) st.epoch_cost = cost;
+        if (ig) { st.global_cost = cost; st.last_improvement = st.iteration + 1; }
+        trail_limits(st.epoch_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
+        const bool from_epoch = source_uniform(cv.key, st.iteration) < P.epoch_source_probability;
+        st.parent_cost = from_epoch ? st.epoch_cost : cost;
+        st.iteration_best = ib;
+        st.iteration_best_cost = cost;
+        st.source_is_epoch = from_epoch;
+        st.construction_steps += steps;
+        st.ls_evaluations += evals;
+        st.reversed_elements += moved;
+        st.default_trail = fmaxf(st.tau_min, st.default_trail * P.retention_f);
+        s_st = st;
+        s_best = ib; s_improve_epoch = ie; s_improve_global = ig; s_from_epoch = from_epoch;
+        s_tmin = st.tau_min; s_tmax = st.tau_max;
+        s_inc = (float)(1.0 / (double)st.parent_cost);
+        s_sum_final = (long long)sum_final; s_sum_cons = (long long)sum_cons; s_best_cost = cost;
+        s_steps = steps; s_evals = evals; s_used_mne = st.mne_target;
+        s_restart = 0;
+    }
+    __syncthreads();
+    const node_t* best_tour = cv.ant_tours + (size_t)s_best * cv.n_pad;
+    const bool ie = s_improve_epoch, ig = s_improve_global, fe = s_from_epoch;
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const node_t v = best_tour[i];
+        if (ie) cv.epoch[i] = v;
+        if (ig) cv.global[i] = v;
+        cv.parent[i] = fe ? cv.epoch[i] : v;
+    }
+    __syncthreads();
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
+                                      ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
+    __syncthreads();
+    trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, in.eta, cv.trails,
+                 cv.products, threadIdx.x, blockDim.x);
+    std::int32_t action = -1;
+    if (P.controlled && cv.program) {
+        // mean normalised entropy of the trail rows (exact integer sum)
+        __syncthreads();
+        unsigned long long q = 0;
+        for (std::uint32_t row = threadIdx.x; row < n; row += blockDim.x)
+            q += row_entropy_q(cv.trails + (size_t)row * k, k, P.log2k);
+        for (int o = 16; o; o >>= 1) q += __shfl_xor_sync(kFull, q, o);
+        if (lane == 0) s_red[0][warp] = q;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (std::uint32_t w = 1; w < warps; ++w) q += s_red[0][w];
+            const ColonyState& st = s_st;
+            const std::uint32_t t1 = st.iteration + 1, stag = t1 - st.last_improvement, age = t1 - st.last_restart;
+            const long long b = s_best_cost;
+            s_feat[0] = (float)t1 / (float)P.total_iterations;
+            s_feat[1] = (float)stag / (float)(stag + 16);
+            s_feat[2] = clamp01((double)(s_sum_final - (long long)A * b) / ((double)A * (double)b));
+            s_feat[3] = clamp01((double)q * (1.0 / 1048576.0) / (double)n);
+            s_feat[4] = (float)st.restarts / (float)(st.restarts + 1);
+            s_feat[5] = clamp01((double)(s_sum_cons - s_sum_final) / (double)s_sum_cons * 10.0);
+            s_feat[6] = (float)age / (float)(age + 16);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const float fa7 = (float)(lane & 3) / 3.0f, fa8 = (float)((lane >> 2) & 3) / 3.0f;
+            const float fa9 = lane >= 16 ? 1.0f : 0.0f;
+            const float value = eval_program(*cv.program, [&](int i) {
+                return i < 7 ? s_feat[i] : i == 7 ? fa7 : i == 8 ? fa8 : i == 9 ? fa9 : 0.0f;
+            });
+            const std::uint32_t a = choose_action(value, (cv.action_mask >> lane) & 1u, lane);
+            if (lane == 0) {
+                const std::uint32_t chosen = a < 32 ? a : 0;
+                s_st.action = (std::int32_t)chosen;
+                s_st.mne_target = 2u << (chosen & 3u);
+                s_st.region = (chosen >> 2) & 3u;
+                if (chosen >= 16) {
+                    s_restart = 1;
+                    ++s_st.restarts;
+                    s_st.last_restart = s_st.iteration + 1;
+                    s_st.epoch_cost = s_st.global_cost;
+                    s_st.parent_cost = s_st.global_cost;
+                    trail_limits(s_st.epoch_cost, P.retention, P.p_root, k, s_st.tau_min, s_st.tau_max);
+                    s_st.default_trail = s_st.tau_max;
+                }
+            }
+        }
+        __syncthreads();
+        action = s_st.action;
+        if (s_restart) {
+            // restart: parent and epoch <- global best, trails <- tau_max
+            for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) cv.parent[i] = cv.epoch[i] = cv.global[i];
+            __syncthreads();
+            for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+                cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
+                                              ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
+            const float tmax = s_st.tau_max;
+            for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
+                cv.trails[i] = tmax;
+                cv.products[i] = tmax * in.eta[i];
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ColonyState st = s_st;
+        if (trace && st.iteration < trace_cap) {
+            TraceRow& row = trace[(size_t)st.iteration * colony_count + c];
+            row.iteration_best_cost = st.iteration_best_cost;
+            row.global_cost = st.global_cost;
+            row.parent_cost = st.parent_cost;
+            row.iteration_best = st.iteration_best;
+            row.source_is_epoch = st.source_is_epoch;
+            row.tau_min = st.tau_min;
+            row.tau_max = st.tau_max;
+            row.mne_target = s_used_mne;
+            row.action = action;
+            row.construction_steps = s_steps;
+            row.ls_evaluations = s_evals;
+        }
+        ++st.iteration;
+        states[c] = st;
+    }
+}
+
+__global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
+                                      const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
+                                      const float* eta, float* trails, float* products) {
+    trail_update(n, k, primary, parent_nbr, ret, tmin, tmax, inc, eta, trails, products,
+                 blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// GP scoring: one warp per colony, lane = action (cuda/gp_score.cuh:64-102).
+// ---------------------------------------------------------------------------
+__global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
+                             const std::uint32_t* masks, float* scores, std::int32_t* actions,
+                             std::uint32_t colonies) {
+    const std::uint32_t colony = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (colony >= colonies) return;
+    const Program& p = programs[colony / replicas];
+    const float value =
+        eval_program(p, [&](int i) { return features[((size_t)i * colonies + colony) * 32 + lane]; });
+    scores[(size_t)colony * 32 + lane] = value;
+    const std::uint32_t chosen = choose_action(value, (masks[colony] >> lane) & 1u, lane);
     if (lane == 0) actions[colony] = (std::int32_t)chosen;
 }
 

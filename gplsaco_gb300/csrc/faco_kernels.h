@@ -13,14 +13,6 @@ namespace faco {
 constexpr std::uint32_t kMaxWarpsPerBlock = 4;
 constexpr std::uint32_t kAntBlocksPerSM = 6;
 
-// Device mirror of faco_program (include/faco_gb300.h).
-struct Program {
-    std::uint16_t ir_version, numeric_spec_id, feature_spec_id, length, constants_count;
-    std::uint8_t opcode[63];
-    std::uint8_t operand[63];
-    float constants[63];
-};
-
 struct ColonyParams {
     std::uint32_t ants;
     std::uint32_t mne_target;
@@ -28,6 +20,9 @@ struct ColonyParams {
     float retention_f;
     double p_root;                   // p_best^(1/k), computed once on the host
     double epoch_source_probability;
+    std::uint32_t controlled;        // GP controllers choose MNE, start region and restarts
+    std::uint32_t total_iterations;  // T of the evaluation (iteration-fraction feature)
+    float log2k;                     // log2(k) by the engine's own log2
 };
 
 // Host-side launchers (the kernels are defined in faco_kernels.cu).

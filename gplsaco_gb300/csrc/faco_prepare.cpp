@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <stdexcept>
 #include <thread>
@@ -19,6 +20,43 @@ namespace faco {
 std::int32_t host_euc2d(std::int64_t x0, std::int64_t y0, std::int64_t x1, std::int64_t y1) {
     const std::int64_t dx = x0 - x1, dy = y0 - y1;
     return static_cast<std::int32_t>(std::floor(std::sqrt(static_cast<double>(dx * dx + dy * dy)) + 0.5));
+}
+
+// The engine's log2 (same single-rounding FP32 steps as the device's): the
+// exponent plus (2/ln 2) atanh((m-1)/(m+1)) as a 4-term series.
+float host_log2(float x) {
+    std::uint32_t bits;
+    std::memcpy(&bits, &x, 4);
+    int e = static_cast<int>((bits >> 23) & 255u) - 127;
+    const std::uint32_t mb = (bits & 0x7FFFFFu) | 0x3F800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    const float t = (m - 1.0f) / (m + 1.0f), t2 = t * t;
+    const float s = t * (1.0f + t2 * (0x1.555556p-2f + t2 * (0x1.99999ap-3f + t2 * 0x1.24924ap-3f)));
+    return static_cast<float>(e) + s * 0x1.715476p+1f;
+}
+
+// Nodes grouped by quadrant around the bounding-box centre (start regions of
+// the controller's actions); offsets[r]..offsets[r+1] index `list`.
+void host_regions(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t offsets[5],
+                  std::vector<std::uint16_t>& list) {
+    std::int64_t minx = xy[0], maxx = xy[0], miny = xy[1], maxy = xy[1];
+    for (std::uint32_t i = 0; i < n; ++i) {
+        minx = std::min<std::int64_t>(minx, xy[2 * i]); maxx = std::max<std::int64_t>(maxx, xy[2 * i]);
+        miny = std::min<std::int64_t>(miny, xy[2 * i + 1]); maxy = std::max<std::int64_t>(maxy, xy[2 * i + 1]);
+    }
+    auto quadrant = [&](std::uint32_t i) {
+        return (2 * static_cast<std::int64_t>(xy[2 * i]) >= minx + maxx ? 1u : 0u) +
+               (2 * static_cast<std::int64_t>(xy[2 * i + 1]) >= miny + maxy ? 2u : 0u);
+    };
+    std::uint32_t count[4] = {0, 0, 0, 0};
+    for (std::uint32_t i = 0; i < n; ++i) ++count[quadrant(i)];
+    offsets[0] = 0;
+    for (int r = 0; r < 4; ++r) offsets[r + 1] = offsets[r] + count[r];
+    std::uint32_t fill[4] = {offsets[0], offsets[1], offsets[2], offsets[3]};
+    list.assign(n, 0);
+    for (std::uint32_t i = 0; i < n; ++i) list[fill[quadrant(i)]++] = static_cast<std::uint16_t>(i);
 }
 
 std::int64_t host_tour_length(const std::vector<std::int32_t>& xy, const std::uint32_t* order, std::uint32_t n) {

@@ -137,12 +137,50 @@ class FacoBatchEngine:
                                   trace=False) -> dict:
         """evaluate_faco_evaluations (bindings.cpp:701-720): plain FACO with a
         constant MNE target, budget in ant-tour evaluations per colony."""
+        mne = _exact_int(mne, "mne", 1, 2**32 - 1)
+        return self._evaluate(instance_keys, seeds, evaluation_limit_per_colony, mne, preparation_mode,
+                              checkpoint_iterations, profile_events_only, trace, None, 0xFFFFFFFF)
+
+    def evaluate_program_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, program,
+                                     preparation_mode="cached", experiment_mask=0xFFFFFFFF, *,
+                                     checkpoint_iterations=(), initial_mne=8, trace=False) -> dict:
+        """evaluate_program_evaluations (bindings.cpp:721-757): every colony is
+        driven by one GP controller program (feature spec 3)."""
+        return self.evaluate_population_evaluations(instance_keys, seeds, evaluation_limit_per_colony, [program],
+                                                    experiment_mask, checkpoint_iterations=checkpoint_iterations,
+                                                    initial_mne=initial_mne, trace=trace,
+                                                    preparation_mode=preparation_mode)
+
+    def evaluate_population_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, programs,
+                                        experiment_mask=0xFFFFFFFF, *, checkpoint_iterations=(), initial_mne=8,
+                                        trace=False, preparation_mode="cached") -> dict:
+        """evaluate_population_evaluations (bindings.cpp:776-817): colony c is
+        driven by programs[c // (colonies // len(programs))]; the panel of
+        (instance, seed) tasks is given already replicated per program, in
+        individual-major order.  Returns the plain result dict plus
+        `individual_costs` [programs][replicas]."""
+        if not isinstance(programs, (list, tuple)) or not programs:
+            raise ValueError("programs must be a non-empty list of IR dicts")
+        mask = _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF)
+        mne = _exact_int(initial_mne, "initial_mne", 1, 2**32 - 1)
+        arr = (_lib.Program * len(programs))(*[program_to_c(p) for p in programs])
+        for p in arr:
+            if p.feature_spec_id != 3:
+                raise ValueError("controller programs use feature spec 3")
+        result = self._evaluate(instance_keys, seeds, evaluation_limit_per_colony, mne, preparation_mode,
+                                checkpoint_iterations, False, trace, arr, mask)
+        costs = np.array([it["cost"] for it in result["items"]], np.int64)
+        result["individual_costs"] = costs.reshape(len(programs), -1)
+        result["population_size"] = len(programs)
+        return result
+
+    def _evaluate(self, instance_keys, seeds, evaluation_limit_per_colony, mne, preparation_mode,
+                  checkpoint_iterations, profile_events_only, trace, programs, mask) -> dict:
         keys = _u64_array(instance_keys, "instance_keys")
         seeds = _u64_array(seeds, "seeds")
         if keys.size != seeds.size:
             raise ValueError("instance_keys and seeds differ in length")
         limit = _exact_int(evaluation_limit_per_colony, "evaluation_limit_per_colony")
-        mne = _exact_int(mne, "mne", 1, 2**32 - 1)
         if preparation_mode not in ("cached", "cached_charged"):
             raise ValueError("unknown preparation mode")
         if type(profile_events_only) is not bool or type(trace) is not bool:
@@ -159,8 +197,15 @@ class FacoBatchEngine:
         if not self._lock.acquire(blocking=False):
             raise RuntimeError("only one active evaluation per engine")
         try:
-            _lib.check(self._L.faco_evaluate(self._handle, keys.ctypes.data, seeds.ctypes.data, count, limit, mne,
-                                             _lib.ptr(cps) if cps.size else None, cps.size, C.byref(out)))
+            cp_ptr = _lib.ptr(cps) if cps.size else None
+            if programs is None:
+                code = self._L.faco_evaluate(self._handle, keys.ctypes.data, seeds.ctypes.data, count, limit, mne,
+                                             cp_ptr, cps.size, C.byref(out))
+            else:
+                code = self._L.faco_evaluate_programs(self._handle, keys.ctypes.data, seeds.ctypes.data, count, limit,
+                                                      C.cast(programs, C.c_void_p), len(programs), mask, mne, cp_ptr,
+                                                      cps.size, C.byref(out))
+            _lib.check(code)
         finally:
             self._lock.release()
         items = []
@@ -178,6 +223,7 @@ class FacoBatchEngine:
             "completed_batches": int(out.completed_batches),
             "completed_construction_steps": int(out.construction_steps),
             "completed_ls_evaluations": int(out.ls_evaluations),
+            "reversed_elements": int(out.reversed_elements),
             "production_kernel_milliseconds": {"iteration_loop": out.kernel_milliseconds},
             "elapsed_seconds": out.solve_seconds,
             "actual_seconds": out.solve_seconds,
@@ -191,7 +237,6 @@ class FacoBatchEngine:
         if trace:
             result["trace"] = trace_rows
         return result
-
 
     # ---- stepwise evaluation (caller-driven ant batches) -------------------
     def begin(self, instance_keys, seeds, mne=8, *, trace_iterations: int = 0) -> None:

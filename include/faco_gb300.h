@@ -53,6 +53,7 @@ void faco_default_settings(faco_settings* s);
 const char* faco_last_error(void);
 
 typedef struct faco_engine faco_engine;
+struct faco_program;
 
 /* FacoBatchEngine(dimension, colonies, settings) (bindings.cpp:558-573).
  * `dimension` is the largest instance size the engine accepts; instances of
@@ -116,6 +117,22 @@ typedef struct faco_outputs {
 int faco_evaluate(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds, uint32_t count,
                   uint64_t evaluation_limit_per_colony, uint32_t mne_target, const uint64_t* checkpoint_iterations,
                   uint32_t n_checkpoints, faco_outputs* out);
+
+/* evaluate_program_evaluations / evaluate_population_evaluations
+ * (bindings.cpp:721-757,776-817; engine cuda/batch_engine.cu:379-437,
+ * per-batch control :884-950): colony c is driven by programs[c / (count /
+ * n_programs)], a postfix program of feature spec 3 that scores the 32
+ * actions of its colony after every iteration from 7 colony features
+ * (iteration fraction, stagnation, mean/best gap, trail-row entropy,
+ * restarts, LS gain, reference-tour age) and 3 action descriptors; the first
+ * best legal action (action_mask) sets the next MNE target 2<<(a&3), the
+ * start region (a>>2)&3 and, for a >= 16, a restart from the global best with
+ * trails reset to tau_max.  initial_mne is the target of the first
+ * iteration.  Traces record the target used and the action chosen. */
+int faco_evaluate_programs(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds,
+                           uint32_t count, uint64_t evaluation_limit_per_colony, const struct faco_program* programs,
+                           uint32_t n_programs, uint32_t action_mask, uint32_t initial_mne,
+                           const uint64_t* checkpoint_iterations, uint32_t n_checkpoints, faco_outputs* out);
 
 /* The same evaluation in explicit steps (the reference's per-batch loop,
  * cuda/batch_engine.cu:875-1135, driven by the caller): faco_begin uploads the

@@ -562,6 +562,109 @@ int64_t orc_prepare(uint32_t n, const int32_t* xy, const orc_prep_cfg_t* cfg, ui
 }
 
 /* ---------------------------------------------------------------------- */
+/* GP controller of the engine (feature spec 3).  The reference scores 32   */
+/* actions per colony from 12 features (cuda/control_state.cuh:200-364);  */
+/* the engine's own set is 7 colony features + 3 action descriptors:      */
+/*  f0 iteration fraction (t+1)/T, f1 stagnation s/(s+16), f2 mean/best gap,*/
+/*  f3 mean normalised entropy of the trail rows, f4 restarts r/(r+1),     */
+/*  f5 LS gain (10x relative, clipped), f6 reference-tour age a/(a+16);     */
+/*  f7 MNE level (a&3)/3, f8 start region ((a>>2)&3)/3, f9 restart flag.    */
+/* Action a: MNE target 2<<(a&3), start region (a>>2)&3 (quadrant around  */
+/* the bounding-box centre), restart when a >= 16 (parent and epoch <- the */
+/* global best, trails <- tau_max).  Everything below is exact or single- */
+/* rounding FP32/FP64 arithmetic so that the GPU reproduces it bit for bit.*/
+/* ---------------------------------------------------------------------- */
+static int arity_of(int op);
+
+float orc_log2(float x) {
+    /* x = m 2^e, m in [sqrt(2)/2, sqrt(2)); log2 m = (2/ln 2) atanh((m-1)/(m+1)) */
+    uint32_t bits;
+    memcpy(&bits, &x, 4);
+    int e = (int)((bits >> 23) & 255u) - 127;
+    uint32_t mb = (bits & 0x7FFFFFu) | 0x3F800000u;
+    float m;
+    memcpy(&m, &mb, 4);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    const float t = (m - 1.0f) / (m + 1.0f), t2 = t * t;
+    const float s = t * (1.0f + t2 * (0x1.555556p-2f + t2 * (0x1.99999ap-3f + t2 * 0x1.24924ap-3f)));
+    return (float)e + s * 0x1.715476p+1f;
+}
+
+uint32_t orc_row_entropy_q(const float* tau, uint32_t k, float log2k) {
+    float sum = 0.0f;
+    for (uint32_t j = 0; j < k; ++j) sum = sum + tau[j];
+    if (!(sum > 0.0f)) return 0;
+    float h = 0.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        const float p = tau[j] / sum;
+        if (p > 0.0f) h = h - p * orc_log2(p);
+    }
+    float hn = h / log2k;
+    hn = hn < 0.0f ? 0.0f : hn > 1.0f ? 1.0f : hn;
+    return (uint32_t)(hn * 1048576.0f + 0.5f);
+}
+
+void orc_regions(uint32_t n, const int32_t* xy, uint32_t* offsets, uint32_t* list) {
+    int64_t minx = xy[0], maxx = xy[0], miny = xy[1], maxy = xy[1];
+    for (uint32_t i = 0; i < n; ++i) {
+        minx = xy[2 * i] < minx ? xy[2 * i] : minx; maxx = xy[2 * i] > maxx ? xy[2 * i] : maxx;
+        miny = xy[2 * i + 1] < miny ? xy[2 * i + 1] : miny; maxy = xy[2 * i + 1] > maxy ? xy[2 * i + 1] : maxy;
+    }
+    uint32_t count[4] = {0, 0, 0, 0};
+    for (uint32_t i = 0; i < n; ++i)
+        ++count[(2 * (int64_t)xy[2 * i] >= minx + maxx) + 2 * (2 * (int64_t)xy[2 * i + 1] >= miny + maxy)];
+    offsets[0] = 0;
+    for (int r = 0; r < 4; ++r) offsets[r + 1] = offsets[r] + count[r];
+    uint32_t fill[4] = {offsets[0], offsets[1], offsets[2], offsets[3]};
+    for (uint32_t i = 0; i < n; ++i)
+        list[fill[(2 * (int64_t)xy[2 * i] >= minx + maxx) + 2 * (2 * (int64_t)xy[2 * i + 1] >= miny + maxy)]++] = i;
+}
+
+uint32_t orc_region_start(uint64_t key, uint32_t batch, uint32_t ant, uint32_t n, const uint32_t* offsets,
+                          const uint32_t* list, uint32_t region) {
+    if (region >= 4 || offsets[region + 1] == offsets[region]) return orc_start_node(key, batch, ant, n);
+    uint32_t x[4];
+    orc_philox4x32(0, ant, batch, 1, (uint32_t)key, (uint32_t)(key >> 32), x);
+    const uint32_t size = offsets[region + 1] - offsets[region];
+    return list[offsets[region] + (uint32_t)(((uint64_t)x[0] * size) >> 32)];
+}
+
+static float clamp01(double v) { return (float)(v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v); }
+
+/* Scores the 32 actions of one colony from its 7 colony features and picks
+ * the first maximum within 1e-6 among legal actions (score_cpu rule). */
+int32_t orc_control_choose(const orc_program_t* p, const float colony[7], uint32_t mask, float* scores) {
+    float maximum = -INFINITY;
+    for (int a = 0; a < 32; ++a) {
+        float f[12];
+        for (int i = 0; i < 7; ++i) f[i] = colony[i];
+        f[7] = (float)(a & 3) / 3.0f;
+        f[8] = (float)((a >> 2) & 3) / 3.0f;
+        f[9] = a >= 16 ? 1.0f : 0.0f;
+        f[10] = f[11] = 0.0f;
+        float stack[16] = {0};
+        int top = 0;
+        for (int i = 0; i < p->length; ++i) {
+            const int op = p->opcode[i];
+            if (op == 0) stack[top++] = f[p->operand[i]];
+            else if (op == 1) stack[top++] = p->constants[p->operand[i]];
+            else {
+                const int ar = arity_of(op);
+                const float third = ar == 3 ? stack[--top] : 0.0f;
+                const float right = ar >= 2 ? stack[--top] : 0.0f;
+                const float left = stack[--top];
+                stack[top++] = orc_apply_operation(op, left, right, third);
+            }
+        }
+        scores[a] = stack[0];
+        if ((mask >> a) & 1u) maximum = fmaxf(maximum, stack[0]);
+    }
+    for (int a = 0; a < 32; ++a)
+        if (((mask >> a) & 1u) && maximum - scores[a] <= 1e-6f) return a;
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
 /* A whole colony in engine arithmetic: reset_colony + initialize_products */
 /* (colony_state.cuh:72-110), per batch every ant, reduce_and_select      */
 /* (:148-208) and the FP32 trail update.                                  */
@@ -570,7 +673,8 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    const uint32_t* ls, const uint32_t* initial, int64_t initial_cost,
                    const orc_run_cfg_t* c, uint64_t key, uint32_t iterations, uint32_t* global_tour,
                    int64_t* global_cost_out, orc_iter_trace_t* trace, float* trails_out,
-                   float* products_out) {
+                   float* products_out, const orc_program_t* program, uint32_t mask,
+                   uint32_t total_iterations) {
     const orc_dist_t d = {n, xy, NULL};
     const uint32_t k = c->k, A = c->ants;
     const size_t cells = (size_t)n * k;
@@ -580,13 +684,16 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     uint32_t* parent = (uint32_t*)malloc(sizeof(uint32_t) * n);
     uint32_t* epoch = (uint32_t*)malloc(sizeof(uint32_t) * n);
     uint32_t* tours = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n * A);
+    uint32_t* region_list = (uint32_t*)malloc(sizeof(uint32_t) * n);
     orc_ant_info_t* infos = (orc_ant_info_t*)malloc(sizeof(orc_ant_info_t) * A);
-    if (!eta || !trails || !products || !parent || !epoch || !tours || !infos) return -1;
+    if (!eta || !trails || !products || !parent || !epoch || !tours || !infos || !region_list) return -1;
     for (size_t i = 0; i < cells; ++i) {
         const uint32_t to = primary[i];
         const double dist = to < n ? (double)orc_distance(&d, (uint32_t)(i / k), to) : 0.0;
         eta[i] = to >= n ? 0.0f : (float)(dist > 0 ? (c->beta == 1.0 ? 1.0 / dist : 1.0 / pow(dist, c->beta)) : 1.0);
     }
+    uint32_t region_offsets[5] = {0, 0, 0, 0, 0};
+    orc_regions(n, xy, region_offsets, region_list);
     const double p_root = pow(c->p_best, 1.0 / (double)k);
     int64_t epoch_cost = initial_cost, global_cost = initial_cost;
     double tmin, tmax;
@@ -596,6 +703,8 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     memcpy(parent, initial, sizeof(uint32_t) * n);
     memcpy(epoch, initial, sizeof(uint32_t) * n);
     memcpy(global_tour, initial, sizeof(uint32_t) * n);
+    uint32_t mne = c->mne_target, region = 4, restarts = 0, last_improvement = 0, last_restart = 0;
+    const float log2k = orc_log2((float)k);
     int failed = 0;
     for (uint32_t batch = 0; batch < iterations; ++batch) {
 #ifdef _OPENMP
@@ -610,10 +719,10 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
 #endif
             for (int ant = 0; ant < (int)A; ++ant) {
                 for (uint32_t s = 1; s < n; ++s) uni[s] = orc_uniform(key, batch, (uint32_t)ant, s);
-                const orc_choices_t ch = {NULL, uni, orc_start_node(key, batch, (uint32_t)ant, n), primary,
-                                          products, NULL, k, backup, c->b};
-                if (orc_ant(parent, &d, ls, c->w, &ch, c->mne_target, c->ls_evaluation_limit, c->ls_mode, NULL,
-                            ptour, ppos,
+                const uint32_t start = orc_region_start(key, batch, (uint32_t)ant, n, region_offsets, region_list,
+                                                        region);
+                const orc_choices_t ch = {NULL, uni, start, primary, products, NULL, k, backup, c->b};
+                if (orc_ant(parent, &d, ls, c->w, &ch, mne, c->ls_evaluation_limit, c->ls_mode, NULL, ptour, ppos,
                             NULL, NULL, &infos[ant]) != 0)
                     failed = 1;
                 memcpy(tours + (size_t)ant * n, ptour, sizeof(uint32_t) * n);
@@ -622,32 +731,68 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
         }
         uint32_t best = 0;
         uint64_t steps = 0, evals = 0;
+        int64_t sum_final = 0, sum_cons = 0;
         for (uint32_t a = 0; a < A; ++a) {
             steps += infos[a].cons.steps; evals += infos[a].ls.move_evaluations;
+            sum_final += infos[a].final_cost; sum_cons += infos[a].construction_cost;
             if (infos[a].final_cost < infos[best].final_cost) best = a;
         }
         const int64_t cost = infos[best].final_cost;
         const uint32_t* best_tour = tours + (size_t)best * n;
         if (cost < epoch_cost) { epoch_cost = cost; memcpy(epoch, best_tour, sizeof(uint32_t) * n); }
-        if (cost < global_cost) { global_cost = cost; memcpy(global_tour, best_tour, sizeof(uint32_t) * n); }
+        if (cost < global_cost) {
+            global_cost = cost;
+            memcpy(global_tour, best_tour, sizeof(uint32_t) * n);
+            last_improvement = batch + 1;
+        }
         orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
         const int from_epoch = orc_source_uniform(key, batch) < c->epoch_source_probability;
-        const int64_t parent_cost = from_epoch ? epoch_cost : cost;
+        int64_t parent_cost = from_epoch ? epoch_cost : cost;
         memcpy(parent, from_epoch ? epoch : best_tour, sizeof(uint32_t) * n);
         orc_pheromone32(n, k, primary, parent, (float)c->retention, (float)tmin, (float)tmax,
                         (float)(1.0 / (double)parent_cost), eta, trails, products, &dflt);
+        const uint32_t used_mne = mne;
+        int32_t action = -1;
+        if (program) {
+            uint64_t sumq = 0;
+            for (uint32_t row = 0; row < n; ++row) sumq += orc_row_entropy_q(trails + (size_t)row * k, k, log2k);
+            const uint32_t t1 = batch + 1, stag = t1 - last_improvement, age = t1 - last_restart;
+            float f[7], scores[32];
+            f[0] = (float)t1 / (float)total_iterations;
+            f[1] = (float)stag / (float)(stag + 16);
+            f[2] = clamp01((double)(sum_final - (int64_t)A * cost) / ((double)A * (double)cost));
+            f[3] = clamp01((double)sumq * (1.0 / 1048576.0) / (double)n);
+            f[4] = (float)restarts / (float)(restarts + 1);
+            f[5] = clamp01((double)(sum_cons - sum_final) / (double)sum_cons * 10.0);
+            f[6] = (float)age / (float)(age + 16);
+            action = orc_control_choose(program, f, mask, scores);
+            mne = 2u << (action & 3);
+            region = ((uint32_t)action >> 2) & 3u;
+            if (action >= 16) {
+                ++restarts;
+                last_restart = t1;
+                memcpy(parent, global_tour, sizeof(uint32_t) * n);
+                memcpy(epoch, global_tour, sizeof(uint32_t) * n);
+                epoch_cost = global_cost;
+                parent_cost = global_cost;
+                orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
+                for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * eta[i]; }
+                dflt = (float)tmax;
+            }
+        }
         if (trace) {
             orc_iter_trace_t* r = &trace[batch];
             r->iteration_best_cost = cost; r->global_cost = global_cost; r->parent_cost = parent_cost;
             r->iteration_best = best; r->source_is_epoch = (uint32_t)from_epoch;
             r->tau_min = (float)tmin; r->tau_max = (float)tmax;
+            r->mne_target = used_mne; r->action = action;
             r->construction_steps = steps; r->ls_evaluations = evals;
         }
     }
     *global_cost_out = global_cost;
     if (trails_out) memcpy(trails_out, trails, sizeof(float) * cells);
     if (products_out) memcpy(products_out, products, sizeof(float) * cells);
-    free(eta); free(trails); free(products); free(parent); free(epoch); free(tours); free(infos);
+    free(eta); free(trails); free(products); free(parent); free(epoch); free(tours); free(infos); free(region_list);
     return failed ? -2 : 0;
 }
 
@@ -679,7 +824,7 @@ static int arity_of(int op) { return op == 7 ? 1 : op == 10 ? 3 : 2; }
 int orc_validate_program(const orc_program_t* p) {
     const int extended = p->numeric_spec_id == 2;
     if (p->ir_version != 1 || (p->numeric_spec_id != 1 && !extended) ||
-        (p->feature_spec_id != 1 && p->feature_spec_id != 2) || p->length == 0 || p->length > 63 ||
+        (p->feature_spec_id < 1 || p->feature_spec_id > 3) || p->length == 0 || p->length > 63 ||
         p->constants_count > 63)
         return -1;
     for (int i = 0; i < p->constants_count; ++i)

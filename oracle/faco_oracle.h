@@ -24,6 +24,8 @@
 extern "C" {
 #endif
 
+struct orc_program;
+
 /* ---- distances ---------------------------------------------------------- */
 typedef struct {
     uint32_t n;
@@ -158,6 +160,8 @@ typedef struct {
     int64_t iteration_best_cost, global_cost, parent_cost;
     uint32_t iteration_best, source_is_epoch;
     float tau_min, tau_max;
+    uint32_t mne_target;
+    int32_t action;
     uint64_t construction_steps, ls_evaluations;
 } orc_iter_trace_t;
 
@@ -167,10 +171,11 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    const uint32_t* ls, const uint32_t* initial, int64_t initial_cost,
                    const orc_run_cfg_t* cfg, uint64_t key, uint32_t iterations,
                    uint32_t* global_tour, int64_t* global_cost, orc_iter_trace_t* trace,
-                   float* trails_out, float* products_out);
+                   float* trails_out, float* products_out, const struct orc_program* program, uint32_t mask,
+                   uint32_t total_iterations);
 
 /* ---- GP controller scoring (postfix IR) --------------------------------- */
-typedef struct {
+typedef struct orc_program {
     uint16_t ir_version, numeric_spec_id, feature_spec_id, length, constants_count;
     uint8_t opcode[63];
     uint8_t operand[63];
@@ -182,6 +187,14 @@ int orc_validate_program(const orc_program_t* p);
 /* features [F][C][32] (feature-major), masks [C] -> scores [C][32], actions [C]. */
 void orc_score(const orc_program_t* p, uint32_t features_count, const float* features,
                const uint32_t* masks, uint32_t colonies, float* scores, int32_t* actions);
+
+/* ---- the engine's GP controller (feature spec 3; see the .c file) -------- */
+float orc_log2(float x);
+uint32_t orc_row_entropy_q(const float* tau, uint32_t k, float log2k);
+void orc_regions(uint32_t n, const int32_t* xy, uint32_t* offsets, uint32_t* list);
+uint32_t orc_region_start(uint64_t key, uint32_t batch, uint32_t ant, uint32_t n, const uint32_t* offsets,
+                          const uint32_t* list, uint32_t region);
+int32_t orc_control_choose(const orc_program_t* p, const float colony[7], uint32_t mask, float* scores);
 
 #ifdef __cplusplus
 }

@@ -80,7 +80,8 @@ class RunCfg(C.Structure):
 class IterTrace(C.Structure):
     _fields_ = [("iteration_best_cost", C.c_int64), ("global_cost", C.c_int64), ("parent_cost", C.c_int64),
                 ("iteration_best", C.c_uint32), ("source_is_epoch", C.c_uint32), ("tau_min", C.c_float),
-                ("tau_max", C.c_float), ("construction_steps", C.c_uint64), ("ls_evaluations", C.c_uint64)]
+                ("tau_max", C.c_float), ("mne_target", C.c_uint32), ("action", C.c_int32),
+                ("construction_steps", C.c_uint64), ("ls_evaluations", C.c_uint64)]
 
 
 class Program(C.Structure):
@@ -126,7 +127,14 @@ def lib():
         L.orc_run_colony.restype = C.c_int
         L.orc_run_colony.argtypes = [C.c_uint32, i32p, u32p, u32p, u32p, u32p, C.c_int64, C.POINTER(RunCfg),
                                      C.c_uint64, C.c_uint32, u32p, C.POINTER(C.c_int64), C.c_void_p,
-                                     C.c_void_p, C.c_void_p]
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]
+        L.orc_log2.restype = C.c_float
+        L.orc_log2.argtypes = [C.c_float]
+        L.orc_row_entropy_q.restype = C.c_uint32
+        L.orc_row_entropy_q.argtypes = [f32p, C.c_uint32, C.c_float]
+        L.orc_regions.argtypes = [C.c_uint32, i32p, u32p, u32p]
+        L.orc_control_choose.restype = C.c_int32
+        L.orc_control_choose.argtypes = [C.POINTER(Program), f32p, C.c_uint32, f32p]
         L.orc_validate_program.restype = C.c_int
         L.orc_validate_program.argtypes = [C.POINTER(Program)]
         L.orc_score.argtypes = [C.POINTER(Program), C.c_uint32, f32p, u32p, C.c_uint32, f32p, i32p]
@@ -239,7 +247,8 @@ def prepare(xy, k, b, w, initial_ls_limit=100000):
 
 
 def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, retention=0.98, p_best=0.1,
-               epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True, ls_mode=0):
+               epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True, ls_mode=0,
+               program=None, mask=0xFFFFFFFF, total_iterations=None):
     xy = np.ascontiguousarray(xy, dtype=np.int32)
     n = xy.shape[0]
     cfg = RunCfg(ants, k, b, w, mne, beta, retention, p_best, epoch_source_probability, ls_limit, threads, ls_mode)
@@ -248,12 +257,15 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
     trace = (IterTrace * max(iterations, 1))() if want_trace else None
     trails = np.zeros(n * k, np.float32); products = np.zeros(n * k, np.float32)
     backup = np.ascontiguousarray(prep["backup"] if b else np.zeros((n, 1), np.uint32), dtype=np.uint32)
+    pstruct = program_struct(program) if program is not None else None
     rc = lib().orc_run_colony(n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
                               np.ascontiguousarray(prep["ls"], dtype=np.uint32),
                               np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),
                               key, iterations, tour, C.byref(cost),
                               C.cast(trace, C.c_void_p) if trace is not None else None,
-                              trails.ctypes.data, products.ctypes.data)
+                              trails.ctypes.data, products.ctypes.data,
+                              C.cast(C.pointer(pstruct), C.c_void_p) if pstruct is not None else None, mask,
+                              total_iterations or iterations)
     if rc != 0:
         raise RuntimeError(f"oracle colony run failed ({rc})")
     rows = None
@@ -261,6 +273,7 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
         rows = [dict(iteration_best_cost=t.iteration_best_cost, global_cost=t.global_cost,
                      parent_cost=t.parent_cost, iteration_best=t.iteration_best,
                      source_is_epoch=t.source_is_epoch, tau_min=t.tau_min, tau_max=t.tau_max,
+                     mne_target=t.mne_target, action=t.action,
                      construction_steps=t.construction_steps, ls_evaluations=t.ls_evaluations)
                 for t in trace[:iterations]]
     return dict(tour=tour, cost=int(cost.value), trace=rows, trails=trails.reshape(n, k),

@@ -29,7 +29,7 @@ def _stack_peak(code, ops):
     return peak
 
 
-def random_program(rng, *, extended=False, max_depth=None, features=12, stack_limit=None):
+def random_program(rng, *, extended=False, max_depth=None, features=12, stack_limit=None, feature_spec_id=1):
     ops = EXTENDED_OPS if extended else REFERENCE_OPS
     max_depth = max_depth if max_depth is not None else (6 if extended else 5)
     stack_limit = stack_limit or (16 if extended else 6)
@@ -43,6 +43,6 @@ def random_program(rng, *, extended=False, max_depth=None, features=12, stack_li
     remap = {a: i for i, a in enumerate(used)}
     code = [(op, remap[a] if op == 1 else a) for op, a in code]
     consts = rng.uniform(-consts_range, consts_range, size=len(used)).astype(np.float32)
-    return dict(ir_version=1, numeric_spec_id=2 if extended else 1, feature_spec_id=1,
+    return dict(ir_version=1, numeric_spec_id=2 if extended else 1, feature_spec_id=feature_spec_id,
                 opcode=[op for op, _ in code], operand=[a for _, a in code],
                 constant_bits=[int(b) for b in consts.view(np.uint32)])

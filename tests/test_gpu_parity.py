@@ -264,3 +264,41 @@ def test_invalid_inputs_raise_before_search(api):
     rows = engine.problem_rows(1)
     assert zero["items"][0]["tour"] == rows["initial_tour"].tolist()
     engine.close()
+
+
+@pytest.mark.parametrize("n,ants,iterations", [(60, 8, 10), (250, 16, 12), (1000, 32, 6)])
+def test_gp_controlled_population_matches_oracle(api, oracle, n, ants, iterations):
+    """GP-controlled colonies (feature spec 3: features, warp scoring of 32
+    actions, MNE / start region / restart actions) agree bit-for-bit with the
+    oracle: final tours and costs, and per iteration the best/global/parent
+    costs, trail bounds, MNE target used and action chosen."""
+    rng = np.random.default_rng(2024 + n)
+    programs = [_programs.random_program(rng, extended=bool(i % 2), features=10, feature_spec_id=3)
+                for i in range(5)]
+    programs.append(dict(ir_version=1, numeric_spec_id=2, feature_spec_id=3, opcode=[0], operand=[9],
+                         constant_bits=[]))                              # always restart
+    replicas = 2
+    xy = _cases.uniform_instance(n, seed=n + 5)
+    settings = _settings(api, ants, retention=0.9)
+    engine = api.FacoBatchEngine(n, len(programs) * replicas, settings)
+    engine.register_problem(42, xy.astype(np.float64))
+    prep = oracle.prepare(xy, 16, 64, 20)
+    keys = np.full(len(programs) * replicas, 42, np.uint64)
+    seeds = np.tile(np.arange(replicas, dtype=np.uint64) + 3, len(programs))
+    mask = 0xFFFFFFFF if n != 250 else 0x00FF00FF
+    res = engine.evaluate_population_evaluations(keys, seeds, ants * iterations, programs, mask, trace=True)
+    assert res["individual_costs"].shape == (len(programs), replicas)
+    for c in range(keys.size):
+        key = oracle.lib().orc_colony_key(int(seeds[c]), 42)
+        ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations, key=key,
+                                retention=0.9, program=programs[c // replicas], mask=mask,
+                                total_iterations=iterations)
+        assert res["items"][c]["cost"] == ref["cost"], c
+        assert res["items"][c]["tour"] == ref["tour"].tolist(), c
+        for it in range(iterations):
+            row, want = res["trace"][it, c], ref["trace"][it]
+            for field in ("iteration_best_cost", "global_cost", "parent_cost", "iteration_best", "mne_target",
+                          "action", "construction_steps", "ls_evaluations"):
+                assert int(row[field]) == int(want[field]), (c, it, field)
+            assert row["tau_min"] == np.float32(want["tau_min"]) and row["tau_max"] == np.float32(want["tau_max"])
+    engine.close()
