@@ -26,7 +26,8 @@ EXPORTED = (
     "faco_default_settings", "faco_last_error", "faco_engine_create", "faco_engine_destroy",
     "faco_register_problem", "faco_problem_rows", "faco_evaluate", "faco_validate_program", "faco_score",
     "faco_ant_diagnostic", "faco_pheromone_step", "faco_begin", "faco_step", "faco_step_timed", "faco_finish",
-    "faco_engine_stream", "faco_evaluate_programs",
+    "faco_engine_stream", "faco_evaluate_programs", "faco_mlp_param_count", "faco_mlp_forward", "faco_mlp_gradient",
+    "faco_mlp_train", "faco_edge_data", "faco_prior_set", "faco_prior_refresh", "faco_current_costs",
 )
 
 
@@ -119,6 +120,14 @@ def load():
                                       vp, vp, vp]
     L.faco_evaluate_programs.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint64, vp, C.c_uint32, C.c_uint32,
                                          C.c_uint32, vp, C.c_uint32, C.POINTER(Outputs)]
+    L.faco_mlp_param_count.argtypes = []
+    L.faco_mlp_forward.argtypes = [vp, vp, C.c_uint32, vp]
+    L.faco_mlp_gradient.argtypes = [vp, vp, vp, C.c_uint32, vp, vp]
+    L.faco_mlp_train.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, vp]
+    L.faco_edge_data.argtypes = [vp, vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.faco_prior_set.argtypes = [vp, vp, C.c_float, vp]
+    L.faco_prior_refresh.argtypes = [vp]
+    L.faco_current_costs.argtypes = [vp, vp, C.POINTER(C.c_uint32)]
     L.faco_begin.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32]
     L.faco_step.argtypes = [vp, C.c_uint32]
     L.faco_step_timed.argtypes = [vp, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]

@@ -86,6 +86,7 @@ struct InstanceView {
     long long initial_cost;
     const node_t* region_list;     // nodes grouped by quadrant of the bounding box
     std::uint32_t region_offsets[5];
+    float mean_nn;                 // mean nearest-neighbour distance (prior features)
 };
 
 // GP program (postfix IR; device mirror of faco_program).
@@ -132,6 +133,7 @@ struct ColonyView {
     unsigned long long key;        // Philox key
     float* trails;                 // [n][k]
     float* products;               // [n][k]
+    float* eta;                    // [n][k] heuristic of this colony (instance eta, or reweighted by the prior)
     node_t* parent;                // [n_pad] (16-byte aligned)
     std::uint32_t* parent_nbr;     // [n]: parent successor | predecessor << 16
     node_t* epoch;                 // [n]

@@ -24,6 +24,7 @@
 #include "../../include/faco_gb300.h"
 #include "faco_host.h"
 #include "faco_kernels.h"
+#include "prior_kernels.h"
 
 namespace {
 
@@ -146,11 +147,13 @@ struct Instance {
     DeviceBuffer<float> d_eta;
     DeviceBuffer<faco::node_t> d_regions;
     std::uint32_t region_offsets[5] = {0, 0, 0, 0, 0};
+    float mean_nn = 1.0f;
     faco::InstanceView view() const {
         faco::InstanceView v{n, k, b, w, d_xy.get(), d_primary.get(), d_backup.get(), d_ls.get(), d_ls_dist.get(),
                              d_eta.get(), d_initial.get(), static_cast<long long>(initial_cost), d_regions.get(),
                              {0, 0, 0, 0, 0}};
         for (int r = 0; r < 5; ++r) v.region_offsets[r] = region_offsets[r];
+        v.mean_nn = mean_nn;
         return v;
     }
 };
@@ -181,7 +184,7 @@ struct faco_engine {
     std::vector<std::uint64_t> instance_order;  // device table index -> key
     DeviceBuffer<faco::InstanceView> d_instances;
     // evaluation buffers (grow-only)
-    DeviceBuffer<float> trails, products;
+    DeviceBuffer<float> trails, products, colony_eta;
     DeviceBuffer<faco::node_t> parent, epoch, global, ant_tours;
     DeviceBuffer<std::uint32_t> parent_nbr;
     DeviceBuffer<long long> ant_costs, ant_ccosts;
@@ -192,6 +195,12 @@ struct faco_engine {
     DeviceBuffer<uint2> work;
     DeviceBuffer<faco::TraceRow> trace;
     DeviceBuffer<faco::node_t> checkpoints;
+    // learned edge prior
+    DeviceBuffer<faco::MlpParams> prior_params;
+    DeviceBuffer<faco::MlpOperands> prior_ops;
+    DeviceBuffer<std::uint8_t> prior_enabled;
+    float prior_floor = 0.05f;
+    bool prior_loaded = false;
 
     // the evaluation in progress (begin .. finish)
     struct EvalState {
@@ -337,6 +346,9 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         std::vector<std::uint16_t> regions;
         faco::host_regions(inst->xy, n, inst->region_offsets, regions);
         inst->d_regions.upload(regions, s);
+        double nn_sum = 0.0;
+        for (std::uint32_t a = 0; a < n; ++a) nn_sum += ls_dist[static_cast<std::size_t>(a) * inst->w];
+        inst->mean_nn = static_cast<float>(std::max(1.0, nn_sum / n));
         // initial checklist 2-opt over the NN tour on the GPU (prepared_problem.cpp:159-162)
         std::vector<faco::node_t> tour16(nn.begin(), nn.end());
         const long long nn_cost = faco::host_tour_length(inst->xy, nn.data(), n);
@@ -470,6 +482,7 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     // node arrays padded to 8 nodes so that every row starts 16-byte aligned
     e->trails.resize(tau_total);
     e->products.resize(tau_total);
+    e->colony_eta.resize(tau_total);
     e->parent.resize(node_total);
     e->parent_nbr.resize(node_total);
     e->epoch.resize(node_total);
@@ -502,6 +515,7 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         cv.key = mix64(seeds[c] ^ mix64(keys[c]));
         cv.trails = e->trails.get() + tau_off;
         cv.products = e->products.get() + tau_off;
+        cv.eta = e->colony_eta.get() + tau_off;
         cv.parent = e->parent.get() + node_off;
         cv.parent_nbr = e->parent_nbr.get() + node_off;
         cv.epoch = e->epoch.get() + node_off;
@@ -1055,6 +1069,203 @@ int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const u
         d_tr.download(trails, cells, s);
         d_pr.download(products, cells, s);
         cuda_check(cudaStreamSynchronize(s), "pheromone");
+    });
+}
+
+
+// ---------------------------------------------------------------------------
+// Learned edge prior: the MLP on its own (training and checks) and its use
+// inside a stepwise evaluation.
+// ---------------------------------------------------------------------------
+int faco_mlp_param_count(void) { return faco::kMlpParamCount; }
+
+static void upload_mlp(DeviceBuffer<faco::MlpParams>& P, DeviceBuffer<faco::MlpOperands>& O, const float* params,
+                       cudaStream_t s) {
+    P.resize(1);
+    O.resize(1);
+    P.upload(reinterpret_cast<const faco::MlpParams*>(params), 1, s);
+    faco::refresh_operands_kernel<<<4, 256, 0, s>>>(P.get(), O.get());
+    cuda_check(cudaGetLastError(), "operand refresh");
+}
+
+static std::uint32_t mlp_blocks(std::uint64_t chunks) {
+    return static_cast<std::uint32_t>(std::max<std::uint64_t>(1, std::min<std::uint64_t>(chunks, 152ull * 8)));
+}
+
+int faco_mlp_forward(const float* params, const uint16_t* x, uint32_t count, float* prob) {
+    return guarded([&] {
+        require(params && x && prob && count > 0, "invalid arguments");
+        cudaStream_t s = nullptr;
+        DeviceBuffer<faco::MlpParams> P;
+        DeviceBuffer<faco::MlpOperands> O;
+        upload_mlp(P, O, params, s);
+        DeviceBuffer<__nv_bfloat16> dx;
+        dx.upload(reinterpret_cast<const __nv_bfloat16*>(x), static_cast<std::size_t>(count) * faco::kMlpIn, s);
+        DeviceBuffer<float> dp(count);
+        faco::mlp_forward_kernel<<<mlp_blocks((count + 63) / 64), 128, 0, s>>>(P.get(), O.get(), dx.get(), count,
+                                                                             dp.get());
+        cuda_check(cudaGetLastError(), "mlp forward");
+        dp.download(prob, count, s);
+        cuda_check(cudaStreamSynchronize(s), "mlp forward");
+    });
+}
+
+int faco_mlp_gradient(const float* params, const uint16_t* x, const float* y, uint32_t count, float* grad,
+                      float* loss) {
+    return guarded([&] {
+        require(params && x && y && grad && loss && count > 0, "invalid arguments");
+        cudaStream_t s = nullptr;
+        DeviceBuffer<faco::MlpParams> P, G;
+        DeviceBuffer<faco::MlpOperands> O;
+        upload_mlp(P, O, params, s);
+        DeviceBuffer<__nv_bfloat16> dx;
+        dx.upload(reinterpret_cast<const __nv_bfloat16*>(x), static_cast<std::size_t>(count) * faco::kMlpIn, s);
+        DeviceBuffer<float> dy, dl(1);
+        dy.upload(y, count, s);
+        G.resize(1);
+        cuda_check(cudaMemsetAsync(G.get(), 0, sizeof(faco::MlpParams), s), "memset");
+        cuda_check(cudaMemsetAsync(dl.get(), 0, sizeof(float), s), "memset");
+        faco::mlp_grad_kernel<<<mlp_blocks((count + 63) / 64), 128, 0, s>>>(P.get(), O.get(), dx.get(), dy.get(),
+                                                                          count, 1.0f / count, G.get(), dl.get());
+        cuda_check(cudaGetLastError(), "mlp gradient");
+        G.download(reinterpret_cast<faco::MlpParams*>(grad), 1, s);
+        dl.download(loss, 1, s);
+        cuda_check(cudaStreamSynchronize(s), "mlp gradient");
+    });
+}
+
+int faco_mlp_train(float* params, const uint16_t* x, const float* y, uint32_t count, uint32_t epochs,
+                   uint32_t batch, float lr, float* epoch_losses) {
+    return guarded([&] {
+        require(params && x && y && count > 0 && batch > 0 && epochs > 0 && lr > 0, "invalid arguments");
+        cudaStream_t s = nullptr;
+        DeviceBuffer<faco::MlpParams> P, G, M, V;
+        DeviceBuffer<faco::MlpOperands> O;
+        upload_mlp(P, O, params, s);
+        G.resize(1); M.resize(1); V.resize(1);
+        cuda_check(cudaMemsetAsync(M.get(), 0, sizeof(faco::MlpParams), s), "memset");
+        cuda_check(cudaMemsetAsync(V.get(), 0, sizeof(faco::MlpParams), s), "memset");
+        DeviceBuffer<__nv_bfloat16> dx;
+        dx.upload(reinterpret_cast<const __nv_bfloat16*>(x), static_cast<std::size_t>(count) * faco::kMlpIn, s);
+        DeviceBuffer<float> dy, dl(epochs);
+        dy.upload(y, count, s);
+        cuda_check(cudaMemsetAsync(dl.get(), 0, sizeof(float) * epochs, s), "memset");
+        const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+        std::uint64_t step = 0;
+        for (std::uint32_t ep = 0; ep < epochs; ++ep) {
+            for (std::uint32_t first = 0; first < count; first += batch) {
+                const std::uint32_t size = std::min(batch, count - first);
+                ++step;
+                cuda_check(cudaMemsetAsync(G.get(), 0, sizeof(faco::MlpParams), s), "memset");
+                faco::mlp_grad_kernel<<<mlp_blocks((size + 63) / 64), 128, 0, s>>>(
+                    P.get(), O.get(), dx.get() + static_cast<std::size_t>(first) * faco::kMlpIn, dy.get() + first,
+                    size, 1.0f / size, G.get(), dl.get() + ep);
+                const float b1 = 1.0f - std::pow(beta1, static_cast<float>(step));
+                const float b2 = 1.0f - std::pow(beta2, static_cast<float>(step));
+                faco::adam_kernel<<<20, 256, 0, s>>>(P.get(), G.get(), M.get(), V.get(), lr, beta1, beta2, eps, b1, b2);
+                faco::refresh_operands_kernel<<<4, 256, 0, s>>>(P.get(), O.get());
+                cuda_check(cudaGetLastError(), "training step");
+            }
+        }
+        P.download(reinterpret_cast<faco::MlpParams*>(params), 1, s);
+        std::vector<float> losses(epochs);
+        dl.download(losses.data(), epochs, s);
+        cuda_check(cudaStreamSynchronize(s), "mlp training");
+        if (epoch_losses)
+            for (std::uint32_t ep = 0; ep < epochs; ++ep) epoch_losses[ep] = losses[ep] / count;
+    });
+}
+
+int faco_edge_data(faco_engine* e, uint16_t* x_out, float* y_out, uint64_t capacity_rows, uint64_t* rows) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        std::vector<std::uint64_t> offsets(v.count);
+        std::uint64_t total = 0;
+        for (std::uint32_t c = 0; c < v.count; ++c) {
+            offsets[c] = total;
+            total += static_cast<std::uint64_t>(v.sizes[c]) * e->instances.at(v.keys[c])->k;
+        }
+        if (rows) *rows = total;
+        if (!x_out && !y_out) return;
+        require(total <= capacity_rows, "output capacity too small");
+        cudaStream_t s = e->stream;
+        DeviceBuffer<std::uint64_t> d_off;
+        d_off.upload(offsets, s);
+        DeviceBuffer<__nv_bfloat16> dx;
+        DeviceBuffer<float> dy;
+        if (x_out) dx.resize(total * faco::kMlpIn);
+        if (y_out) dy.resize(total);
+        const std::uint32_t smem = 4u * v.n_max;
+        cuda_check(cudaFuncSetAttribute(faco::edge_features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(smem)), "attribute");
+        faco::edge_features_kernel<<<v.count, 256, smem, s>>>(e->d_instances.get(), e->colonies.get(),
+                                                              e->states.get(), 0, d_off.get(),
+                                                              x_out ? dx.get() : nullptr, y_out ? dy.get() : nullptr);
+        cuda_check(cudaGetLastError(), "edge features");
+        if (x_out) dx.download(reinterpret_cast<__nv_bfloat16*>(x_out), total * faco::kMlpIn, s);
+        if (y_out) dy.download(y_out, total, s);
+        cuda_check(cudaStreamSynchronize(s), "edge data");
+    });
+}
+
+static void apply_prior(faco_engine* e) {
+    auto& v = e->eval;
+    const std::uint32_t smem = 4u * v.n_max;
+    cuda_check(cudaFuncSetAttribute(faco::prior_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)), "attribute");
+    faco::prior_apply_kernel<<<v.count, 128, smem, e->stream>>>(e->d_instances.get(), e->colonies.get(),
+                                                                 e->states.get(), e->prior_enabled.get(),
+                                                                 e->prior_params.get(), e->prior_ops.get(),
+                                                                 e->prior_floor);
+    cuda_check(cudaGetLastError(), "prior apply");
+}
+
+int faco_prior_set(faco_engine* e, const float* params, float floor, const uint8_t* enabled) {
+    return guarded([&] {
+        require(e && enabled, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        require(std::isfinite(floor) && floor > 0.0f, "the prior floor must be positive (no candidate removed)");
+        if (params) {
+            for (int i = 0; i < faco::kMlpParamCount; ++i) require(std::isfinite(params[i]), "non-finite parameter");
+            upload_mlp(e->prior_params, e->prior_ops, params, e->stream);
+            e->prior_loaded = true;
+        }
+        require(e->prior_loaded, "no prior parameters loaded");
+        e->prior_floor = floor;
+        e->prior_enabled.upload(enabled, v.count, e->stream);
+        apply_prior(e);
+    });
+}
+
+int faco_prior_refresh(faco_engine* e) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        require(e->eval.active && e->prior_loaded && e->prior_enabled.size() >= e->eval.count, "no prior set");
+        apply_prior(e);
+    });
+}
+
+int faco_current_costs(faco_engine* e, int64_t* costs, uint32_t* iterations) {
+    return guarded([&] {
+        require(e && costs, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        std::vector<faco::ColonyState> st(v.count);
+        e->states.download(st.data(), v.count, e->stream);
+        cuda_check(cudaStreamSynchronize(e->stream), "costs");
+        for (std::uint32_t c = 0; c < v.count; ++c) costs[c] = st[c].global_cost;
+        if (iterations) *iterations = st[0].iteration;
     });
 }
 

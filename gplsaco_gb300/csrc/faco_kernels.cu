@@ -386,6 +386,7 @@ __global__ void colony_init_kernel(const InstanceView* instances, const ColonyVi
     const float tmax = s_tmax;
     for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
         cv.trails[i] = tmax;
+        cv.eta[i] = in.eta[i];
         cv.products[i] = tmax * in.eta[i];
     }
 }
@@ -598,7 +599,7 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
         cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
                                       ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
     __syncthreads();
-    trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, in.eta, cv.trails,
+    trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, cv.eta, cv.trails,
                  cv.products, threadIdx.x, blockDim.x);
     std::int32_t action = -1;
     if (P.controlled && cv.program) {
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
             const float tmax = s_st.tau_max;
             for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
                 cv.trails[i] = tmax;
-                cv.products[i] = tmax * in.eta[i];
+                cv.products[i] = tmax * cv.eta[i];
             }
         }
     }

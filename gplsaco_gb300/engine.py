@@ -281,6 +281,33 @@ class FacoBatchEngine:
                 "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
                 "reversed_elements": int(out.reversed_elements), "trace": trace_rows}
 
+    # ---- learned edge prior on the active stepwise evaluation ---------------
+    def edge_data(self, features: bool = True, labels: bool = True):
+        """Candidate-edge features (BF16 bits [E, 8]) and labels (edge of each
+        colony's global-best tour) of the current colony states."""
+        rows = C.c_uint64()
+        _lib.check(self._L.faco_edge_data(self._handle, None, None, 0, C.byref(rows)))
+        x = np.zeros((rows.value, 8), np.uint16) if features else None
+        y = np.zeros(rows.value, np.float32) if labels else None
+        _lib.check(self._L.faco_edge_data(self._handle, _lib.ptr(x), _lib.ptr(y), rows.value, C.byref(rows)))
+        return x, y
+
+    def prior_set(self, params, enabled, floor: float = 0.05) -> None:
+        """Reweights eta by (floor + p) on colonies with enabled[c]; the others
+        use the plain heuristic.  params None keeps the loaded network."""
+        enabled = np.ascontiguousarray(enabled, np.uint8)
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        _lib.check(self._L.faco_prior_set(self._handle, _lib.ptr(p), float(floor), enabled.ctypes.data))
+
+    def prior_refresh(self) -> None:
+        _lib.check(self._L.faco_prior_refresh(self._handle))
+
+    def current_costs(self, count: int):
+        costs = np.zeros(count, np.int64)
+        it = C.c_uint32()
+        _lib.check(self._L.faco_current_costs(self._handle, costs.ctypes.data, C.byref(it)))
+        return costs, int(it.value)
+
     @property
     def stream_ptr(self) -> int:
         """The engine's cudaStream_t as an integer (torch.cuda.ExternalStream)."""

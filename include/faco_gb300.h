@@ -202,6 +202,40 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
                         uint32_t b, const uint32_t* mne_targets, uint32_t tasks, uint64_t evaluation_limit,
                         uint32_t ls_mode, faco_ant_outputs* out);
 
+/* ---- learned edge prior ----------------------------------------------------
+ * No counterpart in the reference (its only candidate prior is an external
+ * LKH export, python/gp_faco/candidate_prior.py:20-36).  A 6 -> 64 -> 64 -> 1
+ * MLP (ReLU, sigmoid output) scores every directed candidate edge from
+ * [normalised distance, k-rank, angle to the nearest neighbour, ratio to the
+ * k-th neighbour distance, normalised trail, in-global-best flag]; BF16
+ * operands, FP32 accumulation on the tensor cores.  Parameters are one FP32
+ * array of faco_mlp_param_count() values: w1[64][8] (inputs 6,7 unused),
+ * b1[64], w2[64][64], b2[64], w3[64], b3, 3 padding.  Edge rows x are
+ * [count][8] BF16 bit patterns. */
+int faco_mlp_param_count(void);
+int faco_mlp_forward(const float* params, const uint16_t* x, uint32_t count, float* probabilities);
+/* Gradient of the mean binary cross-entropy over `count` rows (labels y). */
+int faco_mlp_gradient(const float* params, const uint16_t* x, const float* y, uint32_t count, float* gradient,
+                      float* loss_sum);
+/* Adam over `epochs` passes of minibatches of `batch` consecutive rows
+ * (shuffle the rows first); params updated in place; mean loss per epoch. */
+int faco_mlp_train(float* params, const uint16_t* x, const float* y, uint32_t count, uint32_t epochs,
+                   uint32_t batch, float learning_rate, float* epoch_losses);
+/* During a stepwise evaluation: features (and labels: edge of the colony's
+ * global-best tour) of every candidate entry of every colony, rows ordered
+ * (colony, node, rank); `rows` receives the row count (pass NULL outputs to
+ * query it). */
+int faco_edge_data(faco_engine* engine, uint16_t* x, float* y, uint64_t capacity_rows, uint64_t* rows);
+/* Enables the prior on colonies with enabled[c] != 0 (params may be NULL to
+ * keep the loaded ones): eta' = eta * (floor + p), products refreshed; floor
+ * > 0 so that no candidate is removed.  Colonies with enabled[c] == 0 get
+ * the plain heuristic back (the per-instance fallback). */
+int faco_prior_set(faco_engine* engine, const float* params, float floor, const uint8_t* enabled);
+/* Recomputes the prior from the colonies' current trails and best tours. */
+int faco_prior_refresh(faco_engine* engine);
+/* Current global-best lengths of the colonies (synchronises). */
+int faco_current_costs(faco_engine* engine, int64_t* costs, uint32_t* iterations);
+
 /* One MMAS evaporate/deposit step (cuda/colony_state.cuh:210-229) on FP32
  * trails [n][k] along `parent`; refreshes products = trails * eta. */
 int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent, float retention,

@@ -1,0 +1,105 @@
+"""Learned edge prior on the GPU: tensor-core forward/backward against the
+CPU oracle, training, edge data, and the plain-FACO fallback."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle
+from tests import _cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def prior(engine_lib):
+    from gplsaco_gb300 import prior
+    return prior
+
+
+def _data(prior, rng, E):
+    x = np.zeros((E, 8), np.float32)
+    x[:, :6] = rng.random((E, 6), dtype=np.float32)
+    x[:, 5] = (rng.random(E) < 0.2).astype(np.float32)
+    bits = prior.to_bf16_bits(x)
+    y = ((x[:, 0] < 0.3) ^ (x[:, 5] > 0.5)).astype(np.float32)
+    return bits, prior.from_bf16_bits(bits).astype(np.float64), y
+
+
+@pytest.mark.parametrize("E", [1, 15, 64, 1000, 4099])
+def test_forward_matches_oracle(prior, E):
+    rng = np.random.default_rng(E)
+    params = prior.init_params(seed=E)
+    bits, x, _ = _data(prior, rng, E)
+    got = prior.forward(params, bits)
+    want = mlp_oracle.forward(params, x)["prob"]
+    assert np.max(np.abs(got - want)) <= 2e-4
+
+
+@pytest.mark.parametrize("E", [16, 64, 777, 8192])
+def test_gradient_matches_oracle(prior, E):
+    """Weight gradients from the tensor-core backward agree with the CPU
+    oracle (same BF16 operand roundings; FP32 vs FP64 accumulation order):
+    |err| <= 1e-3 * max|grad| per tensor."""
+    rng = np.random.default_rng(100 + E)
+    params = prior.init_params(seed=E)
+    bits, x, y = _data(prior, rng, E)
+    grad, loss = prior.gradient(params, bits, y)
+    want, want_loss = mlp_oracle.gradient(params, x, y)
+    assert abs(loss - want_loss) <= 1e-3 * abs(want_loss) + 1e-3
+    view = prior.unpack(grad)
+    ref = mlp_oracle.unpack(want)
+    for name in ("w1", "b1", "w2", "b2", "w3", "b3"):
+        g, r = view[name].astype(np.float64), ref[name]
+        if name == "w1":
+            g, r = g[:, :6], r[:, :6]
+        scale = max(np.max(np.abs(r)), 1e-12)
+        assert np.max(np.abs(g - r)) <= 1e-3 * scale, name
+
+
+def test_training_reduces_loss(prior):
+    rng = np.random.default_rng(7)
+    bits, x, y = _data(prior, rng, 50000)
+    params = prior.init_params(seed=1)
+    trained, losses = prior.train(params, bits, y, epochs=8, batch=4096, lr=3e-3)
+    assert losses[-1] < 0.5 * losses[0]
+    acc = np.mean((prior.forward(trained, bits) > 0.5) == (y > 0.5))
+    assert acc > 0.9
+
+
+def test_edge_data_and_fallback(prior):
+    import gplsaco_gb300 as g
+    from oracle import oracle
+    n, ants = 300, 8
+    xy = _cases.uniform_instance(n, seed=12)
+    settings = g.FixedFacoSettings(ants=ants, retention=0.9)
+    keys = np.array([5, 5, 5], np.uint64)
+    seeds = np.array([1, 2, 3], np.uint64)
+    engine = g.FacoBatchEngine(n, 3, settings)
+    engine.register_problem(5, xy.astype(np.float64))
+    # plain reference result
+    plain = engine.evaluate_faco_evaluations(keys, seeds, ants * 6, 8)
+    # features/labels mid-run; prior with every colony disabled == plain FACO bit for bit
+    engine.begin(keys, seeds, 8)
+    engine.step(3)
+    x, y = engine.edge_data()
+    assert x.shape == (3 * n * 16, 8) and y.shape == (3 * n * 16,)
+    xf = prior.from_bf16_bits(x)
+    assert np.array_equal(xf[:, 5], y)                       # in-best-tour flag == label at the same state
+    assert np.all((xf[:, :6] >= 0) & (xf[:, :6] <= 1))
+    assert np.all(y.reshape(3, n, 16).sum(axis=2) <= 2)     # at most the two tour neighbours per node
+    engine.prior_set(prior.init_params(seed=3), np.zeros(3, np.uint8))
+    engine.step(3)
+    res = engine.finish()
+    assert [int(c) for c in res["costs"]] == [it["cost"] for it in plain["items"]]
+    # enabled prior: valid tours, exact lengths
+    engine.begin(keys, seeds, 8)
+    engine.prior_set(prior.init_params(seed=3), np.ones(3, np.uint8), floor=0.05)
+    for _ in range(3):
+        engine.step(2)
+        engine.prior_refresh()
+    res = engine.finish()
+    m = oracle.euc2d_matrix(xy)
+    for c in range(3):
+        t = np.asarray(res["tours"][c], np.int64)
+        assert np.array_equal(np.sort(t), np.arange(n))
+        assert int(np.sum(m[t, np.roll(t, -1)])) == int(res["costs"][c])
+    engine.close()
