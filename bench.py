@@ -273,6 +273,20 @@ def run_gb300(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_time_to_gap(args) -> None:
+    import torch
+
+    torch.cuda.set_device(0)
+    from gplsaco_gb300 import experiments
+    res = experiments.time_to_gap(log=lambda m: print(m, file=sys.stderr, flush=True))
+    line = {"metric": "time to 1% mean gap, learned-prior vs plain GPU FACO (ratio)", "value": res["ratio"],
+            "unit": "prior/plain wall-clock", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "16 instances (N=1000/2000, uniform/clustered, seeds 100-115), 32 ants, "
+                                   "k=20, MNE 8, 2-opt; reference = best of 2 plain runs of 1500 iterations"},
+            "time_to_gap": res}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -280,11 +294,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--workload", default="throughput", choices=["throughput", "time-to-gap"],
+                    help="time-to-gap: learned-prior vs plain FACO wall-clock to a 1%% mean gap (N=1000/2000)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "time-to-gap":
+        run_time_to_gap(args)
         return
     if world > 1:
         import torch

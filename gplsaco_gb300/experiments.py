@@ -1,0 +1,170 @@
+"""Time to a 1% gap: learned-prior FACO against plain GPU FACO.
+
+Pipeline (all GPU work through the engine's C ABI):
+ 1. training data from the engine's own plain runs on a training pool of
+    instances: candidate-edge features at an early snapshot iteration,
+    labels = membership in the colony's best tour at the end of the run;
+ 2. training of the edge-prior MLP with the tensor-core kernels;
+ 3. on the evaluation instances: a long plain run's best as the reference
+    length per instance; then plain FACO and learned-prior FACO are each run
+    in chunks of iterations, recording the mean gap over instances against
+    wall-clock; the prior is disabled per instance (plain fallback) when,
+    after the warm-up, it trails the plain colony at the same iteration.
+    The plain warm-up iterations the fallback decision needs are charged to
+    the prior method's clock.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import instances as inst
+from . import prior as prior_mod
+from .engine import FacoBatchEngine, FixedFacoSettings
+
+
+@dataclass
+class GapConfig:
+    ants: int = 32
+    k: int = 20
+    ls_width: int = 20
+    retention: float = 0.98
+    mne: int = 8
+    chunk: int = 10                 # iterations between cost reads (and prior refreshes)
+    iterations: int = 400           # timed budget per method
+    reference_iterations: int = 1500
+    reference_seeds: int = 2
+    warmup: int = 40                # iterations before the fallback decision
+    floor: float = 0.05
+    target_gap: float = 0.01
+    train_pool: int = 32
+    train_snapshot: int = 25
+    train_iterations: int = 300
+    epochs: int = 12
+    batch: int = 8192
+    lr: float = 3e-3
+    eval_instances: list = field(default_factory=lambda: [
+        ("uniform", 1000, 100), ("uniform", 1000, 101), ("uniform", 1000, 102), ("uniform", 1000, 103),
+        ("clustered", 1000, 104), ("clustered", 1000, 105), ("clustered", 1000, 106), ("clustered", 1000, 107),
+        ("uniform", 2000, 108), ("uniform", 2000, 109), ("uniform", 2000, 110), ("uniform", 2000, 111),
+        ("clustered", 2000, 112), ("clustered", 2000, 113), ("clustered", 2000, 114), ("clustered", 2000, 115)])
+
+
+def _settings(cfg: GapConfig) -> FixedFacoSettings:
+    return FixedFacoSettings(ants=cfg.ants, primary_width=cfg.k, backup_width=64, ls_width=cfg.ls_width,
+                             retention=cfg.retention)
+
+
+def _xy(kind: str, n: int, seed: int) -> np.ndarray:
+    return inst.uniform(n, seed) if kind == "uniform" else inst.clustered(n, seed)
+
+
+def collect_training_data(cfg: GapConfig, device: int = 0):
+    """Features at iteration cfg.train_snapshot, labels at cfg.train_iterations."""
+    pool = []
+    for i in range(cfg.train_pool):
+        rng = np.random.default_rng(500 + i)
+        n = int(rng.integers(500, 1001))
+        pool.append(_xy("clustered" if i % 4 else "uniform", n, 500 + i))
+    dim = max(len(p) for p in pool)
+    engine = FacoBatchEngine(dim, 2 * len(pool), _settings(cfg), device=device)
+    for i, xy in enumerate(pool):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    keys = np.repeat(np.arange(1, len(pool) + 1, dtype=np.uint64), 2)
+    seeds = np.tile(np.array([11, 12], np.uint64), len(pool))
+    engine.begin(keys, seeds, cfg.mne)
+    engine.step(cfg.train_snapshot)
+    x, _ = engine.edge_data(features=True, labels=False)
+    engine.step(cfg.train_iterations - cfg.train_snapshot)
+    _, y = engine.edge_data(features=False, labels=True)
+    engine.finish()
+    engine.close()
+    return x, y
+
+
+def reference_lengths(cfg: GapConfig, xys: list, device: int = 0) -> np.ndarray:
+    dim = max(len(xy) for xy in xys)
+    engine = FacoBatchEngine(dim, len(xys) * cfg.reference_seeds, _settings(cfg), device=device)
+    for i, xy in enumerate(xys):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    keys = np.repeat(np.arange(1, len(xys) + 1, dtype=np.uint64), cfg.reference_seeds)
+    seeds = np.tile(np.arange(cfg.reference_seeds, dtype=np.uint64) + 900, len(xys))
+    res = engine.evaluate_faco_evaluations(keys, seeds, cfg.ants * cfg.reference_iterations, cfg.mne)
+    engine.close()
+    costs = np.array([it["cost"] for it in res["items"]], np.int64).reshape(len(xys), cfg.reference_seeds)
+    return costs.min(axis=1)
+
+
+def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0):
+    """One method on all evaluation instances (one colony each, seed 1).
+    Returns rows (iteration, seconds, mean gap, costs) and the fallback mask."""
+    dim = max(len(xy) for xy in xys)
+    engine = FacoBatchEngine(dim, len(xys), _settings(cfg), device=device)
+    for i, xy in enumerate(xys):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    keys = np.arange(1, len(xys) + 1, dtype=np.uint64)
+    seeds = np.ones(len(xys), np.uint64)
+    rows = []
+    enabled = np.ones(len(xys), np.uint8)
+    engine.begin(keys, seeds, cfg.mne)
+    costs, _ = engine.current_costs(len(xys))
+    t0 = time.perf_counter()
+    if params is not None:
+        engine.prior_set(params, enabled, cfg.floor)
+    rows.append((0, 0.0, float(np.mean((costs - refs) / refs)), costs.copy()))
+    done = 0
+    while done < cfg.iterations:
+        engine.step(cfg.chunk)
+        done += cfg.chunk
+        if params is not None:
+            if done == cfg.warmup and plain_warmup_costs is not None:
+                now, _ = engine.current_costs(len(xys))
+                enabled = (now <= plain_warmup_costs).astype(np.uint8)
+                engine.prior_set(None, enabled, cfg.floor)
+            else:
+                engine.prior_refresh()
+        costs, _ = engine.current_costs(len(xys))
+        rows.append((done, time.perf_counter() - t0, float(np.mean((costs - refs) / refs)), costs.copy()))
+    engine.finish()
+    engine.close()
+    return rows, enabled
+
+
+def first_time_below(rows, target: float, extra_seconds: float = 0.0):
+    for it, sec, gap, _ in rows:
+        if gap <= target:
+            return sec + extra_seconds, it
+    return None, None
+
+
+def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dict:
+    cfg = cfg or GapConfig()
+    t_start = time.perf_counter()
+    x, y = collect_training_data(cfg, device)
+    log(f"training rows {len(y)}, positive rate {float(np.mean(y)):.3f}")
+    params, losses = prior_mod.train(prior_mod.init_params(seed=1), x, y, epochs=cfg.epochs, batch=cfg.batch,
+                                     lr=cfg.lr)
+    log(f"training losses {np.round(losses, 4).tolist()}")
+    xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
+    refs = reference_lengths(cfg, xys, device)
+    plain_rows, _ = gap_run(cfg, xys, refs, None, None, device)
+    warm = next(r for r in plain_rows if r[0] == cfg.warmup)
+    prior_rows, enabled = gap_run(cfg, xys, refs, params, warm[3], device)
+    t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
+    t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
+    out = {
+        "target_gap": cfg.target_gap,
+        "plain_seconds": t_plain, "plain_iterations": it_plain,
+        "prior_seconds": t_prior, "prior_iterations": it_prior,
+        "ratio": (t_prior / t_plain) if (t_prior is not None and t_plain) else None,
+        "prior_charged_warmup_seconds": warm[1],
+        "prior_enabled_after_warmup": int(enabled.sum()), "instances": len(xys),
+        "final_gap_plain": plain_rows[-1][2], "final_gap_prior": prior_rows[-1][2],
+        "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(plain_rows, prior_rows)
+                   if r[0] % 50 == 0},
+        "training_rows": int(len(y)), "training_loss": [float(v) for v in losses],
+        "total_seconds": time.perf_counter() - t_start,
+    }
+    return out
