@@ -36,7 +36,7 @@ class Settings(C.Structure):
                 ("ls_width", C.c_uint32), ("beta", C.c_double), ("retention", C.c_double),
                 ("p_best", C.c_double), ("epoch_source_probability", C.c_double),
                 ("ls_evaluation_limit", C.c_uint64), ("initial_ls_evaluation_limit", C.c_uint64),
-                ("ls_mode", C.c_uint32), ("reserved", C.c_uint32)]
+                ("ls_mode", C.c_uint32), ("autotune", C.c_uint32)]
 
 
 class Registration(C.Structure):
@@ -125,7 +125,7 @@ def load():
     L.faco_mlp_gradient.argtypes = [vp, vp, vp, C.c_uint32, vp, vp]
     L.faco_mlp_train.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, vp]
     L.faco_edge_data.argtypes = [vp, vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]
-    L.faco_prior_set.argtypes = [vp, vp, C.c_float, vp]
+    L.faco_prior_set.argtypes = [vp, vp, C.c_float, C.c_int, vp]
     L.faco_prior_refresh.argtypes = [vp]
     L.faco_current_costs.argtypes = [vp, vp, C.POINTER(C.c_uint32)]
     L.faco_begin.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32]

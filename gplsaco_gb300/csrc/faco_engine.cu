@@ -200,24 +200,39 @@ struct faco_engine {
     DeviceBuffer<faco::MlpOperands> prior_ops;
     DeviceBuffer<std::uint8_t> prior_enabled;
     float prior_floor = 0.05f;
+    int prior_gamma = 1;
     bool prior_loaded = false;
+    DeviceBuffer<std::uint32_t> prior_gnbr, prior_offsets;
 
     // the evaluation in progress (begin .. finish)
+    // One ant-kernel launch per instance size class (n rounded up to a power
+    // of two, at least 256): shared memory is sized for the class's largest
+    // instance, and the classes run as parallel branches of each iteration.
+    struct AntClass {
+        std::uint32_t n_max = 0, warps = 1, smem = 0, blocks = 0, first_job = 0;
+        faco::AntLaunch L{};
+    };
     struct EvalState {
         bool active = false;
-        std::uint32_t count = 0, n_max = 0, warps = 0, blocks = 0, smem = 0, trace_cap = 0, done = 0;
+        std::uint32_t count = 0, n_max = 0, trace_cap = 0, done = 0;
         std::size_t node_total = 0;
         std::vector<std::uint32_t> sizes;
         std::vector<std::uint64_t> keys;
+        std::vector<AntClass> classes;
         faco::ColonyParams P{};
         faco::AntLaunch L{};
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
     } eval;
+    std::vector<cudaStream_t> branch_streams;
+    std::vector<cudaEvent_t> branch_events;   // [0] fork, [1 + i] join of branch i
+    std::map<std::uint64_t, std::uint32_t> tuned_warps;  // (class, n_max, ants, blocks, mode) -> warps
 
     ~faco_engine() {
         if (eval.exec) cudaGraphExecDestroy(eval.exec);
         if (eval.graph) cudaGraphDestroy(eval.graph);
+        for (auto st : branch_streams) cudaStreamDestroy(st);
+        for (auto ev : branch_events) cudaEventDestroy(ev);
         if (stream) {
             cudaSetDevice(device);
             cudaStreamSynchronize(stream);
@@ -434,13 +449,112 @@ void destroy_graph(faco_engine* e) {
     e->eval.graph = nullptr;
 }
 
+// All ant launches of one iteration: class 0 on `st`, the others on branch
+// streams forked from and joined back into `st` (parallel graph branches).
+void enqueue_ants(faco_engine* e, cudaStream_t st) {
+    auto& v = e->eval;
+    const std::size_t branches = v.classes.size();
+    if (branches > 1) cuda_check(cudaEventRecord(e->branch_events[0], st), "fork");
+    for (std::size_t i = 0; i < branches; ++i) {
+        const auto& c = v.classes[i];
+        cudaStream_t bs = i == 0 ? st : e->branch_streams[i - 1];
+        if (i > 0) cuda_check(cudaStreamWaitEvent(bs, e->branch_events[0], 0), "fork wait");
+        cuda_check(faco::launch_ant_kernel(faco::kModeEngine, c.L, c.blocks, c.warps, c.smem, bs), "ant launch");
+        if (i > 0) cuda_check(cudaEventRecord(e->branch_events[i], bs), "join");
+    }
+    for (std::size_t i = 1; i < branches; ++i) cuda_check(cudaStreamWaitEvent(st, e->branch_events[i], 0), "join wait");
+}
+
 void enqueue_iteration(faco_engine* e, cudaStream_t st) {
     auto& v = e->eval;
-    cuda_check(faco::launch_ant_kernel(faco::kModeEngine, v.L, v.blocks, v.warps, v.smem, st), "ant launch");
+    enqueue_ants(e, st);
     faco::colony_update_kernel<<<v.count, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
                                                          v.P, v.trace_cap ? e->trace.get() : nullptr, v.count,
                                                          v.trace_cap);
     cuda_check(cudaGetLastError(), "update launch");
+}
+
+// Work tables of the size classes: jobs (colony, first ant) of W = warps
+// ants each.  With autotuning, every candidate W of a class is timed on the
+// freshly initialised colonies (the ant kernel alone, which changes no
+// colony state: its outputs are rewritten by the first real iteration) and
+// the fastest is kept, cached per (class, size, ants, blocks, LS mode).
+void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32_t>>& members,
+                       const std::vector<std::uint32_t>& class_ids) {
+    auto& v = e->eval;
+    const std::uint32_t A = v.L.ants;
+    cudaStream_t s = e->stream;
+    auto jobs_for = [&](const std::vector<std::uint32_t>& cols, std::uint32_t warps) {
+        std::vector<uint2> jobs;
+        for (const std::uint32_t c : cols)
+            for (std::uint32_t a = 0; a < A; a += warps) jobs.push_back(make_uint2(c, a));
+        return jobs;
+    };
+    if (e->settings.autotune) {
+        DeviceBuffer<uint2> scratch;
+        cudaEvent_t t0, t1;
+        cuda_check(cudaEventCreate(&t0), "event");
+        cuda_check(cudaEventCreate(&t1), "event");
+        for (std::size_t i = 0; i < members.size(); ++i) {
+            auto& cl = v.classes[i];
+            const std::uint64_t key = (static_cast<std::uint64_t>(class_ids[i]) << 56) ^
+                                      (static_cast<std::uint64_t>(cl.n_max) << 40) ^
+                                      (static_cast<std::uint64_t>(A) << 24) ^
+                                      (static_cast<std::uint64_t>(members[i].size()) << 2) ^ e->settings.ls_mode;
+            const auto hit = e->tuned_warps.find(key);
+            if (hit != e->tuned_warps.end()) {
+                cl.warps = hit->second;
+                continue;
+            }
+            float best_ms = 0.0f;
+            for (std::uint32_t w = 1; w <= faco::kMaxWarpsPerBlock && w <= A; w *= 2) {
+                const std::uint32_t smem = faco::block_smem_bytes(cl.n_max, w);
+                if (smem > 227u * 1024u) break;
+                const auto jobs = jobs_for(members[i], w);
+                scratch.upload(jobs, s);
+                faco::AntLaunch L = v.L;
+                L.work = scratch.get();
+                L.warps = w;
+                L.n_max = cl.n_max;
+                cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem), "attribute");
+                float ms = 0.0f;
+                for (int rep = 0; rep < 3; ++rep) {
+                    cuda_check(cudaEventRecord(t0, s), "event");
+                    cuda_check(faco::launch_ant_kernel(faco::kModeEngine, L, static_cast<std::uint32_t>(jobs.size()),
+                                                       w, smem, s), "tuning launch");
+                    cuda_check(cudaEventRecord(t1, s), "event");
+                    cuda_check(cudaEventSynchronize(t1), "tuning");
+                    float one = 0.0f;
+                    cuda_check(cudaEventElapsedTime(&one, t0, t1), "elapsed");
+                    if (rep > 0) ms += one;   // first launch warms caches
+                }
+                if (best_ms == 0.0f || ms < best_ms) {
+                    best_ms = ms;
+                    cl.warps = w;
+                }
+            }
+            e->tuned_warps[key] = cl.warps;
+        }
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    std::vector<uint2> all;
+    for (std::size_t i = 0; i < members.size(); ++i) {
+        auto& cl = v.classes[i];
+        const auto jobs = jobs_for(members[i], cl.warps);
+        cl.first_job = static_cast<std::uint32_t>(all.size());
+        cl.blocks = static_cast<std::uint32_t>(jobs.size());
+        cl.smem = faco::block_smem_bytes(cl.n_max, cl.warps);
+        all.insert(all.end(), jobs.begin(), jobs.end());
+    }
+    e->work.upload(all, s);
+    for (auto& cl : v.classes) {
+        cl.L = v.L;
+        cl.L.work = e->work.get() + cl.first_job;
+        cl.L.warps = cl.warps;
+        cl.L.n_max = cl.n_max;
+        cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, cl.smem), "cudaFuncSetAttribute");
+    }
 }
 
 // Controller programs of a GP-controlled evaluation (null: plain FACO).
@@ -534,18 +648,33 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.count = count;
     v.node_total = node_total;
     v.n_max = n_max;
-    v.warps = choose_warps(n_max, A);
-    // largest instances first so that the long ants start in the first wave
+    // size classes, largest instances first inside each class so that the
+    // longest ants start in the first wave
     std::vector<std::uint32_t> order(count);
     for (std::uint32_t c = 0; c < count; ++c) order[c] = c;
     std::stable_sort(order.begin(), order.end(),
                      [&](std::uint32_t x, std::uint32_t y) { return v.sizes[x] > v.sizes[y]; });
-    std::vector<uint2> jobs;
-    for (const std::uint32_t c : order)
-        for (std::uint32_t a = 0; a < A; a += v.warps) jobs.push_back(make_uint2(c, a));
-    e->work.upload(jobs, s);
-    v.blocks = static_cast<std::uint32_t>(jobs.size());
-    v.smem = faco::block_smem_bytes(n_max, v.warps);
+    auto class_of = [](std::uint32_t n) {
+        std::uint32_t c = 0;
+        while ((256u << c) < n) ++c;
+        return c;
+    };
+    std::vector<std::vector<std::uint32_t>> members;
+    std::vector<std::uint32_t> class_ids;
+    for (const std::uint32_t c : order) {
+        const std::uint32_t id = class_of(v.sizes[c]);
+        if (class_ids.empty() || class_ids.back() != id) {
+            class_ids.push_back(id);
+            members.emplace_back();
+        }
+        members.back().push_back(c);
+    }
+    v.classes.assign(members.size(), faco_engine::AntClass{});
+    for (std::size_t i = 0; i < members.size(); ++i) {
+        auto& cl = v.classes[i];
+        cl.n_max = v.sizes[members[i].front()];
+        cl.warps = choose_warps(cl.n_max, A);
+    }
     v.trace_cap = trace_iterations;
     if (trace_iterations) e->trace.resize(static_cast<std::size_t>(trace_iterations) * count);
     v.P = faco::ColonyParams{};
@@ -562,17 +691,24 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.L.instances = e->d_instances.get();
     v.L.colonies = e->colonies.get();
     v.L.states = e->states.get();
-    v.L.work = e->work.get();
     v.L.ants = A;
-    v.L.warps = v.warps;
-    v.L.n_max = n_max;
     v.L.ls_limit = e->settings.ls_evaluation_limit;
     v.L.ls_mode = e->settings.ls_mode;
     v.L.error = e->error.get();
     e->reset_error();
-    cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, v.smem), "cudaFuncSetAttribute");
     faco::colony_init_kernel<<<count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(), e->states.get(), v.P);
     cuda_check(cudaGetLastError(), "init launch");
+    while (e->branch_streams.size() + 1 < v.classes.size()) {
+        cudaStream_t bs;
+        cuda_check(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "branch stream");
+        e->branch_streams.push_back(bs);
+    }
+    while (e->branch_events.size() < v.classes.size() + 1) {
+        cudaEvent_t ev;
+        cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "branch event");
+        e->branch_events.push_back(ev);
+    }
+    build_work_tables(e, members, class_ids);
     // one graph of kGraphIterations iterations, replayed; the batch index is device state
     destroy_graph(e);
     cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -671,7 +807,7 @@ int faco_step_timed(faco_engine* e, uint32_t iterations, double* ant_ms, double*
         for (auto& x : ev) cuda_check(cudaEventCreate(&x), "event");
         for (std::uint32_t i = 0; i < iterations; ++i) {
             cuda_check(cudaEventRecord(ev[3 * i], s), "event");
-            cuda_check(faco::launch_ant_kernel(faco::kModeEngine, v.L, v.blocks, v.warps, v.smem, s), "ant launch");
+            enqueue_ants(e, s);
             cuda_check(cudaEventRecord(ev[3 * i + 1], s), "event");
             faco::colony_update_kernel<<<v.count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(),
                                                                e->states.get(), v.P,
@@ -1214,17 +1350,29 @@ int faco_edge_data(faco_engine* e, uint16_t* x_out, float* y_out, uint64_t capac
 
 static void apply_prior(faco_engine* e) {
     auto& v = e->eval;
-    const std::uint32_t smem = 4u * v.n_max;
-    cuda_check(cudaFuncSetAttribute(faco::prior_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)), "attribute");
-    faco::prior_apply_kernel<<<v.count, 128, smem, e->stream>>>(e->d_instances.get(), e->colonies.get(),
-                                                                 e->states.get(), e->prior_enabled.get(),
-                                                                 e->prior_params.get(), e->prior_ops.get(),
-                                                                 e->prior_floor);
+    std::vector<std::uint32_t> offsets(v.count);
+    std::uint32_t total = 0, max_cells = 0;
+    for (std::uint32_t c = 0; c < v.count; ++c) {
+        offsets[c] = total;
+        total += faco::pad8(v.sizes[c]);
+        max_cells = std::max(max_cells, v.sizes[c] * e->instances.at(v.keys[c])->k);
+    }
+    e->prior_offsets.upload(offsets, e->stream);
+    e->prior_gnbr.resize(total);
+    faco::global_neighbours_kernel<<<v.count, 256, 0, e->stream>>>(e->colonies.get(), e->prior_gnbr.get(),
+                                                                    e->prior_offsets.get());
+    // enough chunk blocks per colony to fill the GPU about four times over
+    const std::uint32_t chunks = (max_cells + 63) / 64;
+    const std::uint32_t per_colony = std::max<std::uint32_t>(1, std::min(chunks, 4u * 152u * 4u / v.count + 1));
+    const dim3 grid(per_colony, v.count);
+    faco::prior_apply_kernel<<<grid, 128, 0, e->stream>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
+                                                          e->prior_enabled.get(), e->prior_params.get(),
+                                                          e->prior_ops.get(), e->prior_floor, e->prior_gamma,
+                                                          e->prior_gnbr.get(), e->prior_offsets.get());
     cuda_check(cudaGetLastError(), "prior apply");
 }
 
-int faco_prior_set(faco_engine* e, const float* params, float floor, const uint8_t* enabled) {
+int faco_prior_set(faco_engine* e, const float* params, float floor, int gamma, const uint8_t* enabled) {
     return guarded([&] {
         require(e && enabled, "null argument");
         std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
@@ -1238,7 +1386,9 @@ int faco_prior_set(faco_engine* e, const float* params, float floor, const uint8
             e->prior_loaded = true;
         }
         require(e->prior_loaded, "no prior parameters loaded");
+        require(gamma == 1 || gamma == 2, "the prior exponent must be 1 or 2");
         e->prior_floor = floor;
+        e->prior_gamma = gamma;
         e->prior_enabled.upload(enabled, v.count, e->stream);
         apply_prior(e);
     });

@@ -18,8 +18,11 @@ __global__ void refresh_operands_kernel(const MlpParams* P, MlpOperands* O);
 __global__ void edge_features_kernel(const InstanceView* instances, const ColonyView* colonies,
                                      const ColonyState* states, std::uint32_t first, const std::uint64_t* row_offset,
                                      __nv_bfloat16* x_out, float* y_out);
+__global__ void global_neighbours_kernel(const ColonyView* colonies, std::uint32_t* gnbr_all,
+                                         const std::uint32_t* node_offset);
 __global__ void prior_apply_kernel(const InstanceView* instances, const ColonyView* colonies,
                                    const ColonyState* states, const std::uint8_t* enabled, const MlpParams* P,
-                                   const MlpOperands* O, float floor);
+                                   const MlpOperands* O, float floor, int gamma, const std::uint32_t* gnbr_all,
+                                   const std::uint32_t* node_offset);
 
 }  // namespace faco

@@ -303,41 +303,53 @@ __global__ void edge_features_kernel(const InstanceView* instances, const Colony
     }
 }
 
+// Packed neighbours of every colony's global-best tour into gnbr (rows at
+// the colonies' parent_nbr offsets).  One block per colony.
+__global__ void global_neighbours_kernel(const ColonyView* colonies, std::uint32_t* gnbr_all,
+                                         const std::uint32_t* node_offset) {
+    const ColonyView cv = colonies[blockIdx.x];
+    std::uint32_t* gnbr = gnbr_all + node_offset[blockIdx.x];
+    global_neighbours(cv, cv.n, gnbr);
+}
+
 // Applies the prior to the colonies whose flag is set: for every candidate
-// entry eta' = eta * (floor + p), p the MLP probability, and products =
-// trails * eta'.  The factor is never zero, so no candidate is removed.
-// Flag clear: eta' = eta (plain FACO).  One block (4 warps) per colony.
+// entry eta' = eta * (floor + p)^gamma (gamma in {1, 2}), p the MLP
+// probability, and products = trails * eta'.  The factor is never zero, so no
+// candidate is removed.  Flag clear: eta' = eta (plain FACO).  Grid:
+// (chunks of 64 entries, colonies); 4 warps per block, 16 entries per warp.
 __global__ void __launch_bounds__(128) prior_apply_kernel(const InstanceView* instances, const ColonyView* colonies,
                                                           const ColonyState* states, const std::uint8_t* enabled,
-                                                          const MlpParams* P, const MlpOperands* O, float floor) {
-    extern __shared__ std::uint32_t gnbr[];
+                                                          const MlpParams* P, const MlpOperands* O, float floor,
+                                                          int gamma, const std::uint32_t* gnbr_all,
+                                                          const std::uint32_t* node_offset) {
     __shared__ SharedOperands s;
     __shared__ __align__(16) __nv_bfloat16 xs[kWarps][16 * kMlpIn];
-    const std::uint32_t c = blockIdx.x;
+    const std::uint32_t c = blockIdx.y;
     const ColonyView cv = colonies[c];
     const InstanceView in = instances[cv.instance];
     const std::uint32_t n = in.n, k = in.k, cells = n * k;
+    const std::uint32_t first = blockIdx.x * kChunk;
+    if (first >= cells) return;
     if (!enabled[c]) {
-        for (std::uint32_t i = threadIdx.x; i < cells; i += blockDim.x) {
-            cv.eta[i] = in.eta[i];
-            cv.products[i] = cv.trails[i] * in.eta[i];
-        }
+        if (threadIdx.x < kChunk)
+            for (std::uint32_t i = first + threadIdx.x; i < cells; i += gridDim.x * kChunk) {
+                cv.eta[i] = in.eta[i];
+                cv.products[i] = cv.trails[i] * in.eta[i];
+            }
         return;
     }
     const ColonyState st = states[c];
+    const std::uint32_t* gnbr = gnbr_all + node_offset[c];
     load_operands(s, P, O);
-    global_neighbours(cv, n, gnbr);
     __syncthreads();
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (std::uint32_t t0 = warp * 16; t0 < cells; t0 += kWarps * 16) {
-        // features of entries t0 .. t0+15, two lanes per entry
+    for (std::uint32_t t0 = first + warp * 16; t0 < cells; t0 += gridDim.x * kChunk) {
         {
             const std::uint32_t e = t0 + (lane >> 1);
             float x[kMlpFeatures] = {0, 0, 0, 0, 0, 0};
             if (e < cells) edge_features(in, cv, st, gnbr, e / k, e % k, x);
-            const int half = lane & 1;
             __nv_bfloat16* row = xs[warp] + (lane >> 1) * kMlpIn;
-            if (half == 0) {
+            if ((lane & 1) == 0) {
                 row[0] = __float2bfloat16(x[0]); row[1] = __float2bfloat16(x[1]);
                 row[2] = __float2bfloat16(x[2]); row[3] = __float2bfloat16(x[3]);
             } else {
@@ -353,7 +365,8 @@ __global__ void __launch_bounds__(128) prior_apply_kernel(const InstanceView* in
             for (int h = 0; h < 2; ++h) {
                 const std::uint32_t e = t0 + g + 8 * h;
                 if (e < cells) {
-                    const float eta = in.eta[e] * (floor + sigmoid(t.z[h]));
+                    const float f = floor + sigmoid(t.z[h]);
+                    const float eta = in.eta[e] * (gamma == 2 ? f * f : f);
                     cv.eta[e] = eta;
                     cv.products[e] = cv.trails[e] * eta;
                 }

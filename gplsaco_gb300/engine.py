@@ -41,11 +41,12 @@ class FixedFacoSettings:
     ls_evaluation_limit: int = 100000
     initial_ls_evaluation_limit: int = 100000
     ls_mode: int = _lib.FACO_LS_TWO_OPT
+    autotune: int = 1
 
     def to_c(self) -> _lib.Settings:
         s = _lib.Settings()
         for name in ("ants", "primary_width", "backup_width", "ls_width", "ls_evaluation_limit",
-                     "initial_ls_evaluation_limit", "ls_mode"):
+                     "initial_ls_evaluation_limit", "ls_mode", "autotune"):
             setattr(s, name, _exact_int(getattr(self, name), name))
         for name in ("beta", "retention", "p_best", "epoch_source_probability"):
             value = getattr(self, name)
@@ -292,12 +293,13 @@ class FacoBatchEngine:
         _lib.check(self._L.faco_edge_data(self._handle, _lib.ptr(x), _lib.ptr(y), rows.value, C.byref(rows)))
         return x, y
 
-    def prior_set(self, params, enabled, floor: float = 0.05) -> None:
-        """Reweights eta by (floor + p) on colonies with enabled[c]; the others
-        use the plain heuristic.  params None keeps the loaded network."""
+    def prior_set(self, params, enabled, floor: float = 0.05, gamma: int = 1) -> None:
+        """Reweights eta by (floor + p)^gamma on colonies with enabled[c]; the
+        others use the plain heuristic.  params None keeps the loaded network."""
         enabled = np.ascontiguousarray(enabled, np.uint8)
         p = None if params is None else np.ascontiguousarray(params, np.float32)
-        _lib.check(self._L.faco_prior_set(self._handle, _lib.ptr(p), float(floor), enabled.ctypes.data))
+        _lib.check(self._L.faco_prior_set(self._handle, _lib.ptr(p), float(floor), _exact_int(gamma, "gamma", 1, 2),
+                                          enabled.ctypes.data))
 
     def prior_refresh(self) -> None:
         _lib.check(self._L.faco_prior_refresh(self._handle))

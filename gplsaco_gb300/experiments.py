@@ -38,7 +38,10 @@ class GapConfig:
     reference_seeds: int = 2
     warmup: int = 40                # iterations before the fallback decision
     floor: float = 0.05
+    gamma: int = 1
     target_gap: float = 0.01
+    # (floor, gamma, chunk) candidates tuned on validation instances (seeds 200+)
+    tune_grid: tuple = ((0.05, 1, 10), (0.05, 2, 10), (0.02, 2, 10), (0.05, 2, 25), (0.1, 2, 10))
     train_pool: int = 32
     train_snapshot: int = 25
     train_iterations: int = 300
@@ -97,9 +100,13 @@ def reference_lengths(cfg: GapConfig, xys: list, device: int = 0) -> np.ndarray:
     return costs.min(axis=1)
 
 
-def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0):
+def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0,
+            floor: float | None = None, gamma: int | None = None, chunk: int | None = None):
     """One method on all evaluation instances (one colony each, seed 1).
     Returns rows (iteration, seconds, mean gap, costs) and the fallback mask."""
+    floor = cfg.floor if floor is None else floor
+    gamma = cfg.gamma if gamma is None else gamma
+    chunk = cfg.chunk if chunk is None else chunk
     dim = max(len(xy) for xy in xys)
     engine = FacoBatchEngine(dim, len(xys), _settings(cfg), device=device)
     for i, xy in enumerate(xys):
@@ -112,17 +119,18 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     costs, _ = engine.current_costs(len(xys))
     t0 = time.perf_counter()
     if params is not None:
-        engine.prior_set(params, enabled, cfg.floor)
+        engine.prior_set(params, enabled, floor, gamma)
     rows.append((0, 0.0, float(np.mean((costs - refs) / refs)), costs.copy()))
     done = 0
     while done < cfg.iterations:
-        engine.step(cfg.chunk)
-        done += cfg.chunk
+        step = min(chunk, cfg.warmup - done) if done < cfg.warmup else chunk
+        engine.step(step)
+        done += step
         if params is not None:
             if done == cfg.warmup and plain_warmup_costs is not None:
                 now, _ = engine.current_costs(len(xys))
                 enabled = (now <= plain_warmup_costs).astype(np.uint8)
-                engine.prior_set(None, enabled, cfg.floor)
+                engine.prior_set(None, enabled, floor, gamma)
             else:
                 engine.prior_refresh()
         costs, _ = engine.current_costs(len(xys))
@@ -147,11 +155,23 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     params, losses = prior_mod.train(prior_mod.init_params(seed=1), x, y, epochs=cfg.epochs, batch=cfg.batch,
                                      lr=cfg.lr)
     log(f"training losses {np.round(losses, 4).tolist()}")
+    # tune (floor, gamma, refresh chunk) on validation instances, by iterations to the target
+    val = [_xy(kind, n, seed + 100) for kind, n, seed in cfg.eval_instances[::2]]
+    val_refs = reference_lengths(cfg, val, device)
+    val_plain, _ = gap_run(cfg, val, val_refs, None, None, device)
+    val_warm = next(r for r in val_plain if r[0] == cfg.warmup)
+    tuning = []
+    for floor, gamma, chunk in cfg.tune_grid:
+        rows, _ = gap_run(cfg, val, val_refs, params, val_warm[3], device, floor, gamma, chunk)
+        t, it = first_time_below(rows, cfg.target_gap)
+        tuning.append(((floor, gamma, chunk), rows[-1][2], it if it is not None else 10**9))
+    best = min(tuning, key=lambda r: (r[2], r[1]))[0]
+    log(f"tuning {tuning} -> {best}")
     xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
     refs = reference_lengths(cfg, xys, device)
     plain_rows, _ = gap_run(cfg, xys, refs, None, None, device)
     warm = next(r for r in plain_rows if r[0] == cfg.warmup)
-    prior_rows, enabled = gap_run(cfg, xys, refs, params, warm[3], device)
+    prior_rows, enabled = gap_run(cfg, xys, refs, params, warm[3], device, *best)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
     out = {
@@ -161,6 +181,9 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         "ratio": (t_prior / t_plain) if (t_prior is not None and t_plain) else None,
         "prior_charged_warmup_seconds": warm[1],
         "prior_enabled_after_warmup": int(enabled.sum()), "instances": len(xys),
+        "prior_setting": {"floor": best[0], "gamma": best[1], "refresh_every": best[2]},
+        "tuning": [{"floor": a[0], "gamma": a[1], "refresh_every": a[2], "final_gap": g, "iterations_to_target": i}
+                   for a, g, i in tuning],
         "final_gap_plain": plain_rows[-1][2], "final_gap_prior": prior_rows[-1][2],
         "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(plain_rows, prior_rows)
                    if r[0] % 50 == 0},

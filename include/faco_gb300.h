@@ -44,7 +44,7 @@ typedef struct faco_settings {
     uint64_t ls_evaluation_limit;
     uint64_t initial_ls_evaluation_limit;
     uint32_t ls_mode; /* FACO_LS_* */
-    uint32_t reserved;
+    uint32_t autotune; /* 1: pick ants per block per size class by timing the ant kernel */
 } faco_settings;
 
 void faco_default_settings(faco_settings* s);
@@ -227,10 +227,11 @@ int faco_mlp_train(float* params, const uint16_t* x, const float* y, uint32_t co
  * query it). */
 int faco_edge_data(faco_engine* engine, uint16_t* x, float* y, uint64_t capacity_rows, uint64_t* rows);
 /* Enables the prior on colonies with enabled[c] != 0 (params may be NULL to
- * keep the loaded ones): eta' = eta * (floor + p), products refreshed; floor
- * > 0 so that no candidate is removed.  Colonies with enabled[c] == 0 get
- * the plain heuristic back (the per-instance fallback). */
-int faco_prior_set(faco_engine* engine, const float* params, float floor, const uint8_t* enabled);
+ * keep the loaded ones): eta' = eta * (floor + p)^gamma (gamma 1 or 2),
+ * products refreshed; floor > 0 so that no candidate is removed.  Colonies
+ * with enabled[c] == 0 get the plain heuristic back (the per-instance
+ * fallback). */
+int faco_prior_set(faco_engine* engine, const float* params, float floor, int gamma, const uint8_t* enabled);
 /* Recomputes the prior from the colonies' current trails and best tours. */
 int faco_prior_refresh(faco_engine* engine);
 /* Current global-best lengths of the colonies (synchronises). */
