@@ -24,6 +24,7 @@
 #include "../../include/faco_gb300.h"
 #include "faco_host.h"
 #include "faco_kernels.h"
+#include "noalloc_kernels.h"
 #include "prior_kernels.h"
 
 namespace {
@@ -548,13 +549,17 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
         all.insert(all.end(), jobs.begin(), jobs.end());
     }
     e->work.upload(all, s);
+    // the dynamic shared-memory limit is a property of the kernel, shared by
+    // every class: it must admit the largest class
+    std::uint32_t smem_max = 0;
     for (auto& cl : v.classes) {
         cl.L = v.L;
         cl.L.work = e->work.get() + cl.first_job;
         cl.L.warps = cl.warps;
         cl.L.n_max = cl.n_max;
-        cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, cl.smem), "cudaFuncSetAttribute");
+        smem_max = std::max(smem_max, cl.smem);
     }
+    cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem_max), "cudaFuncSetAttribute");
 }
 
 // Controller programs of a GP-controlled evaluation (null: plain FACO).
@@ -1416,6 +1421,42 @@ int faco_current_costs(faco_engine* e, int64_t* costs, uint32_t* iterations) {
         cuda_check(cudaStreamSynchronize(e->stream), "costs");
         for (std::uint32_t c = 0; c < v.count; ++c) costs[c] = st[c].global_cost;
         if (iterations) *iterations = st[0].iteration;
+    });
+}
+
+// The pheromone step on caller-owned device buffers; its only scratch is a
+// fixed per-device array (faco_noalloc.cu), so the success path allocates no
+// device or host memory.  Checks are written without building strings until
+// one fails.
+int faco_pheromone_step_noalloc(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
+                                float retention, float minimum, float maximum, float increment, const float* eta,
+                                float* trails, float* products, void* stream) {
+    return guarded([&] {
+        if (!(primary && parent && eta && trails && products)) throw Error(FACO_EINVAL, "null argument");
+        if (n < 3 || k < 1) throw Error(FACO_EINVAL, "invalid sizes: n >= 3 and k >= 1 are required");
+        if (n > faco::kNoAllocMaxNodes)
+            throw Error(FACO_EINVAL, "n exceeds the 65535 nodes the fixed scratch of "
+                                     "faco_pheromone_step_noalloc holds");
+        if (static_cast<std::uint64_t>(n) * k >= (1ull << 31))
+            throw Error(FACO_EINVAL, "n * k must be below 2^31 candidate entries");
+        int device = 0;
+        cuda_check(cudaGetDevice(&device), "cudaGetDevice");
+        const void* pointers[5] = {primary, parent, eta, trails, products};
+        for (const void* p : pointers) {
+            cudaPointerAttributes a{};
+            cuda_check(cudaPointerGetAttributes(&a, p), "cudaPointerGetAttributes");
+            if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+                throw Error(FACO_EINVAL, "faco_pheromone_step_noalloc takes device pointers only");
+            if (a.type == cudaMemoryTypeDevice && a.device != device)
+                throw Error(FACO_EINVAL, "a buffer lives on another device than the current one");
+        }
+        std::uint32_t bits = 0;
+        cuda_check(faco::pheromone_step_noalloc(n, k, primary, parent, retention, minimum, maximum, increment, eta,
+                                                trails, products, static_cast<cudaStream_t>(stream), &bits),
+                   "pheromone step (no allocation)");
+        if (bits & faco::kNoAllocParentRange) throw Error(FACO_EINVAL, "parent node out of range");
+        if (bits & faco::kNoAllocParentRepeat) throw Error(FACO_EINVAL, "parent is not a permutation");
+        if (bits & faco::kNoAllocPrimaryRange) throw Error(FACO_EINVAL, "primary candidate out of range");
     });
 }
 

@@ -243,6 +243,42 @@ int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const u
                         float minimum, float maximum, float increment, const float* eta, float* trails,
                         float* products);
 
+/* The same pheromone step on buffers that already live in device memory,
+ * allocating nothing: no device memory (no cudaMalloc/cudaFree) and no host
+ * memory on the success path.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate per call: a loop that keeps trails, eta
+ * and candidate lists resident in memory it manages itself (a caching
+ * allocator such as PyTorch's, or one fixed arena).  A cudaFree inside the
+ * library would synchronise the whole device on every step and a cudaMalloc
+ * would compete with the caller's pool for memory it has already reserved.
+ *
+ * Arguments mean what they mean in faco_pheromone_step, but every array is
+ * a device pointer on the current device: primary [n*k] u32 candidate ids,
+ * parent [n] u32 tour, eta/trails/products [n*k] f32 (trails in/out,
+ * products out).  `stream` is a cudaStream_t (NULL: the legacy default
+ * stream); the call enqueues its work there and returns when it is done.
+ *
+ * Limit: n <= 65535 nodes.  The only scratch is one fixed device array per
+ * device (256 KiB of packed parent neighbours, an 8 KiB permutation bitmap
+ * and an error word), declared at file scope in the library; larger n is
+ * rejected with FACO_EINVAL before any work is enqueued.  The bitmap and the
+ * error word must start at zero: every call clears them on `stream` itself
+ * before use.  An invalid parent (out of range or repeated node) or
+ * candidate id is found on the device and returns FACO_EINVAL with trails
+ * and products untouched.
+ *
+ * The first call on each device looks the scratch address up
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any
+ * stream capture on that device.  Calls must not overlap: two calls in
+ * flight at once on one device (from two host threads of one process) race
+ * on the single scratch and corrupt each other's result.  Calls from one
+ * thread never overlap, since each returns only after its work is
+ * complete. */
+int faco_pheromone_step_noalloc(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
+                                float retention, float minimum, float maximum, float increment, const float* eta,
+                                float* trails, float* products, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
