@@ -8,6 +8,7 @@
 //   pheromone_step_kernel   the trail update alone (parity hook)
 //   score_kernel            GP controller scoring, warp per colony
 //                           (cuda/gp_score.cuh:64-102)
+#include <mutex>
 #include <climits>
 
 #include "faco_ant.cuh"
@@ -317,9 +318,23 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
 }
 
 namespace {
+// The dynamic shared-memory limit is a per-kernel, per-device attribute that
+// every engine on the device shares, and instantiated graphs launch against
+// it: it is only ever raised, so that one engine's smaller classes never
+// invalidate another engine's larger ones.
 template <int MODE>
 cudaError_t prepare_mode(std::uint32_t smem) {
-    return cudaFuncSetAttribute(ant_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::mutex lock;
+    static std::uint32_t raised[64] = {};
+    int device = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err != cudaSuccess) return err;
+    std::lock_guard<std::mutex> guard(lock);
+    std::uint32_t& current = raised[device & 63];
+    if (smem <= current) return cudaSuccess;
+    err = cudaFuncSetAttribute(ant_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err == cudaSuccess) current = smem;
+    return err;
 }
 }  // namespace
 

@@ -40,8 +40,9 @@ class GapConfig:
     floor: float = 0.05
     gamma: int = 1
     target_gap: float = 0.01
-    # (floor, gamma, chunk) candidates tuned on validation instances (seeds 200+)
-    tune_grid: tuple = ((0.05, 1, 10), (0.05, 2, 10), (0.02, 2, 10), (0.05, 2, 25), (0.1, 2, 10))
+    # (floor, gamma, chunk) candidates, tuned on validation instances (seeds 200-215)
+    # by wall-clock time to the target gap
+    tune_grid: tuple = ((0.05, 1, 10), (0.05, 2, 10), (0.2, 1, 10), (0.5, 1, 10), (0.2, 2, 10), (0.05, 1, 25))
     train_pool: int = 32
     train_snapshot: int = 25
     train_iterations: int = 300
@@ -103,7 +104,8 @@ def reference_lengths(cfg: GapConfig, xys: list, device: int = 0) -> np.ndarray:
 def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0,
             floor: float | None = None, gamma: int | None = None, chunk: int | None = None):
     """One method on all evaluation instances (one colony each, seed 1).
-    Returns rows (iteration, seconds, mean gap, costs) and the fallback mask."""
+    Returns rows (iteration, seconds, mean gap, costs), the fallback mask and
+    the work per ant-iteration (construction steps, LS evaluations)."""
     floor = cfg.floor if floor is None else floor
     gamma = cfg.gamma if gamma is None else gamma
     chunk = cfg.chunk if chunk is None else chunk
@@ -135,9 +137,13 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
                 engine.prior_refresh()
         costs, _ = engine.current_costs(len(xys))
         rows.append((done, time.perf_counter() - t0, float(np.mean((costs - refs) / refs)), costs.copy()))
-    engine.finish()
+    res = engine.finish()
     engine.close()
-    return rows, enabled
+    ant_iterations = float(cfg.ants * len(xys) * done)
+    work = {"construction_steps": res["construction_steps"] / ant_iterations,
+            "ls_evaluations": res["ls_evaluations"] / ant_iterations,
+            "ms_per_iteration": 1e3 * rows[-1][1] / done}
+    return rows, enabled, work
 
 
 def first_time_below(rows, target: float, extra_seconds: float = 0.0):
@@ -158,20 +164,24 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     # tune (floor, gamma, refresh chunk) on validation instances, by iterations to the target
     val = [_xy(kind, n, seed + 100) for kind, n, seed in cfg.eval_instances[::2]]
     val_refs = reference_lengths(cfg, val, device)
-    val_plain, _ = gap_run(cfg, val, val_refs, None, None, device)
+    val_plain, _, val_work = gap_run(cfg, val, val_refs, None, None, device)
     val_warm = next(r for r in val_plain if r[0] == cfg.warmup)
+    t_val, _ = first_time_below(val_plain, cfg.target_gap)
     tuning = []
     for floor, gamma, chunk in cfg.tune_grid:
-        rows, _ = gap_run(cfg, val, val_refs, params, val_warm[3], device, floor, gamma, chunk)
-        t, it = first_time_below(rows, cfg.target_gap)
-        tuning.append(((floor, gamma, chunk), rows[-1][2], it if it is not None else 10**9))
-    best = min(tuning, key=lambda r: (r[2], r[1]))[0]
-    log(f"tuning {tuning} -> {best}")
+        rows, _, work = gap_run(cfg, val, val_refs, params, val_warm[3], device, floor, gamma, chunk)
+        t, it = first_time_below(rows, cfg.target_gap, extra_seconds=val_warm[1])
+        tuning.append({"floor": floor, "gamma": gamma, "refresh_every": chunk, "final_gap": rows[-1][2],
+                       "iterations_to_target": it, "seconds_to_target": t, **work})
+    best_row = min(tuning, key=lambda r: (r["seconds_to_target"] is None, r["seconds_to_target"] or 0.0,
+                                          r["final_gap"]))
+    best = (best_row["floor"], best_row["gamma"], best_row["refresh_every"])
+    log(f"validation plain: {t_val} s, {val_work}; tuning {tuning} -> {best}")
     xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
     refs = reference_lengths(cfg, xys, device)
-    plain_rows, _ = gap_run(cfg, xys, refs, None, None, device)
+    plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device)
     warm = next(r for r in plain_rows if r[0] == cfg.warmup)
-    prior_rows, enabled = gap_run(cfg, xys, refs, params, warm[3], device, *best)
+    prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, params, warm[3], device, *best)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
     out = {
@@ -182,8 +192,8 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         "prior_charged_warmup_seconds": warm[1],
         "prior_enabled_after_warmup": int(enabled.sum()), "instances": len(xys),
         "prior_setting": {"floor": best[0], "gamma": best[1], "refresh_every": best[2]},
-        "tuning": [{"floor": a[0], "gamma": a[1], "refresh_every": a[2], "final_gap": g, "iterations_to_target": i}
-                   for a, g, i in tuning],
+        "plain_work": plain_work, "prior_work": prior_work,
+        "validation_plain": {"seconds_to_target": t_val, **val_work}, "tuning": tuning,
         "final_gap_plain": plain_rows[-1][2], "final_gap_prior": prior_rows[-1][2],
         "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(plain_rows, prior_rows)
                    if r[0] % 50 == 0},
