@@ -758,12 +758,34 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
     cuda_check(cudaStreamSynchronize(s), "download");
     std::uint64_t steps = 0, evals = 0, reversed = 0;
     std::size_t node_off = 0;
+    // Final verification of every incumbent on the host (batch_engine.cu:1075-1089):
+    // a complete permutation whose recomputed length equals the device cost.
+    std::vector<std::uint32_t> tour;
+    std::vector<std::uint8_t> seen;
+    for (std::uint32_t c = 0; c < v.count; ++c) {
+        const std::uint32_t n = v.sizes[c];
+        tour.assign(global.begin() + node_off, global.begin() + node_off + n);
+        seen.assign(n, 0);
+        for (const std::uint32_t node : tour) {
+            require(node < n && !seen[node], "device incumbent is not a complete permutation");
+            seen[node] = 1;
+        }
+        require(faco::host_tour_length(e->instances.at(v.keys[c])->xy, tour.data(), n) == states[c].global_cost,
+                "device incumbent cost differs from its full recomputation");
+        node_off += faco::pad8(n);
+    }
+    node_off = 0;
     for (std::uint32_t c = 0; c < v.count; ++c) {
         const std::uint32_t n = v.sizes[c];
         if (out->tours)
             for (std::uint32_t i = 0; i < dimension; ++i)
                 out->tours[static_cast<std::size_t>(c) * dimension + i] = i < n ? global[node_off + i] : UINT32_MAX;
         if (out->costs) out->costs[c] = states[c].global_cost;
+        if (out->colony_work) {
+            out->colony_work[3 * c] = states[c].construction_steps;
+            out->colony_work[3 * c + 1] = states[c].ls_evaluations;
+            out->colony_work[3 * c + 2] = states[c].reversed_elements;
+        }
         steps += states[c].construction_steps;
         evals += states[c].ls_evaluations;
         reversed += states[c].reversed_elements;

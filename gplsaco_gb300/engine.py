@@ -70,26 +70,27 @@ def _u64_array(a, name: str) -> np.ndarray:
 
 
 class FacoBatchEngine:
-    """FacoBatchEngine(dimension, colonies, settings) (bindings.cpp:558-573).
+    """FacoBatchEngine(dimension, colonies, settings, population_size=1)
+    (bindings.cpp:558-573).
 
     `dimension` is the largest instance size accepted; instances of different
-    sizes may share an evaluation.  One evaluation at a time per engine.
+    sizes may share an evaluation.  `colonies` is the panel size; an engine
+    with population_size P holds P copies of the panel, one per individual of
+    evaluate_population_evaluations.  One evaluation at a time per engine.
     """
 
     def __init__(self, dimension, colonies, settings: FixedFacoSettings, constraint_mode="unrestricted",
                  population_size=1, device: int = 0):
         _exact_int(dimension, "dimension")
-        _exact_int(colonies, "colonies")
-        _exact_int(population_size, "population_size")
+        _exact_int(colonies, "colonies", 1, 2**32 - 1)
+        _exact_int(population_size, "population_size", 1, 128)
         if constraint_mode != "unrestricted":
             raise ValueError("only the unrestricted candidate graph is supported")
-        if population_size != 1:
-            raise ValueError("population engines are created with population_size=1 and a replicated panel")
         self._L = _lib.load()
         self._handle = C.c_void_p()
-        _lib.check(self._L.faco_engine_create(dimension, colonies, C.byref(settings.to_c()), device,
-                                              C.byref(self._handle)))
-        self.dimension, self.colonies = dimension, colonies
+        _lib.check(self._L.faco_engine_create(dimension, colonies * population_size, C.byref(settings.to_c()),
+                                              device, C.byref(self._handle)))
+        self.dimension, self.colonies, self.population_size = dimension, colonies, population_size
         self.settings = settings
         self.ants = settings.ants or faco_ants(dimension)
         self._sizes: dict[int, int] = {}
@@ -147,19 +148,87 @@ class FacoBatchEngine:
                                      checkpoint_iterations=(), initial_mne=8, trace=False) -> dict:
         """evaluate_program_evaluations (bindings.cpp:721-757): every colony is
         driven by one GP controller program (feature spec 3)."""
-        return self.evaluate_population_evaluations(instance_keys, seeds, evaluation_limit_per_colony, [program],
-                                                    experiment_mask, checkpoint_iterations=checkpoint_iterations,
-                                                    initial_mne=initial_mne, trace=trace,
-                                                    preparation_mode=preparation_mode)
+        return self._programs(_u64_array(instance_keys, "instance_keys"), _u64_array(seeds, "seeds"),
+                              evaluation_limit_per_colony, [program], experiment_mask, checkpoint_iterations,
+                              initial_mne, trace, preparation_mode)
+
+    def evaluate_controller_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, controller,
+                                        experiment_mask=0xFFFFFFFF, *, decision_iterations=()) -> dict:
+        """evaluate_controller_evaluations (bindings.cpp:758-775,
+        cuda/batch_engine.cu:439-447): a controller dict (read_controller,
+        bindings.cpp:58-73) -- a bare program, or {controller_version: 1,
+        representation, controller_id, trees}.  A joint_single controller is
+        its one tree; conditional_three controllers are not supported."""
+        if not isinstance(controller, dict):
+            raise ValueError("controller must be a dict")
+        if "opcode" in controller:
+            program = controller
+        else:
+            if (len(controller) != 4 or type(controller.get("controller_version")) is not int
+                    or controller["controller_version"] != 1 or "controller_id" not in controller
+                    or "trees" not in controller):
+                raise ValueError("unknown controller version or fields")
+            kind = controller.get("representation")
+            if kind not in ("joint_single", "conditional_three"):
+                raise ValueError("unknown controller representation")
+            trees = list(controller["trees"])
+            if len(trees) != (3 if kind == "conditional_three" else 1):
+                raise ValueError("wrong number of role trees for the controller representation")
+            if kind == "conditional_three":
+                raise ValueError("conditional_three controllers are not supported by this engine")
+            program = trees[0]
+        if decision_iterations:
+            raise ValueError("decision recording is not supported by this engine")
+        return self._programs(_u64_array(instance_keys, "instance_keys"), _u64_array(seeds, "seeds"),
+                              evaluation_limit_per_colony, [program], experiment_mask, (), 8, False,
+                              "cached_charged")
 
     def evaluate_population_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, programs,
-                                        experiment_mask=0xFFFFFFFF, *, checkpoint_iterations=(), initial_mne=8,
-                                        trace=False, preparation_mode="cached") -> dict:
-        """evaluate_population_evaluations (bindings.cpp:776-817): colony c is
-        driven by programs[c // (colonies // len(programs))]; the panel of
-        (instance, seed) tasks is given already replicated per program, in
-        individual-major order.  Returns the plain result dict plus
-        `individual_costs` [programs][replicas]."""
+                                        experiment_mask=0xFFFFFFFF, *, factorial_policy=None,
+                                        profile_events_only=False, checkpoint_iterations=(), initial_mne=8,
+                                        trace=False) -> list:
+        """evaluate_population_evaluations (bindings.cpp:776-817,
+        cuda/batch_engine.cu:379-437): every program (individual) runs the
+        whole panel of `colonies` (instance, seed) tasks; all individuals share
+        one batch (colony i*colonies + j = individual i, task j).  Returns one
+        result dict per individual; its time is an equal share of the batch
+        (`population_actual_seconds` keeps the batch's)."""
+        if not isinstance(programs, (list, tuple)) or not 1 <= len(programs) <= self.population_size:
+            raise ValueError("the population needs 1..population_size programs")
+        if factorial_policy is not None:
+            raise ValueError("factorial policies are not supported by this engine")
+        keys = _u64_array(instance_keys, "instance_keys")
+        seeds = _u64_array(seeds, "seeds")
+        if keys.size != self.colonies or seeds.size != self.colonies:
+            raise ValueError("the population entry needs the complete shared panel")
+        count = len(programs)
+        batch = self._programs(np.tile(keys, count), np.tile(seeds, count), evaluation_limit_per_colony, programs,
+                               experiment_mask, checkpoint_iterations, initial_mne, trace, "cached_charged",
+                               profile_events_only)
+        out = []
+        G = self.colonies
+        for i in range(count):
+            part = dict(batch)
+            share = batch["actual_seconds"] / count
+            part["items"] = [dict(it, completed_seconds=it["completed_seconds"] / count)
+                             for it in batch["items"][i * G:(i + 1) * G]]
+            work = batch["colony_work"][i * G:(i + 1) * G]
+            part.update(population_size=count, population_actual_seconds=batch["actual_seconds"],
+                        time_accounting="equal_share_of_population_batch", actual_seconds=share,
+                        elapsed_seconds=share, total_tour_evaluations=batch["completed_tour_evaluations_per_colony"] * G,
+                        completed_construction_steps=int(work[:, 0].sum()),
+                        completed_ls_evaluations=int(work[:, 1].sum()), reversed_elements=int(work[:, 2].sum()),
+                        colony_work=work)
+            if "checkpoints" in batch:
+                part["checkpoints"] = [{"iterations": cp["iterations"], "tours": cp["tours"][i * G:(i + 1) * G]}
+                                       for cp in batch["checkpoints"]]
+            if trace:
+                part["trace"] = batch["trace"][:, i * G:(i + 1) * G]
+            out.append(part)
+        return out
+
+    def _programs(self, keys, seeds, limit, programs, experiment_mask, checkpoint_iterations, initial_mne, trace,
+                  preparation_mode, profile_events_only=False) -> dict:
         if not isinstance(programs, (list, tuple)) or not programs:
             raise ValueError("programs must be a non-empty list of IR dicts")
         mask = _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF)
@@ -168,12 +237,8 @@ class FacoBatchEngine:
         for p in arr:
             if p.feature_spec_id != 3:
                 raise ValueError("controller programs use feature spec 3")
-        result = self._evaluate(instance_keys, seeds, evaluation_limit_per_colony, mne, preparation_mode,
-                                checkpoint_iterations, False, trace, arr, mask)
-        costs = np.array([it["cost"] for it in result["items"]], np.int64)
-        result["individual_costs"] = costs.reshape(len(programs), -1)
-        result["population_size"] = len(programs)
-        return result
+        return self._evaluate(keys, seeds, limit, mne, preparation_mode, checkpoint_iterations, profile_events_only,
+                              trace, arr, mask)
 
     def _evaluate(self, instance_keys, seeds, evaluation_limit_per_colony, mne, preparation_mode,
                   checkpoint_iterations, profile_events_only, trace, programs, mask) -> dict:
@@ -194,7 +259,9 @@ class FacoBatchEngine:
         costs = np.zeros(count, np.int64)
         trace_rows = np.zeros((iterations, count), _lib.TRACE_DTYPE) if trace else None
         cp_tours = np.zeros((cps.size, count, D), np.uint32) if cps.size else None
+        work = np.zeros((count, 3), np.uint64)
         out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), _lib.ptr(cp_tours))
+        out.colony_work = work.ctypes.data
         if not self._lock.acquire(blocking=False):
             raise RuntimeError("only one active evaluation per engine")
         try:
@@ -225,6 +292,7 @@ class FacoBatchEngine:
             "completed_construction_steps": int(out.construction_steps),
             "completed_ls_evaluations": int(out.ls_evaluations),
             "reversed_elements": int(out.reversed_elements),
+            "colony_work": work,
             "production_kernel_milliseconds": {"iteration_loop": out.kernel_milliseconds},
             "elapsed_seconds": out.solve_seconds,
             "actual_seconds": out.solve_seconds,
@@ -280,7 +348,8 @@ class FacoBatchEngine:
         return {"tours": [tours[c, :self._sizes[int(keys[c])]] for c in range(count)], "costs": costs,
                 "completed_batches": int(out.completed_batches),
                 "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
-                "reversed_elements": int(out.reversed_elements), "trace": trace_rows}
+                "reversed_elements": int(out.reversed_elements),
+            "colony_work": work, "trace": trace_rows}
 
     # ---- learned edge prior on the active stepwise evaluation ---------------
     def edge_data(self, features: bool = True, labels: bool = True):
@@ -314,6 +383,39 @@ class FacoBatchEngine:
     def stream_ptr(self) -> int:
         """The engine's cudaStream_t as an integer (torch.cuda.ExternalStream)."""
         return int(self._L.faco_engine_stream(self._handle) or 0)
+
+
+class FixedFacoGpu:
+    """FixedFacoGpu(coordinates f64[n,2], instance_key, settings)
+    (bindings.cpp:972-1006, cuda/fixed_faco.cu:105-177): one instance, one
+    colony.  Every run_iterations call restarts the colony from the prepared
+    initial tour and runs `batches` ant batches with a constant MNE target."""
+
+    def __init__(self, coordinates, instance_key, settings: FixedFacoSettings, device: int = 0):
+        key = _exact_int(instance_key, "instance_key")
+        if (not isinstance(coordinates, np.ndarray) or coordinates.dtype != np.float64 or coordinates.ndim != 2
+                or coordinates.shape[1] != 2):
+            raise ValueError("coordinates must be a float64 [n, 2] array")
+        self._key = key
+        self._engine = FacoBatchEngine(int(coordinates.shape[0]), 1, settings, device=device)
+        self._registration = self._engine.register_problem(key, np.ascontiguousarray(coordinates))
+
+    def run_iterations(self, seed, batches, mne_target) -> dict:
+        seed = _exact_int(seed, "seed")
+        batches = _exact_int(batches, "batches", 0, 2**32 - 1)
+        mne = _exact_int(mne_target, "mne_target", 1, 2**32 - 1)
+        e = self._engine
+        res = e.evaluate_faco_evaluations(np.array([self._key], np.uint64), np.array([seed], np.uint64),
+                                          batches * e.ants, mne)
+        item = res["items"][0]
+        return {"tour": item["tour"], "cost": item["cost"], "initial_cost": self._registration["initial_cost"],
+                "preparation_seconds": self._registration["preparation_seconds"],
+                "solve_seconds": res["elapsed_seconds"], "batches": res["completed_batches"],
+                "construction_steps": res["completed_construction_steps"],
+                "ls_evaluations": res["completed_ls_evaluations"]}
+
+    def close(self) -> None:
+        self._engine.close()
 
 
 def program_to_c(program: dict) -> _lib.Program:

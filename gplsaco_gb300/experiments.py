@@ -40,9 +40,15 @@ class GapConfig:
     floor: float = 0.05
     gamma: int = 1
     target_gap: float = 0.01
-    # (floor, gamma, chunk) candidates, tuned on validation instances (seeds 200-215)
-    # by wall-clock time to the target gap
-    tune_grid: tuple = ((0.05, 1, 10), (0.05, 2, 10), (0.2, 1, 10), (0.5, 1, 10), (0.2, 2, 10), (0.05, 1, 25))
+    extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
+    # (model, floor, gamma, chunk) candidates, tuned on validation instances
+    # (seeds 200-214) by wall-clock time to the target gap.  "full" sees all six
+    # features; "geometry" only the four geometric ones (trail level and
+    # best-tour membership masked), so it does not pull ants back onto the
+    # parent tour's edges.
+    tune_grid: tuple = (("full", 0.05, 1, 10), ("full", 0.5, 1, 10), ("geometry", 0.05, 1, 10),
+                        ("geometry", 0.2, 1, 10), ("geometry", 0.5, 1, 10), ("geometry", 0.05, 2, 10),
+                        ("geometry", 0.2, 2, 10))
     train_pool: int = 32
     train_snapshot: int = 25
     train_iterations: int = 300
@@ -146,6 +152,21 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     return rows, enabled, work
 
 
+GEOMETRY_FEATURES = 4   # x0..x3 of the edge features; x4 trail level, x5 best-tour membership
+
+
+def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
+    """Trains on the geometric features alone and clears the first-layer
+    weights of the others, so applying it ignores trail level and best-tour
+    membership."""
+    xg = x.copy()
+    xg[:, GEOMETRY_FEATURES:] = 0
+    params, losses = prior_mod.train(prior_mod.init_params(seed=1), xg, y, epochs=cfg.epochs, batch=cfg.batch,
+                                     lr=cfg.lr)
+    prior_mod.unpack(params)["w1"][:, GEOMETRY_FEATURES:] = 0.0
+    return params, losses
+
+
 def first_time_below(rows, target: float, extra_seconds: float = 0.0):
     for it, sec, gap, _ in rows:
         if gap <= target:
@@ -161,6 +182,9 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     params, losses = prior_mod.train(prior_mod.init_params(seed=1), x, y, epochs=cfg.epochs, batch=cfg.batch,
                                      lr=cfg.lr)
     log(f"training losses {np.round(losses, 4).tolist()}")
+    geo_params, geo_losses = geometry_model(x, y, cfg)
+    log(f"geometry-model losses {np.round(geo_losses, 4).tolist()}")
+    models = {"full": params, "geometry": geo_params}
     # tune (floor, gamma, refresh chunk) on validation instances, by iterations to the target
     val = [_xy(kind, n, seed + 100) for kind, n, seed in cfg.eval_instances[::2]]
     val_refs = reference_lengths(cfg, val, device)
@@ -168,20 +192,21 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     val_warm = next(r for r in val_plain if r[0] == cfg.warmup)
     t_val, _ = first_time_below(val_plain, cfg.target_gap)
     tuning = []
-    for floor, gamma, chunk in cfg.tune_grid:
-        rows, _, work = gap_run(cfg, val, val_refs, params, val_warm[3], device, floor, gamma, chunk)
+    for model, floor, gamma, chunk in cfg.tune_grid:
+        rows, _, work = gap_run(cfg, val, val_refs, models[model], val_warm[3], device, floor, gamma, chunk)
         t, it = first_time_below(rows, cfg.target_gap, extra_seconds=val_warm[1])
-        tuning.append({"floor": floor, "gamma": gamma, "refresh_every": chunk, "final_gap": rows[-1][2],
-                       "iterations_to_target": it, "seconds_to_target": t, **work})
+        tuning.append({"model": model, "floor": floor, "gamma": gamma, "refresh_every": chunk,
+                       "final_gap": rows[-1][2], "iterations_to_target": it, "seconds_to_target": t, **work})
     best_row = min(tuning, key=lambda r: (r["seconds_to_target"] is None, r["seconds_to_target"] or 0.0,
                                           r["final_gap"]))
     best = (best_row["floor"], best_row["gamma"], best_row["refresh_every"])
-    log(f"validation plain: {t_val} s, {val_work}; tuning {tuning} -> {best}")
+    best_model = best_row["model"]
+    log(f"validation plain: {t_val} s, {val_work}; tuning {tuning} -> {best_model} {best}")
     xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
     refs = reference_lengths(cfg, xys, device)
     plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device)
     warm = next(r for r in plain_rows if r[0] == cfg.warmup)
-    prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, params, warm[3], device, *best)
+    prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, models[best_model], warm[3], device, *best)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
     out = {
@@ -191,13 +216,19 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         "ratio": (t_prior / t_plain) if (t_prior is not None and t_plain) else None,
         "prior_charged_warmup_seconds": warm[1],
         "prior_enabled_after_warmup": int(enabled.sum()), "instances": len(xys),
-        "prior_setting": {"floor": best[0], "gamma": best[1], "refresh_every": best[2]},
+        "prior_setting": {"model": best_model, "floor": best[0], "gamma": best[1], "refresh_every": best[2]},
         "plain_work": plain_work, "prior_work": prior_work,
         "validation_plain": {"seconds_to_target": t_val, **val_work}, "tuning": tuning,
+        "other_targets": {
+            str(g): {"plain_seconds": first_time_below(plain_rows, g)[0],
+                     "prior_seconds": first_time_below(prior_rows, g, extra_seconds=warm[1])[0],
+                     "plain_iterations": first_time_below(plain_rows, g)[1],
+                     "prior_iterations": first_time_below(prior_rows, g)[1]} for g in cfg.extra_targets},
         "final_gap_plain": plain_rows[-1][2], "final_gap_prior": prior_rows[-1][2],
         "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(plain_rows, prior_rows)
                    if r[0] % 50 == 0},
         "training_rows": int(len(y)), "training_loss": [float(v) for v in losses],
+        "geometry_training_loss": [float(v) for v in geo_losses],
         "total_seconds": time.perf_counter() - t_start,
     }
     return out

@@ -107,6 +107,8 @@ typedef struct faco_outputs {
     uint64_t reversed_elements; /* tour elements moved by relocations/reversals */
     double kernel_milliseconds; /* device time of the iteration loop             */
     double solve_seconds;
+    uint64_t* colony_work;      /* [count][3] per colony: construction steps, LS
+                                   evaluations, reversed elements; may be NULL */
 } faco_outputs;
 
 /* evaluate_faco_evaluations(keys, seeds, evaluation_limit_per_colony, mne,

@@ -163,8 +163,37 @@ def ref():
         R.ref_score.restype = C.c_int
         R.ref_score.argtypes = [C.c_uint16, C.c_uint16, C.c_uint16, C.c_uint16, u8p, u8p, C.c_uint16, f32p,
                                 f32p, u32p, C.c_uint32, f32p, i32p]
+        R.ref_colony.restype = C.c_int
+        R.ref_colony.argtypes = [C.c_uint32, f64p, u32p, C.c_uint32, u32p, C.c_uint32, u32p, C.c_uint32, u32p,
+                                 C.c_double, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, C.c_double,
+                                 C.c_double, C.c_double, C.c_uint64, C.c_uint64, u32p, C.POINTER(C.c_double)]
         _ref = R
     return _ref
+
+
+def ref_colony(xy, prep, *, ants, k, b, w, mne, iterations, seed, beta=1.0, retention=0.98, p_best=0.1,
+               epoch_source_probability=0.01, ls_limit=100000):
+    """A whole colony run by the reference's own CPU core (needs oracle/_ref),
+    on the EUC_2D integer metric, from the oracle's prepared rows; draws from
+    std::mt19937_64(seed).  Returns (tour, cost)."""
+    R = ref()
+    if R is None:
+        raise RuntimeError("oracle/_ref is not built")
+    xy = np.ascontiguousarray(xy, dtype=np.int32)
+    n = xy.shape[0]
+    matrix = np.ascontiguousarray(euc2d_matrix(xy), dtype=np.float64)
+    kk, bb = prep["primary"].shape[1], prep["backup"].shape[1]
+    backup = np.ascontiguousarray(prep["backup"] if bb else np.zeros((n, 1), np.uint32), dtype=np.uint32)
+    tour = np.zeros(n, np.uint32)
+    cost = C.c_double()
+    code = R.ref_colony(n, matrix, np.ascontiguousarray(prep["primary"], np.uint32), kk, backup, bb,
+                        np.ascontiguousarray(prep["ls"], np.uint32), prep["ls"].shape[1],
+                        np.ascontiguousarray(prep["initial"], np.uint32), float(prep["cost"]), ants,
+                        mne, iterations, beta, retention, p_best, epoch_source_probability, ls_limit, seed, tour,
+                        C.byref(cost))
+    if code != 0:
+        raise RuntimeError(f"ref_colony failed ({code})")
+    return tour, cost.value
 
 
 # ---------------------------------------------------------------- helpers

@@ -12,6 +12,8 @@
 
 #include <cstring>
 #include <exception>
+#include <limits>
+#include <random>
 #include <vector>
 
 using gp_faco::Node;
@@ -130,6 +132,76 @@ int ref_score(std::uint16_t ir_version, std::uint16_t numeric_spec_id, std::uint
                                             std::vector<std::uint32_t>(masks, masks + colonies));
         std::memcpy(scores, out.scores.data(), out.scores.size() * sizeof(float));
         std::memcpy(actions, out.actions.data(), out.actions.size() * sizeof(std::int32_t));
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// A whole plain-FACO colony run from the reference's CPU pieces, composed the
+// way tests/cpp/test_fixed_faco.cpp:58-119 replays the GPU engine (the
+// reduce/select/update order of cuda/colony_state.cuh:148-229): per
+// iteration, products = trails x 1/d^beta (SparsePheromone::product_cache);
+// every ant starts at a uniform node, builds by FocusedConstruction +
+// select_next and runs checklist_two_opt; the first strictly shortest ant is
+// the iteration best; the global best improves only strictly; the parent is
+// the global best with probability epoch_source_probability, else the
+// iteration best; trails evaporate to the new limits and take 1/cost of the
+// source along the parent.  Draws come from std::mt19937_64(seed): the start
+// node, one uniform per construction step, one per iteration for the source.
+int ref_colony(std::uint32_t n, const double* matrix, const std::uint32_t* primary, std::uint32_t k,
+               const std::uint32_t* backup, std::uint32_t b, const std::uint32_t* ls_rows, std::uint32_t w,
+               const std::uint32_t* initial, double initial_cost, std::uint32_t ants, std::uint32_t mne,
+               std::uint32_t iterations, double beta, double retention, double p_best, double source_probability,
+               std::uint64_t ls_limit, std::uint64_t seed, std::uint32_t* tour_out, double* cost_out) {
+    try {
+        const auto distance = matrix_distance(matrix, n);
+        const auto primary_rows = rows_of(primary, n, k);
+        const auto backup_rows = b ? rows_of(backup, n, b) : gp_faco::CandidateRows(n);
+        gp_faco::DistanceOrderedCandidates ls(rows_of(ls_rows, n, w), distance);
+        std::mt19937_64 random(seed);
+        std::uniform_real_distribution<double> uniform(0, 1);
+        std::uniform_int_distribution<Node> start(0, n - 1);
+        std::vector<Node> parent(initial, initial + n), best(parent);
+        double best_cost = initial_cost;
+        const auto initial_limits = gp_faco::candidate_trail_limits(k, p_best, retention, best_cost);
+        gp_faco::SparsePheromone pheromone(primary_rows, initial_limits.maximum, true);
+        for (std::uint32_t it = 0; it < iterations; ++it) {
+            const auto products = pheromone.product_cache(distance, beta);
+            gp_faco::CpuTour reference(parent, distance);
+            std::vector<Node> iteration_tour;
+            double iteration_cost = std::numeric_limits<double>::infinity();
+            for (std::uint32_t ant = 0; ant < ants; ++ant) {
+                gp_faco::FocusedConstruction cpu(reference, start(random), mne);
+                while (!cpu.done()) {
+                    const Node current = cpu.current();
+                    const std::vector<double> row(products.begin() + static_cast<std::size_t>(current) * k,
+                                                  products.begin() + static_cast<std::size_t>(current + 1) * k);
+                    const auto chosen = gp_faco::select_next(current, primary_rows[current], row,
+                                                             backup_rows[current], cpu.visited(), distance,
+                                                             uniform(random));
+                    cpu.step(chosen.node);
+                }
+                cpu.tour().checklist_two_opt(ls, cpu.checklist(), ls_limit);
+                if (cpu.tour().cost() < iteration_cost) {
+                    iteration_cost = cpu.tour().cost();
+                    iteration_tour = cpu.tour().order();
+                }
+            }
+            if (iteration_cost < best_cost) {
+                best_cost = iteration_cost;
+                best = iteration_tour;
+            }
+            const bool from_best = uniform(random) < source_probability;
+            parent = from_best ? best : iteration_tour;
+            const double deposit_cost = from_best ? best_cost : iteration_cost;
+            const auto limits = gp_faco::candidate_trail_limits(k, p_best, retention, best_cost);
+            pheromone.evaporate(retention, limits.minimum);
+            for (Node i = 0; i < n; ++i)
+                pheromone.deposit(parent[(i + n - 1) % n], parent[i], 1.0 / deposit_cost, limits.maximum);
+        }
+        std::memcpy(tour_out, best.data(), n * sizeof(Node));
+        *cost_out = gp_faco::CpuTour(best, distance).recomputed_cost();
         return 0;
     } catch (const std::exception&) {
         return -1;

@@ -280,25 +280,73 @@ def test_gp_controlled_population_matches_oracle(api, oracle, n, ants, iteration
     replicas = 2
     xy = _cases.uniform_instance(n, seed=n + 5)
     settings = _settings(api, ants, retention=0.9)
-    engine = api.FacoBatchEngine(n, len(programs) * replicas, settings)
+    engine = api.FacoBatchEngine(n, replicas, settings, population_size=len(programs))
     engine.register_problem(42, xy.astype(np.float64))
     prep = oracle.prepare(xy, 16, 64, 20)
-    keys = np.full(len(programs) * replicas, 42, np.uint64)
-    seeds = np.tile(np.arange(replicas, dtype=np.uint64) + 3, len(programs))
+    keys = np.full(replicas, 42, np.uint64)
+    seeds = np.arange(replicas, dtype=np.uint64) + 3
     mask = 0xFFFFFFFF if n != 250 else 0x00FF00FF
     res = engine.evaluate_population_evaluations(keys, seeds, ants * iterations, programs, mask, trace=True)
-    assert res["individual_costs"].shape == (len(programs), replicas)
-    for c in range(keys.size):
-        key = oracle.lib().orc_colony_key(int(seeds[c]), 42)
-        ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations, key=key,
-                                retention=0.9, program=programs[c // replicas], mask=mask,
-                                total_iterations=iterations)
-        assert res["items"][c]["cost"] == ref["cost"], c
-        assert res["items"][c]["tour"] == ref["tour"].tolist(), c
-        for it in range(iterations):
-            row, want = res["trace"][it, c], ref["trace"][it]
-            for field in ("iteration_best_cost", "global_cost", "parent_cost", "iteration_best", "mne_target",
-                          "action", "construction_steps", "ls_evaluations"):
-                assert int(row[field]) == int(want[field]), (c, it, field)
-            assert row["tau_min"] == np.float32(want["tau_min"]) and row["tau_max"] == np.float32(want["tau_max"])
+    assert len(res) == len(programs)
+    for i, program in enumerate(programs):
+        part = res[i]
+        assert part["population_size"] == len(programs) and len(part["items"]) == replicas
+        assert part["completed_construction_steps"] == int(part["colony_work"][:, 0].sum())
+        for j in range(replicas):
+            key = oracle.lib().orc_colony_key(int(seeds[j]), 42)
+            ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations, key=key,
+                                    retention=0.9, program=program, mask=mask, total_iterations=iterations)
+            assert part["items"][j]["cost"] == ref["cost"], (i, j)
+            assert part["items"][j]["tour"] == ref["tour"].tolist(), (i, j)
+            for it in range(iterations):
+                row, want = part["trace"][it, j], ref["trace"][it]
+                for field in ("iteration_best_cost", "global_cost", "parent_cost", "iteration_best", "mne_target",
+                              "action", "construction_steps", "ls_evaluations"):
+                    assert int(row[field]) == int(want[field]), (i, j, it, field)
+                assert row["tau_min"] == np.float32(want["tau_min"]) and row["tau_max"] == np.float32(want["tau_max"])
+    # a joint_single controller dict is its one tree; a conditional one is refused
+    one = engine.evaluate_controller_evaluations(
+        np.full(2, 42, np.uint64), seeds, ants * iterations,
+        {"controller_version": 1, "representation": "joint_single", "controller_id": 7, "trees": [programs[0]]},
+        mask)
+    assert [it["cost"] for it in one["items"]] == [it["cost"] for it in res[0]["items"]]
+    with pytest.raises(ValueError):
+        engine.evaluate_controller_evaluations(
+            keys, seeds, ants * iterations,
+            {"controller_version": 1, "representation": "conditional_three", "controller_id": 7,
+             "trees": programs[:3]})
+    with pytest.raises(ValueError):
+        engine.evaluate_population_evaluations(np.full(3, 42, np.uint64), np.arange(3, dtype=np.uint64),
+                                               ants * iterations, programs)     # not the whole panel
     engine.close()
+
+
+def test_fixed_faco_gpu_and_sessions(api, oracle):
+    """FixedFacoGpu.run_iterations restarts its colony on every call and
+    equals the batch engine's colony for the same (instance, seed);
+    GpuSession.solve_population returns one result per program."""
+    n, ants, iterations = 120, 8, 6
+    xy = _cases.uniform_instance(n, seed=77)
+    settings = _settings(api, ants)
+    fixed = api.FixedFacoGpu(xy.astype(np.float64), 5, settings)
+    first = fixed.run_iterations(3, iterations, 8)
+    again = fixed.run_iterations(3, iterations, 8)
+    assert first["tour"] == again["tour"] and first["cost"] == again["cost"]
+    assert first["batches"] == iterations and first["cost"] <= first["initial_cost"]
+    prep = oracle.prepare(xy, 16, 64, 20)
+    ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations,
+                            key=oracle.lib().orc_colony_key(3, 5), retention=0.98)
+    assert first["cost"] == ref["cost"] and first["tour"] == ref["tour"].tolist()
+    with pytest.raises(ValueError):
+        fixed.run_iterations(True, 1, 8)
+    fixed.close()
+    from gplsaco_gb300.session import GpuSession, Instance
+    session = GpuSession(colonies=2, settings=settings)
+    problems = {"a": Instance(5, xy)}
+    programs = [dict(ir_version=1, numeric_spec_id=1, feature_spec_id=3, opcode=[0], operand=[4], constant_bits=[]),
+                dict(ir_version=1, numeric_spec_id=1, feature_spec_id=3, opcode=[0], operand=[5], constant_bits=[])]
+    results, timing = session.solve_population(problems, [("a", 3), ("a", 4)], iterations, programs)
+    assert len(results) == 2 and all(len(r["items"]) == 2 for r in results)
+    plain, _ = session.solve(problems, [("a", 3), ("a", 4)], iterations)
+    assert plain["items"][0]["cost"] == ref["cost"]
+    session.close()
