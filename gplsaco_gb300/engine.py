@@ -342,14 +342,15 @@ class FacoBatchEngine:
         tours = np.zeros((count, D), np.uint32)
         costs = np.zeros(count, np.int64)
         trace_rows = np.zeros((min(cap, done), count), _lib.TRACE_DTYPE) if cap else None
+        work = np.zeros((count, 3), np.uint64)
         out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), None)
+        out.colony_work = work.ctypes.data
         self._active = None
         _lib.check(self._L.faco_finish(self._handle, C.byref(out)))
         return {"tours": [tours[c, :self._sizes[int(keys[c])]] for c in range(count)], "costs": costs,
                 "completed_batches": int(out.completed_batches),
                 "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
-                "reversed_elements": int(out.reversed_elements),
-            "colony_work": work, "trace": trace_rows}
+                "reversed_elements": int(out.reversed_elements), "colony_work": work, "trace": trace_rows}
 
     # ---- learned edge prior on the active stepwise evaluation ---------------
     def edge_data(self, features: bool = True, labels: bool = True):
