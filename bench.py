@@ -1,15 +1,25 @@
-"""Benchmark: plain Focused-ACO ant-tours+LS per second at N=1000 on GB300.
+"""Benchmark: Focused-ACO ant-tours+LS per second on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload throughput|uneven|large|gp-population|time-to-gap]
 
 A step is one ACO iteration of the whole panel: every ant of every colony
 constructs a tour from its colony's parent and runs its local search, then
-each colony reduces, selects and updates its trails.  Workload: 16 instances
-of N=1000 integer coordinates uniform in [0,10^6]^2 x 16 seeds = 256 colonies,
-32 ants each, k=16, backup 64, LS width 20, MNE 8, 2-opt, retention 0.98.
+each colony reduces, selects and updates its trails.  Default workload
+(throughput): 16 instances of N=1000 integer coordinates uniform in
+[0,10^6]^2 x 16 seeds = 256 colonies, 32 ants each, k=16, backup 64, LS
+width 20, MNE 8, 2-opt, retention 0.98.  Other workloads:
+  uneven         256 clustered instances, N ~ U[200,1000], 16 ants, k=16
+                 (one colony each; size-class launches in one CUDA graph);
+  large          16 clustered instances, N ~ U[5000,10000] in [0,10^7]^2,
+                 5 seeds, 64 ants, k=32, 2-opt window 32 + Or-opt (<= 3);
+  gp-population  one N=500 instance, 128 random GP controller programs, one
+                 colony each, 32 ants, k=16, 1000 iterations per call (a step
+                 is one population evaluation);
+  time-to-gap    learned-prior vs plain FACO wall-clock to a 1% mean gap.
 The data are synthetic (seeded), standing in for the reference's uniform
-TSP1000 rows.  With N>1 each rank runs its own panel (independent colonies,
-weak scaling, no collective on the data path).
+TSP1000 rows and its batch workloads.  With N>1 each rank runs its own
+panel (independent colonies, weak scaling, no collective on the data path).
 """
 from __future__ import annotations
 
@@ -19,6 +29,7 @@ import os
 import subprocess
 import sys
 import time
+from dataclasses import dataclass
 from pathlib import Path
 
 import numpy as np
@@ -26,26 +37,104 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-N = 1000
-INSTANCES = 16
-SEEDS_PER_INSTANCE = 16
-ANTS, K_PRIMARY, BACKUP, LS_WIDTH, MNE, RETENTION = 32, 16, 64, 20, 8, 0.98
-PRECONDITION = 100   # untimed iterations before the timed steps (steady-state trails)
-CPU_COLONIES_PER_THREAD = 6
-METRIC = "ant-tours+LS/sec (plain FACO, N=1000)"
 L2_BYTES = 129 * 2**20
+CPU_COLONIES_PER_THREAD = 16
+# DRAM bytes (read + write) of one steady-state ant_kernel<engine> launch of
+# the default panel, from ncu dram__bytes_read.sum + dram__bytes_write.sum
+# (profiles/ant_kernel_plain_faco_n1000.md, launches 105-106: 15.09 / 15.29 MB
+# read, 0 written).  Reported for the default workload only.
+ANT_TRAFFIC_BYTES_PER_LAUNCH = 15.19e6
 
 
-def instance_xy(i: int) -> np.ndarray:
+@dataclass
+class Workload:
+    """One benchmark panel: instances, the colony -> (instance, seed) map and
+    the FACO settings every colony runs with."""
+    name: str
+    metric: str
+    description: str
+    xys: list
+    colony_instance: np.ndarray
+    seeds: np.ndarray
+    ants: int
+    k: int
+    b: int
+    w: int
+    ls_mode: int = 0
+    mne: int = 8
+    retention: float = 0.98
+    precondition: int = 100          # untimed iterations before the timed steps (steady-state trails)
+    e2e_iterations: int | None = None  # iterations of the end-to-end call (None: precondition + steps)
+    cpu_colonies_per_thread: int = CPU_COLONIES_PER_THREAD
+
+    def run_iterations(self, steps: int) -> int:
+        """Iterations of the end-to-end call; the CPU sample spans the same."""
+        return self.e2e_iterations or (self.precondition + steps)
+
+    @property
+    def colonies(self) -> int:
+        return int(self.colony_instance.size)
+
+    def sizes(self) -> np.ndarray:
+        return np.array([len(self.xys[i]) for i in self.colony_instance], np.int64)
+
+
+def instance_xy(i: int, n: int = 1000) -> np.ndarray:
     rng = np.random.default_rng(1000 + i)
-    return rng.integers(0, 10**6 + 1, size=(N, 2)).astype(np.int32)
+    return rng.integers(0, 10**6 + 1, size=(n, 2)).astype(np.int32)
 
 
-def bytes_per_fe(n, k, ants, steps_per_fe, evals_per_fe, moved_per_fe) -> float:
-    """Algorithmic bytes per ant-tour+LS: parent read + tour write (8N),
-    candidate id + weight per construction step (8k each), 20 B per LS move
-    evaluation, 16 B per moved tour element, trail update amortised per ant."""
-    return 8 * n + 8 * k * steps_per_fe + 20 * evals_per_fe + 16 * moved_per_fe + 16 * n * k / ants
+def make_workload(name: str, rank: int = 0) -> Workload:
+    from gplsaco_gb300 import instances
+    if name == "throughput":
+        return Workload(
+            "throughput", "ant-tours+LS/sec (plain FACO, N=1000)",
+            "plain FACO, N=1000 uniform int coords, 16 instances x 16 seeds = 256 colonies, 32 ants, k=16, "
+            "backup 64, LS width 20, MNE 8, 2-opt, retention 0.98",
+            [instance_xy(i) for i in range(16)], np.repeat(np.arange(16), 16),
+            np.tile(np.arange(16, dtype=np.uint64), 16) + np.uint64(1000 * rank), 32, 16, 64, 20)
+    if name == "uneven":
+        return Workload(
+            "uneven", "ant-tours+LS/sec (uneven batch, N~U[200,1000])",
+            "plain FACO, 256 clustered instances (4-16 Gaussian clusters, sigma 2-8% of [0,10^6], 20% uniform "
+            "noise), N ~ U[200,1000], one colony each, 16 ants, k=16, backup 64, LS width 20, MNE 8, 2-opt, "
+            "retention 0.98; size-class ant launches as parallel graph branches, warps per block autotuned",
+            instances.uneven_batch(256, (200, 1000)), np.arange(256),
+            np.full(256, 1 + 1000 * rank, np.uint64), 16, 16, 64, 20, e2e_iterations=500)
+    if name == "large":
+        return Workload(
+            "large", "ant-tours+LS/sec (large clustered, N~U[5000,10000])",
+            "plain FACO, 16 clustered instances (32-64 clusters, [0,10^7]^2), N ~ U[5000,10000], 5 seeds each "
+            "= 80 colonies, 64 ants, k=32, backup 64, 2-opt window 32 + Or-opt (segments <= 3), MNE 8, "
+            "retention 0.98",
+            instances.large_clustered(16), np.repeat(np.arange(16), 5),
+            np.tile(np.arange(5, dtype=np.uint64), 16) + np.uint64(1000 * rank), 64, 32, 64, 32, ls_mode=1,
+            precondition=20, e2e_iterations=100, cpu_colonies_per_thread=2)
+    raise ValueError(f"unknown workload {name}")
+
+
+def size_classes(sizes) -> int:
+    """Ant-kernel launches per iteration: one per instance size class
+    (n rounded up to a power of two, at least 256)."""
+    def class_of(n):
+        c = 0
+        while (256 << c) < n:
+            c += 1
+        return c
+    return len({class_of(int(n)) for n in sizes})
+
+
+def launch_bytes(wl: Workload, work: np.ndarray, iterations: int) -> float:
+    """Algorithmic bytes of one iteration (one ant launch per size class over
+    every ant): per ant parent read + tour write (8 B per node), per colony
+    the trail update (16 B per candidate entry), and the counted work --
+    candidate id + weight per construction step (8 B x k), 20 B per LS move
+    evaluation, 16 B per moved tour element -- averaged over the iterations
+    the counters cover."""
+    n = wl.sizes().astype(np.float64)
+    fixed = float(np.sum(8.0 * wl.ants * n + 16.0 * n * wl.k))
+    counted = 8.0 * wl.k * float(work[:, 0].sum()) + 20.0 * float(work[:, 1].sum()) + 16.0 * float(work[:, 2].sum())
+    return fixed + counted / iterations
 
 
 class ClockSampler:
@@ -98,37 +187,44 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_colonies(threads: int, colonies: int, iterations: int) -> float:
-    """Runs `colonies` N=1000 colonies of `iterations` iterations each with the
-    oracle port (C), one colony per host thread; returns elapsed seconds."""
+def cpu_colonies(wl: Workload, threads: int, colonies: int, iterations: int, program=None) -> float:
+    """Runs `colonies` colonies of the workload (its colonies in order,
+    cycling) for `iterations` iterations each with the oracle port (C), one
+    colony per host thread; returns elapsed seconds (preparation excluded)."""
     from concurrent.futures import ThreadPoolExecutor
 
     from oracle import oracle
     oracle.lib()
-    xy = instance_xy(0)
-    prep = oracle.prepare(xy, K_PRIMARY, BACKUP, LS_WIDTH)
+    picks = [c % wl.colonies for c in range(colonies)]
+    needed = sorted({int(wl.colony_instance[c]) for c in picks})
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        preps = dict(zip(needed, pool.map(lambda i: oracle.prepare(wl.xys[i], wl.k, wl.b, wl.w), needed)))
 
-    def one(i):
-        oracle.run_colony(xy, prep, ants=ANTS, k=K_PRIMARY, b=BACKUP, w=LS_WIDTH, mne=MNE, iterations=iterations,
-                          key=oracle.lib().orc_colony_key(i, 1), retention=RETENTION, threads=1, want_trace=False)
+    def one(c):
+        i = int(wl.colony_instance[c])
+        oracle.run_colony(wl.xys[i], preps[i], ants=wl.ants, k=wl.k, b=wl.b, w=wl.w, mne=wl.mne,
+                          iterations=iterations, key=oracle.lib().orc_colony_key(int(wl.seeds[c]), 1 + i),
+                          retention=wl.retention, threads=1, want_trace=False, ls_mode=wl.ls_mode,
+                          program=program, total_iterations=iterations if program else None)
 
     start = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as pool:
-        list(pool.map(one, range(colonies)))
+        list(pool.map(one, picks))
     return time.perf_counter() - start
 
 
-def cpu_baseline(iterations: int) -> dict:
-    """The oracle port on a bounded sample of the same workload: one N=1000
-    colony of 32 ants per host thread, `iterations` iterations from the
-    prepared initial tour (the span of the e2e measurement)."""
+def cpu_baseline(wl: Workload, iterations: int) -> dict:
+    """The oracle port on a bounded sample of the same workload: one colony
+    per host thread at a time, `iterations` iterations from the prepared
+    initial tour."""
     threads = os.cpu_count() or 1
-    colonies = CPU_COLONIES_PER_THREAD * threads
-    elapsed = cpu_colonies(threads, colonies, iterations)
-    fe = colonies * ANTS * iterations
+    colonies = min(wl.cpu_colonies_per_thread * threads, wl.colonies)
+    elapsed = cpu_colonies(wl, threads, colonies, iterations)
+    fe = colonies * wl.ants * iterations
     return {"value": fe / elapsed, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
-            "sample": f"{colonies} N=1000 colonies x 32 ants x {iterations} iterations ({fe} ant-tours+LS) "
-                      f"from the prepared initial tour, one colony per host thread, {elapsed:.1f} s"}
+            "sample": f"{colonies} colonies of the {wl.name} panel x {wl.ants} ants x {iterations} iterations "
+                      f"({fe} ant-tours+LS) from the prepared initial tour, one colony per host thread, "
+                      f"{elapsed:.1f} s"}
 
 
 def measured_peak():
@@ -140,29 +236,42 @@ def measured_peak():
 
 def run_reference(args, rank: int) -> None:
     """The CPU implementation of the path (the oracle port; the reference's own
-    C++ core cannot be built on this host) on all host threads: one colony per
-    thread, PRECONDITION + steps iterations each, like the e2e measurement."""
+    C++ core is built only where its sources are) on all host threads: one
+    colony per thread at a time, the workload's CPU sample length."""
     if rank != 0:
         return
+    if args.workload == "gp-population":
+        run_population_reference(args)
+        return
+    wl = make_workload(args.workload)
     threads = os.cpu_count() or 1
-    iterations = PRECONDITION + args.steps
-    colonies = CPU_COLONIES_PER_THREAD * threads
-    cpu_colonies(threads, threads, max(1, args.warmup))
-    elapsed = cpu_colonies(threads, colonies, iterations)
-    fe = colonies * ANTS * iterations
+    iterations = wl.run_iterations(args.steps)
+    colonies = min(wl.cpu_colonies_per_thread * threads, wl.colonies)
+    cpu_colonies(wl, threads, threads, max(1, min(args.warmup, 3)))
+    elapsed = cpu_colonies(wl, threads, colonies, iterations)
+    fe = colonies * wl.ants * iterations
     value = fe / elapsed
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ant-tours+LS/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / iterations,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
-            "data": "synthetic",
-            "config": {"workload": f"plain FACO N=1000 uniform, {colonies} colonies x 32 ants ({threads} host "
-                                   f"threads, one colony each at a time), k=16, backup 64, LS width 20, MNE 8, "
-                                   f"2-opt, retention 0.98, {iterations} iterations from the initial tour",
-                       "colonies": colonies, "ants": ANTS, "n": N},
+    line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": "ant-tours+LS/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / iterations,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": {"workload": f"{wl.description}; CPU: {colonies} colonies ({threads} host threads, one "
+                                   f"colony each at a time), {iterations} iterations from the initial tour",
+                       "colonies": colonies, "ants": wl.ants},
             "cpu_baseline": {"value": value, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
                              "sample": f"{colonies} colonies x {iterations} iterations"},
             "e2e": {"value": value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _engine(wl: Workload, device: int):
+    import gplsaco_gb300 as g
+    settings = g.FixedFacoSettings(ants=wl.ants, primary_width=wl.k, backup_width=wl.b, ls_width=wl.w,
+                                   retention=wl.retention, ls_mode=wl.ls_mode)
+    engine = g.FacoBatchEngine(int(max(len(x) for x in wl.xys)), wl.colonies, settings, device=device)
+    t0 = time.perf_counter()
+    for i, xy in enumerate(wl.xys):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    return engine, time.perf_counter() - t0
 
 
 def run_gb300(args, rank: int, world: int) -> None:
@@ -170,27 +279,19 @@ def run_gb300(args, rank: int, world: int) -> None:
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    import gplsaco_gb300 as g
-
-    colonies = INSTANCES * SEEDS_PER_INSTANCE
-    settings = g.FixedFacoSettings(ants=ANTS, primary_width=K_PRIMARY, backup_width=BACKUP, ls_width=LS_WIDTH,
-                                   retention=RETENTION)
-    engine = g.FacoBatchEngine(N, colonies, settings, device=local)
-    t0 = time.perf_counter()
-    for i in range(INSTANCES):
-        engine.register_problem(1 + i, instance_xy(i).astype(np.float64))
-    registration_s = time.perf_counter() - t0
-    keys = np.repeat(np.arange(1, INSTANCES + 1, dtype=np.uint64), SEEDS_PER_INSTANCE)
-    seeds = (np.tile(np.arange(SEEDS_PER_INSTANCE, dtype=np.uint64), INSTANCES)
-             + np.uint64(1000 * rank))
+    wl = make_workload(args.workload, rank)
+    engine, registration_s = _engine(wl, local)
+    keys = (wl.colony_instance + 1).astype(np.uint64)
+    seeds = wl.seeds
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.ExternalStream(engine.stream_ptr)
+    classes = size_classes(wl.sizes())
 
     # ---- device throughput: inputs resident, L2 flushed before every step ----
-    # the panel first runs PRECONDITION iterations so that the timed steps see
+    # the panel first runs `precondition` iterations so that the timed steps see
     # converged trails (construction steps per tour grow as they converge)
-    engine.begin(keys, seeds, MNE)
-    engine.step(PRECONDITION + args.warmup)
+    engine.begin(keys, seeds, wl.mne)
+    engine.step(wl.precondition + args.warmup)
     torch.cuda.synchronize()
     step_ms = []
     with ClockSampler(local) as clocks:
@@ -214,61 +315,194 @@ def run_gb300(args, rank: int, world: int) -> None:
     ant_ms, upd_ms = engine.step_timed(kernel_steps)
     totals = engine.finish()
     iters = totals["completed_batches"]
-    fe_total = iters * colonies * ANTS
-    s_fe = totals["construction_steps"] / fe_total
-    e_fe = totals["ls_evaluations"] / fe_total
-    r_fe = totals["reversed_elements"] / fe_total
+    work = totals["colony_work"].astype(np.float64)
+    fe_total = iters * wl.colonies * wl.ants
     elapsed_ms = float(np.sum(step_ms))
     if world > 1:
         t = torch.tensor([elapsed_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed_ms = float(t.item())
-    fe_timed = args.steps * colonies * ANTS * world
+    fe_timed = args.steps * wl.colonies * wl.ants * world
     value = fe_timed / (elapsed_ms / 1e3)
 
     # ---- end to end through the public API: host keys/seeds in, tours out;
-    # one solve call of PRECONDITION + steps iterations from the initial tours ----
-    e2e_iters = PRECONDITION + args.steps
-    engine.evaluate_faco_evaluations(keys, seeds, ANTS * args.warmup, MNE)
+    # one solve call from the initial tours ----
+    e2e_iters = wl.run_iterations(args.steps)
+    engine.evaluate_faco_evaluations(keys, seeds, wl.ants * max(1, args.warmup), wl.mne)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = engine.evaluate_faco_evaluations(keys, seeds, ANTS * e2e_iters, MNE)
+    res = engine.evaluate_faco_evaluations(keys, seeds, wl.ants * e2e_iters, wl.mne)
     e2e_s = time.perf_counter() - t0
-    e2e_value = e2e_iters * colonies * ANTS / e2e_s
+    e2e_value = e2e_iters * wl.colonies * wl.ants / e2e_s
     h2d = keys.nbytes + seeds.nbytes
-    d2h = colonies * N * 4 + colonies * 8
-    assert all(len(it["tour"]) == N for it in res["items"])
+    d2h = wl.colonies * engine.dimension * 4 + wl.colonies * 8
+    assert all(len(it["tour"]) == n for it, n in zip(res["items"], wl.sizes()))
 
-    # ---- roofline of the ant kernel (per launch = one step of all ants) ----
-    bfe = bytes_per_fe(N, K_PRIMARY, ANTS, s_fe, e_fe, r_fe)
-    ants_per_launch = colonies * ANTS
-    achieved = bfe * ants_per_launch / (ant_ms / kernel_steps / 1e3) / 1e9
+    # ---- roofline of the ant kernel (per launch set = one step of all ants) ----
+    per_launch = launch_bytes(wl, work, iters)
+    achieved = per_launch / (ant_ms / kernel_steps / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     engine.close()
     if rank != 0:
         return
-    base = cpu_baseline(PRECONDITION + 4) if args.cpu_baseline else None
+    base = None
+    if args.cpu_baseline:
+        base = cpu_baseline(wl, e2e_iters)
     line = {
-        "metric": METRIC, "value": value, "unit": "ant-tours+LS/s", "n_gpus": world, "steps": args.steps,
+        "metric": wl.metric, "value": value, "unit": "ant-tours+LS/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic",
-        "config": {"workload": "plain FACO, N=1000 uniform int coords, 16 instances x 16 seeds = 256 colonies, "
-                               "32 ants, k=16, backup 64, LS width 20, MNE 8, 2-opt, retention 0.98",
-                   "colonies": colonies, "ants": ANTS, "n": N, "l2": "flushed before every timed step "
-                   "(258 MB write)", "timed_iterations_start_at": PRECONDITION + args.warmup,
-                   "registration_seconds": registration_s},
+        "config": {"workload": wl.description, "colonies": wl.colonies, "ants": wl.ants,
+                   "n_range": [int(wl.sizes().min()), int(wl.sizes().max())],
+                   "l2": "flushed before every timed step (258 MB write)",
+                   "timed_iterations_start_at": wl.precondition + args.warmup,
+                   "registration_seconds": registration_s, "size_classes": classes},
         "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d / e2e_iters,
                 "d2h_bytes_per_step": d2h / e2e_iters, "iterations": e2e_iters,
                 "call": "FacoBatchEngine.evaluate_faco_evaluations (C ABI faco_evaluate), host keys/seeds in, "
                         "host tours/costs out"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "ant_kernel<engine>", "peak_source": peak_kind,
-                     "bytes_per_fe": bfe, "per_fe": {"construction_steps": s_fe, "ls_evaluations": e_fe,
-                                                      "moved_elements": r_fe},
+                     "traffic": ANT_TRAFFIC_BYTES_PER_LAUNCH if wl.name == "throughput" else None,
+                     "traffic_source": "ncu capture (profiles/ant_kernel_plain_faco_n1000.md)"
+                     if wl.name == "throughput" else None,
+                     "kernel": "ant_kernel<engine>", "peak_source": peak_kind,
+                     "bytes_per_launch": per_launch,
+                     "bytes_per_fe": per_launch / (wl.colonies * wl.ants),
+                     "per_fe": {"construction_steps": float(work[:, 0].sum()) / fe_total,
+                                "ls_evaluations": float(work[:, 1].sum()) / fe_total,
+                                "moved_elements": float(work[:, 2].sum()) / fe_total},
                      "ant_kernel_ms": ant_ms / kernel_steps, "update_kernel_ms": upd_ms / kernel_steps},
         "cpu_baseline": base,
         "clocks": clocks.summary(),
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": (classes + 1) * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---- GP evaluation batch: 128 controller programs on one N=500 instance ----
+POP_N, POP_SEED, POP_PROGRAMS, POP_ITERATIONS = 500, 2, 128, 1000
+POP_METRIC = "GP individuals evaluated/sec (N=500, 32 ants, 1000 iterations each)"
+
+
+def population_programs() -> list:
+    from gplsaco_gb300.programs import random_program
+    rng = np.random.default_rng(POP_SEED)
+    return [random_program(rng, extended=True, features=10, feature_spec_id=3) for _ in range(POP_PROGRAMS)]
+
+
+def population_workload() -> Workload:
+    from gplsaco_gb300 import instances
+    return Workload("gp-population", POP_METRIC, "", [instances.uniform(POP_N, POP_SEED)], np.zeros(1, np.int64),
+                    np.ones(1, np.uint64), 32, 16, 64, 20)
+
+
+def population_cpu(threads: int, colonies: int, iterations: int) -> float:
+    """Elapsed seconds of `colonies` controller-driven colonies (programs in
+    order) of `iterations` iterations on the oracle port, one per thread."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle
+    oracle.lib()
+    wl = population_workload()
+    programs = population_programs()
+    prep = oracle.prepare(wl.xys[0], wl.k, wl.b, wl.w)
+
+    def one(c):
+        oracle.run_colony(wl.xys[0], prep, ants=wl.ants, k=wl.k, b=wl.b, w=wl.w, mne=wl.mne, iterations=iterations,
+                          key=oracle.lib().orc_colony_key(1, 1), retention=wl.retention, threads=1,
+                          want_trace=False, program=programs[c % len(programs)], total_iterations=POP_ITERATIONS)
+
+    start = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        list(pool.map(one, range(colonies)))
+    return time.perf_counter() - start
+
+
+def population_cpu_line(colonies_per_thread: int = 2) -> dict:
+    """Whole 1000-iteration controller-driven runs of the first programs on
+    the oracle port, one colony per host thread at a time."""
+    threads = os.cpu_count() or 1
+    colonies = min(POP_PROGRAMS, colonies_per_thread * threads)
+    elapsed = population_cpu(threads, colonies, POP_ITERATIONS)
+    value = colonies / elapsed
+    return {"value": value, "unit": "individuals/s", "cores": threads, "kind": "port",
+            "sample": f"{colonies} of the {POP_PROGRAMS} programs, whole {POP_ITERATIONS}-iteration colony runs, "
+                      f"one per host thread at a time, {elapsed:.1f} s"}
+
+
+def run_population_reference(args) -> None:
+    base = population_cpu_line()
+    line = {"impl": "reference", "metric": POP_METRIC, "value": base["value"], "unit": "individuals/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": {"workload": "GP evaluation batch on the oracle port (CPU sample)"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "individuals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_population(args, rank: int, world: int) -> None:
+    import torch
+
+    import gplsaco_gb300 as g
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    wl = population_workload()
+    programs = population_programs()
+    settings = g.FixedFacoSettings(ants=wl.ants, primary_width=wl.k, backup_width=wl.b, ls_width=wl.w,
+                                   retention=wl.retention)
+    engine = g.FacoBatchEngine(POP_N, 1, settings, population_size=POP_PROGRAMS, device=local)
+    engine.register_problem(1, wl.xys[0].astype(np.float64))
+    keys, seeds = np.ones(1, np.uint64), np.array([1 + 1000 * rank], np.uint64)
+    stream = torch.cuda.ExternalStream(engine.stream_ptr)
+    budget = wl.ants * POP_ITERATIONS
+    for _ in range(args.warmup):
+        engine.evaluate_population_evaluations(keys, seeds, budget, programs)
+    torch.cuda.synchronize()
+    dev_ms, wall = [], []
+    with ClockSampler(local) as clocks:
+        if world > 1:
+            torch.distributed.barrier()
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            a.record(stream)
+            res = engine.evaluate_population_evaluations(keys, seeds, budget, programs)
+            b.record(stream)
+            b.synchronize()
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(a.elapsed_time(b))
+        if world > 1:
+            torch.distributed.barrier()
+    assert len(res) == POP_PROGRAMS and all(len(r["items"][0]["tour"]) == POP_N for r in res)
+    elapsed_ms = float(np.sum(dev_ms))
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    engine.close()
+    if rank != 0:
+        return
+    value = args.steps * POP_PROGRAMS * world / (elapsed_ms / 1e3)
+    e2e = args.steps * POP_PROGRAMS / float(np.sum(wall))
+    base = population_cpu_line() if args.cpu_baseline else None
+    line = {
+        "metric": POP_METRIC, "value": value, "unit": "individuals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": {"workload": "GP evaluation batch: 1 uniform N=500 instance (seed 2), 128 random controller "
+                               "programs (feature spec 3, depth <= 6), one colony each, 32 ants, k=16, 1000 "
+                               "iterations; a step is one evaluate_population_evaluations call",
+                   "l2": "each step runs 1000 iterations; the panel's working set (~30 MB) is L2-resident by design"},
+        "e2e": {"value": e2e, "unit": "individuals/s", "h2d_bytes_per_step": float(keys.nbytes + seeds.nbytes),
+                "d2h_bytes_per_step": float(POP_PROGRAMS * (POP_N * 4 + 8)),
+                "call": "FacoBatchEngine.evaluate_population_evaluations (C ABI faco_evaluate_programs)"},
+        "roofline": None,
+        "cpu_baseline": base,
+        "clocks": clocks.summary(),
+        "gpu_launches": (1 + 2 * POP_ITERATIONS) * args.steps,
     }
     print(json.dumps(line), flush=True)
 
@@ -294,7 +528,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="throughput", choices=["throughput", "time-to-gap"],
+    ap.add_argument("--workload", default="throughput",
+                    choices=["throughput", "uneven", "large", "gp-population", "time-to-gap"],
                     help="time-to-gap: learned-prior vs plain FACO wall-clock to a 1%% mean gap (N=1000/2000)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -308,7 +543,10 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    run_gb300(args, rank, world)
+    if args.workload == "gp-population":
+        run_population(args, rank, world)
+    else:
+        run_gb300(args, rank, world)
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()

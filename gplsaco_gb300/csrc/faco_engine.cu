@@ -19,6 +19,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/faco_gb300.h"
@@ -760,19 +761,43 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
     std::size_t node_off = 0;
     // Final verification of every incumbent on the host (batch_engine.cu:1075-1089):
     // a complete permutation whose recomputed length equals the device cost.
-    std::vector<std::uint32_t> tour;
-    std::vector<std::uint8_t> seen;
-    for (std::uint32_t c = 0; c < v.count; ++c) {
-        const std::uint32_t n = v.sizes[c];
-        tour.assign(global.begin() + node_off, global.begin() + node_off + n);
-        seen.assign(n, 0);
-        for (const std::uint32_t node : tour) {
-            require(node < n && !seen[node], "device incumbent is not a complete permutation");
-            seen[node] = 1;
+    // Colonies are split over host threads; the first failure is reported.
+    {
+        std::vector<std::size_t> offsets(v.count);
+        for (std::uint32_t c = 0; c < v.count; ++c) {
+            offsets[c] = node_off;
+            node_off += faco::pad8(v.sizes[c]);
         }
-        require(faco::host_tour_length(e->instances.at(v.keys[c])->xy, tour.data(), n) == states[c].global_cost,
-                "device incumbent cost differs from its full recomputation");
-        node_off += faco::pad8(n);
+        std::vector<const std::vector<std::int32_t>*> coords(v.count);
+        for (std::uint32_t c = 0; c < v.count; ++c) coords[c] = &e->instances.at(v.keys[c])->xy;
+        std::vector<int> verdict(v.count, 0);
+        auto verify = [&](std::uint32_t first, std::uint32_t stride) {
+            std::vector<std::uint32_t> tour;
+            std::vector<std::uint8_t> seen;
+            for (std::uint32_t c = first; c < v.count; c += stride) {
+                const std::uint32_t n = v.sizes[c];
+                tour.assign(global.begin() + offsets[c], global.begin() + offsets[c] + n);
+                seen.assign(n, 0);
+                bool permutation = true;
+                for (const std::uint32_t node : tour) {
+                    if (node >= n || seen[node]) { permutation = false; break; }
+                    seen[node] = 1;
+                }
+                verdict[c] = !permutation ? 1
+                           : faco::host_tour_length(*coords[c], tour.data(), n) != states[c].global_cost ? 2 : 0;
+            }
+        };
+        const std::size_t total_nodes = node_off;
+        const std::uint32_t workers = static_cast<std::uint32_t>(std::min<std::size_t>(
+            std::max(1u, std::min(16u, std::thread::hardware_concurrency())), 1 + total_nodes / 65536));
+        std::vector<std::thread> pool;
+        for (std::uint32_t t = 1; t < workers; ++t) pool.emplace_back(verify, t, workers);
+        verify(0, workers);
+        for (auto& th : pool) th.join();
+        for (std::uint32_t c = 0; c < v.count; ++c) {
+            require(verdict[c] != 1, "device incumbent is not a complete permutation");
+            require(verdict[c] != 2, "device incumbent cost differs from its full recomputation");
+        }
     }
     node_off = 0;
     for (std::uint32_t c = 0; c < v.count; ++c) {

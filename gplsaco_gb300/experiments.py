@@ -232,3 +232,27 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         "total_seconds": time.perf_counter() - t_start,
     }
     return out
+
+
+def profile_prior_application(refreshes: int = 3, device: int = 0) -> None:
+    """A short run of the prior application on the 16 evaluation instances
+    (random-initialised network): `python -m gplsaco_gb300.experiments`."""
+    cfg = GapConfig()
+    xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
+    engine = FacoBatchEngine(max(len(xy) for xy in xys), len(xys), _settings(cfg), device=device)
+    for i, xy in enumerate(xys):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    engine.begin(np.arange(1, len(xys) + 1, dtype=np.uint64), np.ones(len(xys), np.uint64), cfg.mne)
+    engine.step(10)
+    engine.prior_set(prior_mod.init_params(1), np.ones(len(xys), np.uint8), 0.2, 2)
+    for _ in range(refreshes):
+        engine.step(10)
+        engine.prior_refresh()
+    costs, it = engine.current_costs(len(xys))
+    engine.finish()
+    engine.close()
+    print(f"prior applied {refreshes + 1} times over {it} iterations; mean cost {float(np.mean(costs)):.1f}")
+
+
+if __name__ == "__main__":
+    profile_prior_application()

@@ -89,3 +89,35 @@ def train(params: np.ndarray, x_bits: np.ndarray, y: np.ndarray, *, epochs: int 
     _lib.check(_lib.load().faco_mlp_train(params.ctypes.data, xs.ctypes.data, ys.ctypes.data, ys.size, epochs,
                                           batch, lr, losses.ctypes.data))
     return params, losses
+
+
+def _profile_main(argv=None) -> None:
+    """A short, self-contained run of the MLP kernels for profiling:
+    `python -m gplsaco_gb300.prior --rows R --epochs E --forward-rows F`
+    trains on R synthetic rows (features uniform in [0, 1], labels from a
+    fixed rule) and runs one forward pass over F rows."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rows", type=int, default=1 << 20)
+    ap.add_argument("--epochs", type=int, default=1)
+    ap.add_argument("--batch", type=int, default=8192)
+    ap.add_argument("--forward-rows", type=int, default=1 << 22)
+    args = ap.parse_args(argv)
+    rng = np.random.default_rng(7)
+    x = rng.random((args.rows, IN), dtype=np.float32)
+    x[:, 6:] = 0.0
+    y = ((x[:, 0] < 0.2) | (x[:, 5] > 0.8)).astype(np.float32)
+    xb = to_bf16_bits(x)
+    t = time.perf_counter()
+    params, losses = train(init_params(1), xb, y, epochs=args.epochs, batch=args.batch)
+    print(f"train {args.rows} rows x {args.epochs} epochs: {time.perf_counter() - t:.3f} s, loss {losses.tolist()}")
+    xf = to_bf16_bits(rng.random((args.forward_rows, IN), dtype=np.float32) * np.array([1, 1, 1, 1, 1, 1, 0, 0],
+                                                                                       np.float32))
+    t = time.perf_counter()
+    p = forward(params, xf)
+    print(f"forward {args.forward_rows} rows: {time.perf_counter() - t:.3f} s, mean p {float(p.mean()):.4f}")
+
+
+if __name__ == "__main__":
+    _profile_main()
