@@ -10,9 +10,11 @@
 //   - every per-ant scalar is warp-uniform and lives in registers of all 32
 //     lanes (no shared State struct, no lane-0 serial sections beyond the
 //     single store of a queue slot or flag word);
-//   - the tour, its inverse and the checklist ring live in shared memory as
-//     16-bit nodes, the visited/pending flags as bitsets; coordinates are
-//     staged once per block for all its ants (one colony per block);
+//   - the tour and its inverse live in shared memory as 16-bit nodes, the
+//     visited/pending flags as bitsets; coordinates are staged once per
+//     block for all its ants (one colony per block); the checklist ring
+//     lives in the ant's own output-tour slot in global memory (L1-cached),
+//     which nothing reads before the ant writes its final tour there;
 //   - distances are exact EUC_2D integers computed on the fly, so gains and
 //     tour lengths are exact int64 and ties are decided by index only;
 //   - the roulette decides from an FP32 warp scan whenever a proven error
@@ -36,7 +38,13 @@ enum AntMode : int {
     kModeVisits = 1,    // explicit visit orders (diagnostic)
     kModeUniforms = 2,  // injected uniforms + given products (diagnostic)
     kModePrepare = 3,   // no construction; LS over the whole tour (registration)
+    kModeEngineGlobal = 4,  // kModeEngine with tour/inverse in global memory and
+                            // coordinates read from global (large instances)
 };
+
+__host__ __device__ constexpr bool engine_mode(int mode) {
+    return mode == kModeEngine || mode == kModeEngineGlobal;
+}
 
 struct AntLaunch {
     // instance (all ants of a block share one instance)
@@ -45,6 +53,9 @@ struct AntLaunch {
     const ColonyView* colonies;
     ColonyState* states;
     const uint2* work;            // per block: (colony, first ant)
+    node_t* workspace;            // kModeEngineGlobal: tour + inverse per ant, laid out
+                                  // like the colonies' ant_tours with rows of 2 x n_pad
+    const node_t* ant_tours_base; // start of the buffer the colonies' ant_tours point into
     std::uint32_t ants;           // ants per colony
     std::uint32_t warps;          // warps per block
     std::uint32_t n_max;          // smem layout size
@@ -62,7 +73,7 @@ struct AntLaunch {
     const float* task_products;      // [n][k]
     // diagnostic outputs (may be null)
     node_t* out_construction;     // [tasks][n]
-    node_t* out_tours;            // [tasks][n]
+    node_t* out_tours;            // [tasks][n]; required: also each task's checklist ring during the run
     node_t* out_pos;              // [tasks][n]
     node_t* out_selected;         // [tasks][n]
     std::uint32_t* out_checklist; // [tasks][checklist_cap]
@@ -74,26 +85,40 @@ struct AntLaunch {
 
 __host__ __device__ inline std::uint32_t pad8(std::uint32_t n) { return (n + 7u) & ~7u; }
 
-// Per-warp shared-memory workspace: tour, inverse, checklist ring (16-bit),
-// visited and pending bitsets.
+// Per-warp shared-memory workspace: tour and inverse (16-bit), visited and
+// pending bitsets.
 __host__ __device__ inline std::uint32_t ant_smem_bytes(std::uint32_t n) {
-    return (6u * pad8(n) + 8u * ((n + 31u) / 32u) + 15u) & ~15u;
+    return (4u * pad8(n) + 8u * ((n + 31u) / 32u) + 15u) & ~15u;
 }
 __host__ __device__ inline std::uint32_t block_smem_bytes(std::uint32_t n, std::uint32_t warps) {
     return ((8u * n + 15u) & ~15u) + warps * ant_smem_bytes(n);
 }
+// Global-workspace variant: only the two bitsets per ant stay in shared memory.
+__host__ __device__ inline std::uint32_t ant_bitset_bytes(std::uint32_t n) {
+    return (8u * ((n + 31u) / 32u) + 15u) & ~15u;
+}
+__host__ __device__ inline std::uint32_t block_smem_bytes_global(std::uint32_t n, std::uint32_t warps) {
+    return warps * ant_bitset_bytes(n);
+}
 
 struct AntSmem {
-    node_t* tour;
-    node_t* pos;
-    node_t* ring;
-    std::uint32_t* visited;
-    std::uint32_t* queued;
-    __device__ static AntSmem at(unsigned char* base, std::uint32_t n_max) {
+    node_t* tour;                 // shared
+    node_t* pos;                  // shared
+    node_t* ring;                 // global: the ant's checklist ring (n entries)
+    std::uint32_t* visited;       // shared
+    std::uint32_t* queued;        // shared
+    __device__ static AntSmem at(unsigned char* base, std::uint32_t n_max, node_t* ring) {
         const std::uint32_t np = pad8(n_max), words = (n_max + 31u) / 32u;
-        return {reinterpret_cast<node_t*>(base), reinterpret_cast<node_t*>(base + 2 * np),
-                reinterpret_cast<node_t*>(base + 4 * np), reinterpret_cast<std::uint32_t*>(base + 6 * np),
-                reinterpret_cast<std::uint32_t*>(base + 6 * np) + words};
+        return {reinterpret_cast<node_t*>(base), reinterpret_cast<node_t*>(base + 2 * np), ring,
+                reinterpret_cast<std::uint32_t*>(base + 4 * np),
+                reinterpret_cast<std::uint32_t*>(base + 4 * np) + words};
+    }
+    // tour/inverse at `global` (2 x n_pad nodes), bitsets at `bits` (shared)
+    __device__ static AntSmem split(node_t* global, std::uint32_t n_pad, unsigned char* bits,
+                                    std::uint32_t n_max, node_t* ring) {
+        const std::uint32_t words = (n_max + 31u) / 32u;
+        return {global, global + n_pad, ring, reinterpret_cast<std::uint32_t*>(bits),
+                reinterpret_cast<std::uint32_t*>(bits) + words};
     }
 };
 

@@ -212,6 +212,7 @@ struct faco_engine {
     // instance, and the classes run as parallel branches of each iteration.
     struct AntClass {
         std::uint32_t n_max = 0, warps = 1, smem = 0, blocks = 0, first_job = 0;
+        int mode = faco::kModeEngine;   // or kModeEngineGlobal (tour/inverse in global memory)
         faco::AntLaunch L{};
     };
     struct EvalState {
@@ -228,7 +229,9 @@ struct faco_engine {
     } eval;
     std::vector<cudaStream_t> branch_streams;
     std::vector<cudaEvent_t> branch_events;   // [0] fork, [1 + i] join of branch i
-    std::map<std::uint64_t, std::uint32_t> tuned_warps;  // (class, n_max, ants, blocks, mode) -> warps
+    // (class, n_max, ants, blocks, LS mode) -> (warps, kernel mode)
+    std::map<std::uint64_t, std::pair<std::uint32_t, int>> tuned_warps;
+    DeviceBuffer<faco::node_t> ant_workspace;  // kModeEngineGlobal: tour + inverse per ant
 
     ~faco_engine() {
         if (eval.exec) cudaGraphExecDestroy(eval.exec);
@@ -283,6 +286,8 @@ void faco_default_settings(faco_settings* s) {
     s->ls_evaluation_limit = 100000;
     s->initial_ls_evaluation_limit = 100000;
     s->ls_mode = FACO_LS_TWO_OPT;
+    s->autotune = 1;
+    s->workspace = FACO_WORKSPACE_AUTO;
 }
 
 int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_settings* settings, int device,
@@ -299,6 +304,7 @@ int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_setting
                 "invalid FACO settings");
         require(c.primary_width <= 32 && c.ls_width <= 32, "primary and LS widths are limited to 32 (one warp)");
         require(c.ls_mode == FACO_LS_TWO_OPT || c.ls_mode == FACO_LS_TWO_OPT_OR_OPT, "unknown local-search mode");
+        require(c.workspace <= FACO_WORKSPACE_GLOBAL, "unknown ant workspace placement");
         auto e = std::make_unique<faco_engine>();
         e->settings = c;
         e->dimension = dimension;
@@ -461,7 +467,7 @@ void enqueue_ants(faco_engine* e, cudaStream_t st) {
         const auto& c = v.classes[i];
         cudaStream_t bs = i == 0 ? st : e->branch_streams[i - 1];
         if (i > 0) cuda_check(cudaStreamWaitEvent(bs, e->branch_events[0], 0), "fork wait");
-        cuda_check(faco::launch_ant_kernel(faco::kModeEngine, c.L, c.blocks, c.warps, c.smem, bs), "ant launch");
+        cuda_check(faco::launch_ant_kernel(c.mode, c.L, c.blocks, c.warps, c.smem, bs), "ant launch");
         if (i > 0) cuda_check(cudaEventRecord(e->branch_events[i], bs), "join");
     }
     for (std::size_t i = 1; i < branches; ++i) cuda_check(cudaStreamWaitEvent(st, e->branch_events[i], 0), "join wait");
@@ -476,24 +482,66 @@ void enqueue_iteration(faco_engine* e, cudaStream_t st) {
     cuda_check(cudaGetLastError(), "update launch");
 }
 
+// Kernel variant of a size class: the global-memory workspace (tour and
+// inverse in global memory, coordinates read from global) lets large classes
+// run a full block per SM slot instead of one or two shared-memory-bound ants.
+constexpr std::uint32_t kGlobalWorkspaceFrom = 2048;   // auto: n_max above this may use it
+
+bool may_use_global(const faco_settings& c, std::uint32_t n_max) {
+    return c.workspace == FACO_WORKSPACE_GLOBAL ||
+           (c.workspace == FACO_WORKSPACE_AUTO && n_max > kGlobalWorkspaceFrom);
+}
+bool may_use_shared(const faco_settings& c, std::uint32_t n_max) {
+    return c.workspace != FACO_WORKSPACE_GLOBAL && faco::block_smem_bytes(n_max, 1) <= 227u * 1024u;
+}
+std::uint32_t class_smem(int mode, std::uint32_t n_max, std::uint32_t warps) {
+    return mode == faco::kModeEngineGlobal ? faco::block_smem_bytes_global(n_max, warps)
+                                           : faco::block_smem_bytes(n_max, warps);
+}
+
 // Work tables of the size classes: jobs (colony, first ant) of W = warps
-// ants each.  With autotuning, every candidate W of a class is timed on the
-// freshly initialised colonies (the ant kernel alone, which changes no
-// colony state: its outputs are rewritten by the first real iteration) and
-// the fastest is kept, cached per (class, size, ants, blocks, LS mode).
+// ants each.  With autotuning, every candidate (W, workspace placement) of a
+// class is timed on the freshly initialised colonies (the ant kernel alone,
+// which changes no colony state: its outputs are rewritten by the first real
+// iteration) and the fastest is kept, cached per (class, size, ants, blocks,
+// LS mode).  Without it, the default is the shared-memory kernel with
+// choose_warps, or the global workspace with 4 warps where only that fits
+// or the settings ask for it.
 void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32_t>>& members,
                        const std::vector<std::uint32_t>& class_ids) {
     auto& v = e->eval;
     const std::uint32_t A = v.L.ants;
     cudaStream_t s = e->stream;
+    const faco_settings& c = e->settings;
     auto jobs_for = [&](const std::vector<std::uint32_t>& cols, std::uint32_t warps) {
         std::vector<uint2> jobs;
-        for (const std::uint32_t c : cols)
-            for (std::uint32_t a = 0; a < A; a += warps) jobs.push_back(make_uint2(c, a));
+        for (const std::uint32_t col : cols)
+            for (std::uint32_t a = 0; a < A; a += warps) jobs.push_back(make_uint2(col, a));
         return jobs;
     };
-    if (e->settings.autotune) {
-        DeviceBuffer<uint2> scratch;
+    bool need_workspace = false;
+    for (const auto& cl : v.classes) need_workspace = need_workspace || may_use_global(c, cl.n_max);
+    if (need_workspace) e->ant_workspace.resize(2 * e->ant_tours.size());
+    for (auto& cl : v.classes) {
+        const bool shared_ok = may_use_shared(c, cl.n_max);
+        require(shared_ok || may_use_global(c, cl.n_max), "instance too large for a shared-memory ant block");
+        if (shared_ok && !(c.workspace == FACO_WORKSPACE_AUTO && !c.autotune && may_use_global(c, cl.n_max))) {
+            cl.mode = faco::kModeEngine;
+        } else {
+            cl.mode = faco::kModeEngineGlobal;
+            cl.warps = std::min<std::uint32_t>(faco::kMaxWarpsPerBlock, std::max(1u, A));
+        }
+    }
+    auto launch_of = [&](std::uint32_t first_job, std::uint32_t warps, std::uint32_t n_max) {
+        faco::AntLaunch L = v.L;
+        L.work = e->work.get() + first_job;
+        L.warps = warps;
+        L.n_max = n_max;
+        L.workspace = need_workspace ? e->ant_workspace.get() : nullptr;
+        L.ant_tours_base = e->ant_tours.get();
+        return L;
+    };
+    if (c.autotune) {
         cudaEvent_t t0, t1;
         cuda_check(cudaEventCreate(&t0), "event");
         cuda_check(cudaEventCreate(&t1), "event");
@@ -502,40 +550,44 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
             const std::uint64_t key = (static_cast<std::uint64_t>(class_ids[i]) << 56) ^
                                       (static_cast<std::uint64_t>(cl.n_max) << 40) ^
                                       (static_cast<std::uint64_t>(A) << 24) ^
-                                      (static_cast<std::uint64_t>(members[i].size()) << 2) ^ e->settings.ls_mode;
+                                      (static_cast<std::uint64_t>(members[i].size()) << 4) ^
+                                      (static_cast<std::uint64_t>(c.workspace) << 2) ^ c.ls_mode;
             const auto hit = e->tuned_warps.find(key);
             if (hit != e->tuned_warps.end()) {
-                cl.warps = hit->second;
+                cl.warps = hit->second.first;
+                cl.mode = hit->second.second;
                 continue;
             }
             float best_ms = 0.0f;
-            for (std::uint32_t w = 1; w <= faco::kMaxWarpsPerBlock && w <= A; w *= 2) {
-                const std::uint32_t smem = faco::block_smem_bytes(cl.n_max, w);
-                if (smem > 227u * 1024u) break;
-                const auto jobs = jobs_for(members[i], w);
-                scratch.upload(jobs, s);
-                faco::AntLaunch L = v.L;
-                L.work = scratch.get();
-                L.warps = w;
-                L.n_max = cl.n_max;
-                cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem), "attribute");
-                float ms = 0.0f;
-                for (int rep = 0; rep < 3; ++rep) {
-                    cuda_check(cudaEventRecord(t0, s), "event");
-                    cuda_check(faco::launch_ant_kernel(faco::kModeEngine, L, static_cast<std::uint32_t>(jobs.size()),
-                                                       w, smem, s), "tuning launch");
-                    cuda_check(cudaEventRecord(t1, s), "event");
-                    cuda_check(cudaEventSynchronize(t1), "tuning");
-                    float one = 0.0f;
-                    cuda_check(cudaEventElapsedTime(&one, t0, t1), "elapsed");
-                    if (rep > 0) ms += one;   // first launch warms caches
-                }
-                if (best_ms == 0.0f || ms < best_ms) {
-                    best_ms = ms;
-                    cl.warps = w;
+            for (const int mode : {static_cast<int>(faco::kModeEngine), static_cast<int>(faco::kModeEngineGlobal)}) {
+                if (mode == faco::kModeEngine && !may_use_shared(c, cl.n_max)) continue;
+                if (mode == faco::kModeEngineGlobal && !may_use_global(c, cl.n_max)) continue;
+                for (std::uint32_t w = 1; w <= faco::kMaxWarpsPerBlock && w <= A; w *= 2) {
+                    const std::uint32_t smem = class_smem(mode, cl.n_max, w);
+                    if (smem > 227u * 1024u) break;
+                    const auto jobs = jobs_for(members[i], w);
+                    e->work.upload(jobs, s);
+                    const faco::AntLaunch L = launch_of(0, w, cl.n_max);
+                    cuda_check(faco::prepare_ant_kernel(mode, smem), "attribute");
+                    float ms = 0.0f;
+                    for (int rep = 0; rep < 3; ++rep) {
+                        cuda_check(cudaEventRecord(t0, s), "event");
+                        cuda_check(faco::launch_ant_kernel(mode, L, static_cast<std::uint32_t>(jobs.size()), w, smem, s),
+                                   "tuning launch");
+                        cuda_check(cudaEventRecord(t1, s), "event");
+                        cuda_check(cudaEventSynchronize(t1), "tuning");
+                        float one = 0.0f;
+                        cuda_check(cudaEventElapsedTime(&one, t0, t1), "elapsed");
+                        if (rep > 0) ms += one;   // first launch warms caches
+                    }
+                    if (best_ms == 0.0f || ms < best_ms) {
+                        best_ms = ms;
+                        cl.warps = w;
+                        cl.mode = mode;
+                    }
                 }
             }
-            e->tuned_warps[key] = cl.warps;
+            e->tuned_warps[key] = {cl.warps, cl.mode};
         }
         cudaEventDestroy(t0);
         cudaEventDestroy(t1);
@@ -546,21 +598,21 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
         const auto jobs = jobs_for(members[i], cl.warps);
         cl.first_job = static_cast<std::uint32_t>(all.size());
         cl.blocks = static_cast<std::uint32_t>(jobs.size());
-        cl.smem = faco::block_smem_bytes(cl.n_max, cl.warps);
+        cl.smem = class_smem(cl.mode, cl.n_max, cl.warps);
         all.insert(all.end(), jobs.begin(), jobs.end());
     }
     e->work.upload(all, s);
-    // the dynamic shared-memory limit is a property of the kernel, shared by
-    // every class: it must admit the largest class
-    std::uint32_t smem_max = 0;
+    // the dynamic shared-memory limit is a property of each kernel variant,
+    // shared by every class that uses it: it must admit the largest one
+    std::uint32_t smem_max[2] = {0, 0};
     for (auto& cl : v.classes) {
-        cl.L = v.L;
-        cl.L.work = e->work.get() + cl.first_job;
-        cl.L.warps = cl.warps;
-        cl.L.n_max = cl.n_max;
-        smem_max = std::max(smem_max, cl.smem);
+        cl.L = launch_of(cl.first_job, cl.warps, cl.n_max);
+        auto& m = smem_max[cl.mode == faco::kModeEngineGlobal ? 1 : 0];
+        m = std::max(m, cl.smem);
     }
-    cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem_max), "cudaFuncSetAttribute");
+    if (smem_max[0]) cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem_max[0]), "cudaFuncSetAttribute");
+    if (smem_max[1])
+        cuda_check(faco::prepare_ant_kernel(faco::kModeEngineGlobal, smem_max[1]), "cudaFuncSetAttribute");
 }
 
 // Controller programs of a GP-controlled evaluation (null: plain FACO).

@@ -47,11 +47,12 @@ __device__ __forceinline__ void load_parent(const AntSmem& s, const node_t* pare
 
 template <int MODE>
 __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_kernel(const AntLaunch L) {
+    constexpr bool kEngine = engine_mode(MODE), kGlobalWs = MODE == kModeEngineGlobal;
     extern __shared__ __align__(16) unsigned char smem[];
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     std::uint32_t colony = 0, ant = 0, task = 0;
     bool active;
-    if (MODE == kModeEngine) {
+    if (kEngine) {
         const uint2 job = L.work[blockIdx.x];
         colony = job.x;
         ant = job.y + warp;
@@ -61,22 +62,38 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         ant = task;
         active = task < L.tasks;
     }
-    const InstanceView* in_ptr = L.instances + (MODE == kModeEngine ? L.colonies[colony].instance : 0);
+    const InstanceView* in_ptr = L.instances + (kEngine ? L.colonies[colony].instance : 0);
     const InstanceView in = *in_ptr;
     const std::uint32_t n = in.n;
-    int2* xy = reinterpret_cast<int2*>(smem);
-    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) xy[i] = in.xy[i];
-    __syncthreads();
+    const int2* xy;
+    if (kGlobalWs) {
+        xy = in.xy;
+    } else {
+        int2* staged = reinterpret_cast<int2*>(smem);
+        for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) staged[i] = in.xy[i];
+        __syncthreads();
+        xy = staged;
+    }
     if (!active) return;
 
-    const AntSmem s = AntSmem::at(smem + ((8u * L.n_max + 15u) & ~15u) + warp * ant_smem_bytes(L.n_max), L.n_max);
+    node_t* ring = kEngine ? L.colonies[colony].ant_tours + (size_t)ant * L.colonies[colony].n_pad
+                           : L.out_tours + (size_t)task * n;
+    AntSmem s;
+    if (kGlobalWs) {
+        const std::uint32_t n_pad = L.colonies[colony].n_pad;
+        node_t* ws = L.workspace + 2 * ((size_t)(L.colonies[colony].ant_tours - L.ant_tours_base) +
+                                        (size_t)ant * n_pad);
+        s = AntSmem::split(ws, n_pad, smem + warp * ant_bitset_bytes(L.n_max), L.n_max, ring);
+    } else {
+        s = AntSmem::at(smem + ((8u * L.n_max + 15u) & ~15u) + warp * ant_smem_bytes(L.n_max), L.n_max, ring);
+    }
     const node_t* parent;
     const std::uint32_t* parent_nbr;
     long long cost;
     std::uint32_t target, batch = 0, region = 4;
     unsigned long long key = 0;
     ColonyView cv{};
-    if (MODE == kModeEngine) {
+    if (kEngine) {
         cv = L.colonies[colony];
         const ColonyState& st = L.states[colony];
         parent = cv.parent;
@@ -92,7 +109,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         cost = L.task_costs[task];
         target = MODE == kModePrepare ? 0 : L.task_targets[task];
     }
-    load_parent(s, parent, n, lane, MODE == kModeEngine);
+    load_parent(s, parent, n, lane, kEngine);
     const std::uint32_t words = (n + 31) / 32;
     for (std::uint32_t i = lane; i < words; i += 32) {
         s.visited[i] = 0;
@@ -118,13 +135,13 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
     } else {
         // ---------------- focused construction ----------------
         std::uint32_t current;
-        if (MODE == kModeEngine) current = region_start(key, batch, ant, in_ptr, region);
+        if (kEngine) current = region_start(key, batch, ant, in_ptr, region);
         else if (MODE == kModeVisits) current = L.task_visits[(size_t)task * n];
         else current = L.task_starts[task];
         if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n] = (node_t)current;
         if (lane == 0) s.visited[current >> 5] |= 1u << (current & 31u);
         __syncwarp();
-        const float* products = MODE == kModeEngine ? cv.products : L.task_products;
+        const float* products = kEngine ? cv.products : L.task_products;
         const std::uint32_t k = in.k, b = in.b;
         const unsigned long long loop_cap = 2ull * n + 2;
         unsigned long long guard = 0;
@@ -146,7 +163,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                 std::uint32_t rhi = 0, rlo = 0;
                 double u_given = 0.0;
                 float uf;
-                if (MODE == kModeEngine) {
+                if (kEngine) {
                     const uint4v rb = philox4x32(step, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
                     rhi = rb.x;
                     rlo = rb.y;
@@ -181,7 +198,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                     }
                     if (j < 0) {
                         // exact path: ordered FP64 prefix sums (faco_cpu.cpp:254-279)
-                        const double u = MODE == kModeEngine ? u53(rhi, rlo) : u_given;
+                        const double u = kEngine ? u53(rhi, rlo) : u_given;
                         double total = 0.0, mine = 0.0;
                         for (unsigned m = mask; m; m &= m - 1) {
                             const int jj = __ffs(m) - 1;
@@ -286,7 +303,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
     if (log && q.pushed > log_cap && lane == 0) atomicOr(L.error, kErrQueueOverflow);
     __syncwarp();
 
-    if (MODE == kModeEngine) {
+    if (kEngine) {
         uint4* out = reinterpret_cast<uint4*>(cv.ant_tours + (size_t)ant * cv.n_pad);
         const uint4* src = reinterpret_cast<const uint4*>(s.tour);
         for (std::uint32_t c = lane; c * 8 < n; c += 32) out[c] = src[c];
@@ -344,6 +361,7 @@ cudaError_t prepare_ant_kernel(int mode, std::uint32_t smem) {
         case kModeVisits: return prepare_mode<kModeVisits>(smem);
         case kModeUniforms: return prepare_mode<kModeUniforms>(smem);
         case kModePrepare: return prepare_mode<kModePrepare>(smem);
+        case kModeEngineGlobal: return prepare_mode<kModeEngineGlobal>(smem);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -356,6 +374,7 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
         case kModeVisits: ant_kernel<kModeVisits><<<grid, block, smem, stream>>>(L); break;
         case kModeUniforms: ant_kernel<kModeUniforms><<<grid, block, smem, stream>>>(L); break;
         case kModePrepare: ant_kernel<kModePrepare><<<grid, block, smem, stream>>>(L); break;
+        case kModeEngineGlobal: ant_kernel<kModeEngineGlobal><<<grid, block, smem, stream>>>(L); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

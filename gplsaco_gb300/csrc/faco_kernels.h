@@ -11,7 +11,7 @@ namespace faco {
 // Ants (warps) per block of the ant kernel, and the resident blocks per SM the
 // register budget is sized for (6 x 4 warps x 85 registers fills the file).
 constexpr std::uint32_t kMaxWarpsPerBlock = 4;
-constexpr std::uint32_t kAntBlocksPerSM = 6;
+constexpr std::uint32_t kAntBlocksPerSM = 8;
 
 struct ColonyParams {
     std::uint32_t ants;

@@ -30,6 +30,13 @@ extern "C" {
 #define FACO_LS_TWO_OPT 0       /* checklist 2-opt, best gain per node (reference) */
 #define FACO_LS_TWO_OPT_OR_OPT 1 /* 2-opt + Or-opt (segments <= 3), first improvement */
 
+/* Ant workspace placement.  Shared memory is fastest per access but holds
+ * few large-instance ants per SM; the global-memory workspace (L1/L2-cached)
+ * holds a full block per SM slot at any size. */
+#define FACO_WORKSPACE_AUTO 0   /* shared; above 2048 nodes the autotuner may pick global */
+#define FACO_WORKSPACE_SHARED 1
+#define FACO_WORKSPACE_GLOBAL 2
+
 /* FixedFacoSettings (cpp/include/gp_faco/fixed_faco_gpu.hpp:10-21;
  * bindings.cpp:508-519).  ants == 0 selects 64*ceil(sqrt(n)/16). */
 typedef struct faco_settings {
@@ -44,7 +51,8 @@ typedef struct faco_settings {
     uint64_t ls_evaluation_limit;
     uint64_t initial_ls_evaluation_limit;
     uint32_t ls_mode; /* FACO_LS_* */
-    uint32_t autotune; /* 1: pick ants per block per size class by timing the ant kernel */
+    uint32_t autotune; /* 1: pick ants per block (and workspace placement) per size class by timing */
+    uint32_t workspace; /* FACO_WORKSPACE_*: where an ant keeps its tour and inverse */
 } faco_settings;
 
 void faco_default_settings(faco_settings* s);

@@ -138,24 +138,27 @@ def test_scores_reference_and_extended(api, oracle):
     assert got["actions"].tolist() == [0, 31, 7]
 
 
-def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000, ls_mode=0):
+def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000, ls_mode=0, workspace=0):
     return api.FixedFacoSettings(ants=ants, primary_width=k, backup_width=b, ls_width=w, retention=retention,
-                                 epoch_source_probability=epoch, ls_evaluation_limit=ls_limit, ls_mode=ls_mode)
+                                 epoch_source_probability=epoch, ls_evaluation_limit=ls_limit, ls_mode=ls_mode,
+                                 workspace=workspace)
 
 
-@pytest.mark.parametrize("n,ants,iterations,variant,ls_mode", [
-    (7, 4, 8, 0, 0), (17, 8, 8, 1, 0), (100, 32, 20, 2, 0), (500, 16, 6, 3, 0), (1000, 32, 4, 0, 0),
-    (17, 8, 8, 1, 1), (100, 32, 20, 2, 1), (1000, 32, 4, 0, 1)])
-def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode):
+@pytest.mark.parametrize("n,ants,iterations,variant,ls_mode,workspace", [
+    (7, 4, 8, 0, 0, 0), (17, 8, 8, 1, 0, 0), (100, 32, 20, 2, 0, 0), (500, 16, 6, 3, 0, 0), (1000, 32, 4, 0, 0, 0),
+    (17, 8, 8, 1, 1, 0), (100, 32, 20, 2, 1, 0), (1000, 32, 4, 0, 1, 0),
+    (7, 4, 8, 0, 0, 2), (100, 32, 20, 2, 0, 2), (500, 16, 6, 3, 1, 2), (1000, 32, 4, 0, 0, 2)])
+def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode, workspace):
     """Whole plain-FACO runs: registration rows and initial tour, every
     iteration's best/global/parent costs and trail bounds, the final global
-    tour and the FP32 trails agree bit-for-bit with the oracle."""
+    tour and the FP32 trails agree bit-for-bit with the oracle -- with the
+    ants' tours in shared memory and in the global-memory workspace."""
     k = 2 if variant % 2 else 16
     b = 1 if variant % 2 else 64
     retention = (0.25, 0.5, 0.75, 0.98)[variant]
     epoch = (0.0, 0.01, 1.0, 0.3)[variant]
     xy = _cases.uniform_instance(n, seed=4703 + n)
-    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000, ls_mode)
+    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000, ls_mode, workspace)
     engine = api.FacoBatchEngine(n, 3, settings)
     info = engine.register_problem(n + 8999, xy.astype(np.float64))
     kk, bb, ww = min(k, n - 1), min(b, n - 1 - min(k, n - 1)), min(20, n - 1)
@@ -186,12 +189,13 @@ def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls
     engine.close()
 
 
-def test_uneven_batch_matches_independent_runs(api, oracle):
+@pytest.mark.parametrize("workspace", [0, 2])
+def test_uneven_batch_matches_independent_runs(api, oracle, workspace):
     """Instances of different sizes share one evaluation; each colony equals
     its own oracle run (tests/cpp/test_batch_engine.cpp:39-88)."""
     sizes = [200, 537, 1000, 311]
     ants, iterations = 16, 5
-    settings = _settings(api, ants)
+    settings = _settings(api, ants, workspace=workspace)
     engine = api.FacoBatchEngine(1000, 8, settings)
     preps = {}
     for i, n in enumerate(sizes):
