@@ -27,13 +27,24 @@ enum DeviceError : unsigned {
 // every |coordinate| < 2^26.
 // The estimate comes from 32-bit dx, dy in FP32 (GB300 runs 64-bit
 // integer/float conversions on its narrow FP64 pipe, so none are used).
+// The estimate only has to be close: m is the exact result iff
+// m^2 - m < s <= m^2 + m, which one 64-bit product decides; the correction
+// loops run only when that test fails (an estimate off by one or more).
+__device__ __forceinline__ float sqrt_estimate(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ int euc2d(int2 p, int2 q) {
     const int dx = p.x - q.x, dy = p.y - q.y;  // |dx|, |dy| < 2^27
     const float fx = (float)dx, fy = (float)dy;
-    int m = __float2int_rn(sqrtf(fx * fx + fy * fy));
+    int m = __float2int_rn(sqrt_estimate(fx * fx + fy * fy));
     const long long s = (long long)dx * dx + (long long)dy * dy;
-    while (s > (long long)m * m + m) ++m;
-    while (m > 0 && s <= (long long)m * m - m) --m;
+    const long long t = s - (long long)m * m;
+    if (t > m || t <= -m) {
+        while (s > (long long)m * m + m) ++m;
+        while (m > 0 && s <= (long long)m * m - m) --m;
+    }
     return m;
 }
 
