@@ -22,7 +22,7 @@ ROOT = PKG.parent
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               f"-I{ROOT / 'include'}", f"-I{CSRC}"]
-SOURCES = ["faco_kernels.cu", "faco_engine.cu", "faco_prepare.cpp", "prior_mlp.cu", "faco_noalloc.cu"]
+SOURCES = ["faco_kernels.cu", "faco_engine.cu", "faco_prepare.cpp", "prior_mlp.cu", "faco_noalloc.cu", "faco_knn.cu"]
 
 
 def nvcc() -> str:

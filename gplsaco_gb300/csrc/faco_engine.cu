@@ -111,6 +111,20 @@ std::uint64_t mix64(std::uint64_t z) {
 using Clock = std::chrono::steady_clock;
 double seconds_since(Clock::time_point t) { return std::chrono::duration<double>(Clock::now() - t).count(); }
 
+// Below a 2^24 span per axis every EUC_2D length is < 2^25, where the
+// reference's floor(sqrt(dx^2 + dy^2) + 0.5) in double precision equals the
+// exactly rounded integer the device computes; wider spans could round the
+// two differently at half-integer boundaries, so they are refused.
+void require_euc2d_span(const std::int32_t* xy, std::uint32_t n) {
+    std::int32_t lo[2] = {xy[0], xy[1]}, hi[2] = {xy[0], xy[1]};
+    for (std::size_t i = 0; i < 2ull * n; ++i) {
+        lo[i & 1] = std::min(lo[i & 1], xy[i]);
+        hi[i & 1] = std::max(hi[i & 1], xy[i]);
+    }
+    require(static_cast<std::int64_t>(hi[0]) - lo[0] < (1 << 24) && static_cast<std::int64_t>(hi[1]) - lo[1] < (1 << 24),
+            "coordinate spans must be below 2^24 per axis (exact EUC_2D lengths)");
+}
+
 std::vector<std::int32_t> integer_coordinates(const double* xy, std::uint32_t n) {
     std::vector<std::int32_t> out(2ull * n);
     for (std::size_t i = 0; i < 2ull * n; ++i) {
@@ -119,6 +133,7 @@ std::vector<std::int32_t> integer_coordinates(const double* xy, std::uint32_t n)
                 "coordinates must be finite integers with |x| < 2^26 (EUC_2D)");
         out[i] = static_cast<std::int32_t>(v);
     }
+    require_euc2d_span(out.data(), n);
     return out;
 }
 
@@ -354,12 +369,31 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         const double cheap_seconds = seconds_since(started);
         std::vector<std::int32_t> ls_dist;
         std::vector<float> eta;
-        faco::host_candidates(inst->xy, n, inst->k, inst->b, inst->w, inst->primary, inst->backup, inst->ls,
-                              ls_dist, eta, c.beta);
-        const auto nn = faco::host_nearest_neighbour_tour(inst->xy, n);
-        // device-resident instance
+        // device-resident instance; candidate rows from the GPU near lists
+        // (prepared_problem.cpp:58-91), the host sort only for rows wider
+        // than the kernel's list
         cudaStream_t s = e->stream;
         inst->d_xy.upload(reinterpret_cast<const int2*>(inst->xy.data()), n, s);
+        const std::uint32_t needed = std::max(inst->k + inst->b, inst->w);
+        std::vector<std::uint32_t> nn;
+        if (needed <= faco::kKnnMaxNeeded) {
+            DeviceBuffer<faco::node_t> d_near(static_cast<std::size_t>(n) * needed);
+            DeviceBuffer<std::int32_t> d_near_dist(static_cast<std::size_t>(n) * needed);
+            cuda_check(faco::launch_knn(inst->d_xy.get(), n, needed, d_near.get(), d_near_dist.get(), s),
+                       "candidate rows");
+            std::vector<std::uint16_t> near(static_cast<std::size_t>(n) * needed);
+            std::vector<std::int32_t> near_dist(near.size());
+            d_near.download(near.data(), near.size(), s);
+            d_near_dist.download(near_dist.data(), near_dist.size(), s);
+            cuda_check(cudaStreamSynchronize(s), "candidate rows");
+            faco::host_rows_from_near(near, near_dist, n, needed, inst->k, inst->b, inst->w, c.beta, inst->primary,
+                                      inst->backup, inst->ls, ls_dist, eta);
+            nn = faco::host_nearest_neighbour_tour_near(inst->xy, n, near, needed);
+        } else {
+            faco::host_candidates(inst->xy, n, inst->k, inst->b, inst->w, inst->primary, inst->backup, inst->ls,
+                                  ls_dist, eta, c.beta);
+            nn = faco::host_nearest_neighbour_tour(inst->xy, n);
+        }
         inst->d_primary.upload(inst->primary, s);
         inst->d_backup.resize(std::max<std::size_t>(inst->backup.size(), 1));
         inst->d_backup.upload(inst->backup, s);
@@ -1141,6 +1175,7 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
         if (uniforms) require(starts && primary && products && k >= 1 && k <= 32 && k <= n - 1, "roulette inputs missing");
         std::vector<std::int32_t> hxy(xy, xy + 2ull * n);
         for (auto v : hxy) require(std::abs(v) < (1 << 26), "coordinates must satisfy |x| < 2^26");
+        require_euc2d_span(hxy.data(), n);
         std::vector<std::uint16_t> ls;
         std::vector<std::int32_t> ls_dist;
         faco::host_distance_order(hxy, n, w, ls_rows, ls, ls_dist);

@@ -16,6 +16,16 @@ void host_candidates(const std::vector<std::int32_t>& xy, std::uint32_t n, std::
                      std::vector<std::uint16_t>& ls, std::vector<std::int32_t>& ls_dist, std::vector<float>& eta,
                      double beta);
 std::vector<std::uint32_t> host_nearest_neighbour_tour(const std::vector<std::int32_t>& xy, std::uint32_t n);
+// Rows and eta from sorted near lists ([n][needed] ids and lengths).
+void host_rows_from_near(const std::vector<std::uint16_t>& near, const std::vector<std::int32_t>& near_dist,
+                         std::uint32_t n, std::uint32_t needed, std::uint32_t k, std::uint32_t b, std::uint32_t w,
+                         double beta, std::vector<std::uint16_t>& primary, std::vector<std::uint16_t>& backup,
+                         std::vector<std::uint16_t>& ls, std::vector<std::int32_t>& ls_dist, std::vector<float>& eta);
+// The nearest-neighbour tour using the near lists; a full scan only when
+// every listed node is already visited.
+std::vector<std::uint32_t> host_nearest_neighbour_tour_near(const std::vector<std::int32_t>& xy, std::uint32_t n,
+                                                            const std::vector<std::uint16_t>& near,
+                                                            std::uint32_t needed);
 void host_distance_order(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t w,
                          const std::uint32_t* rows, std::vector<std::uint16_t>& ls,
                          std::vector<std::int32_t>& ls_dist);

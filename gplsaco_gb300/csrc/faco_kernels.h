@@ -25,6 +25,14 @@ struct ColonyParams {
     float log2k;                     // log2(k) by the engine's own log2
 };
 
+// Candidate rows of registration on the GPU (faco_knn.cu): per node its
+// `needed` nearest nodes in (EUC_2D length, id) order, ids and lengths
+// [n][needed]; needed <= kKnnMaxNeeded and < n, shared memory 8 n bytes.
+constexpr std::uint32_t kKnnMaxNeeded = 256;
+std::uint32_t knn_smem_bytes(std::uint32_t n);
+cudaError_t launch_knn(const int2* xy, std::uint32_t n, std::uint32_t needed, node_t* near_ids,
+                       std::int32_t* near_dist, cudaStream_t stream);
+
 // Host-side launchers (the kernels are defined in faco_kernels.cu).
 cudaError_t prepare_ant_kernel(int mode, std::uint32_t smem_bytes);
 cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks, std::uint32_t warps,

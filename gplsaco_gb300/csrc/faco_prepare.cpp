@@ -8,6 +8,7 @@
 #include "faco_host.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -127,6 +128,66 @@ std::vector<std::uint32_t> host_nearest_neighbour_tour(const std::vector<std::in
             if (seen[v]) continue;
             const std::int32_t d = host_euc2d(xy[2 * current], xy[2 * current + 1], xy[2 * v], xy[2 * v + 1]);
             if (d < shortest) { shortest = d; next = v; }
+        }
+        current = next;
+    }
+    return tour;
+}
+
+// The rows of host_candidates, taken from each node's near list sorted by
+// (length, id): primary = the first k, backup = the next b, LS = the first w.
+void host_rows_from_near(const std::vector<std::uint16_t>& near, const std::vector<std::int32_t>& near_dist,
+                         std::uint32_t n, std::uint32_t needed, std::uint32_t k, std::uint32_t b, std::uint32_t w,
+                         double beta, std::vector<std::uint16_t>& primary, std::vector<std::uint16_t>& backup,
+                         std::vector<std::uint16_t>& ls, std::vector<std::int32_t>& ls_dist, std::vector<float>& eta) {
+    if (k + b > needed || w > needed) throw std::invalid_argument("near lists shorter than the rows");
+    primary.assign(static_cast<std::size_t>(n) * k, 0);
+    backup.assign(static_cast<std::size_t>(n) * b, 0);
+    ls.assign(static_cast<std::size_t>(n) * w, 0);
+    ls_dist.assign(static_cast<std::size_t>(n) * w, 0);
+    eta.assign(static_cast<std::size_t>(n) * k, 0.0f);
+    for (std::uint32_t a = 0; a < n; ++a) {
+        const std::size_t row = static_cast<std::size_t>(a) * needed;
+        for (std::uint32_t j = 0; j < k; ++j) {
+            primary[static_cast<std::size_t>(a) * k + j] = near[row + j];
+            const double d = near_dist[row + j];
+            eta[static_cast<std::size_t>(a) * k + j] =
+                static_cast<float>(d > 0 ? (beta == 1.0 ? 1.0 / d : 1.0 / std::pow(d, beta)) : 1.0);
+        }
+        for (std::uint32_t j = 0; j < b; ++j) backup[static_cast<std::size_t>(a) * b + j] = near[row + k + j];
+        for (std::uint32_t j = 0; j < w; ++j) {
+            ls[static_cast<std::size_t>(a) * w + j] = near[row + j];
+            ls_dist[static_cast<std::size_t>(a) * w + j] = near_dist[row + j];
+        }
+    }
+}
+
+// The first unvisited node of the current node's near list is the nearest
+// unvisited node with the lowest id among equals (every node outside the list
+// has a larger (length, id) key than every listed one), which is the choice
+// of the full scan in host_nearest_neighbour_tour.
+std::vector<std::uint32_t> host_nearest_neighbour_tour_near(const std::vector<std::int32_t>& xy, std::uint32_t n,
+                                                            const std::vector<std::uint16_t>& near,
+                                                            std::uint32_t needed) {
+    std::vector<std::uint32_t> tour;
+    tour.reserve(n);
+    std::vector<std::uint8_t> seen(n, 0);
+    std::uint32_t current = 0;
+    for (std::uint32_t i = 0; i < n; ++i) {
+        tour.push_back(current);
+        seen[current] = 1;
+        if (i + 1 == n) break;
+        std::uint32_t next = n;
+        const std::uint16_t* list = near.data() + static_cast<std::size_t>(current) * needed;
+        for (std::uint32_t j = 0; j < needed; ++j)
+            if (!seen[list[j]]) { next = list[j]; break; }
+        if (next == n) {
+            std::int32_t shortest = INT32_MAX;
+            for (std::uint32_t v = 0; v < n; ++v) {
+                if (seen[v]) continue;
+                const std::int32_t d = host_euc2d(xy[2 * current], xy[2 * current + 1], xy[2 * v], xy[2 * v + 1]);
+                if (d < shortest) { shortest = d; next = v; }
+            }
         }
         current = next;
     }

@@ -253,6 +253,9 @@ def test_invalid_inputs_raise_before_search(api):
     bad = xy.copy(); bad[0, 0] = np.nan
     with pytest.raises(ValueError):
         engine.register_problem(1, bad)
+    bad = xy.copy(); bad[0, 0] = -2.0**23; bad[1, 0] = 2.0**23      # span 2^24: EUC_2D no longer exact in double
+    with pytest.raises(ValueError):
+        engine.register_problem(1, bad)
     bad = xy.copy(); bad[0, 0] = 0.5
     with pytest.raises(ValueError):
         engine.register_problem(1, bad)
@@ -354,3 +357,26 @@ def test_fixed_faco_gpu_and_sessions(api, oracle):
     plain, _ = session.solve(problems, [("a", 3), ("a", 4)], iterations)
     assert plain["items"][0]["cost"] == ref["cost"]
     session.close()
+
+
+@pytest.mark.parametrize("n,k,b,w", [(2500, 32, 64, 32), (600, 16, 250, 20)])
+def test_registration_rows_match_oracle(api, oracle, n, k, b, w):
+    """Registration on a clustered instance with duplicated points (length
+    ties order by node id): candidate rows from the GPU near lists (or the
+    host sort when the rows are wider than the kernel's list), the
+    nearest-neighbour tour and its initial 2-opt equal the oracle's
+    preparation (prepared_problem.cpp:58-120)."""
+    from gplsaco_gb300 import instances
+    xy = instances.clustered(n, 31).astype(np.int32)
+    xy[1::97] = xy[0]                      # duplicates of node 0
+    xy[5::101] = xy[3]
+    settings = _settings(api, 8, k, b, w)
+    engine = api.FacoBatchEngine(n, 1, settings)
+    info = engine.register_problem(7, xy.astype(np.float64))
+    rows = engine.problem_rows(7)
+    prep = oracle.prepare(xy, k, b, w)
+    assert np.array_equal(rows["primary"], prep["primary"])
+    assert np.array_equal(rows["backup"], prep["backup"])
+    assert np.array_equal(rows["ls"], prep["ls"])
+    assert np.array_equal(rows["initial_tour"], prep["initial"]) and info["initial_cost"] == prep["cost"]
+    engine.close()
