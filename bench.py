@@ -113,6 +113,17 @@ def make_workload(name: str, rank: int = 0) -> Workload:
     raise ValueError(f"unknown workload {name}")
 
 
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The job's time is the slowest rank's: MAX all-reduce of one float
+    (NCCL on the GPU ranks; any initialised process group works)."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def size_classes(sizes) -> int:
     """Ant-kernel launches per iteration: one per instance size class
     (n rounded up to a power of two, at least 256)."""
@@ -317,11 +328,7 @@ def run_gb300(args, rank: int, world: int) -> None:
     iters = totals["completed_batches"]
     work = totals["colony_work"].astype(np.float64)
     fe_total = iters * wl.colonies * wl.ants
-    elapsed_ms = float(np.sum(step_ms))
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(float(np.sum(step_ms)), world, "cuda")
     fe_timed = args.steps * wl.colonies * wl.ants * world
     value = fe_timed / (elapsed_ms / 1e3)
 
@@ -477,11 +484,7 @@ def run_population(args, rank: int, world: int) -> None:
         if world > 1:
             torch.distributed.barrier()
     assert len(res) == POP_PROGRAMS and all(len(r["items"][0]["tour"]) == POP_N for r in res)
-    elapsed_ms = float(np.sum(dev_ms))
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(float(np.sum(dev_ms)), world, "cuda")
     engine.close()
     if rank != 0:
         return
