@@ -28,7 +28,7 @@ EXPORTED = (
     "faco_ant_diagnostic", "faco_pheromone_step", "faco_begin", "faco_step", "faco_step_timed", "faco_finish",
     "faco_engine_stream", "faco_evaluate_programs", "faco_mlp_param_count", "faco_mlp_forward", "faco_mlp_gradient",
     "faco_mlp_train", "faco_edge_data", "faco_prior_set", "faco_prior_refresh", "faco_current_costs",
-    "faco_pheromone_step_noalloc",
+    "faco_pheromone_step_noalloc", "faco_begin_programs", "faco_snapshot", "faco_restore",
 )
 
 
@@ -119,6 +119,10 @@ def load():
                                       C.c_uint32, vp, C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(AntOutputs)]
     L.faco_pheromone_step.argtypes = [C.c_uint32, C.c_uint32, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float,
                                       vp, vp, vp]
+    L.faco_begin_programs.argtypes = [vp, vp, vp, C.c_uint32, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                      C.c_uint32]
+    L.faco_snapshot.argtypes = [vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.faco_restore.argtypes = [vp, vp, C.c_uint64, C.c_uint32]
     L.faco_pheromone_step_noalloc.argtypes = [C.c_uint32, C.c_uint32, vp, vp, C.c_float, C.c_float, C.c_float,
                                               C.c_float, vp, vp, vp, vp]
     L.faco_evaluate_programs.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint64, vp, C.c_uint32, C.c_uint32,

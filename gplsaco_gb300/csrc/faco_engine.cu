@@ -233,9 +233,11 @@ struct faco_engine {
     struct EvalState {
         bool active = false;
         std::uint32_t count = 0, n_max = 0, trace_cap = 0, done = 0;
-        std::size_t node_total = 0;
+        std::size_t node_total = 0, tau_total = 0;
         std::vector<std::uint32_t> sizes;
-        std::vector<std::uint64_t> keys;
+        std::vector<std::uint64_t> keys, seeds;
+        std::vector<faco_program> programs;     // host copy of the controllers (snapshots)
+        std::uint32_t action_mask = 0xFFFFFFFFu;
         std::vector<AntClass> classes;
         faco::ColonyParams P{};
         faco::AntLaunch L{};
@@ -668,6 +670,9 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     auto& v = e->eval;
     v.sizes.assign(count, 0);
     v.keys.assign(keys, keys + count);
+    v.seeds.assign(seeds, seeds + count);
+    v.programs.assign(control.programs, control.programs + (control.programs ? control.n_programs : 0));
+    v.action_mask = control.action_mask;
     std::vector<faco::ColonyView> views(count);
     std::size_t tau_total = 0, node_total = 0, ant_total = 0;
     std::uint32_t n_max = 3, k_common = 0;
@@ -684,6 +689,7 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         n_max = std::max(n_max, in.n);
     }
     cudaStream_t s = e->stream;
+    v.tau_total = tau_total;
     // HBM layout: per colony, trails and products [n][k] (16-byte aligned),
     // node arrays padded to 8 nodes so that every row starts 16-byte aligned
     e->trails.resize(tau_total);
@@ -913,6 +919,231 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
 extern "C" {
 
 void* faco_engine_stream(faco_engine* e) { return e ? static_cast<void*>(e->stream) : nullptr; }
+
+}  // extern "C"
+
+namespace {
+
+// ---- colony snapshots (counted_state.hpp:23-38, batch_engine.cu:207-261) ----
+// A snapshot is the whole persistent state of a stepwise evaluation: the
+// panel, the controllers, every ColonyState and the per-colony trails,
+// products, eta and parent/epoch/global tours, framed by a header and closed
+// by an FNV-1a checksum.  Ant tours are scratch of one iteration and are not
+// kept.  The Philox streams are keyed by the iteration counter kept in the
+// colony states, so a restored evaluation continues bit for bit.
+constexpr char kSnapshotMagic[8] = {'F', 'A', 'C', 'O', 'S', 'N', 'P', '1'};
+constexpr std::uint32_t kSnapshotVersion = 1;
+static_assert(sizeof(faco::ColonyState) == 104, "snapshot layout (the Python reader's ColonyState size)");
+
+struct SnapshotHeader {
+    char magic[8];
+    std::uint32_t version, count, ants, k_common;
+    std::uint32_t mne_target, n_programs, action_mask, total_iterations;
+    std::uint32_t controlled, done, reserved0, reserved1;
+    std::uint64_t settings_digest, tau_total, node_total;
+};
+
+std::uint64_t fnv1a(const void* data, std::size_t bytes, std::uint64_t h = 1469598103934665603ull) {
+    const auto* p = static_cast<const unsigned char*>(data);
+    for (std::size_t i = 0; i < bytes; ++i) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+}
+
+// Everything in the settings that changes the search after registration.
+std::uint64_t settings_digest(const faco_settings& c, std::uint32_t ants) {
+    std::uint64_t h = fnv1a(&ants, sizeof ants);
+    const std::uint32_t u[4] = {c.primary_width, c.backup_width, c.ls_width, c.ls_mode};
+    const double d[4] = {c.beta, c.retention, c.p_best, c.epoch_source_probability};
+    h = fnv1a(u, sizeof u, h);
+    h = fnv1a(d, sizeof d, h);
+    return fnv1a(&c.ls_evaluation_limit, sizeof c.ls_evaluation_limit, h);
+}
+
+std::uint64_t coordinate_digest(const Instance& in) { return fnv1a(in.xy.data(), in.xy.size() * sizeof(std::int32_t)); }
+
+struct SnapshotWriter {
+    unsigned char* out;
+    std::uint64_t capacity, used = 0;
+    void put(const void* data, std::size_t bytes) {
+        if (out && used + bytes <= capacity) std::memcpy(out + used, data, bytes);
+        used += bytes;
+    }
+};
+
+template <class T>
+std::vector<T> fetch(const DeviceBuffer<T>& d, std::size_t count, cudaStream_t s) {
+    std::vector<T> h(count);
+    d.download(h.data(), count, s);
+    return h;
+}
+
+}  // namespace
+
+extern "C" {
+
+int faco_begin_programs(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+                        const struct faco_program* programs, uint32_t n_programs, uint32_t action_mask,
+                        uint32_t initial_mne, uint32_t total_iterations, uint32_t trace_iterations) {
+    return guarded([&] {
+        require(e != nullptr && programs != nullptr, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        require(total_iterations >= 1, "total_iterations must be positive");
+        Control control;
+        control.programs = programs;
+        control.n_programs = n_programs;
+        control.action_mask = action_mask;
+        control.total_iterations = total_iterations;
+        begin_evaluation(e, keys, seeds, count, initial_mne, trace_iterations, control);
+    });
+}
+
+int faco_snapshot(faco_engine* e, void* buffer, uint64_t capacity, uint64_t* bytes) {
+    return guarded([&] {
+        require(e && bytes, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        cudaStream_t s = e->stream;
+        cuda_check(cudaStreamSynchronize(s), "snapshot");
+        const unsigned err = e->read_error();
+        if (err) throw Error(FACO_EDEVICE, "device error word " + std::to_string(err));
+        SnapshotHeader h{};
+        std::memcpy(h.magic, kSnapshotMagic, 8);
+        h.version = kSnapshotVersion;
+        h.count = v.count;
+        h.ants = e->ants;
+        h.k_common = e->instances.at(v.keys[0])->k;
+        h.mne_target = v.P.mne_target;
+        h.n_programs = static_cast<std::uint32_t>(v.programs.size());
+        h.action_mask = v.action_mask;
+        h.total_iterations = v.P.total_iterations;
+        h.controlled = v.P.controlled;
+        h.done = v.done;
+        h.settings_digest = settings_digest(e->settings, e->ants);
+        h.tau_total = v.tau_total;
+        h.node_total = v.node_total;
+        SnapshotWriter w{static_cast<unsigned char*>(buffer), buffer ? capacity : 0};
+        w.put(&h, sizeof h);
+        w.put(v.keys.data(), v.count * sizeof(std::uint64_t));
+        w.put(v.seeds.data(), v.count * sizeof(std::uint64_t));
+        for (std::uint32_t c = 0; c < v.count; ++c) {
+            const std::uint64_t d = coordinate_digest(*e->instances.at(v.keys[c]));
+            w.put(&d, sizeof d);
+        }
+        w.put(v.programs.data(), v.programs.size() * sizeof(faco_program));
+        if (buffer) {
+            const auto states = fetch(e->states, v.count, s);
+            const auto trails = fetch(e->trails, v.tau_total, s);
+            const auto products = fetch(e->products, v.tau_total, s);
+            const auto eta = fetch(e->colony_eta, v.tau_total, s);
+            const auto parent = fetch(e->parent, v.node_total, s);
+            const auto nbr = fetch(e->parent_nbr, v.node_total, s);
+            const auto epoch = fetch(e->epoch, v.node_total, s);
+            const auto global = fetch(e->global, v.node_total, s);
+            cuda_check(cudaStreamSynchronize(s), "snapshot download");
+            w.put(states.data(), states.size() * sizeof(faco::ColonyState));
+            w.put(trails.data(), trails.size() * sizeof(float));
+            w.put(products.data(), products.size() * sizeof(float));
+            w.put(eta.data(), eta.size() * sizeof(float));
+            w.put(parent.data(), parent.size() * sizeof(faco::node_t));
+            w.put(nbr.data(), nbr.size() * sizeof(std::uint32_t));
+            w.put(epoch.data(), epoch.size() * sizeof(faco::node_t));
+            w.put(global.data(), global.size() * sizeof(faco::node_t));
+        } else {
+            w.used += v.count * sizeof(faco::ColonyState) + 3 * v.tau_total * sizeof(float) +
+                      v.node_total * (3 * sizeof(faco::node_t) + sizeof(std::uint32_t));
+        }
+        const std::uint64_t total = w.used + sizeof(std::uint64_t);
+        *bytes = total;
+        if (!buffer) return;
+        require(capacity >= total, "snapshot buffer too small");
+        const std::uint64_t sum = fnv1a(buffer, w.used);
+        std::memcpy(static_cast<unsigned char*>(buffer) + w.used, &sum, sizeof sum);
+    });
+}
+
+int faco_restore(faco_engine* e, const void* buffer, uint64_t bytes, uint32_t trace_iterations) {
+    return guarded([&] {
+        require(e && buffer, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        const auto* p = static_cast<const unsigned char*>(buffer);
+        require(bytes >= sizeof(SnapshotHeader) + sizeof(std::uint64_t), "snapshot too short");
+        std::uint64_t sum;
+        std::memcpy(&sum, p + bytes - sizeof sum, sizeof sum);
+        require(fnv1a(p, bytes - sizeof sum) == sum, "snapshot checksum mismatch");
+        SnapshotHeader h;
+        std::memcpy(&h, p, sizeof h);
+        require(std::memcmp(h.magic, kSnapshotMagic, 8) == 0 && h.version == kSnapshotVersion,
+                "not a snapshot of this engine version");
+        require(h.ants == e->ants && h.settings_digest == settings_digest(e->settings, e->ants),
+                "snapshot settings differ from the engine's");
+        require(h.count >= 1 && h.count <= e->capacity, "snapshot panel exceeds the engine's colonies");
+        std::size_t off = sizeof h;
+        auto take = [&](std::size_t n) {
+            require(off + n + sizeof sum <= bytes, "snapshot truncated");
+            const unsigned char* at = p + off;
+            off += n;
+            return at;
+        };
+        std::vector<std::uint64_t> keys(h.count), seeds(h.count), digests(h.count);
+        std::memcpy(keys.data(), take(h.count * 8ull), h.count * 8ull);
+        std::memcpy(seeds.data(), take(h.count * 8ull), h.count * 8ull);
+        std::memcpy(digests.data(), take(h.count * 8ull), h.count * 8ull);
+        for (std::uint32_t c = 0; c < h.count; ++c) {
+            const auto it = e->instances.find(keys[c]);
+            require(it != e->instances.end(), "snapshot instance not registered");
+            require(coordinate_digest(*it->second) == digests[c], "snapshot instance coordinates differ");
+        }
+        std::vector<faco_program> programs(h.n_programs);
+        std::memcpy(programs.data(), take(h.n_programs * sizeof(faco_program)), h.n_programs * sizeof(faco_program));
+        require(static_cast<bool>(h.controlled) == (h.n_programs > 0), "snapshot controller fields inconsistent");
+        const unsigned char* states = take(h.count * sizeof(faco::ColonyState));
+        const unsigned char* trails = take(h.tau_total * sizeof(float));
+        const unsigned char* products = take(h.tau_total * sizeof(float));
+        const unsigned char* eta = take(h.tau_total * sizeof(float));
+        const unsigned char* parent = take(h.node_total * sizeof(faco::node_t));
+        const unsigned char* nbr = take(h.node_total * sizeof(std::uint32_t));
+        const unsigned char* epoch = take(h.node_total * sizeof(faco::node_t));
+        const unsigned char* global = take(h.node_total * sizeof(faco::node_t));
+        require(off + sizeof sum == bytes, "snapshot has trailing bytes");
+        Control control;
+        if (h.n_programs) {
+            control.programs = programs.data();
+            control.n_programs = h.n_programs;
+            control.action_mask = h.action_mask;
+        }
+        control.total_iterations = h.total_iterations;
+        begin_evaluation(e, keys.data(), seeds.data(), h.count, h.mne_target, trace_iterations, control);
+        auto& v = e->eval;
+        try {
+            require(v.tau_total == h.tau_total && v.node_total == h.node_total &&
+                        e->instances.at(keys[0])->k == h.k_common,
+                    "snapshot layout differs from the engine's");
+            cudaStream_t s = e->stream;
+            auto put = [&](void* dst, const unsigned char* src, std::size_t n) {
+                cuda_check(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s), "snapshot upload");
+            };
+            put(e->states.get(), states, h.count * sizeof(faco::ColonyState));
+            put(e->trails.get(), trails, h.tau_total * sizeof(float));
+            put(e->products.get(), products, h.tau_total * sizeof(float));
+            put(e->colony_eta.get(), eta, h.tau_total * sizeof(float));
+            put(e->parent.get(), parent, h.node_total * sizeof(faco::node_t));
+            put(e->parent_nbr.get(), nbr, h.node_total * sizeof(std::uint32_t));
+            put(e->epoch.get(), epoch, h.node_total * sizeof(faco::node_t));
+            put(e->global.get(), global, h.node_total * sizeof(faco::node_t));
+            cuda_check(cudaStreamSynchronize(s), "snapshot upload");
+            v.done = h.done;
+        } catch (...) {
+            v.active = false;
+            destroy_graph(e);
+            cudaStreamSynchronize(e->stream);
+            throw;
+        }
+    });
+}
 
 int faco_begin(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count, uint32_t mne_target,
                uint32_t trace_iterations) {

@@ -353,6 +353,118 @@ class FacoBatchEngine:
                 "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
                 "reversed_elements": int(out.reversed_elements), "colony_work": work, "trace": trace_rows}
 
+    def begin_programs(self, instance_keys, seeds, programs, experiment_mask=0xFFFFFFFF, *, initial_mne=8,
+                       total_iterations, trace_iterations: int = 0) -> None:
+        """begin() for GP-controlled colonies (programs as in
+        evaluate_population_evaluations, replicated panel order)."""
+        keys = _u64_array(instance_keys, "instance_keys")
+        seeds = _u64_array(seeds, "seeds")
+        if keys.size != seeds.size:
+            raise ValueError("instance_keys and seeds differ in length")
+        arr = self._program_array(programs)
+        _lib.check(self._L.faco_begin_programs(self._handle, keys.ctypes.data, seeds.ctypes.data, keys.size,
+                                               C.cast(arr, C.c_void_p), len(arr),
+                                               _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF),
+                                               _exact_int(initial_mne, "initial_mne", 1, 2**32 - 1),
+                                               _exact_int(total_iterations, "total_iterations", 1, 2**32 - 1),
+                                               _exact_int(trace_iterations, "trace_iterations", 0, 2**32 - 1)))
+        self._active = (keys.copy(), trace_iterations, 0)
+
+    def capture_state(self) -> CountedState:
+        """Snapshot of the active stepwise evaluation (it stays active)."""
+        size = C.c_uint64()
+        _lib.check(self._L.faco_snapshot(self._handle, None, 0, C.byref(size)))
+        buf = (C.c_ubyte * size.value)()
+        _lib.check(self._L.faco_snapshot(self._handle, C.cast(buf, C.c_void_p), size.value, C.byref(size)))
+        return CountedState(bytes(buf))
+
+    def restore_state(self, state: CountedState, *, trace_iterations: int = 0) -> None:
+        """Begins a stepwise evaluation from a snapshot; step() continues it."""
+        if not isinstance(state, CountedState):
+            raise ValueError("state must be a CountedState")
+        data = state.to_bytes()
+        _lib.check(self._L.faco_restore(self._handle, data, len(data),
+                                        _exact_int(trace_iterations, "trace_iterations", 0, 2**32 - 1)))
+        info = state.describe()
+        self._active = (np.asarray(info["instance_keys"], np.uint64), trace_iterations, info["completed_batches"])
+
+    def _stepwise_output(self, res: dict, limit: int) -> dict:
+        keys = self._active_keys
+        items = [{"has_incumbent": True, "tour": tour.tolist(), "cost": int(cost), "completed_seconds": None}
+                 for tour, cost in zip(res["tours"], res["costs"])]
+        return {"items": items, "budget_seconds": None, "budget_kind": "search_tour_evaluations",
+                "evaluation_limit_per_colony": limit,
+                "completed_tour_evaluations_per_colony": res["completed_batches"] * self.ants,
+                "total_tour_evaluations": res["completed_batches"] * self.ants * len(keys),
+                "completed_batches": res["completed_batches"],
+                "completed_construction_steps": res["construction_steps"],
+                "completed_ls_evaluations": res["ls_evaluations"], "reversed_elements": res["reversed_elements"],
+                "colony_work": res["colony_work"]}
+
+    def _batches(self, evaluations, name: str) -> int:
+        value = _exact_int(evaluations, name)
+        if value % self.ants:
+            raise ValueError(f"{name} must be a whole number of ant batches ({self.ants} ants)")
+        return value // self.ants
+
+    def capture_faco_state(self, instance_keys, seeds, capture_after_evaluations, mne=8) -> dict:
+        """Plain FACO for `capture_after_evaluations` per colony, then a
+        snapshot: {"evaluation": result so far, "state": CountedState}."""
+        batches = self._batches(capture_after_evaluations, "capture_after_evaluations")
+        self.begin(instance_keys, seeds, mne)
+        self._active_keys = self._active[0]
+        self.step(batches)
+        state = self.capture_state()
+        return {"evaluation": self._stepwise_output(self.finish(), capture_after_evaluations), "state": state}
+
+    def capture_program_state(self, instance_keys, seeds, source_evaluation_limit_per_colony,
+                              capture_after_evaluations, program, experiment_mask=0xFFFFFFFF) -> dict:
+        """capture_program_state (bindings.cpp:880-894): a controlled run
+        budgeted for `source_evaluation_limit_per_colony`, captured after
+        `capture_after_evaluations`."""
+        total = self._batches(source_evaluation_limit_per_colony, "source_evaluation_limit_per_colony")
+        batches = self._batches(capture_after_evaluations, "capture_after_evaluations")
+        if batches > total:
+            raise ValueError("capture point beyond the source budget")
+        self.begin_programs(instance_keys, seeds, [program], experiment_mask, total_iterations=max(1, total))
+        self._active_keys = self._active[0]
+        self.step(batches)
+        state = self.capture_state()
+        return {"evaluation": self._stepwise_output(self.finish(), capture_after_evaluations), "state": state}
+
+    def continue_faco_state(self, state: CountedState, additional_evaluations_per_colony) -> dict:
+        batches = self._batches(additional_evaluations_per_colony, "additional_evaluations_per_colony")
+        if state.describe()["controlled"]:
+            raise ValueError("the state is of a controlled run: use continue_program_state")
+        self.restore_state(state)
+        self._active_keys = self._active[0]
+        self.step(batches)
+        return self._stepwise_output(self.finish(), additional_evaluations_per_colony)
+
+    def continue_program_state(self, state: CountedState, additional_evaluations_per_colony, program) -> dict:
+        """continue_program_state (bindings.cpp:922-928): resumes a captured
+        controlled run for more evaluations; `program` must be the captured one."""
+        batches = self._batches(additional_evaluations_per_colony, "additional_evaluations_per_colony")
+        info = state.describe()
+        if not info["controlled"] or info["programs"] != 1:
+            raise ValueError("the state is not of a single-program controlled run")
+        captured = state.to_bytes()[_SNAPSHOT_HEADER.itemsize + 24 * info["colonies"]:][:C.sizeof(_lib.Program)]
+        if bytes(program_to_c(program)) != captured:
+            raise ValueError("program differs from the captured one")
+        self.restore_state(state)
+        self._active_keys = self._active[0]
+        self.step(batches)
+        return self._stepwise_output(self.finish(), additional_evaluations_per_colony)
+
+    def _program_array(self, programs):
+        if not isinstance(programs, (list, tuple)) or not programs:
+            raise ValueError("programs must be a non-empty list of IR dicts")
+        arr = (_lib.Program * len(programs))(*[program_to_c(p) for p in programs])
+        for p in arr:
+            if p.feature_spec_id != 3:
+                raise ValueError("controller programs use feature spec 3")
+        return arr
+
     # ---- learned edge prior on the active stepwise evaluation ---------------
     def edge_data(self, features: bool = True, labels: bool = True):
         """Candidate-edge features (BF16 bits [E, 8]) and labels (edge of each
@@ -385,6 +497,47 @@ class FacoBatchEngine:
     def stream_ptr(self) -> int:
         """The engine's cudaStream_t as an integer (torch.cuda.ExternalStream)."""
         return int(self._L.faco_engine_stream(self._handle) or 0)
+
+
+_SNAPSHOT_HEADER = np.dtype([
+    ("magic", "S8"), ("version", "<u4"), ("count", "<u4"), ("ants", "<u4"), ("k_common", "<u4"),
+    ("mne_target", "<u4"), ("n_programs", "<u4"), ("action_mask", "<u4"), ("total_iterations", "<u4"),
+    ("controlled", "<u4"), ("done", "<u4"), ("reserved0", "<u4"), ("reserved1", "<u4"),
+    ("settings_digest", "<u8"), ("tau_total", "<u8"), ("node_total", "<u8")])
+_COLONY_STATE_BYTES = 104      # sizeof(ColonyState); global_cost at byte 8
+
+
+class CountedState:
+    """A colony snapshot (the reference's CountedState,
+    cpp/include/gp_faco/counted_state.hpp:23-38): opaque bytes made by
+    FacoBatchEngine.capture_state and accepted by restore_state."""
+
+    def __init__(self, data: bytes):
+        data = bytes(data)
+        if len(data) < _SNAPSHOT_HEADER.itemsize + 8 or data[:8] != b"FACOSNP1":
+            raise ValueError("not a colony snapshot")
+        self._data = data
+
+    @staticmethod
+    def from_bytes(data) -> "CountedState":
+        return CountedState(data)
+
+    def to_bytes(self) -> bytes:
+        return self._data
+
+    def describe(self) -> dict:
+        h = np.frombuffer(self._data, _SNAPSHOT_HEADER, count=1)[0]
+        c = int(h["count"])
+        off = _SNAPSHOT_HEADER.itemsize
+        keys = np.frombuffer(self._data, "<u8", c, off)
+        seeds = np.frombuffer(self._data, "<u8", c, off + 8 * c)
+        off += 24 * c + int(h["n_programs"]) * C.sizeof(_lib.Program)
+        costs = [int(np.frombuffer(self._data, "<i8", 1, off + _COLONY_STATE_BYTES * i + 8)[0]) for i in range(c)]
+        return {"version": int(h["version"]), "colonies": c, "completed_batches": int(h["done"]),
+                "instance_keys": keys.tolist(), "seeds": seeds.tolist(), "global_costs": costs,
+                "controlled": bool(h["controlled"]), "programs": int(h["n_programs"]),
+                "mne_target": int(h["mne_target"]), "total_iterations": int(h["total_iterations"]),
+                "bytes": len(self._data)}
 
 
 class FixedFacoGpu:

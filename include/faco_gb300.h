@@ -162,6 +162,26 @@ int faco_finish(faco_engine* engine, faco_outputs* out);
 /* The engine's cudaStream_t (for events recorded by the caller). */
 void* faco_engine_stream(faco_engine* engine);
 
+/* faco_begin for GP-controlled colonies: the programs, action mask and
+ * initial MNE of faco_evaluate_programs; total_iterations is the budget T
+ * that the iteration-fraction feature divides by. */
+int faco_begin_programs(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds, uint32_t count,
+                        const struct faco_program* programs, uint32_t n_programs, uint32_t action_mask,
+                        uint32_t initial_mne, uint32_t total_iterations, uint32_t trace_iterations);
+
+/* Colony snapshot and resume (CountedState capture/restore,
+ * cpp/include/gp_faco/counted_state.hpp:23-38, cuda/batch_engine.cu:207-261).
+ * faco_snapshot writes the whole persistent state of the active stepwise
+ * evaluation (panel, controllers, colony states, trails, products, eta and
+ * parent/epoch/global tours; versioned, checksummed) into `buffer`; with
+ * buffer NULL it only reports the size in *bytes.  faco_restore begins a
+ * stepwise evaluation from such a snapshot on an engine with the same
+ * settings and the same instances registered (coordinates are checked);
+ * stepping it continues the saved run bit for bit.  Trace rows are indexed
+ * by absolute iteration. */
+int faco_snapshot(faco_engine* engine, void* buffer, uint64_t capacity, uint64_t* bytes);
+int faco_restore(faco_engine* engine, const void* buffer, uint64_t bytes, uint32_t trace_iterations);
+
 /* ---- GP programs -------------------------------------------------------- */
 /* Program (cpp/include/gp_faco/program.hpp:10-19). numeric_spec_id 1 is the
  * reference IR (opcodes 0-8, depth <= 5); 2 adds protected division (9) and

@@ -380,3 +380,63 @@ def test_registration_rows_match_oracle(api, oracle, n, k, b, w):
     assert np.array_equal(rows["ls"], prep["ls"])
     assert np.array_equal(rows["initial_tour"], prep["initial"]) and info["initial_cost"] == prep["cost"]
     engine.close()
+
+
+def test_snapshot_resume_continues_bit_for_bit(api):
+    """Colony snapshots (CountedState, counted_state.hpp:23-38): a run
+    captured after 5 iterations and continued for 7 on a fresh engine equals
+    a straight 12-iteration run -- plain and GP-controlled; corrupted or
+    mismatched snapshots are refused."""
+    ants, n1, n2 = 8, 150, 230
+    xys = {11: _cases.uniform_instance(n1, seed=21), 12: _cases.uniform_instance(n2, seed=22)}
+    settings = _settings(api, ants, retention=0.9)
+
+    def engine():
+        e = api.FacoBatchEngine(n2, 4, settings)
+        for key, xy in xys.items():
+            e.register_problem(key, xy.astype(np.float64))
+        return e
+
+    keys = np.array([11, 12, 12, 11], np.uint64)
+    seeds = np.array([1, 2, 3, 4], np.uint64)
+    a = engine()
+    full = a.evaluate_faco_evaluations(keys, seeds, ants * 12, 8)
+    cap = a.capture_faco_state(keys, seeds, ants * 5)
+    state = api.CountedState.from_bytes(cap["state"].to_bytes())
+    info = state.describe()
+    assert info["completed_batches"] == 5 and info["instance_keys"] == keys.tolist()
+    assert info["global_costs"] == [it["cost"] for it in cap["evaluation"]["items"]]
+    b = engine()
+    rest = b.continue_faco_state(state, ants * 7)
+    assert [it["tour"] for it in rest["items"]] == [it["tour"] for it in full["items"]]
+    assert [it["cost"] for it in rest["items"]] == [it["cost"] for it in full["items"]]
+    assert rest["completed_batches"] == 12
+    assert rest["completed_construction_steps"] == full["completed_construction_steps"]
+    assert rest["completed_ls_evaluations"] == full["completed_ls_evaluations"]
+
+    program = dict(ir_version=1, numeric_spec_id=2, feature_spec_id=3, opcode=[0, 0, 2], operand=[1, 8, 0],
+                   constant_bits=[])
+    full_p = a.evaluate_program_evaluations(keys, seeds, ants * 12, program)
+    cap_p = a.capture_program_state(keys, seeds, ants * 12, ants * 5, program)
+    rest_p = b.continue_program_state(cap_p["state"], ants * 7, program)
+    assert [it["tour"] for it in rest_p["items"]] == [it["tour"] for it in full_p["items"]]
+    assert [it["cost"] for it in rest_p["items"]] == [it["cost"] for it in full_p["items"]]
+    other = dict(program, operand=[2, 8, 0])
+    with pytest.raises(ValueError):
+        b.continue_program_state(cap_p["state"], ants * 7, other)
+
+    raw = bytearray(state.to_bytes())
+    raw[len(raw) // 2] ^= 0x40
+    with pytest.raises(ValueError):
+        b.restore_state(api.CountedState(bytes(raw)))              # checksum
+    c = api.FacoBatchEngine(n2, 4, _settings(api, ants, retention=0.5))
+    for key, xy in xys.items():
+        c.register_problem(key, xy.astype(np.float64))
+    with pytest.raises(ValueError):
+        c.restore_state(state)                                     # other settings
+    d = api.FacoBatchEngine(n2, 4, settings)
+    d.register_problem(11, xys[11].astype(np.float64))
+    with pytest.raises(ValueError):
+        d.restore_state(state)                                     # instance 12 missing
+    for e in (a, b, c, d):
+        e.close()
