@@ -18,13 +18,15 @@ enum DeviceError : unsigned {
     kErrBadChoice = 1u << 1,
     kErrLoopCap = 1u << 2,
     kErrShape = 1u << 3,
+    kErrTensorWait = 1u << 4,   // a tcgen05 MMA completion wait ran out
 };
 
 // TSPLIB EUC_2D: round(sqrt(dx^2+dy^2)) with halves up.  sqrt(s) is never a
 // half-integer for integer s, so the result is the unique m with
 // m*m - m < s <= m*m + m (m > 0) -- found from an FP32 estimate and at most
-// a few exact int64 corrections.  Equal to floor(sqrt((double)s) + 0.5) for
-// every |coordinate| < 2^26.
+// a few exact int64 corrections.  Equal to floor(sqrt((double)s) + 0.5)
+// for lengths below 2^25, which covers every instance registration admits
+// (coordinate spans below 2^24 per axis).
 // The estimate comes from 32-bit dx, dy in FP32 (GB300 runs 64-bit
 // integer/float conversions on its narrow FP64 pipe, so none are used).
 // The estimate only has to be close: m is the exact result iff

@@ -1594,6 +1594,20 @@ static void upload_mlp(DeviceBuffer<faco::MlpParams>& P, DeviceBuffer<faco::MlpO
     cuda_check(cudaGetLastError(), "operand refresh");
 }
 
+// The tcgen05 kernels ask for tc::kLaunchSmemBytes of dynamic shared memory
+// (above the 48 KB default), which caps them at tc::kCtasPerSm CTAs per SM.
+static cudaError_t prepare_tensor_kernels() {
+    cudaError_t err = cudaFuncSetAttribute(faco::mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(faco::tc::kLaunchSmemBytes));
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(faco::prior_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(faco::tc::kLaunchSmemBytes));
+    return err;
+}
+static std::uint32_t tensor_grid(std::uint64_t tiles) {
+    return static_cast<std::uint32_t>(std::max<std::uint64_t>(1, std::min<std::uint64_t>(tiles, 152u * faco::tc::kCtasPerSm)));
+}
+
 static std::uint32_t mlp_blocks(std::uint64_t chunks) {
     return static_cast<std::uint32_t>(std::max<std::uint64_t>(1, std::min<std::uint64_t>(chunks, 152ull * 8)));
 }
@@ -1608,11 +1622,18 @@ int faco_mlp_forward(const float* params, const uint16_t* x, uint32_t count, flo
         DeviceBuffer<__nv_bfloat16> dx;
         dx.upload(reinterpret_cast<const __nv_bfloat16*>(x), static_cast<std::size_t>(count) * faco::kMlpIn, s);
         DeviceBuffer<float> dp(count);
-        faco::mlp_forward_kernel<<<mlp_blocks((count + 63) / 64), 128, 0, s>>>(P.get(), O.get(), dx.get(), count,
-                                                                             dp.get());
+        DeviceBuffer<unsigned> derr(1);
+        cuda_check(cudaMemsetAsync(derr.get(), 0, sizeof(unsigned), s), "memset");
+        cuda_check(prepare_tensor_kernels(), "tcgen05 kernel attributes");
+        faco::mlp_forward_kernel<<<tensor_grid((count + faco::tc::kRows - 1) / faco::tc::kRows), 128,
+                                   faco::tc::kLaunchSmemBytes, s>>>(P.get(), O.get(), dx.get(), count, dp.get(),
+                                                                    derr.get());
         cuda_check(cudaGetLastError(), "mlp forward");
+        unsigned err = 0;
         dp.download(prob, count, s);
+        derr.download(&err, 1, s);
         cuda_check(cudaStreamSynchronize(s), "mlp forward");
+        if (err) throw Error(FACO_EDEVICE, "device error word " + std::to_string(err) + " in the MLP forward pass");
     });
 }
 
@@ -1732,13 +1753,16 @@ static void apply_prior(faco_engine* e) {
     faco::global_neighbours_kernel<<<v.count, 256, 0, e->stream>>>(e->colonies.get(), e->prior_gnbr.get(),
                                                                     e->prior_offsets.get());
     // enough chunk blocks per colony to fill the GPU about four times over
-    const std::uint32_t chunks = (max_cells + 63) / 64;
-    const std::uint32_t per_colony = std::max<std::uint32_t>(1, std::min(chunks, 4u * 152u * 4u / v.count + 1));
+    // 128-entry tiles; about one resident wave of CTAs (4 per SM) over all colonies
+    const std::uint32_t tiles = (max_cells + faco::tc::kRows - 1) / faco::tc::kRows;
+    const std::uint32_t wave = 152u * faco::tc::kCtasPerSm;
+    const std::uint32_t per_colony = std::max<std::uint32_t>(1, std::min(tiles, (wave + v.count - 1) / v.count));
     const dim3 grid(per_colony, v.count);
-    faco::prior_apply_kernel<<<grid, 128, 0, e->stream>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
-                                                          e->prior_enabled.get(), e->prior_params.get(),
-                                                          e->prior_ops.get(), e->prior_floor, e->prior_gamma,
-                                                          e->prior_gnbr.get(), e->prior_offsets.get());
+    cuda_check(prepare_tensor_kernels(), "tcgen05 kernel attributes");
+    faco::prior_apply_kernel<<<grid, 128, faco::tc::kLaunchSmemBytes, e->stream>>>(
+        e->d_instances.get(), e->colonies.get(), e->states.get(), e->prior_enabled.get(), e->prior_params.get(),
+        e->prior_ops.get(), e->prior_floor, e->prior_gamma, e->prior_gnbr.get(), e->prior_offsets.get(),
+        e->error.get());
     cuda_check(cudaGetLastError(), "prior apply");
 }
 

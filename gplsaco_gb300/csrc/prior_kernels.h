@@ -5,11 +5,14 @@
 
 #include "faco_common.cuh"
 #include "prior_mlp.cuh"
+#include "prior_mlp_tc.cuh"
 
 namespace faco {
 
+// tcgen05 kernels (prior_mlp_tc.cuh): 128 threads, dynamic shared memory
+// tc::kLaunchSmemBytes, at most tc::kCtasPerSm CTAs per SM.
 __global__ void mlp_forward_kernel(const MlpParams* P, const MlpOperands* O, const __nv_bfloat16* x, std::uint32_t E,
-                                   float* prob);
+                                   float* prob, unsigned* error);
 __global__ void mlp_grad_kernel(const MlpParams* P, const MlpOperands* O, const __nv_bfloat16* x, const float* y,
                                 std::uint32_t E, float inv_count, MlpParams* grad, float* loss);
 __global__ void adam_kernel(MlpParams* P, const MlpParams* grad, MlpParams* m, MlpParams* v, float lr, float beta1,
@@ -23,6 +26,6 @@ __global__ void global_neighbours_kernel(const ColonyView* colonies, std::uint32
 __global__ void prior_apply_kernel(const InstanceView* instances, const ColonyView* colonies,
                                    const ColonyState* states, const std::uint8_t* enabled, const MlpParams* P,
                                    const MlpOperands* O, float floor, int gamma, const std::uint32_t* gnbr_all,
-                                   const std::uint32_t* node_offset);
+                                   const std::uint32_t* node_offset, unsigned* error);
 
 }  // namespace faco

@@ -1,8 +1,9 @@
 // prior_mlp.cu -- forward, backward and Adam kernels of the edge-prior MLP.
 #include <cuda_runtime.h>
 
-#include "prior_mlp.cuh"
 #include "prior_kernels.h"
+#include "prior_mlp.cuh"
+#include "prior_mlp_tc.cuh"
 
 namespace faco {
 
@@ -37,31 +38,16 @@ __device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + expf(-
 
 }  // namespace
 
-// Probabilities for E edges (x: [E][8] BF16).  Grid-stride over 16-edge tiles.
+// Probabilities for E edges (x: [E][8] BF16) on the tcgen05 tensor cores:
+// 128-edge tiles, 128 threads per CTA (one TMEM lane per edge).
 __global__ void __launch_bounds__(128) mlp_forward_kernel(const MlpParams* P, const MlpOperands* O,
-                                                          const __nv_bfloat16* x, std::uint32_t E, float* prob) {
-    __shared__ SharedOperands s;
-    __shared__ __align__(16) __nv_bfloat16 xs[kWarps][16 * kMlpIn];
-    load_operands(s, P, O);
-    __syncthreads();
-    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const std::uint32_t tiles = (E + 15) / 16;
-    for (std::uint32_t tile = blockIdx.x * kWarps + warp; tile < tiles; tile += gridDim.x * kWarps) {
-        const std::uint32_t e0 = tile * 16;
-        for (std::uint32_t i = lane; i < 16 * kMlpIn; i += 32) {
-            const std::uint32_t e = e0 + i / kMlpIn;
-            xs[warp][i] = e < E ? x[(size_t)e * kMlpIn + i % kMlpIn] : __float2bfloat16(0.f);
-        }
-        __syncwarp();
-        MlpTile t;
-        mlp_forward_tile(xs[warp], s.w1, s.w2, s.b1, s.b2, s.w3, s.b3, lane, t);
-        const std::uint32_t g = lane >> 2;
-        if ((lane & 3) == 0) {
-            if (e0 + g < E) prob[e0 + g] = sigmoid(t.z[0]);
-            if (e0 + g + 8 < E) prob[e0 + g + 8] = sigmoid(t.z[1]);
-        }
-        __syncwarp();
-    }
+                                                          const __nv_bfloat16* x, std::uint32_t E, float* prob,
+                                                          unsigned* error) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    tc::forward_rows(
+        P, O, E, smem, error,
+        [&](std::uint32_t row) { return *reinterpret_cast<const uint4*>(x + (size_t)row * kMlpIn); },
+        [&](std::uint32_t row, float z) { prob[row] = sigmoid(z); });
 }
 
 // Binary cross-entropy gradients of the mean loss over `scale_count` edges,
@@ -314,66 +300,42 @@ __global__ void global_neighbours_kernel(const ColonyView* colonies, std::uint32
 
 // Applies the prior to the colonies whose flag is set: for every candidate
 // entry eta' = eta * (floor + p)^gamma (gamma in {1, 2}), p the MLP
-// probability, and products = trails * eta'.  The factor is never zero, so no
+// probability (tcgen05 forward over 128-entry tiles, features computed per
+// entry), and products = trails * eta'.  The factor is never zero, so no
 // candidate is removed.  Flag clear: eta' = eta (plain FACO).  Grid:
-// (chunks of 64 entries, colonies); 4 warps per block, 16 entries per warp.
+// (CTAs per colony, colonies), 128 threads.
 __global__ void __launch_bounds__(128) prior_apply_kernel(const InstanceView* instances, const ColonyView* colonies,
                                                           const ColonyState* states, const std::uint8_t* enabled,
                                                           const MlpParams* P, const MlpOperands* O, float floor,
                                                           int gamma, const std::uint32_t* gnbr_all,
-                                                          const std::uint32_t* node_offset) {
-    __shared__ SharedOperands s;
-    __shared__ __align__(16) __nv_bfloat16 xs[kWarps][16 * kMlpIn];
+                                                          const std::uint32_t* node_offset, unsigned* error) {
+    extern __shared__ __align__(16) unsigned char smem[];
     const std::uint32_t c = blockIdx.y;
     const ColonyView cv = colonies[c];
     const InstanceView in = instances[cv.instance];
-    const std::uint32_t n = in.n, k = in.k, cells = n * k;
-    const std::uint32_t first = blockIdx.x * kChunk;
-    if (first >= cells) return;
+    const std::uint32_t k = in.k, cells = in.n * k;
     if (!enabled[c]) {
-        if (threadIdx.x < kChunk)
-            for (std::uint32_t i = first + threadIdx.x; i < cells; i += gridDim.x * kChunk) {
-                cv.eta[i] = in.eta[i];
-                cv.products[i] = cv.trails[i] * in.eta[i];
-            }
+        for (std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += gridDim.x * blockDim.x) {
+            cv.eta[i] = in.eta[i];
+            cv.products[i] = cv.trails[i] * in.eta[i];
+        }
         return;
     }
     const ColonyState st = states[c];
     const std::uint32_t* gnbr = gnbr_all + node_offset[c];
-    load_operands(s, P, O);
-    __syncthreads();
-    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (std::uint32_t t0 = first + warp * 16; t0 < cells; t0 += gridDim.x * kChunk) {
-        {
-            const std::uint32_t e = t0 + (lane >> 1);
-            float x[kMlpFeatures] = {0, 0, 0, 0, 0, 0};
-            if (e < cells) edge_features(in, cv, st, gnbr, e / k, e % k, x);
-            __nv_bfloat16* row = xs[warp] + (lane >> 1) * kMlpIn;
-            if ((lane & 1) == 0) {
-                row[0] = __float2bfloat16(x[0]); row[1] = __float2bfloat16(x[1]);
-                row[2] = __float2bfloat16(x[2]); row[3] = __float2bfloat16(x[3]);
-            } else {
-                row[4] = __float2bfloat16(x[4]); row[5] = __float2bfloat16(x[5]);
-                row[6] = row[7] = __float2bfloat16(0.0f);
-            }
-        }
-        __syncwarp();
-        MlpTile t;
-        mlp_forward_tile(xs[warp], s.w1, s.w2, s.b1, s.b2, s.w3, s.b3, lane, t);
-        if ((lane & 3) == 0) {
-            const std::uint32_t g = lane >> 2;
-            for (int h = 0; h < 2; ++h) {
-                const std::uint32_t e = t0 + g + 8 * h;
-                if (e < cells) {
-                    const float f = floor + sigmoid(t.z[h]);
-                    const float eta = in.eta[e] * (gamma == 2 ? f * f : f);
-                    cv.eta[e] = eta;
-                    cv.products[e] = cv.trails[e] * eta;
-                }
-            }
-        }
-        __syncwarp();
-    }
+    tc::forward_rows(
+        P, O, cells, smem, error,
+        [&](std::uint32_t e) {
+            float x[kMlpFeatures];
+            edge_features(in, cv, st, gnbr, e / k, e % k, x);
+            return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), 0u);
+        },
+        [&](std::uint32_t e, float z) {
+            const float f = floor + sigmoid(z);
+            const float eta = in.eta[e] * (gamma == 2 ? f * f : f);
+            cv.eta[e] = eta;
+            cv.products[e] = cv.trails[e] * eta;
+        });
 }
 
 // BF16 operand copies of the masters (input columns 6, 7 stay zero).

@@ -1,0 +1,242 @@
+// prior_mlp_tc.cuh -- the edge-prior MLP forward pass on the 5th-generation
+// tensor cores (tcgen05): 128-edge tiles, BF16 operands staged in shared
+// memory and read by the tensor core through matrix descriptors, FP32
+// accumulators in tensor memory (TMEM), epilogues from tcgen05.ld.
+//
+// Per tile (128 edges = 128 TMEM lanes, one row per thread):
+//   layer 1  D1[128][64] = X[128][16] . W1[64][16]^T      (1 MMA, K = 16)
+//   epilogue h1 = relu(D1 + b1) as BF16 -> shared memory (A operand)
+//   layer 2  D2[128][64] = H1[128][64] . W2[64][64]^T     (4 MMAs, K = 16 each)
+//   epilogue z = w3 . relu(D2 + b2) + b3 per row, p = sigmoid(z)
+// One thread issues the MMAs and commits them to an mbarrier; every wait on
+// it is bounded and sets the error word when it runs out.
+//
+// Operand layout (no swizzle, K-major): 8-row x 16-byte core matrices; in a
+// K = 16 slab, element (r, k) sits at (r / 8) * 256 + (k / 8) * 128 +
+// (r % 8) * 16 + (k % 8) * 2 bytes, i.e. core matrices 128 bytes apart along
+// K and 256 bytes apart along the rows; slabs follow each other.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "faco_common.cuh"
+#include "prior_mlp.cuh"
+
+namespace faco {
+namespace tc {
+
+constexpr std::uint32_t kRows = 128;                 // edges per tile (M)
+constexpr std::uint32_t kTmemColumns = 128;          // D1 in columns 0-63, D2 in 64-127
+constexpr std::uint32_t kXBytes = kRows * 16 * 2;    // one K = 16 slab
+constexpr std::uint32_t kHBytes = kRows * 64 * 2;    // four slabs
+constexpr std::uint32_t kW1Bytes = 64 * 16 * 2;
+constexpr std::uint32_t kW2Bytes = 64 * 64 * 2;
+constexpr std::uint32_t kSmemBytes = kXBytes + kHBytes + kW1Bytes + kW2Bytes;   // 30 KB
+// Dynamic shared memory requested per CTA: at most four CTAs per SM, whose
+// 4 x 128 TMEM columns fill the SM's 512, so an allocation never waits.
+constexpr std::uint32_t kLaunchSmemBytes = 56u * 1024u;
+constexpr std::uint32_t kCtasPerSm = 4;
+constexpr std::uint32_t kWaitLimit = 1u << 20;       // try_wait attempts (about a second)
+// No-swizzle K-major layout: core matrices 128 bytes apart along K (leading
+// byte offset), 256 bytes apart along the rows (stride byte offset).
+constexpr std::uint32_t kLbo = 128, kSbo = 256;
+
+__device__ __forceinline__ std::uint32_t smem_u32(const void* p) {
+    return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Byte offset of element (r, k) in a K-major no-swizzle operand with `rows`
+// rows (rows a multiple of 8, K slabs of 16 elements).
+__device__ __forceinline__ std::uint32_t operand_offset(std::uint32_t r, std::uint32_t k, std::uint32_t rows) {
+    return (k >> 4) * rows * 32u + (r >> 3) * 256u + ((k >> 3) & 1u) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Shared-memory matrix descriptor: start address, leading (K-direction) and
+// stride (row-direction) byte offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ std::uint64_t matrix_desc(std::uint32_t saddr, std::uint32_t lbo, std::uint32_t sbo) {
+    return (std::uint64_t)((saddr >> 4) & 0x3FFFu) | ((std::uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((std::uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulate, BF16 A and B, both
+// K-major, N = 64, M = 128.
+constexpr std::uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b, std::uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(std::uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Waits for the barrier's phase `parity` to complete, at most `limit` tries.
+__device__ __forceinline__ bool wait_parity(std::uint64_t* bar, std::uint32_t parity, std::uint32_t limit) {
+    const std::uint32_t addr = smem_u32(bar);
+    for (std::uint32_t i = 0; i < limit; ++i) {
+        std::uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void load16(std::uint32_t taddr, float (&v)[16]) {
+    std::uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Forward pass over rows [0, count): feat(row) gives the row's 8 BF16
+// features as a uint4, out(row, z) receives its logit.  Rows are split
+// over the CTAs of blockIdx.x / gridDim.x in 128-row tiles.  128 threads;
+// `smem` holds kSmemBytes (16-byte aligned).  Returns false (and sets
+// kErrTensorWait) if an MMA completion wait ran out.
+template <class Feat, class Out>
+__device__ bool forward_rows(const MlpParams* P, const MlpOperands* O, std::uint32_t count, unsigned char* smem,
+                             unsigned* error, Feat feat, Out out) {
+    __shared__ std::uint64_t bar;
+    __shared__ std::uint32_t tmem_slot;
+    __shared__ float s_b1[64], s_b2[64], s_w3[64];
+    const std::uint32_t tid = threadIdx.x, warp = tid >> 5;
+    unsigned char* xs = smem;
+    unsigned char* hs = xs + kXBytes;
+    unsigned char* w1s = hs + kHBytes;
+    unsigned char* w2s = w1s + kW1Bytes;
+    // weights as B operands (N = 64 rows = output units, K-major); W1's K
+    // padded from 8 to 16 with zeros
+    for (std::uint32_t i = tid; i < 64 * 16; i += blockDim.x) {
+        const std::uint32_t n = i >> 4, k = i & 15u;
+        const __nv_bfloat16 v = k < kMlpIn ? O->w1[n * kMlpIn + k] : __float2bfloat16(0.0f);
+        *reinterpret_cast<__nv_bfloat16*>(w1s + operand_offset(n, k, 64)) = v;
+    }
+    for (std::uint32_t i = tid; i < 64 * 64; i += blockDim.x) {
+        const std::uint32_t n = i >> 6, k = i & 63u;
+        *reinterpret_cast<__nv_bfloat16*>(w2s + operand_offset(n, k, 64)) = O->w2[n * 64 + k];
+    }
+    for (std::uint32_t i = tid; i < 64; i += blockDim.x) {
+        s_b1[i] = P->b1[i];
+        s_b2[i] = P->b2[i];
+        s_w3[i] = P->w3[i];
+    }
+    const float b3 = P->b3;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(kTmemColumns)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const std::uint32_t tmem = tmem_slot;
+    const std::uint32_t lane_base = (warp * 32u) << 16;     // this warp's TMEM lane quarter
+    const std::uint64_t dx = matrix_desc(smem_u32(xs), kLbo, kSbo);
+    const std::uint64_t dw1 = matrix_desc(smem_u32(w1s), kLbo, kSbo);
+    std::uint32_t phase = 0;
+    bool ok = true;
+    for (std::uint32_t first = blockIdx.x * kRows; first < count; first += gridDim.x * kRows) {
+        // X tile: this thread's row, K = 8 features + 8 zeros
+        const std::uint32_t row = first + tid;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (row < count) v = feat(row);
+        *reinterpret_cast<uint4*>(xs + operand_offset(tid, 0, kRows)) = v;
+        *reinterpret_cast<uint4*>(xs + operand_offset(tid, 8, kRows)) = make_uint4(0, 0, 0, 0);
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (tid == 0) {
+            mma(tmem, dx, dw1, 0);
+            commit(&bar);
+        }
+        bool waited = wait_parity(&bar, phase, kWaitLimit);
+        if (__syncthreads_or(!waited)) { ok = false; break; }
+        phase ^= 1u;
+        fence_after();
+        // epilogue 1: h1 = relu(D1 + b1) -> BF16 A operand of layer 2
+#pragma unroll
+        for (std::uint32_t c = 0; c < 64; c += 16) {
+            float a[16];
+            load16(tmem + lane_base + c, a);
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                uint4 packed;
+                std::uint32_t* w = reinterpret_cast<std::uint32_t*>(&packed);
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const std::uint32_t n = c + g * 8 + 2 * t;
+                    w[t] = pack_bf16(fmaxf(a[g * 8 + 2 * t] + s_b1[n], 0.f), fmaxf(a[g * 8 + 2 * t + 1] + s_b1[n + 1], 0.f));
+                }
+                *reinterpret_cast<uint4*>(hs + operand_offset(tid, c + g * 8, kRows)) = packed;
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (std::uint32_t kk = 0; kk < 4; ++kk)
+                mma(tmem + 64, matrix_desc(smem_u32(hs + kk * kRows * 32u), kLbo, kSbo),
+                    matrix_desc(smem_u32(w2s + kk * 64u * 32u), kLbo, kSbo), kk > 0);
+            commit(&bar);
+        }
+        waited = wait_parity(&bar, phase, kWaitLimit);
+        if (__syncthreads_or(!waited)) { ok = false; break; }
+        phase ^= 1u;
+        fence_after();
+        // epilogue 2: z = w3 . relu(D2 + b2) + b3
+        float z = 0.f;
+#pragma unroll
+        for (std::uint32_t c = 0; c < 64; c += 16) {
+            float a[16];
+            load16(tmem + 64 + lane_base + c, a);
+#pragma unroll
+            for (int t = 0; t < 16; ++t) z += fmaxf(a[t] + s_b2[c + t], 0.f) * s_w3[c + t];
+        }
+        if (row < count) out(row, z + b3);
+        fence_before();
+        __syncthreads();     // TMEM and shared operands are reused by the next tile
+        fence_after();
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(error, kErrTensorWait);
+        // give the MMAs of the phase that ran out a bounded second chance to
+        // finish before the tensor memory is released
+        wait_parity(&bar, phase, kWaitLimit);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemColumns) : "memory");
+    return ok;
+}
+
+}  // namespace tc
+}  // namespace faco
