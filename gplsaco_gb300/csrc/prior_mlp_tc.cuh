@@ -7,6 +7,8 @@
 //   layer 1  D1[128][64] = X[128][16] . W1[64][16]^T      (1 MMA, K = 16)
 //   epilogue h1 = relu(D1 + b1) as BF16 -> shared memory (A operand)
 //   layer 2  D2[128][64] = H1[128][64] . W2[64][64]^T     (4 MMAs, K = 16 each)
+//            into the same TMEM columns; meanwhile every thread fetches its
+//            row of the next tile
 //   epilogue z = w3 . relu(D2 + b2) + b3 per row, p = sigmoid(z)
 // One thread issues the MMAs and commits them to an mbarrier; every wait on
 // it is bounded and sets the error word when it runs out.
@@ -28,16 +30,16 @@ namespace faco {
 namespace tc {
 
 constexpr std::uint32_t kRows = 128;                 // edges per tile (M)
-constexpr std::uint32_t kTmemColumns = 128;          // D1 in columns 0-63, D2 in 64-127
+constexpr std::uint32_t kTmemColumns = 64;           // D1, then D2 over it (D1 is read out first)
 constexpr std::uint32_t kXBytes = kRows * 16 * 2;    // one K = 16 slab
 constexpr std::uint32_t kHBytes = kRows * 64 * 2;    // four slabs
 constexpr std::uint32_t kW1Bytes = 64 * 16 * 2;
 constexpr std::uint32_t kW2Bytes = 64 * 64 * 2;
 constexpr std::uint32_t kSmemBytes = kXBytes + kHBytes + kW1Bytes + kW2Bytes;   // 30 KB
-// Dynamic shared memory requested per CTA: at most four CTAs per SM, whose
-// 4 x 128 TMEM columns fill the SM's 512, so an allocation never waits.
-constexpr std::uint32_t kLaunchSmemBytes = 56u * 1024u;
-constexpr std::uint32_t kCtasPerSm = 4;
+// Dynamic shared memory per CTA: 30 KB, so at most seven CTAs share an SM
+// and their 7 x 64 TMEM columns fit in its 512 (an allocation never waits).
+constexpr std::uint32_t kLaunchSmemBytes = kSmemBytes;
+constexpr std::uint32_t kCtasPerSm = 7;
 constexpr std::uint32_t kWaitLimit = 1u << 20;       // try_wait attempts (about a second)
 // No-swizzle K-major layout: core matrices 128 bytes apart along K (leading
 // byte offset), 256 bytes apart along the rows (stride byte offset).
@@ -109,6 +111,18 @@ __device__ __forceinline__ void load16(std::uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 16 consecutive floats of a 16-byte aligned shared array (4 vector loads).
+__device__ __forceinline__ void load_vec16(const float* p, float (&v)[16]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float4 t = reinterpret_cast<const float4*>(p)[q];
+        v[4 * q] = t.x;
+        v[4 * q + 1] = t.y;
+        v[4 * q + 2] = t.z;
+        v[4 * q + 3] = t.w;
+    }
+}
+
 // Forward pass over rows [0, count): feat(row) gives the row's 8 BF16
 // features as a uint4, out(row, z) receives its logit.  Rows are split
 // over the CTAs of blockIdx.x / gridDim.x in 128-row tiles.  128 threads;
@@ -119,7 +133,7 @@ __device__ bool forward_rows(const MlpParams* P, const MlpOperands* O, std::uint
                              unsigned* error, Feat feat, Out out) {
     __shared__ std::uint64_t bar;
     __shared__ std::uint32_t tmem_slot;
-    __shared__ float s_b1[64], s_b2[64], s_w3[64];
+    __shared__ __align__(16) float s_b1[64], s_b2[64], s_w3[64];
     const std::uint32_t tid = threadIdx.x, warp = tid >> 5;
     unsigned char* xs = smem;
     unsigned char* hs = xs + kXBytes;
@@ -160,11 +174,12 @@ __device__ bool forward_rows(const MlpParams* P, const MlpOperands* O, std::uint
     const std::uint64_t dw1 = matrix_desc(smem_u32(w1s), kLbo, kSbo);
     std::uint32_t phase = 0;
     bool ok = true;
-    for (std::uint32_t first = blockIdx.x * kRows; first < count; first += gridDim.x * kRows) {
+    const std::uint32_t stride = gridDim.x * kRows;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (blockIdx.x * kRows + tid < count) v = feat(blockIdx.x * kRows + tid);
+    for (std::uint32_t first = blockIdx.x * kRows; first < count; first += stride) {
         // X tile: this thread's row, K = 8 features + 8 zeros
         const std::uint32_t row = first + tid;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (row < count) v = feat(row);
         *reinterpret_cast<uint4*>(xs + operand_offset(tid, 0, kRows)) = v;
         *reinterpret_cast<uint4*>(xs + operand_offset(tid, 8, kRows)) = make_uint4(0, 0, 0, 0);
         fence_async_smem();
@@ -182,16 +197,17 @@ __device__ bool forward_rows(const MlpParams* P, const MlpOperands* O, std::uint
         // epilogue 1: h1 = relu(D1 + b1) -> BF16 A operand of layer 2
 #pragma unroll
         for (std::uint32_t c = 0; c < 64; c += 16) {
-            float a[16];
+            float a[16], bias[16];
             load16(tmem + lane_base + c, a);
+            load_vec16(s_b1 + c, bias);
 #pragma unroll
             for (int g = 0; g < 2; ++g) {
                 uint4 packed;
                 std::uint32_t* w = reinterpret_cast<std::uint32_t*>(&packed);
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
-                    const std::uint32_t n = c + g * 8 + 2 * t;
-                    w[t] = pack_bf16(fmaxf(a[g * 8 + 2 * t] + s_b1[n], 0.f), fmaxf(a[g * 8 + 2 * t + 1] + s_b1[n + 1], 0.f));
+                    const int i = g * 8 + 2 * t;
+                    w[t] = pack_bf16(fmaxf(a[i] + bias[i], 0.f), fmaxf(a[i + 1] + bias[i + 1], 0.f));
                 }
                 *reinterpret_cast<uint4*>(hs + operand_offset(tid, c + g * 8, kRows)) = packed;
             }
@@ -203,10 +219,13 @@ __device__ bool forward_rows(const MlpParams* P, const MlpOperands* O, std::uint
         if (tid == 0) {
 #pragma unroll
             for (std::uint32_t kk = 0; kk < 4; ++kk)
-                mma(tmem + 64, matrix_desc(smem_u32(hs + kk * kRows * 32u), kLbo, kSbo),
+                mma(tmem, matrix_desc(smem_u32(hs + kk * kRows * 32u), kLbo, kSbo),
                     matrix_desc(smem_u32(w2s + kk * 64u * 32u), kLbo, kSbo), kk > 0);
             commit(&bar);
         }
+        // the next tile's row while the layer-2 MMAs run
+        v = make_uint4(0, 0, 0, 0);
+        if (row + stride < count) v = feat(row + stride);
         waited = wait_parity(&bar, phase, kWaitLimit);
         if (__syncthreads_or(!waited)) { ok = false; break; }
         phase ^= 1u;
@@ -215,10 +234,12 @@ __device__ bool forward_rows(const MlpParams* P, const MlpOperands* O, std::uint
         float z = 0.f;
 #pragma unroll
         for (std::uint32_t c = 0; c < 64; c += 16) {
-            float a[16];
-            load16(tmem + 64 + lane_base + c, a);
+            float a[16], bias[16], w3[16];
+            load16(tmem + lane_base + c, a);
+            load_vec16(s_b2 + c, bias);
+            load_vec16(s_w3 + c, w3);
 #pragma unroll
-            for (int t = 0; t < 16; ++t) z += fmaxf(a[t] + s_b2[c + t], 0.f) * s_w3[c + t];
+            for (int t = 0; t < 16; ++t) z += fmaxf(a[t] + bias[t], 0.f) * w3[t];
         }
         if (row < count) out(row, z + b3);
         fence_before();
