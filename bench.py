@@ -516,7 +516,9 @@ def run_time_to_gap(args) -> None:
     torch.cuda.set_device(0)
     from gplsaco_gb300 import experiments
     res = experiments.time_to_gap(log=lambda m: print(m, file=sys.stderr, flush=True))
+    pair = res["two_colonies_per_instance"]["targets"][str(res["target_gap"])]
     line = {"metric": "time to 1% mean gap, learned-prior vs plain GPU FACO (ratio)", "value": res["ratio"],
+            "value_two_colonies_per_instance": pair["ratio"],
             "unit": "prior/plain wall-clock", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
             "config": {"workload": "16 instances (N=1000/2000, uniform/clustered, seeds 100-115), 32 ants, "
                                    "k=20, MNE 8, 2-opt; reference = best of 2 plain runs of 1500 iterations"},

@@ -167,6 +167,51 @@ def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
     return params, losses
 
 
+def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: int = 0, floor: float | None = None,
+             gamma: int | None = None, chunk: int | None = None):
+    """Two colonies per instance, the instance's length the better of the
+    two.  params None: both plain (seeds 1 and 2).  Otherwise colony 2 runs
+    with the prior and colony 1 stays plain -- the per-instance fallback is
+    the concurrent plain colony, with no warm-up run to charge.  Returns rows
+    (iteration, seconds, mean gap, best costs) and the work per ant-iteration."""
+    floor = cfg.floor if floor is None else floor
+    gamma = cfg.gamma if gamma is None else gamma
+    chunk = cfg.chunk if chunk is None else chunk
+    count = 2 * len(xys)
+    engine = FacoBatchEngine(max(len(xy) for xy in xys), count, _settings(cfg), device=device)
+    for i, xy in enumerate(xys):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    keys = np.repeat(np.arange(1, len(xys) + 1, dtype=np.uint64), 2)
+    seeds = np.tile(np.array([1, 2], np.uint64), len(xys))
+    engine.begin(keys, seeds, cfg.mne)
+    costs, _ = engine.current_costs(count)
+    t0 = time.perf_counter()
+    if params is not None:
+        engine.prior_set(params, np.tile(np.array([0, 1], np.uint8), len(xys)), floor, gamma)
+
+    def row(it, costs):
+        best = costs.reshape(len(xys), 2).min(axis=1)
+        return it, time.perf_counter() - t0, float(np.mean((best - refs) / refs)), best
+
+    rows = [row(0, costs)]
+    rows[0] = (0, 0.0) + rows[0][2:]
+    done = 0
+    while done < cfg.iterations:
+        engine.step(chunk)
+        done += chunk
+        if params is not None:
+            engine.prior_refresh()
+        costs, _ = engine.current_costs(count)
+        rows.append(row(done, costs))
+    res = engine.finish()
+    engine.close()
+    ant_iterations = float(cfg.ants * count * done)
+    work = {"construction_steps": res["construction_steps"] / ant_iterations,
+            "ls_evaluations": res["ls_evaluations"] / ant_iterations,
+            "ms_per_iteration": 1e3 * rows[-1][1] / done}
+    return rows, work
+
+
 def first_time_below(rows, target: float, extra_seconds: float = 0.0):
     for it, sec, gap, _ in rows:
         if gap <= target:
@@ -209,6 +254,17 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, models[best_model], warm[3], device, *best)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
+    # equal resources: two colonies per instance in both arms
+    pair_plain, pair_plain_work = pair_run(cfg, xys, refs, None, device)
+    pair_prior, pair_prior_work = pair_run(cfg, xys, refs, models[best_model], device, *best)
+
+    def targets(rows_a, rows_b):
+        out = {}
+        for g in (cfg.target_gap,) + tuple(cfg.extra_targets):
+            (ta, ia), (tb, ib) = first_time_below(rows_a, g), first_time_below(rows_b, g)
+            out[str(g)] = {"plain_seconds": ta, "plain_iterations": ia, "prior_seconds": tb, "prior_iterations": ib,
+                           "ratio": (tb / ta) if (ta and tb is not None) else None}
+        return out
     out = {
         "target_gap": cfg.target_gap,
         "plain_seconds": t_plain, "plain_iterations": it_plain,
@@ -225,6 +281,13 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
                      "plain_iterations": first_time_below(plain_rows, g)[1],
                      "prior_iterations": first_time_below(prior_rows, g)[1]} for g in cfg.extra_targets},
         "final_gap_plain": plain_rows[-1][2], "final_gap_prior": prior_rows[-1][2],
+        "two_colonies_per_instance": {
+            "arms": "plain: seeds 1 and 2 plain; prior: seed 1 plain + seed 2 with the prior; best of the two",
+            "targets": targets(pair_plain, pair_prior),
+            "final_gap_plain": pair_plain[-1][2], "final_gap_prior": pair_prior[-1][2],
+            "plain_work": pair_plain_work, "prior_work": pair_prior_work,
+            "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(pair_plain, pair_prior)
+                       if r[0] % 50 == 0}},
         "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(plain_rows, prior_rows)
                    if r[0] % 50 == 0},
         "training_rows": int(len(y)), "training_loss": [float(v) for v in losses],

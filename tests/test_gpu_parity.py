@@ -440,3 +440,23 @@ def test_snapshot_resume_continues_bit_for_bit(api):
         d.restore_state(state)                                     # instance 12 missing
     for e in (a, b, c, d):
         e.close()
+
+
+def test_gp_evolution_on_the_engine(api):
+    """A short evolution (8 programs, 3 generations) evaluated as population
+    batches on the engine: every generation's programs run, the elites carry
+    the best fitness forward (same panel and seeds, so re-evaluation is exact)."""
+    from gplsaco_gb300 import evolution as ev
+    n, ants = 60, 8
+    xy = _cases.uniform_instance(n, seed=321)
+    settings = _settings(api, ants)
+    engine = api.FacoBatchEngine(n, 2, settings, population_size=8)
+    info = engine.register_problem(5, xy.astype(np.float64))
+    keys, seeds = np.full(2, 5, np.uint64), np.array([1, 2], np.uint64)
+    refs = np.full(2, float(info["initial_cost"]))
+    evo = ev.evolve(engine, keys, seeds, refs, 6, ev.EvolutionSettings(population=8, generations=3, elites=2), 9)
+    fitness = [w["fitness"] for w in evo.winners]
+    assert len(fitness) == 3 and all(0 < f <= 1.0 for f in fitness)
+    assert fitness[1] <= fitness[0] and fitness[2] <= fitness[1]
+    assert len(evo.shortlist()) >= 3
+    engine.close()
