@@ -460,3 +460,36 @@ def test_gp_evolution_on_the_engine(api):
     assert fitness[1] <= fitness[0] and fitness[2] <= fitness[1]
     assert len(evo.shortlist()) >= 3
     engine.close()
+
+
+@pytest.mark.parametrize("case", ["n3", "single_ant", "all_identical", "mostly_duplicates"])
+def test_degenerate_instances_match_oracle(api, oracle, case):
+    """Edge cases: the smallest instance, one colony of one ant, every point
+    identical (all lengths 0: zero-weight roulette and no improving move),
+    and an instance that is mostly duplicates -- each equal to the oracle
+    bit for bit, every returned tour a permutation of its length."""
+    rng = np.random.default_rng(77)
+    ants, iterations, k, b, w = 4, 6, 16, 64, 20
+    if case == "n3":
+        xy = np.array([[0, 0], [3, 4], [6, 0]], np.int32)
+    elif case == "single_ant":
+        xy = _cases.uniform_instance(40, seed=3)
+        ants = 1
+    elif case == "all_identical":
+        xy = np.full((25, 2), 123456, np.int32)
+    else:
+        xy = np.repeat(_cases.uniform_instance(6, seed=9), 8, axis=0)[rng.permutation(48)]
+    n = xy.shape[0]
+    settings = _settings(api, ants, k, b, w)
+    engine = api.FacoBatchEngine(n, 2, settings)
+    engine.register_problem(3, xy.astype(np.float64))
+    kk, bb, ww = min(k, n - 1), min(b, n - 1 - min(k, n - 1)), min(w, n - 1)
+    prep = oracle.prepare(xy, kk, bb, ww)
+    seeds = np.array([1, 2], np.uint64)
+    res = engine.evaluate_faco_evaluations(np.full(2, 3, np.uint64), seeds, ants * iterations, 8)
+    for c in range(2):
+        ref = oracle.run_colony(xy, prep, ants=ants, k=kk, b=bb, w=ww, mne=8, iterations=iterations,
+                                key=oracle.lib().orc_colony_key(int(seeds[c]), 3), retention=0.98)
+        assert res["items"][c]["cost"] == ref["cost"] and res["items"][c]["tour"] == ref["tour"].tolist()
+        assert sorted(res["items"][c]["tour"]) == list(range(n))
+    engine.close()
