@@ -29,6 +29,7 @@ EXPORTED = (
     "faco_engine_stream", "faco_evaluate_programs", "faco_mlp_param_count", "faco_mlp_forward", "faco_mlp_gradient",
     "faco_mlp_train", "faco_edge_data", "faco_prior_set", "faco_prior_refresh", "faco_current_costs",
     "faco_pheromone_step_noalloc", "faco_begin_programs", "faco_snapshot", "faco_restore",
+    "faco_evaluate_controllers", "faco_validate_controller", "faco_score_controllers",
 )
 
 
@@ -119,6 +120,10 @@ def load():
                                       C.c_uint32, vp, C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(AntOutputs)]
     L.faco_pheromone_step.argtypes = [C.c_uint32, C.c_uint32, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float,
                                       vp, vp, vp]
+    L.faco_evaluate_controllers.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint64, vp, vp, C.c_uint32, C.c_uint32,
+                                            C.c_uint32, vp, C.c_uint32, C.POINTER(Outputs)]
+    L.faco_validate_controller.argtypes = [vp, C.c_uint32]
+    L.faco_score_controllers.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32, vp, vp]
     L.faco_begin_programs.argtypes = [vp, vp, vp, C.c_uint32, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                       C.c_uint32]
     L.faco_snapshot.argtypes = [vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]

@@ -156,8 +156,9 @@ struct ColonyView {
     long long* ant_costs;          // [ants] final (after LS)
     long long* ant_ccosts;         // [ants] after construction
     unsigned* ant_counts;          // [ants][3]: construction steps, LS evaluations, moved elements
-    const Program* program;        // GP controller of this colony (null: plain FACO)
+    const Program* program;        // GP controller of this colony: 3 tree slots (null: plain FACO)
     std::uint32_t action_mask;     // legal actions
+    std::uint32_t controller_kind; // 0 joint_single (slot 0), 1 conditional_three (slots 0-2 = roles)
 };
 
 struct TraceRow {

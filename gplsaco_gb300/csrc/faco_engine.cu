@@ -236,7 +236,8 @@ struct faco_engine {
         std::size_t node_total = 0, tau_total = 0;
         std::vector<std::uint32_t> sizes;
         std::vector<std::uint64_t> keys, seeds;
-        std::vector<faco_program> programs;     // host copy of the controllers (snapshots)
+        std::vector<faco_program> programs;     // host copy of the controller slots (snapshots)
+        std::vector<std::uint32_t> kinds;
         std::uint32_t action_mask = 0xFFFFFFFFu;
         std::vector<AntClass> classes;
         faco::ColonyParams P{};
@@ -652,12 +653,48 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
 }
 
 // Controller programs of a GP-controlled evaluation (null: plain FACO).
+// Controllers of a GP-controlled evaluation (null: plain FACO): three tree
+// slots per controller and its kind (0 joint_single: slot 0 scores all 32
+// actions; 1 conditional_three: slots 0-2 are the restart, start-region and
+// MNE-level roles).
 struct Control {
-    const faco_program* programs = nullptr;
+    const faco_program* programs = nullptr;   // [n_programs][3]
+    const std::uint32_t* kinds = nullptr;     // [n_programs]
     std::uint32_t n_programs = 0;
     std::uint32_t action_mask = 0xFFFFFFFFu;
     std::uint32_t total_iterations = 1;
 };
+
+// Slots and kinds of plain joint programs (one tree each).
+struct JointSlots {
+    std::vector<faco_program> slots;
+    std::vector<std::uint32_t> kinds;
+    JointSlots(const faco_program* programs, std::uint32_t n) : slots(3ull * n), kinds(n, 0) {
+        for (std::uint32_t i = 0; i < n; ++i) slots[3ull * i] = programs[i];
+    }
+};
+
+// Validation of one controller (validate_controller, cpp/src/program_cpu.cpp:11-24,
+// with this engine's feature spec 3): every used tree valid and of spec 3,
+// at most 63 nodes over the roles, and a role reads no descriptor of a
+// decision taken after it (role 0 neither the MNE level (7) nor the start
+// region (8); role 1 not the MNE level).
+void validate_controller(const faco_program* slots, std::uint32_t kind) {
+    require(kind <= 1, "unknown controller kind");
+    std::uint32_t total = 0;
+    for (std::uint32_t role = 0; role < (kind ? 3u : 1u); ++role) {
+        const faco_program& p = slots[role];
+        if (faco_validate_program(&p) != FACO_OK) throw Error(FACO_EINVAL, g_error);
+        require(p.feature_spec_id == 3, "controllers use feature spec 3");
+        total += p.length;
+        for (std::uint32_t i = 0; kind && i < p.length; ++i) {
+            const std::uint32_t f = p.operand[i];
+            require(!(p.opcode[i] == 0 && ((role == 0 && (f == 7 || f == 8)) || (role == 1 && f == 7))),
+                    "a role tree reads the descriptor of a later decision");
+        }
+    }
+    require(total <= 63, "a controller has more than 63 nodes");
+}
 
 void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
                       uint32_t mne_target, uint32_t trace_iterations, const Control& control = Control{}) {
@@ -671,7 +708,8 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.sizes.assign(count, 0);
     v.keys.assign(keys, keys + count);
     v.seeds.assign(seeds, seeds + count);
-    v.programs.assign(control.programs, control.programs + (control.programs ? control.n_programs : 0));
+    v.programs.assign(control.programs, control.programs + (control.programs ? 3ull * control.n_programs : 0));
+    v.kinds.assign(control.kinds, control.kinds + (control.programs ? control.n_programs : 0));
     v.action_mask = control.action_mask;
     std::vector<faco::ColonyView> views(count);
     std::size_t tau_total = 0, node_total = 0, ant_total = 0;
@@ -707,13 +745,13 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         require(control.n_programs >= 1 && count % control.n_programs == 0,
                 "colonies must be a whole number of replicas per program");
         require(control.action_mask != 0, "the action mask leaves no legal action");
-        for (std::uint32_t i = 0; i < control.n_programs; ++i) {
-            if (faco_validate_program(control.programs + i) != FACO_OK) throw Error(FACO_EINVAL, g_error);
-            require(control.programs[i].feature_spec_id == 3, "controllers use feature spec 3");
-        }
+        require(control.kinds != nullptr, "controller kinds missing");
+        for (std::uint32_t i = 0; i < control.n_programs; ++i)
+            validate_controller(control.programs + 3ull * i, control.kinds[i]);
         replicas = count / control.n_programs;
         static_assert(sizeof(faco::Program) == sizeof(faco_program), "program layout");
-        e->programs.upload(reinterpret_cast<const faco::Program*>(control.programs), control.n_programs, e->stream);
+        e->programs.upload(reinterpret_cast<const faco::Program*>(control.programs), 3ull * control.n_programs,
+                           e->stream);
     }
     e->ant_counts.resize(3ull * A * count);
     e->states.resize(count);
@@ -735,8 +773,9 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         cv.ant_tours = e->ant_tours.get() + ant_off;
         cv.ant_costs = e->ant_costs.get() + static_cast<std::size_t>(c) * A;
         cv.ant_ccosts = e->ant_ccosts.get() + static_cast<std::size_t>(c) * A;
-        cv.program = control.programs ? e->programs.get() + c / replicas : nullptr;
+        cv.program = control.programs ? e->programs.get() + 3ull * (c / replicas) : nullptr;
         cv.action_mask = control.action_mask;
+        cv.controller_kind = control.programs ? control.kinds[c / replicas] : 0u;
         cv.ant_counts = e->ant_counts.get() + 3ull * c * A;
         tau_off += (static_cast<std::size_t>(in.n) * in.k + 3) & ~std::size_t{3};
         node_off += cv.n_pad;
@@ -989,8 +1028,11 @@ int faco_begin_programs(faco_engine* e, const uint64_t* keys, const uint64_t* se
         std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
         if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
         require(total_iterations >= 1, "total_iterations must be positive");
+        require(n_programs >= 1, "controller programs missing");
+        const JointSlots joint(programs, n_programs);
         Control control;
-        control.programs = programs;
+        control.programs = joint.slots.data();
+        control.kinds = joint.kinds.data();
         control.n_programs = n_programs;
         control.action_mask = action_mask;
         control.total_iterations = total_iterations;
@@ -1016,7 +1058,7 @@ int faco_snapshot(faco_engine* e, void* buffer, uint64_t capacity, uint64_t* byt
         h.ants = e->ants;
         h.k_common = e->instances.at(v.keys[0])->k;
         h.mne_target = v.P.mne_target;
-        h.n_programs = static_cast<std::uint32_t>(v.programs.size());
+        h.n_programs = static_cast<std::uint32_t>(v.kinds.size());
         h.action_mask = v.action_mask;
         h.total_iterations = v.P.total_iterations;
         h.controlled = v.P.controlled;
@@ -1032,7 +1074,8 @@ int faco_snapshot(faco_engine* e, void* buffer, uint64_t capacity, uint64_t* byt
             const std::uint64_t d = coordinate_digest(*e->instances.at(v.keys[c]));
             w.put(&d, sizeof d);
         }
-        w.put(v.programs.data(), v.programs.size() * sizeof(faco_program));
+        w.put(v.programs.data(), v.programs.size() * sizeof(faco_program));   // 3 slots per controller
+        w.put(v.kinds.data(), v.kinds.size() * sizeof(std::uint32_t));
         if (buffer) {
             const auto states = fetch(e->states, v.count, s);
             const auto trails = fetch(e->trails, v.tau_total, s);
@@ -1097,8 +1140,10 @@ int faco_restore(faco_engine* e, const void* buffer, uint64_t bytes, uint32_t tr
             require(it != e->instances.end(), "snapshot instance not registered");
             require(coordinate_digest(*it->second) == digests[c], "snapshot instance coordinates differ");
         }
-        std::vector<faco_program> programs(h.n_programs);
-        std::memcpy(programs.data(), take(h.n_programs * sizeof(faco_program)), h.n_programs * sizeof(faco_program));
+        std::vector<faco_program> programs(3ull * h.n_programs);
+        std::vector<std::uint32_t> kinds(h.n_programs);
+        std::memcpy(programs.data(), take(programs.size() * sizeof(faco_program)), programs.size() * sizeof(faco_program));
+        std::memcpy(kinds.data(), take(kinds.size() * sizeof(std::uint32_t)), kinds.size() * sizeof(std::uint32_t));
         require(static_cast<bool>(h.controlled) == (h.n_programs > 0), "snapshot controller fields inconsistent");
         const unsigned char* states = take(h.count * sizeof(faco::ColonyState));
         const unsigned char* trails = take(h.tau_total * sizeof(float));
@@ -1112,6 +1157,7 @@ int faco_restore(faco_engine* e, const void* buffer, uint64_t bytes, uint32_t tr
         Control control;
         if (h.n_programs) {
             control.programs = programs.data();
+            control.kinds = kinds.data();
             control.n_programs = h.n_programs;
             control.action_mask = h.action_mask;
         }
@@ -1313,12 +1359,38 @@ int faco_evaluate_programs(faco_engine* e, const uint64_t* keys, const uint64_t*
         g_error = "controller programs missing";
         return FACO_EINVAL;
     }
+    const JointSlots joint(programs, n_programs);
     Control control;
-    control.programs = programs;
+    control.programs = joint.slots.data();
+    control.kinds = joint.kinds.data();
     control.n_programs = n_programs;
     control.action_mask = action_mask;
     return evaluate_impl(e, keys, seeds, count, evaluation_limit, initial_mne, checkpoint_iterations, n_checkpoints,
                          out, control);
+}
+
+int faco_evaluate_controllers(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
+                              uint64_t evaluation_limit, const faco_program* trees, const uint32_t* kinds,
+                              uint32_t n_controllers, uint32_t action_mask, uint32_t initial_mne,
+                              const uint64_t* checkpoint_iterations, uint32_t n_checkpoints, faco_outputs* out) {
+    if (!trees || !kinds || n_controllers == 0) {
+        g_error = "controllers missing";
+        return FACO_EINVAL;
+    }
+    Control control;
+    control.programs = trees;
+    control.kinds = kinds;
+    control.n_programs = n_controllers;
+    control.action_mask = action_mask;
+    return evaluate_impl(e, keys, seeds, count, evaluation_limit, initial_mne, checkpoint_iterations, n_checkpoints,
+                         out, control);
+}
+
+int faco_validate_controller(const faco_program* trees, uint32_t kind) {
+    return guarded([&] {
+        require(trees != nullptr, "null controller");
+        validate_controller(trees, kind);
+    });
 }
 
 int faco_validate_program(const faco_program* p) {
@@ -1384,6 +1456,43 @@ int faco_score(const faco_program* programs, uint32_t n_programs, const float* f
         const std::uint32_t blocks = (colonies * 32 + 127) / 128;
         faco::score_kernel<<<blocks, 128, 0, s>>>(d_prog.get(), colonies / n_programs, d_feat.get(), d_masks.get(),
                                                   d_scores.get(), d_actions.get(), colonies);
+        cuda_check(cudaGetLastError(), "score launch");
+        d_scores.download(scores, static_cast<std::size_t>(colonies) * 32, s);
+        d_actions.download(actions, colonies, s);
+        cuda_check(cudaStreamSynchronize(s), "score");
+    });
+}
+
+int faco_score_controllers(const faco_program* trees, const uint32_t* kinds, uint32_t n_controllers,
+                           const float* features, uint32_t features_count, const uint32_t* masks, uint32_t colonies,
+                           float* scores, int32_t* actions) {
+    return guarded([&] {
+        require(trees && kinds && features && masks && scores && actions, "null argument");
+        require(n_controllers >= 1 && colonies >= 1 && colonies % n_controllers == 0,
+                "colonies must be a multiple of the controller count");
+        require(features_count == 12, "features must be [12, colonies, 32]");
+        for (std::uint32_t i = 0; i < n_controllers; ++i) validate_controller(trees + 3ull * i, kinds[i]);
+        const std::size_t nf = static_cast<std::size_t>(features_count) * colonies * 32;
+        for (std::size_t i = 0; i < nf; ++i)
+            require(std::isfinite(features[i]) && features[i] >= 0.0f && features[i] <= 1.0f,
+                    "features must be finite and in [0, 1]");
+        for (std::uint32_t c = 0; c < colonies; ++c) require(masks[c] != 0, "a colony has no legal action");
+        DeviceBuffer<faco::Program> d_trees;
+        DeviceBuffer<std::uint32_t> d_kinds, d_masks;
+        DeviceBuffer<float> d_feat, d_scores;
+        DeviceBuffer<std::int32_t> d_actions;
+        cudaStream_t s = nullptr;
+        d_trees.upload(reinterpret_cast<const faco::Program*>(trees), 3ull * n_controllers, s);
+        d_kinds.upload(kinds, n_controllers, s);
+        d_feat.upload(features, nf, s);
+        d_masks.upload(masks, colonies, s);
+        d_scores.resize(static_cast<std::size_t>(colonies) * 32);
+        cuda_check(cudaMemsetAsync(d_scores.get(), 0, static_cast<std::size_t>(colonies) * 32 * sizeof(float), s),
+                   "memset");
+        d_actions.resize(colonies);
+        faco::score_controllers_kernel<<<(colonies * 32 + 127) / 128, 128, 0, s>>>(
+            d_trees.get(), d_kinds.get(), colonies / n_controllers, d_feat.get(), d_masks.get(), d_scores.get(),
+            d_actions.get(), colonies);
         cuda_check(cudaGetLastError(), "score launch");
         d_scores.download(scores, static_cast<std::size_t>(colonies) * 32, s);
         d_actions.download(actions, colonies, s);

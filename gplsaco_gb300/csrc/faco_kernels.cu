@@ -543,6 +543,32 @@ __device__ __forceinline__ std::uint32_t choose_action(float value, bool legal, 
     return __reduce_min_sync(kFull, legal && maximum - value <= 1e-6f ? lane : 32u);
 }
 
+// conditional_three controllers (python/gp_faco/controller.py:60-84,
+// cuda/gp_score.cuh role loop): role 0 picks the restart half (2 options,
+// stride 16), role 1 the start region (4, stride 4), role 2 the MNE level
+// (4, stride 1), each from the prefix the earlier roles fixed.  Lane i <
+// width scores the role's tree on the features of action prefix + i*stride
+// (feature_of(index, action)); a lane is legal when any action of its
+// stride-wide window is; the first maximum within 1e-6 wins.  Role scores
+// go to slots 0-1, 2-5 and 6-9 of `role_scores` (may be null).
+template <class FeatureOf>
+__device__ __forceinline__ std::uint32_t choose_conditional(const Program* trees, FeatureOf feature_of,
+                                                            std::uint32_t mask, std::uint32_t lane,
+                                                            float* role_scores) {
+    std::uint32_t prefix = 0;
+#pragma unroll 1
+    for (int role = 0; role < 3; ++role) {
+        const std::uint32_t width = role == 0 ? 2u : 4u, stride = role == 0 ? 16u : role == 1 ? 4u : 1u;
+        const std::uint32_t action = prefix + (lane < width ? lane : 0u) * stride;
+        const bool legal = lane < width && ((mask >> action) & ((1u << stride) - 1u)) != 0u;
+        const float value = eval_program(trees[role], [&](int i) { return feature_of(i, action); });
+        if (role_scores && lane < width) role_scores[(role == 0 ? 0 : role == 1 ? 2 : 6) + lane] = value;
+        const std::uint32_t pick = choose_action(value, legal, lane);
+        prefix += stride * (pick < 32u ? pick : 0u);
+    }
+    return prefix;
+}
+
 __device__ __forceinline__ float clamp01(double v) { return (float)(v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v); }
 
 // Fused reduce_and_select + update_pheromone for one colony, then (GP-controlled
@@ -660,12 +686,19 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
         }
         __syncthreads();
         if (warp == 0) {
-            const float fa7 = (float)(lane & 3) / 3.0f, fa8 = (float)((lane >> 2) & 3) / 3.0f;
-            const float fa9 = lane >= 16 ? 1.0f : 0.0f;
-            const float value = eval_program(*cv.program, [&](int i) {
-                return i < 7 ? s_feat[i] : i == 7 ? fa7 : i == 8 ? fa8 : i == 9 ? fa9 : 0.0f;
-            });
-            const std::uint32_t a = choose_action(value, (cv.action_mask >> lane) & 1u, lane);
+            // features of action a: the 7 colony features, then its MNE level,
+            // start region and restart flag
+            auto feature_of = [&](int i, std::uint32_t a) {
+                return i < 7 ? s_feat[i] : i == 7 ? (float)(a & 3u) / 3.0f : i == 8 ? (float)((a >> 2) & 3u) / 3.0f
+                                                   : i == 9 ? (a >= 16u ? 1.0f : 0.0f) : 0.0f;
+            };
+            std::uint32_t a;
+            if (cv.controller_kind == 1) {
+                a = choose_conditional(cv.program, feature_of, cv.action_mask, lane, nullptr);
+            } else {
+                const float value = eval_program(*cv.program, [&](int i) { return feature_of(i, lane); });
+                a = choose_action(value, (cv.action_mask >> lane) & 1u, lane);
+            }
             if (lane == 0) {
                 const std::uint32_t chosen = a < 32 ? a : 0;
                 s_st.action = (std::int32_t)chosen;
@@ -730,6 +763,27 @@ __global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const no
 // ---------------------------------------------------------------------------
 // GP scoring: one warp per colony, lane = action (cuda/gp_score.cuh:64-102).
 // ---------------------------------------------------------------------------
+// Controllers (3 tree slots each, kinds[i]): joint ones score all 32 lanes,
+// conditional ones write their role scores to slots 0-9 of the colony's row.
+__global__ void score_controllers_kernel(const Program* trees, const std::uint32_t* kinds, std::uint32_t replicas,
+                                         const float* features, const std::uint32_t* masks, float* scores,
+                                         std::int32_t* actions, std::uint32_t colonies) {
+    const std::uint32_t colony = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (colony >= colonies) return;
+    const std::uint32_t controller = colony / replicas;
+    const Program* slots = trees + 3 * (size_t)controller;
+    auto feature_of = [&](int i, std::uint32_t a) { return features[((size_t)i * colonies + colony) * 32 + a]; };
+    std::uint32_t chosen;
+    if (kinds[controller] == 1) {
+        chosen = choose_conditional(slots, feature_of, masks[colony], lane, scores + (size_t)colony * 32);
+    } else {
+        const float value = eval_program(slots[0], [&](int i) { return feature_of(i, lane); });
+        scores[(size_t)colony * 32 + lane] = value;
+        chosen = choose_action(value, (masks[colony] >> lane) & 1u, lane);
+    }
+    if (lane == 0) actions[colony] = (std::int32_t)chosen;
+}
+
 __global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
                              const std::uint32_t* masks, float* scores, std::int32_t* actions,
                              std::uint32_t colonies) {

@@ -46,6 +46,9 @@ __global__ void colony_update_kernel(const InstanceView* instances, const Colony
 __global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
                                       const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
                                       const float* eta, float* trails, float* products);
+__global__ void score_controllers_kernel(const Program* trees, const std::uint32_t* kinds, std::uint32_t replicas,
+                                         const float* features, const std::uint32_t* masks, float* scores,
+                                         std::int32_t* actions, std::uint32_t colonies);
 __global__ void score_kernel(const Program* programs, std::uint32_t replicas, const float* features,
                              const std::uint32_t* masks, float* scores, std::int32_t* actions,
                              std::uint32_t colonies);

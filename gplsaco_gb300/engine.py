@@ -159,7 +159,8 @@ class FacoBatchEngine:
         cuda/batch_engine.cu:439-447): a controller dict (read_controller,
         bindings.cpp:58-73) -- a bare program, or {controller_version: 1,
         representation, controller_id, trees}.  A joint_single controller is
-        its one tree; conditional_three controllers are not supported."""
+        its one tree; a conditional_three controller's role trees pick restart,
+        start region and MNE level in turn (faco_evaluate_controllers)."""
         if not isinstance(controller, dict):
             raise ValueError("controller must be a dict")
         if "opcode" in controller:
@@ -176,7 +177,10 @@ class FacoBatchEngine:
             if len(trees) != (3 if kind == "conditional_three" else 1):
                 raise ValueError("wrong number of role trees for the controller representation")
             if kind == "conditional_three":
-                raise ValueError("conditional_three controllers are not supported by this engine")
+                if decision_iterations:
+                    raise ValueError("decision recording is not supported by this engine")
+                return self._controllers(_u64_array(instance_keys, "instance_keys"), _u64_array(seeds, "seeds"),
+                                         evaluation_limit_per_colony, [controller], experiment_mask)
             program = trees[0]
         if decision_iterations:
             raise ValueError("decision recording is not supported by this engine")
@@ -203,9 +207,15 @@ class FacoBatchEngine:
         if keys.size != self.colonies or seeds.size != self.colonies:
             raise ValueError("the population entry needs the complete shared panel")
         count = len(programs)
-        batch = self._programs(np.tile(keys, count), np.tile(seeds, count), evaluation_limit_per_colony, programs,
-                               experiment_mask, checkpoint_iterations, initial_mne, trace, "cached_charged",
-                               profile_events_only)
+        if any(isinstance(p, dict) and "opcode" not in p for p in programs):
+            if checkpoint_iterations or trace or initial_mne != 8:
+                raise ValueError("controller populations take no checkpoints, traces or initial MNE")
+            batch = self._controllers(np.tile(keys, count), np.tile(seeds, count), evaluation_limit_per_colony,
+                                      programs, experiment_mask)
+        else:
+            batch = self._programs(np.tile(keys, count), np.tile(seeds, count), evaluation_limit_per_colony,
+                                   programs, experiment_mask, checkpoint_iterations, initial_mne, trace,
+                                   "cached_charged", profile_events_only)
         out = []
         G = self.colonies
         for i in range(count):
@@ -227,6 +237,11 @@ class FacoBatchEngine:
                 part["trace"] = batch["trace"][:, i * G:(i + 1) * G]
             out.append(part)
         return out
+
+    def _controllers(self, keys, seeds, limit, controllers, experiment_mask) -> dict:
+        arr, kinds = controller_arrays(controllers)
+        mask = _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF)
+        return self._evaluate(keys, seeds, limit, 8, "cached_charged", (), False, False, (arr, kinds), mask)
 
     def _programs(self, keys, seeds, limit, programs, experiment_mask, checkpoint_iterations, initial_mne, trace,
                   preparation_mode, profile_events_only=False) -> dict:
@@ -270,6 +285,11 @@ class FacoBatchEngine:
             if programs is None:
                 code = self._L.faco_evaluate(self._handle, keys.ctypes.data, seeds.ctypes.data, count, limit, mne,
                                              cp_ptr, cps.size, C.byref(out))
+            elif isinstance(programs, tuple):
+                arr, kinds = programs
+                code = self._L.faco_evaluate_controllers(self._handle, keys.ctypes.data, seeds.ctypes.data, count,
+                                                         limit, C.cast(arr, C.c_void_p), kinds.ctypes.data,
+                                                         kinds.size, mask, mne, cp_ptr, cps.size, C.byref(out))
             else:
                 code = self._L.faco_evaluate_programs(self._handle, keys.ctypes.data, seeds.ctypes.data, count, limit,
                                                       C.cast(programs, C.c_void_p), len(programs), mask, mne, cp_ptr,
@@ -531,7 +551,7 @@ class CountedState:
         off = _SNAPSHOT_HEADER.itemsize
         keys = np.frombuffer(self._data, "<u8", c, off)
         seeds = np.frombuffer(self._data, "<u8", c, off + 8 * c)
-        off += 24 * c + int(h["n_programs"]) * C.sizeof(_lib.Program)
+        off += 24 * c + int(h["n_programs"]) * (3 * C.sizeof(_lib.Program) + 4)
         costs = [int(np.frombuffer(self._data, "<i8", 1, off + _COLONY_STATE_BYTES * i + 8)[0]) for i in range(c)]
         return {"version": int(h["version"]), "colonies": c, "completed_batches": int(h["done"]),
                 "instance_keys": keys.tolist(), "seeds": seeds.tolist(), "global_costs": costs,
@@ -600,6 +620,60 @@ def program_to_c(program: dict) -> _lib.Program:
         p.constants[i] = struct.unpack("<f", struct.pack("<I", b))[0]
     _lib.check(_lib.load().faco_validate_program(C.byref(p)))
     return p
+
+
+def controller_arrays(controllers):
+    """Controller dicts (or bare program dicts) as three program slots each
+    and their kinds (0 joint_single, 1 conditional_three); validated like
+    read_controller (bindings.cpp:58-73)."""
+    if not isinstance(controllers, (list, tuple)) or not controllers:
+        raise ValueError("controllers must be a non-empty list")
+    slots, kinds = [], []
+    for c in controllers:
+        if not isinstance(c, dict):
+            raise ValueError("a controller must be a dict")
+        if "opcode" in c:
+            trees, kind = [c], 0
+        else:
+            if (len(c) != 4 or type(c.get("controller_version")) is not int or c["controller_version"] != 1
+                    or "controller_id" not in c or "trees" not in c):
+                raise ValueError("unknown controller version or fields")
+            rep = c.get("representation")
+            if rep not in ("joint_single", "conditional_three"):
+                raise ValueError("unknown controller representation")
+            trees = list(c["trees"])
+            kind = 1 if rep == "conditional_three" else 0
+            if len(trees) != (3 if kind else 1):
+                raise ValueError("wrong number of role trees for the controller representation")
+        structs = [program_to_c(t) for t in trees]
+        while len(structs) < 3:
+            structs.append(_lib.Program())
+        slots += structs
+        kinds.append(kind)
+    arr = (_lib.Program * len(slots))(*slots)
+    kinds = np.asarray(kinds, np.uint32)
+    L = _lib.load()
+    for i in range(kinds.size):
+        _lib.check(L.faco_validate_controller(C.cast(C.byref(arr, 3 * i * C.sizeof(_lib.Program)), C.c_void_p),
+                                              int(kinds[i])))
+    return arr, kinds
+
+
+def score_controller_cuda(controller, features, masks) -> dict:
+    """score_controller_cuda (bindings.cpp:1010-1016, gp_score.cu:32-47):
+    joint controllers score all 32 actions, conditional_three ones return
+    their role scores in slots 0-1, 2-5 and 6-9; actions chosen per colony."""
+    arr, kinds = controller_arrays([controller])
+    features = np.ascontiguousarray(features, dtype=np.float32)
+    masks = np.ascontiguousarray(masks, dtype=np.uint32)
+    if features.ndim != 3 or features.shape[0] != 12 or features.shape[2] != 32 or masks.shape != (features.shape[1],):
+        raise ValueError("features must be [12, C, 32] and masks [C]")
+    scores = np.zeros((masks.size, 32), np.float32)
+    actions = np.zeros(masks.size, np.int32)
+    _lib.check(_lib.load().faco_score_controllers(C.cast(arr, C.c_void_p), kinds.ctypes.data, 1,
+                                                  features.ctypes.data, 12, masks.ctypes.data, masks.size,
+                                                  scores.ctypes.data, actions.ctypes.data))
+    return {"scores": scores, "actions": actions}
 
 
 def score_cuda(programs, features, masks) -> dict:

@@ -146,6 +146,29 @@ int faco_evaluate_programs(faco_engine* engine, const uint64_t* instance_keys, c
                            uint32_t n_programs, uint32_t action_mask, uint32_t initial_mne,
                            const uint64_t* checkpoint_iterations, uint32_t n_checkpoints, faco_outputs* out);
 
+/* Controllers (read_controller / validate_controller, bindings.cpp:58-73,
+ * cpp/src/program_cpu.cpp:11-24): three program slots per controller and its
+ * kind -- 0 joint_single (slot 0 scores all 32 actions, as
+ * faco_evaluate_programs), 1 conditional_three (slots 0-2 are role trees
+ * that pick, in turn, restart or not (actions 0-15 / 16-31), the start
+ * region (stride 4) and the MNE level (stride 1), each from the features of
+ * its candidate actions, python/gp_faco/controller.py:60-84).  A role tree
+ * may not read the descriptor of a later decision (role 0: features 7, 8;
+ * role 1: feature 7); a controller has at most 63 nodes over its roles.
+ * Colony c is driven by controller c / (count / n_controllers). */
+int faco_evaluate_controllers(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds,
+                              uint32_t count, uint64_t evaluation_limit_per_colony, const struct faco_program* trees,
+                              const uint32_t* kinds, uint32_t n_controllers, uint32_t action_mask,
+                              uint32_t initial_mne, const uint64_t* checkpoint_iterations, uint32_t n_checkpoints,
+                              faco_outputs* out);
+int faco_validate_controller(const struct faco_program* trees, uint32_t kind);
+/* score_controller_cuda (gp_score.cu:32-47): features f32[12][C][32], masks
+ * u32[C]; joint controllers write 32 scores per colony, conditional ones the
+ * role scores in slots 0-1, 2-5, 6-9 (the rest 0); actions i32[C]. */
+int faco_score_controllers(const struct faco_program* trees, const uint32_t* kinds, uint32_t n_controllers,
+                           const float* features, uint32_t features_count, const uint32_t* masks, uint32_t colonies,
+                           float* scores, int32_t* actions);
+
 /* The same evaluation in explicit steps (the reference's per-batch loop,
  * cuda/batch_engine.cu:875-1135, driven by the caller): faco_begin uploads the
  * panel and resets every colony; faco_step enqueues `iterations` ant batches

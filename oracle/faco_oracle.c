@@ -633,35 +633,105 @@ static float clamp01(double v) { return (float)(v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : 
 
 /* Scores the 32 actions of one colony from its 7 colony features and picks
  * the first maximum within 1e-6 among legal actions (score_cpu rule). */
+/* One program on the 12 features of one action (postfix evaluation as in
+ * score_cpu, cpp/src/program_cpu.cpp:79-116). */
+static float orc_eval12(const orc_program_t* p, const float f[12]) {
+    float stack[16] = {0};
+    int top = 0;
+    for (int i = 0; i < p->length; ++i) {
+        const int op = p->opcode[i];
+        if (op == 0) stack[top++] = f[p->operand[i]];
+        else if (op == 1) stack[top++] = p->constants[p->operand[i]];
+        else {
+            const int ar = arity_of(op);
+            const float third = ar == 3 ? stack[--top] : 0.0f;
+            const float right = ar >= 2 ? stack[--top] : 0.0f;
+            const float left = stack[--top];
+            stack[top++] = orc_apply_operation(op, left, right, third);
+        }
+    }
+    return stack[0];
+}
+
+/* Feature spec 3 of action a: the 7 colony features, then its MNE level,
+ * start region and restart flag. */
+static void orc_action_features(const float colony[7], int a, float f[12]) {
+    for (int i = 0; i < 7; ++i) f[i] = colony[i];
+    f[7] = (float)(a & 3) / 3.0f;
+    f[8] = (float)((a >> 2) & 3) / 3.0f;
+    f[9] = a >= 16 ? 1.0f : 0.0f;
+    f[10] = f[11] = 0.0f;
+}
+
 int32_t orc_control_choose(const orc_program_t* p, const float colony[7], uint32_t mask, float* scores) {
     float maximum = -INFINITY;
     for (int a = 0; a < 32; ++a) {
         float f[12];
-        for (int i = 0; i < 7; ++i) f[i] = colony[i];
-        f[7] = (float)(a & 3) / 3.0f;
-        f[8] = (float)((a >> 2) & 3) / 3.0f;
-        f[9] = a >= 16 ? 1.0f : 0.0f;
-        f[10] = f[11] = 0.0f;
-        float stack[16] = {0};
-        int top = 0;
-        for (int i = 0; i < p->length; ++i) {
-            const int op = p->opcode[i];
-            if (op == 0) stack[top++] = f[p->operand[i]];
-            else if (op == 1) stack[top++] = p->constants[p->operand[i]];
-            else {
-                const int ar = arity_of(op);
-                const float third = ar == 3 ? stack[--top] : 0.0f;
-                const float right = ar >= 2 ? stack[--top] : 0.0f;
-                const float left = stack[--top];
-                stack[top++] = orc_apply_operation(op, left, right, third);
-            }
-        }
-        scores[a] = stack[0];
-        if ((mask >> a) & 1u) maximum = fmaxf(maximum, stack[0]);
+        orc_action_features(colony, a, f);
+        scores[a] = orc_eval12(p, f);
+        if ((mask >> a) & 1u) maximum = fmaxf(maximum, scores[a]);
     }
     for (int a = 0; a < 32; ++a)
         if (((mask >> a) & 1u) && maximum - scores[a] <= 1e-6f) return a;
     return 0;
+}
+
+/* conditional_three (python/gp_faco/controller.py:60-84): role 0 picks the
+ * restart half (2 options, stride 16), role 1 the start region (4, stride
+ * 4), role 2 the MNE level (4, stride 1), from the prefix fixed so far; each
+ * candidate is scored on the features of action prefix + i * stride and is
+ * legal when any action of its stride-wide window is; the first maximum
+ * within 1e-6 wins.  values(trees + role, action) gives a score. */
+static int32_t orc_conditional(const orc_program_t* trees, uint32_t mask, float* role_scores,
+                               float (*value)(const orc_program_t*, int, const void*), const void* ctx) {
+    int32_t prefix = 0;
+    for (int role = 0; role < 3; ++role) {
+        const int width = role == 0 ? 2 : 4, stride = role == 0 ? 16 : role == 1 ? 4 : 1;
+        const int slot = role == 0 ? 0 : role == 1 ? 2 : 6;
+        float vals[4], maximum = -INFINITY;
+        int legal[4];
+        for (int i = 0; i < width; ++i) {
+            const int a = prefix + i * stride;
+            vals[i] = value(trees + role, a, ctx);
+            legal[i] = ((mask >> a) & ((1u << stride) - 1u)) != 0u;
+            if (legal[i]) maximum = fmaxf(maximum, vals[i]);
+            if (role_scores) role_scores[slot + i] = vals[i];
+        }
+        int chosen = 0;
+        for (int i = 0; i < width; ++i)
+            if (legal[i] && maximum - vals[i] <= 1e-6f) { chosen = i; break; }
+        prefix += chosen * stride;
+    }
+    return prefix;
+}
+
+static float orc_colony_value(const orc_program_t* p, int a, const void* ctx) {
+    float f[12];
+    orc_action_features((const float*)ctx, a, f);
+    return orc_eval12(p, f);
+}
+
+int32_t orc_control_choose_conditional(const orc_program_t* trees, const float colony[7], uint32_t mask,
+                                       float* role_scores) {
+    return orc_conditional(trees, mask, role_scores, orc_colony_value, colony);
+}
+
+typedef struct { const float* features; uint32_t colonies, colony; } orc_feature_ctx_t;
+
+static float orc_array_value(const orc_program_t* p, int a, const void* ctx) {
+    const orc_feature_ctx_t* c = (const orc_feature_ctx_t*)ctx;
+    float f[12];
+    for (int i = 0; i < 12; ++i) f[i] = c->features[((size_t)i * c->colonies + c->colony) * 32 + (size_t)a];
+    return orc_eval12(p, f);
+}
+
+void orc_score_conditional(const orc_program_t* trees, const float* features, const uint32_t* masks,
+                           uint32_t colonies, float* scores, int32_t* actions) {
+    for (uint32_t c = 0; c < colonies; ++c) {
+        const orc_feature_ctx_t ctx = {features, colonies, c};
+        for (int j = 0; j < 32; ++j) scores[(size_t)c * 32 + j] = 0.0f;
+        actions[c] = orc_conditional(trees, masks[c], scores + (size_t)c * 32, orc_array_value, &ctx);
+    }
 }
 
 /* ---------------------------------------------------------------------- */
@@ -674,7 +744,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    const orc_run_cfg_t* c, uint64_t key, uint32_t iterations, uint32_t* global_tour,
                    int64_t* global_cost_out, orc_iter_trace_t* trace, float* trails_out,
                    float* products_out, const orc_program_t* program, uint32_t mask,
-                   uint32_t total_iterations) {
+                   uint32_t total_iterations, uint32_t controller_kind) {
     const orc_dist_t d = {n, xy, NULL};
     const uint32_t k = c->k, A = c->ants;
     const size_t cells = (size_t)n * k;
@@ -765,7 +835,8 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
             f[4] = (float)restarts / (float)(restarts + 1);
             f[5] = clamp01((double)(sum_cons - sum_final) / (double)sum_cons * 10.0);
             f[6] = (float)age / (float)(age + 16);
-            action = orc_control_choose(program, f, mask, scores);
+            action = controller_kind == 1 ? orc_control_choose_conditional(program, f, mask, scores)
+                                          : orc_control_choose(program, f, mask, scores);
             mne = 2u << (action & 3);
             region = ((uint32_t)action >> 2) & 3u;
             if (action >= 16) {

@@ -172,7 +172,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    const orc_run_cfg_t* cfg, uint64_t key, uint32_t iterations,
                    uint32_t* global_tour, int64_t* global_cost, orc_iter_trace_t* trace,
                    float* trails_out, float* products_out, const struct orc_program* program, uint32_t mask,
-                   uint32_t total_iterations);
+                   uint32_t total_iterations, uint32_t controller_kind);
 
 /* ---- GP controller scoring (postfix IR) --------------------------------- */
 typedef struct orc_program {
@@ -195,6 +195,14 @@ void orc_regions(uint32_t n, const int32_t* xy, uint32_t* offsets, uint32_t* lis
 uint32_t orc_region_start(uint64_t key, uint32_t batch, uint32_t ant, uint32_t n, const uint32_t* offsets,
                           const uint32_t* list, uint32_t region);
 int32_t orc_control_choose(const orc_program_t* p, const float colony[7], uint32_t mask, float* scores);
+/* conditional_three controllers: trees[3] = the restart, start-region and
+ * MNE-level roles; role_scores[10] (slots 0-1, 2-5, 6-9) may be NULL. */
+int32_t orc_control_choose_conditional(const orc_program_t* trees, const float colony[7], uint32_t mask,
+                                       float* role_scores);
+/* score_controller (controller.py:60-84) over features [12][C][32]:
+ * scores [C][32] (role scores in slots 0-9, the rest 0), actions [C]. */
+void orc_score_conditional(const orc_program_t* trees, const float* features, const uint32_t* masks,
+                           uint32_t colonies, float* scores, int32_t* actions);
 
 #ifdef __cplusplus
 }

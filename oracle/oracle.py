@@ -127,7 +127,10 @@ def lib():
         L.orc_run_colony.restype = C.c_int
         L.orc_run_colony.argtypes = [C.c_uint32, i32p, u32p, u32p, u32p, u32p, C.c_int64, C.POINTER(RunCfg),
                                      C.c_uint64, C.c_uint32, u32p, C.POINTER(C.c_int64), C.c_void_p,
-                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_score_conditional.argtypes = [C.c_void_p, f32p, u32p, C.c_uint32, f32p, i32p]
+        L.orc_control_choose_conditional.restype = C.c_int32
+        L.orc_control_choose_conditional.argtypes = [C.c_void_p, f32p, C.c_uint32, f32p]
         L.orc_log2.restype = C.c_float
         L.orc_log2.argtypes = [C.c_float]
         L.orc_row_entropy_q.restype = C.c_uint32
@@ -286,15 +289,15 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
     trace = (IterTrace * max(iterations, 1))() if want_trace else None
     trails = np.zeros(n * k, np.float32); products = np.zeros(n * k, np.float32)
     backup = np.ascontiguousarray(prep["backup"] if b else np.zeros((n, 1), np.uint32), dtype=np.uint32)
-    pstruct = program_struct(program) if program is not None else None
+    slots, kind = controller_slots(program) if program is not None else (None, 0)
     rc = lib().orc_run_colony(n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
                               np.ascontiguousarray(prep["ls"], dtype=np.uint32),
                               np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),
                               key, iterations, tour, C.byref(cost),
                               C.cast(trace, C.c_void_p) if trace is not None else None,
                               trails.ctypes.data, products.ctypes.data,
-                              C.cast(C.pointer(pstruct), C.c_void_p) if pstruct is not None else None, mask,
-                              total_iterations or iterations)
+                              C.cast(slots, C.c_void_p) if slots is not None else None, mask,
+                              total_iterations or iterations, kind)
     if rc != 0:
         raise RuntimeError(f"oracle colony run failed ({rc})")
     rows = None
@@ -307,6 +310,34 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
                 for t in trace[:iterations]]
     return dict(tour=tour, cost=int(cost.value), trace=rows, trails=trails.reshape(n, k),
                 products=products.reshape(n, k))
+
+
+def controller_slots(controller: dict):
+    """A program dict (joint) or a controller dict {controller_version: 1,
+    representation: joint_single | conditional_three, trees} as the C array
+    of program slots (3 for conditional) and the kind (0 joint, 1 conditional)."""
+    if "opcode" in controller:
+        trees, kind = [controller], 0
+    else:
+        kind = 1 if controller["representation"] == "conditional_three" else 0
+        trees = list(controller["trees"])
+    arr = (Program * max(3, len(trees)))()
+    for i, t in enumerate(trees):
+        arr[i] = program_struct(t)
+    return arr, kind
+
+
+def score_conditional(trees: list, features: np.ndarray, masks: np.ndarray):
+    """score_controller of a conditional_three controller (role scores in
+    slots 0-9 of each colony's row, the rest 0)."""
+    features = np.ascontiguousarray(features, dtype=np.float32)
+    masks = np.ascontiguousarray(masks, dtype=np.uint32)
+    arr = (Program * 3)(*[program_struct(t) for t in trees])
+    scores = np.zeros((masks.size, 32), np.float32)
+    actions = np.zeros(masks.size, np.int32)
+    lib().orc_score_conditional(C.cast(arr, C.c_void_p), features.reshape(-1), masks, masks.size,
+                                scores.reshape(-1), actions)
+    return scores, actions
 
 
 def program_struct(d: dict) -> Program:

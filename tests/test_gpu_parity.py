@@ -311,17 +311,20 @@ def test_gp_controlled_population_matches_oracle(api, oracle, n, ants, iteration
                               "action", "construction_steps", "ls_evaluations"):
                     assert int(row[field]) == int(want[field]), (i, j, it, field)
                 assert row["tau_min"] == np.float32(want["tau_min"]) and row["tau_max"] == np.float32(want["tau_max"])
-    # a joint_single controller dict is its one tree; a conditional one is refused
+    # a joint_single controller dict is its one tree; a conditional one whose
+    # restart role reads the MNE-level descriptor is refused
     one = engine.evaluate_controller_evaluations(
         np.full(2, 42, np.uint64), seeds, ants * iterations,
         {"controller_version": 1, "representation": "joint_single", "controller_id": 7, "trees": [programs[0]]},
         mask)
     assert [it["cost"] for it in one["items"]] == [it["cost"] for it in res[0]["items"]]
+    reads_level = dict(ir_version=1, numeric_spec_id=1, feature_spec_id=3, opcode=[0], operand=[7],
+                       constant_bits=[])
     with pytest.raises(ValueError):
         engine.evaluate_controller_evaluations(
             keys, seeds, ants * iterations,
             {"controller_version": 1, "representation": "conditional_three", "controller_id": 7,
-             "trees": programs[:3]})
+             "trees": [reads_level, programs[1], programs[2]]})
     with pytest.raises(ValueError):
         engine.evaluate_population_evaluations(np.full(3, 42, np.uint64), np.arange(3, dtype=np.uint64),
                                                ants * iterations, programs)     # not the whole panel
@@ -492,4 +495,63 @@ def test_degenerate_instances_match_oracle(api, oracle, case):
                                 key=oracle.lib().orc_colony_key(int(seeds[c]), 3), retention=0.98)
         assert res["items"][c]["cost"] == ref["cost"] and res["items"][c]["tour"] == ref["tour"].tolist()
         assert sorted(res["items"][c]["tour"]) == list(range(n))
+    engine.close()
+
+
+def test_score_controllers_match_oracle(api, oracle):
+    """faco_score_controllers: conditional_three role scores (slots 0-9) and
+    actions bit-identical to the oracle; joint controllers equal score_cuda."""
+    rng = np.random.default_rng(4242)
+    for extended in (False, True):
+        for _ in range(48):
+            ctl = _programs.random_conditional(rng, extended=extended)
+            features = (np.round(rng.random((12, 7, 32), dtype=np.float32) * 4) / 4).astype(np.float32)
+            masks = rng.integers(1, 2**32, size=7, dtype=np.uint64).astype(np.uint32)
+            got = api.score_controller_cuda(ctl, features, masks)
+            ref_scores, ref_actions = oracle.score_conditional(ctl["trees"], features, masks)
+            assert np.array_equal(got["actions"], ref_actions)
+            assert np.array_equal(got["scores"], ref_scores)
+    program = _programs.random_program(rng, features=10, feature_spec_id=3)
+    joint = {"controller_version": 1, "representation": "joint_single", "controller_id": 2, "trees": [program]}
+    features = rng.random((12, 5, 32), dtype=np.float32)
+    masks = rng.integers(1, 2**32, size=5, dtype=np.uint64).astype(np.uint32)
+    got = api.score_controller_cuda(joint, features, masks)
+    ref_scores, ref_actions = oracle.score(program, features, masks)
+    assert np.array_equal(got["actions"], ref_actions) and np.array_equal(got["scores"], ref_scores)
+    bad = _programs.random_conditional(rng)
+    bad["trees"][0] = dict(ir_version=1, numeric_spec_id=1, feature_spec_id=3, opcode=[0], operand=[7],
+                           constant_bits=[])                       # role 0 reads the MNE level
+    with pytest.raises(ValueError):
+        api.score_controller_cuda(bad, features, masks)
+
+
+@pytest.mark.parametrize("n,ants,iterations", [(80, 8, 12), (400, 16, 8)])
+def test_conditional_controllers_match_oracle(api, oracle, n, ants, iterations):
+    """conditional_three and joint controllers in one population batch: tours,
+    costs and every trace field (MNE target used, action chosen) equal the
+    oracle's controlled colony runs."""
+    rng = np.random.default_rng(808 + n)
+    controllers = [_programs.random_conditional(rng), _programs.random_conditional(rng, extended=True),
+                   _programs.random_program(rng, features=10, feature_spec_id=3)]
+    replicas = 2
+    xy = _cases.uniform_instance(n, seed=n + 17)
+    settings = _settings(api, ants, retention=0.9)
+    engine = api.FacoBatchEngine(n, replicas, settings, population_size=len(controllers))
+    engine.register_problem(77, xy.astype(np.float64))
+    prep = oracle.prepare(xy, 16, 64, 20)
+    keys = np.full(replicas, 77, np.uint64)
+    seeds = np.arange(replicas, dtype=np.uint64) + 11
+    res = engine.evaluate_population_evaluations(keys, seeds, ants * iterations, controllers, 0xFFFF0FFF)
+    assert len(res) == len(controllers)
+    for i, ctl in enumerate(controllers):
+        for j in range(replicas):
+            ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations,
+                                    key=oracle.lib().orc_colony_key(int(seeds[j]), 77), retention=0.9,
+                                    program=ctl, mask=0xFFFF0FFF, total_iterations=iterations)
+            assert res[i]["items"][j]["cost"] == ref["cost"], (i, j)
+            assert res[i]["items"][j]["tour"] == ref["tour"].tolist(), (i, j)
+    # the single-controller entry point and a trace check on the first one
+    one = engine.evaluate_controller_evaluations(np.full(2, 77, np.uint64), seeds, ants * iterations,
+                                                 controllers[0], 0xFFFF0FFF)
+    assert [it["cost"] for it in one["items"]] == [it["cost"] for it in res[0]["items"]]
     engine.close()

@@ -4,6 +4,7 @@ The reference's 12-feature controller (cuda/control_state.cuh:200-364) is
 replaced by the engine's 7 colony features + 3 action descriptors; these
 tests pin the restated semantics on the CPU."""
 import numpy as np
+import pytest
 
 from tests import _cases, _programs
 
@@ -57,3 +58,36 @@ def test_entropy_and_log2_are_exact_functions(oracle):
     # uniform row: entropy 1 exactly; one-hot row: 0; log2 of powers of two exact
     assert L.orc_row_entropy_q(np.full(20, 3.0, np.float32), 20, L.orc_log2(20.0)) == 1 << 20
     assert all(L.orc_log2(float(2.0 ** e)) == e for e in range(-60, 60))
+
+
+def _reference_conditional(oracle, trees, features, masks):
+    """controller.py:60-84 restated on top of the joint scorer: per role, the
+    tree's scores at the candidate actions prefix + i*stride, legality by the
+    stride-wide mask window, the first maximum within 1e-6."""
+    prefix = np.zeros(masks.size, np.int64)
+    rows = np.arange(masks.size)
+    for tree, width, stride in zip(trees, (2, 4, 4), (16, 4, 1)):
+        scores, _ = oracle.score(tree, features, np.full(masks.size, 0xFFFFFFFF, np.uint32))
+        action = prefix[:, None] + np.arange(width)[None, :] * stride
+        values = scores[rows[:, None], action]
+        legal = ((masks[:, None] >> action.astype(np.uint32)) & np.uint32((1 << stride) - 1)) != 0
+        maximum = np.max(np.where(legal, values, -np.inf), axis=1)
+        chosen = np.argmax(legal & (maximum[:, None] - values <= np.float32(1e-6)), axis=1)
+        prefix += chosen * stride
+    return prefix
+
+
+@pytest.mark.parametrize("extended", [False, True])
+def test_conditional_controllers_follow_the_reference_rule(oracle, extended):
+    rng = np.random.default_rng(31 + extended)
+    for _ in range(64):
+        ctl = _programs.random_conditional(rng, extended=extended)
+        features = rng.random((12, 9, 32), dtype=np.float32)
+        features[:, :, :] = np.round(features * 4) / 4          # ties happen
+        masks = rng.integers(1, 2**32, size=9, dtype=np.uint64).astype(np.uint32)
+        masks[:3] = [1, 1 << 31, 0x00FF0000]
+        _, actions = oracle.score_conditional(ctl["trees"], features, masks)
+        want = _reference_conditional(oracle, ctl["trees"], features, masks)
+        assert np.array_equal(actions, want)
+        for c in range(masks.size):
+            assert (int(masks[c]) >> int(actions[c])) & 1      # the action is legal
