@@ -250,6 +250,14 @@ __device__ __forceinline__ void edge_features(const InstanceView& in, const Colo
     x[4] = span > 0.0f ? fminf(fmaxf((tau - st.tau_min) / span, 0.0f), 1.0f) : 1.0f;
     const std::uint32_t nb2 = gnbr[i];
     x[5] = (j == (nb2 & 0xffffu) || j == (nb2 >> 16)) ? 1.0f : 0.0f;
+    // mutual nearness: where i sits in j's own candidate row (1 if absent)
+    float back = 1.0f;
+    for (std::uint32_t t = 0; t < k; ++t)
+        if (in.primary[(size_t)j * k + t] == i) {
+            back = k > 1 ? (float)t / (float)(k - 1) : 0.0f;
+            break;
+        }
+    x[6] = back;
 }
 
 // Packed neighbours of the colony's global-best tour in shared memory.
@@ -280,7 +288,7 @@ __global__ void edge_features_kernel(const InstanceView* instances, const Colony
             edge_features(in, cv, st, gnbr, i, r, x);
             __nv_bfloat16* row = x_out + (base + idx) * kMlpIn;
             for (int f = 0; f < kMlpFeatures; ++f) row[f] = __float2bfloat16(x[f]);
-            row[6] = row[7] = __float2bfloat16(0.0f);
+            row[7] = __float2bfloat16(0.0f);
         }
         if (y_out) {
             const std::uint32_t j = in.primary[idx], nb = gnbr[i];
@@ -328,7 +336,8 @@ __global__ void __launch_bounds__(128) prior_apply_kernel(const InstanceView* in
         [&](std::uint32_t e) {
             float x[kMlpFeatures];
             edge_features(in, cv, st, gnbr, e / k, e % k, x);
-            return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), 0u);
+            return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]),
+                              pack_bf16(x[6], 0.0f));
         },
         [&](std::uint32_t e, float z) {
             const float f = floor + sigmoid(z);

@@ -1,11 +1,11 @@
 // prior_mlp.cuh -- the learned edge prior: a 6 -> 64 -> 64 -> 1 MLP scored
-// per candidate edge, BF16 operands with FP32 accumulation on the tensor
+// per candidate edge (7 features), BF16 operands with FP32 accumulation on the tensor
 // cores (mma.sync m16n8k16), forward and backward.
 //
 // The reference has no learned prior (its only prior is an external LKH
 // candidate export, python/gp_faco/candidate_prior.py:20-36); this is the
 // engine's own component.  Layout of one warp tile: 16 edges (rows); layer 1
-// K = 16 (6 features + zero padding), layers 2 and the input gradient K = 64;
+// K = 16 (7 features + zero padding), layers 2 and the input gradient K = 64;
 // the weight gradients use the edges as the K dimension, staged through
 // shared memory by the block (4 warps = 64 edges per chunk).
 #pragma once
@@ -16,8 +16,8 @@
 
 namespace faco {
 
-constexpr int kMlpIn = 8;       // feature slots per edge (6 used + 2 zero)
-constexpr int kMlpFeatures = 6;
+constexpr int kMlpIn = 8;       // feature slots per edge (7 used + 1 zero)
+constexpr int kMlpFeatures = 7;
 constexpr int kMlpHidden = 64;
 
 // FP32 master parameters (4,673 used values) and their BF16 operand copies.

@@ -42,8 +42,8 @@ class GapConfig:
     target_gap: float = 0.01
     extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
     # (model, floor, gamma, chunk) candidates, tuned on validation instances
-    # (seeds 200-214) by wall-clock time to the target gap.  "full" sees all six
-    # features; "geometry" only the four geometric ones (trail level and
+    # (seeds 200-214) by wall-clock time to the target gap.  "full" sees all seven
+    # features; "geometry" only the geometric ones (trail level and
     # best-tour membership masked), so it does not pull ants back onto the
     # parent tour's edges.
     tune_grid: tuple = (("full", 0.05, 1, 10), ("full", 0.5, 1, 10), ("geometry", 0.05, 1, 10),
@@ -152,7 +152,9 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     return rows, enabled, work
 
 
-GEOMETRY_FEATURES = 4   # x0..x3 of the edge features; x4 trail level, x5 best-tour membership
+# masked in the geometry model: x4 trail level, x5 best-tour membership
+# (x0-x3 and x6 -- length, rank, angle, length ratio, mutual rank -- stay)
+COLONY_FEATURES = [4, 5]
 
 
 def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
@@ -160,10 +162,10 @@ def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
     weights of the others, so applying it ignores trail level and best-tour
     membership."""
     xg = x.copy()
-    xg[:, GEOMETRY_FEATURES:] = 0
+    xg[:, COLONY_FEATURES] = 0
     params, losses = prior_mod.train(prior_mod.init_params(seed=1), xg, y, epochs=cfg.epochs, batch=cfg.batch,
                                      lr=cfg.lr)
-    prior_mod.unpack(params)["w1"][:, GEOMETRY_FEATURES:] = 0.0
+    prior_mod.unpack(params)["w1"][:, COLONY_FEATURES] = 0.0
     return params, losses
 
 

@@ -38,7 +38,7 @@ def init_params(seed: int = 0) -> np.ndarray:
     rng = np.random.default_rng(seed)
     p = np.zeros(param_count(), np.float32)
     v = unpack(p)
-    v["w1"][:, :6] = rng.normal(0, np.sqrt(2 / 6), (HIDDEN, 6))
+    v["w1"][:, :7] = rng.normal(0, np.sqrt(2 / 7), (HIDDEN, 7))
     v["w2"][:] = rng.normal(0, np.sqrt(2 / HIDDEN), (HIDDEN, HIDDEN))
     v["w3"][:] = rng.normal(0, np.sqrt(1 / HIDDEN), HIDDEN)
     v["b3"][:] = -2.0   # most candidate edges are not in the best tour

@@ -17,7 +17,7 @@ def prior(engine_lib):
 
 def _data(prior, rng, E):
     x = np.zeros((E, 8), np.float32)
-    x[:, :6] = rng.random((E, 6), dtype=np.float32)
+    x[:, :7] = rng.random((E, 7), dtype=np.float32)
     x[:, 5] = (rng.random(E) < 0.2).astype(np.float32)
     bits = prior.to_bf16_bits(x)
     y = ((x[:, 0] < 0.3) ^ (x[:, 5] > 0.5)).astype(np.float32)
@@ -50,7 +50,7 @@ def test_gradient_matches_oracle(prior, E):
     for name in ("w1", "b1", "w2", "b2", "w3", "b3"):
         g, r = view[name].astype(np.float64), ref[name]
         if name == "w1":
-            g, r = g[:, :6], r[:, :6]
+            g, r = g[:, :7], r[:, :7]
         scale = max(np.max(np.abs(r)), 1e-12)
         assert np.max(np.abs(g - r)) <= 1e-3 * scale, name
 
@@ -84,7 +84,18 @@ def test_edge_data_and_fallback(prior):
     assert x.shape == (3 * n * 16, 8) and y.shape == (3 * n * 16,)
     xf = prior.from_bf16_bits(x)
     assert np.array_equal(xf[:, 5], y)                       # in-best-tour flag == label at the same state
-    assert np.all((xf[:, :6] >= 0) & (xf[:, :6] <= 1))
+    assert np.all((xf[:, :7] >= 0) & (xf[:, :7] <= 1))
+    # x6: rank of i in j's candidate row / (k-1), 1 when absent (mutual nearness)
+    primary = engine.problem_rows(5)["primary"].astype(np.int64)
+    k = primary.shape[1]
+    back = np.ones((n, k), np.float32)
+    for i in range(n):
+        for r in range(k):
+            hit = np.nonzero(primary[primary[i, r]] == i)[0]
+            if hit.size:
+                back[i, r] = hit[0] / (k - 1)
+    want6 = prior.from_bf16_bits(prior.to_bf16_bits(np.tile(back.reshape(-1), 3)))
+    assert np.array_equal(xf[:, 6], want6)
     assert np.all(y.reshape(3, n, 16).sum(axis=2) <= 2)     # at most the two tour neighbours per node
     engine.prior_set(prior.init_params(seed=3), np.zeros(3, np.uint8))
     engine.step(3)
