@@ -155,6 +155,8 @@ struct Instance {
     std::uint64_t key = 0;
     std::uint32_t n = 0, k = 0, b = 0, w = 0;
     std::vector<std::int32_t> xy;
+    std::vector<double> source_xy;  // coordinates as registered (identity check on re-registration)
+    faco_registration info{};
     std::vector<std::uint32_t> initial;
     std::vector<std::uint16_t> primary, backup, ls;
     std::int64_t initial_cost = 0;
@@ -354,13 +356,21 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
         require(!e->eval.active, "cannot register while an evaluation is active");
         require(n >= 3 && n <= e->dimension, "instance size must be in [3, dimension]");
-        require(e->instances.find(instance_key) == e->instances.end(), "instance key already registered");
+        const auto existing = e->instances.find(instance_key);
+        if (existing != e->instances.end()) {
+            const Instance& known = *existing->second;
+            require(known.n == n && std::equal(xy, xy + 2 * std::size_t(n), known.source_xy.begin()),
+                    "instance key already registered with different coordinates");
+            if (info) *info = known.info;
+            return;
+        }
         cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
         const auto started = Clock::now();
         auto inst = std::make_unique<Instance>();
         inst->key = instance_key;
         inst->n = n;
         inst->xy = integer_coordinates(xy, n);
+        inst->source_xy.assign(xy, xy + 2 * std::size_t(n));
         const faco_settings& c = e->settings;
         inst->k = std::min(c.primary_width, n - 1);
         inst->b = std::min(c.backup_width, n - 1 - inst->k);
@@ -455,12 +465,11 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         std::vector<faco::node_t> init16(inst->initial.begin(), inst->initial.end());
         inst->d_initial.upload(init16, s);
         cuda_check(cudaStreamSynchronize(s), "synchronize");
-        if (info) {
-            info->cheap_seconds = cheap_seconds;
-            info->preparation_seconds = seconds_since(started);
-            info->initial_cost = inst->initial_cost;
-            info->n = n;
-        }
+        inst->info.cheap_seconds = cheap_seconds;
+        inst->info.preparation_seconds = seconds_since(started);
+        inst->info.initial_cost = inst->initial_cost;
+        inst->info.n = n;
+        if (info) *info = inst->info;
         e->instance_order.push_back(instance_key);
         e->instances.emplace(instance_key, std::move(inst));
         e->upload_instance_table();

@@ -82,7 +82,10 @@ typedef struct faco_registration {
 /* register_problem(instance_key, coordinates f64[n,2]) (bindings.cpp:623-638).
  * Coordinates must be finite integers with |x| < 2^26 and a span below 2^24
  * per axis, the range in which the TSPLIB EUC_2D formula in double precision
- * rounds every length exactly. */
+ * rounds every length exactly.  A registered identity is immutable
+ * (batch_engine.cu:285-289): registering a key again with the same
+ * coordinates returns the first registration's info and does no work; other
+ * coordinates under a registered key are FACO_EINVAL. */
 int faco_register_problem(faco_engine* engine, uint64_t instance_key, const double* xy, uint32_t n,
                           faco_registration* info);
 

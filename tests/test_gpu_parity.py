@@ -382,6 +382,13 @@ def test_registration_rows_match_oracle(api, oracle, n, k, b, w):
     assert np.array_equal(rows["backup"], prep["backup"])
     assert np.array_equal(rows["ls"], prep["ls"])
     assert np.array_equal(rows["initial_tour"], prep["initial"]) and info["initial_cost"] == prep["cost"]
+    # A registered identity is immutable (batch_engine.cu:285-289, test_batch_engine.py:82-86).
+    assert engine.register_problem(7, xy.astype(np.float64)) == info
+    with pytest.raises(ValueError):
+        engine.register_problem(7, xy.astype(np.float64) + 0.1)
+    with pytest.raises(ValueError):
+        engine.register_problem(7, xy[:-1].astype(np.float64))
+    assert np.array_equal(engine.problem_rows(7)["primary"], prep["primary"])
     engine.close()
 
 
