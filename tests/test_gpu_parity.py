@@ -242,6 +242,42 @@ def test_full_size_invariants(api, oracle):
     engine.close()
 
 
+@pytest.mark.parametrize("limit", [1, 2, 19, 20, 21, 39, 40, 41, 1000])
+def test_ls_evaluation_limit_boundaries_with_ties(api, oracle, limit):
+    """The warp 2-opt stops at exactly the LS evaluation budget, with equal
+    lengths and coincident points (zero gains, ties by node order) on a 12x12
+    grid -- plain and GP-controlled colonies equal the oracle's serial scan
+    (tests/python/test_parallel_ls_cuda.py:15-38); checkpoint lists that
+    repeat, decrease or pass the budget are refused (test_v2_cuda.py:34-36)."""
+    n, ants, iterations = 67, 8, 12
+    xy = np.random.default_rng(420).integers(0, 12, (n, 2)).astype(np.int32)
+    settings = _settings(api, ants, ls_limit=limit, retention=0.9)
+    program = _programs.random_program(np.random.default_rng(limit), features=10, feature_spec_id=3)
+    engine = api.FacoBatchEngine(n, 2, settings, population_size=2)
+    engine.register_problem(312, xy.astype(np.float64))
+    prep = oracle.prepare(xy, 16, 50, 20)
+    keys = np.full(2, 312, np.uint64)
+    seeds = np.array([17, 29], np.uint64)
+    plain = engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8, trace=True)
+    controlled = engine.evaluate_population_evaluations(keys, seeds, ants * iterations, [program, program])
+    for c in range(2):
+        key = oracle.lib().orc_colony_key(int(seeds[c]), 312)
+        ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=50, w=20, mne=8, iterations=iterations, key=key,
+                                retention=0.9, ls_limit=limit)
+        assert plain["items"][c]["tour"] == ref["tour"].tolist() and plain["items"][c]["cost"] == ref["cost"]
+        assert [int(x) for x in plain["trace"]["ls_evaluations"][:, c]] == \
+            [int(row["ls_evaluations"]) for row in ref["trace"]]
+        ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=50, w=20, mne=8, iterations=iterations, key=key,
+                                retention=0.9, ls_limit=limit, program=program, total_iterations=iterations)
+        for part in controlled:
+            assert part["items"][c]["tour"] == ref["tour"].tolist() and part["items"][c]["cost"] == ref["cost"]
+    if limit == 1:
+        for points in ([1, 1], [3, 1], [iterations + 1]):
+            with pytest.raises(ValueError):
+                engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8, checkpoint_iterations=points)
+    engine.close()
+
+
 def test_invalid_inputs_raise_before_search(api):
     """Strict inputs (tests/python/test_fixed_faco_gpu.py:39-68, test_batch_engine.py:62-79)."""
     engine = api.FacoBatchEngine(50, 2, _settings(api, 8))
