@@ -64,7 +64,8 @@ class Outputs(C.Structure):
                 ("checkpoint_tours", C.c_void_p), ("completed_batches", C.c_uint64),
                 ("construction_steps", C.c_uint64), ("ls_evaluations", C.c_uint64),
                 ("reversed_elements", C.c_uint64), ("kernel_milliseconds", C.c_double),
-                ("solve_seconds", C.c_double), ("colony_work", C.c_void_p)]
+                ("solve_seconds", C.c_double), ("colony_work", C.c_void_p),
+                ("control_states", C.c_void_p)]
 
 
 class Program(C.Structure):

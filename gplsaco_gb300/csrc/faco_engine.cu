@@ -951,6 +951,13 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
             out->colony_work[3 * c + 1] = states[c].ls_evaluations;
             out->colony_work[3 * c + 2] = states[c].reversed_elements;
         }
+        if (out->control_states) {
+            std::uint32_t* row = out->control_states + 4 * std::size_t(c);
+            row[0] = states[c].restarts;
+            row[1] = states[c].iteration - states[c].last_improvement;
+            row[2] = states[c].region;
+            row[3] = states[c].mne_target;
+        }
         steps += states[c].construction_steps;
         evals += states[c].ls_evaluations;
         reversed += states[c].reversed_elements;

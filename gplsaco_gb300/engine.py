@@ -230,6 +230,8 @@ class FacoBatchEngine:
                         completed_construction_steps=int(work[:, 0].sum()),
                         completed_ls_evaluations=int(work[:, 1].sum()), reversed_elements=int(work[:, 2].sum()),
                         colony_work=work)
+            if "control_states" in batch:
+                part["control_states"] = batch["control_states"][i * G:(i + 1) * G]
             if "checkpoints" in batch:
                 part["checkpoints"] = [{"iterations": cp["iterations"], "tours": cp["tours"][i * G:(i + 1) * G]}
                                        for cp in batch["checkpoints"]]
@@ -276,8 +278,10 @@ class FacoBatchEngine:
         trace_rows = np.zeros((iterations, count), _lib.TRACE_DTYPE) if trace else None
         cp_tours = np.zeros((cps.size, count, D), np.uint32) if cps.size else None
         work = np.zeros((count, 3), np.uint64)
+        control = np.zeros((count, 4), np.uint32)
         out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), _lib.ptr(cp_tours))
         out.colony_work = work.ctypes.data
+        out.control_states = control.ctypes.data
         if not self._lock.acquire(blocking=False):
             raise RuntimeError("only one active evaluation per engine")
         try:
@@ -319,6 +323,8 @@ class FacoBatchEngine:
             "actual_seconds": out.solve_seconds,
             "preparation_mode": preparation_mode,
         }
+        if programs is not None:
+            result["control_states"] = control_state_dicts(control)
         if cps.size:
             result["checkpoints"] = [
                 {"iterations": int(cps[i]),
@@ -364,14 +370,17 @@ class FacoBatchEngine:
         costs = np.zeros(count, np.int64)
         trace_rows = np.zeros((min(cap, done), count), _lib.TRACE_DTYPE) if cap else None
         work = np.zeros((count, 3), np.uint64)
+        control = np.zeros((count, 4), np.uint32)
         out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), None)
         out.colony_work = work.ctypes.data
+        out.control_states = control.ctypes.data
         self._active = None
         _lib.check(self._L.faco_finish(self._handle, C.byref(out)))
         return {"tours": [tours[c, :self._sizes[int(keys[c])]] for c in range(count)], "costs": costs,
                 "completed_batches": int(out.completed_batches),
                 "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
-                "reversed_elements": int(out.reversed_elements), "colony_work": work, "trace": trace_rows}
+                "reversed_elements": int(out.reversed_elements), "colony_work": work, "trace": trace_rows,
+                "control_states": control_state_dicts(control)}
 
     def begin_programs(self, instance_keys, seeds, programs, experiment_mask=0xFFFFFFFF, *, initial_mne=8,
                        total_iterations, trace_iterations: int = 0) -> None:
@@ -620,6 +629,15 @@ def program_to_c(program: dict) -> _lib.Program:
         p.constants[i] = struct.unpack("<f", struct.pack("<I", b))[0]
     _lib.check(_lib.load().faco_validate_program(C.byref(p)))
     return p
+
+
+def control_state_dicts(rows) -> list[dict]:
+    """Per-colony controller feedback after the last batch (the
+    control_states list of bindings.cpp:395-407, for the feature-spec-3
+    controller): restarts, batches since the last global improvement, and
+    the start region (4 = all nodes) and MNE target of the next batch."""
+    return [{"restarts": int(r[0]), "stagnant_batches": int(r[1]), "start_region": int(r[2]),
+             "mne_target": int(r[3])} for r in rows]
 
 
 def controller_arrays(controllers):

@@ -122,6 +122,11 @@ typedef struct faco_outputs {
     double solve_seconds;
     uint64_t* colony_work;      /* [count][3] per colony: construction steps, LS
                                    evaluations, reversed elements; may be NULL */
+    uint32_t* control_states;   /* [count][4] per colony after the last batch
+                                   (the controller feedback of bindings.cpp:395-407):
+                                   restarts, stagnant batches (since the last
+                                   global improvement), start region of the next
+                                   batch (4 = all nodes), its MNE target; may be NULL */
 } faco_outputs;
 
 /* evaluate_faco_evaluations(keys, seeds, evaluation_limit_per_colony, mne,

@@ -309,6 +309,19 @@ def test_invalid_inputs_raise_before_search(api):
     engine.close()
 
 
+def _control_state(trace, initial_cost):
+    """Controller feedback after the last batch, from an oracle trace:
+    restarts (actions >= 16), batches since the last global improvement, and
+    the start region / MNE target the last action set."""
+    best, last = initial_cost, 0
+    for it, row in enumerate(trace):
+        if row["global_cost"] < best:
+            best, last = row["global_cost"], it + 1
+    a = int(trace[-1]["action"])
+    return {"restarts": sum(int(row["action"]) >= 16 for row in trace), "stagnant_batches": len(trace) - last,
+            "start_region": (a >> 2) & 3, "mne_target": 2 << (a & 3)}
+
+
 @pytest.mark.parametrize("n,ants,iterations", [(60, 8, 10), (250, 16, 12), (1000, 32, 6)])
 def test_gp_controlled_population_matches_oracle(api, oracle, n, ants, iterations):
     """GP-controlled colonies (feature spec 3: features, warp scoring of 32
@@ -347,6 +360,7 @@ def test_gp_controlled_population_matches_oracle(api, oracle, n, ants, iteration
                               "action", "construction_steps", "ls_evaluations"):
                     assert int(row[field]) == int(want[field]), (i, j, it, field)
                 assert row["tau_min"] == np.float32(want["tau_min"]) and row["tau_max"] == np.float32(want["tau_max"])
+            assert part["control_states"][j] == _control_state(ref["trace"], prep["cost"]), (i, j)
     # a joint_single controller dict is its one tree; a conditional one whose
     # restart role reads the MNE-level descriptor is refused
     one = engine.evaluate_controller_evaluations(
@@ -506,6 +520,61 @@ def test_gp_evolution_on_the_engine(api):
     assert fitness[1] <= fitness[0] and fitness[2] <= fitness[1]
     assert len(evo.shortlist()) >= 3
     engine.close()
+
+
+def test_population_matches_every_serial_member(api):
+    """A population batch equals each member run on its own: tours, costs,
+    work counters and controller feedback, over two panels of three
+    instances; a duplicated program gets its own colonies and equal results;
+    sub-populations (any slice, fewer than the engine holds) reproduce their
+    members' results; population sizes 0 and 129 and an empty population are
+    refused (tests/python/test_population_cuda.py:27-103)."""
+    from gplsaco_gb300 import evolution as ev
+    n, replicas, iterations, ants = 67, 4, 40, 8
+    settings = _settings(api, ants)
+    evo = ev.Evolution(ev.EvolutionSettings(population=8, elites=2), 1103)
+    evo.initialize()
+    values = evo.programs()
+    values[-1] = values[0]
+    serial = api.FacoBatchEngine(n, replicas, settings)
+    expanded = api.FacoBatchEngine(n, replicas, settings, population_size=len(values))
+    for key in (1, 2, 3):
+        xy = np.random.default_rng(107 + key).integers(0, 5000, (n, 2)).astype(np.float64)
+        for engine in (serial, expanded):
+            engine.register_problem(key, xy)
+    fields = ("completed_construction_steps", "completed_ls_evaluations", "completed_tour_evaluations_per_colony",
+              "total_tour_evaluations", "control_states")
+    for panel, panel_seeds in (([1, 1, 2, 2], [17, 29, 17, 29]), ([3, 2, 3, 1], [41, 29, 53, 17])):
+        keys, seeds = np.asarray(panel, np.uint64), np.asarray(panel_seeds, np.uint64)
+        results = expanded.evaluate_population_evaluations(keys, seeds, iterations * ants, values)
+        assert len(results) == len(values)
+        for program, actual in zip(values, results, strict=True):
+            expected = serial.evaluate_program_evaluations(keys, seeds, iterations * ants, program)
+            assert [(r["tour"], r["cost"]) for r in actual["items"]] == \
+                [(r["tour"], r["cost"]) for r in expected["items"]]
+            for field in fields:
+                assert actual[field] == expected[field], field
+            assert actual["actual_seconds"] * len(values) == pytest.approx(actual["population_actual_seconds"])
+        assert results[0]["items"] == results[-1]["items"]
+        for start, stop in ((3, 8), (0, 1), (0, 3), (0, 8)):
+            chunk = expanded.evaluate_population_evaluations(keys, seeds, iterations * ants, values[start:stop])
+            assert len(chunk) == stop - start
+            for expected, actual in zip(results[start:stop], chunk, strict=True):
+                assert [(r["tour"], r["cost"]) for r in actual["items"]] == \
+                    [(r["tour"], r["cost"]) for r in expected["items"]]
+                for field in fields:
+                    assert actual[field] == expected[field], field
+    for count in (0, 129):
+        with pytest.raises(ValueError):
+            api.FacoBatchEngine(n, replicas, settings, population_size=count)
+    with pytest.raises(ValueError):
+        expanded.evaluate_population_evaluations(keys, seeds, ants, [])
+    single = serial.evaluate_population_evaluations(keys, seeds, ants, [values[1]])[0]
+    expected = serial.evaluate_program_evaluations(keys, seeds, ants, values[1])
+    assert single["control_states"] == expected["control_states"]
+    assert [r["tour"] for r in single["items"]] == [r["tour"] for r in expected["items"]]
+    serial.close()
+    expanded.close()
 
 
 @pytest.mark.parametrize("case", ["n3", "single_ant", "all_identical", "mostly_duplicates"])
