@@ -1,7 +1,8 @@
 #!/bin/sh
 # Builds oracle/_ref/libgplsaco_ref.so from the reference's own CPU sources
-# (cpp/src/faco_cpu.cpp, cpp/src/program_cpu.cpp of LinHuanli/GPLSACO, read in
-# place, never copied) plus oracle/ref_shim.cpp.  Test infrastructure only.
+# (cpp/src/faco_cpu.cpp, program_cpu.cpp, control_cpu.cpp, prepared_problem.cpp
+# and sparse_graph.cpp of LinHuanli/GPLSACO, read in place, never copied) plus
+# oracle/ref_shim.cpp.  Test infrastructure only.
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
 set -e
 REF=${1:-/root/reference}
@@ -12,6 +13,7 @@ if [ ! -f "$REF/cpp/src/faco_cpu.cpp" ]; then
 fi
 mkdir -p "$HERE/_ref"
 g++ -std=c++17 -O2 -fPIC -shared -ffp-contract=off -I"$REF/cpp/include" \
-    "$REF/cpp/src/faco_cpu.cpp" "$REF/cpp/src/program_cpu.cpp" "$HERE/ref_shim.cpp" \
+    "$REF/cpp/src/faco_cpu.cpp" "$REF/cpp/src/program_cpu.cpp" "$REF/cpp/src/control_cpu.cpp" \
+    "$REF/cpp/src/prepared_problem.cpp" "$REF/cpp/src/sparse_graph.cpp" "$HERE/ref_shim.cpp" \
     -o "$HERE/_ref/libgplsaco_ref.so"
 echo "built $HERE/_ref/libgplsaco_ref.so"

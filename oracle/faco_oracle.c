@@ -735,6 +735,128 @@ void orc_score_conditional(const orc_program_t* trees, const float* features, co
 }
 
 /* ---------------------------------------------------------------------- */
+/* Feature spec 2 inside a colony run: the state the reference keeps per   */
+/* colony (ControllerState, control_ops.hpp:160-173) and its per-batch     */
+/* update (update_control, control_state.cuh:124-245).                     */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+    orc_control_in_t in;
+    orc_archive_t archive;
+    uint32_t samples[ORC_SAMPLE_CAPACITY];
+    double* local_scale;
+    double epsilon;
+    double* trails64;
+    uint32_t* ppos;
+    orc_fp_t* ids;
+    int64_t* costs;
+    orc_feedback_t feedback;
+    orc_fp_t active_id, epoch_id;
+    int64_t tracked_global, tracked_epoch, parent_cost;
+} ctl2_t;
+
+static int ctl2_init(ctl2_t* t, uint32_t n, const int32_t* xy, const uint32_t* primary, uint32_t k,
+                     const uint32_t* initial, int64_t initial_cost, uint64_t instance_key) {
+    (void)primary;
+    t->local_scale = (double*)malloc(sizeof(double) * n);
+    t->trails64 = (double*)malloc(sizeof(double) * (size_t)n * k);
+    t->ppos = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    t->archive.tours = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)ORC_ARCHIVE_CAPACITY * n);
+    t->archive.pos = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)ORC_ARCHIVE_CAPACITY * n);
+    if (!t->local_scale || !t->trails64 || !t->ppos || !t->archive.tours || !t->archive.pos) return -1;
+    orc_sample_nodes(n, instance_key, t->samples);
+    orc_local_scale(n, xy, t->local_scale, &t->epsilon);
+    t->archive.n = n;
+    t->archive.size = 1;
+    memcpy(t->archive.tours, initial, sizeof(uint32_t) * n);
+    for (uint32_t i = 0; i < n; ++i) t->archive.pos[initial[i]] = i;
+    t->archive.cost[0] = initial_cost;
+    t->archive.id[0] = orc_fingerprint(initial, n);
+    t->active_id = t->epoch_id = t->archive.id[0];
+    t->tracked_global = t->tracked_epoch = t->parent_cost = initial_cost;
+    return 0;
+}
+
+static void ctl2_free(ctl2_t* t) {
+    free(t->local_scale); free(t->trails64); free(t->ppos); free(t->archive.tours); free(t->archive.pos);
+    free(t->ids); free(t->costs);
+}
+
+static void ctl2_input(ctl2_t* t, uint32_t n, const int32_t* xy, const uint32_t* primary, uint32_t k,
+                       const uint32_t* parent, int64_t parent_cost, const float* trails, float dflt, float tmin,
+                       float tmax, double elapsed, uint64_t key, uint32_t batch, uint32_t mask) {
+    for (uint32_t i = 0; i < n; ++i) t->ppos[parent[i]] = i;
+    for (size_t i = 0; i < (size_t)n * k; ++i) t->trails64[i] = (double)trails[i];
+    orc_control_in_t* in = &t->in;
+    in->n = n; in->xy = xy; in->primary = primary; in->k = k;
+    in->samples = t->samples; in->sample_count = n < ORC_SAMPLE_CAPACITY ? n : ORC_SAMPLE_CAPACITY;
+    in->local_scale = t->local_scale; in->epsilon = t->epsilon;
+    in->active_tour = parent; in->active_pos = t->ppos; in->active_cost = parent_cost; in->active_id = t->active_id;
+    in->archive = &t->archive; in->feedback = t->feedback;
+    in->trails = t->trails64; in->default_trail = (double)dflt;
+    in->tau_min = (double)tmin; in->tau_max = (double)tmax;
+    in->elapsed_ratio = elapsed; in->solve_key = key; in->batch = batch; in->experiment_mask = mask;
+}
+
+static float ctl2_value(const orc_program_t* p, int a, const void* ctx) {
+    const float* f = (const float*)ctx;
+    float col[12];
+    for (int i = 0; i < 12; ++i) col[i] = f[i * 32 + a];
+    return orc_eval12(p, col);
+}
+
+/* joint_single: first maximum within 1e-6 among legal actions; conditional
+ * controllers: the role rule, role scores in slots 0-9. */
+static int32_t ctl2_choose(const orc_program_t* program, uint32_t kind, const float* f, uint32_t legal,
+                           float* scores) {
+    if (kind == 1) {
+        for (int a = 0; a < 32; ++a) scores[a] = 0.0f;
+        return orc_conditional(program, legal, scores, ctl2_value, f);
+    }
+    float maximum = -INFINITY;
+    for (int a = 0; a < 32; ++a) {
+        scores[a] = ctl2_value(program, a, f);
+        if ((legal >> a) & 1u) maximum = fmaxf(maximum, scores[a]);
+    }
+    for (int a = 0; a < 32; ++a)
+        if (((legal >> a) & 1u) && maximum - scores[a] <= 1e-6f) return a;
+    return 0;
+}
+
+static int ctl2_update(ctl2_t* t, uint32_t n, const uint32_t* tours, const orc_ant_info_t* infos, uint32_t A,
+                       uint32_t best, const uint32_t* global_tour, int64_t global_cost, int64_t epoch_cost,
+                       int from_epoch, uint64_t ls_limit) {
+    if (!t->ids) {
+        t->ids = (orc_fp_t*)malloc(sizeof(orc_fp_t) * A);
+        t->costs = (int64_t*)malloc(sizeof(int64_t) * A);
+        if (!t->ids || !t->costs) return -1;
+    }
+    for (uint32_t a = 0; a < A; ++a) {
+        t->ids[a] = orc_fingerprint(tours + (size_t)a * n, n);
+        t->costs[a] = infos[a].final_cost;
+    }
+    const int improved = global_cost < t->tracked_global;
+    if (orc_archive_update(&t->archive, global_tour, global_cost, tours, t->costs, A) != 0) return -1;
+    double returned = 0, work = 0;
+    for (uint32_t a = 0; a < A; ++a) {
+        returned += t->ids[a].first == t->active_id.first && t->ids[a].second == t->active_id.second;
+        if (ls_limit) work += (double)infos[a].ls.move_evaluations / (double)ls_limit;
+    }
+    orc_update_feedback(&t->feedback, improved, returned / A, work / A, A);
+    if (epoch_cost < t->tracked_epoch) t->epoch_id = t->ids[best];
+    t->active_id = from_epoch ? t->epoch_id : t->ids[best];
+    t->tracked_global = global_cost;
+    t->tracked_epoch = epoch_cost;
+    return 0;
+}
+
+/* A start node from a start list (the engine's Philox draw of orc_region_start). */
+static uint32_t orc_list_start(uint64_t key, uint32_t batch, uint32_t ant, const uint32_t* list, uint32_t count) {
+    uint32_t x[4];
+    orc_philox4x32(0, ant, batch, 1, (uint32_t)key, (uint32_t)(key >> 32), x);
+    return list[((uint64_t)x[0] * count) >> 32];
+}
+
+/* ---------------------------------------------------------------------- */
 /* A whole colony in engine arithmetic: reset_colony + initialize_products */
 /* (colony_state.cuh:72-110), per batch every ant, reduce_and_select      */
 /* (:148-208) and the FP32 trail update.                                  */
@@ -744,7 +866,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    const orc_run_cfg_t* c, uint64_t key, uint32_t iterations, uint32_t* global_tour,
                    int64_t* global_cost_out, orc_iter_trace_t* trace, float* trails_out,
                    float* products_out, const orc_program_t* program, uint32_t mask,
-                   uint32_t total_iterations, uint32_t controller_kind) {
+                   uint32_t total_iterations, uint32_t controller_kind, orc_control_io_t* control) {
     const orc_dist_t d = {n, xy, NULL};
     const uint32_t k = c->k, A = c->ants;
     const size_t cells = (size_t)n * k;
@@ -776,7 +898,52 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     uint32_t mne = c->mne_target, region = 4, restarts = 0, last_improvement = 0, last_restart = 0;
     const float log2k = orc_log2((float)k);
     int failed = 0;
+    /* the reference's 12-feature controller (feature spec 2) */
+    const int spec2 = program && program->feature_spec_id == 2;
+    ctl2_t ctl;
+    memset(&ctl, 0, sizeof(ctl));
+    uint32_t start_list[ORC_REGION_CAPACITY], start_count = 0;
+    int32_t used_action = -1;
+    uint32_t cursor = 0;
+    if (spec2 && ctl2_init(&ctl, n, xy, primary, k, initial, initial_cost, control ? control->instance_key : 0) != 0)
+        return -1;
     for (uint32_t batch = 0; batch < iterations; ++batch) {
+        if (spec2) {
+            /* decision before the batch (batch_engine.cu:884-950) */
+            float f[12 * 32], scores[32];
+            uint32_t regions[2 * 4 * ORC_REGION_CAPACITY], alt = ORC_ARCHIVE_CAPACITY;
+            ctl2_input(&ctl, n, xy, primary, k, parent, ctl.parent_cost, trails, dflt, (float)tmin, (float)tmax,
+                       (double)((uint64_t)batch * A) / (double)((uint64_t)total_iterations * A), key, batch, mask);
+            const uint32_t legal = orc_control_features(&ctl.in, f, regions, &alt);
+            if (!legal) { failed = 1; break; }
+            const int32_t a = ctl2_choose(program, controller_kind, f, legal, scores);
+            if (control && cursor < control->count && batch + 1 == control->points[cursor]) {
+                memcpy(control->features + (size_t)cursor * 12 * 32, f, sizeof(f));
+                memcpy(control->scores + (size_t)cursor * 32, scores, sizeof(scores));
+                control->masks[cursor] = legal;
+                control->actions[cursor] = a;
+                ++cursor;
+            }
+            used_action = a;
+            mne = 2u << (a & 3);
+            start_count = n < ORC_REGION_CAPACITY ? n : ORC_REGION_CAPACITY;
+            memcpy(start_list, regions + ((uint32_t)a / 16 * 4 + ((uint32_t)a / 4) % 4) * ORC_REGION_CAPACITY,
+                   sizeof(start_list));
+            if (a >= 16) {
+                /* restart from the alternative reference (control_state.cuh:302-336) */
+                const orc_archive_t* ar = &ctl.archive;
+                epoch_cost = ar->cost[alt];
+                ctl.parent_cost = epoch_cost;
+                orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
+                dflt = (float)tmax;
+                ctl.tracked_epoch = epoch_cost;
+                ctl.active_id = ctl.epoch_id = ar->id[alt];
+                orc_restart_feedback(&ctl.feedback);
+                memcpy(parent, ar->tours + (size_t)alt * n, sizeof(uint32_t) * n);
+                memcpy(epoch, ar->tours + (size_t)alt * n, sizeof(uint32_t) * n);
+                for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * eta[i]; }
+            }
+        }
 #ifdef _OPENMP
 #pragma omp parallel num_threads(c->threads > 0 ? (int)c->threads : 1)
 #endif
@@ -789,8 +956,9 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
 #endif
             for (int ant = 0; ant < (int)A; ++ant) {
                 for (uint32_t s = 1; s < n; ++s) uni[s] = orc_uniform(key, batch, (uint32_t)ant, s);
-                const uint32_t start = orc_region_start(key, batch, (uint32_t)ant, n, region_offsets, region_list,
-                                                        region);
+                const uint32_t start = spec2 ? orc_list_start(key, batch, (uint32_t)ant, start_list, start_count)
+                                             : orc_region_start(key, batch, (uint32_t)ant, n, region_offsets,
+                                                                region_list, region);
                 const orc_choices_t ch = {NULL, uni, start, primary, products, NULL, k, backup, c->b};
                 if (orc_ant(parent, &d, ls, c->w, &ch, mne, c->ls_evaluation_limit, c->ls_mode, NULL, ptour, ppos,
                             NULL, NULL, &infos[ant]) != 0)
@@ -823,7 +991,12 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                         (float)(1.0 / (double)parent_cost), eta, trails, products, &dflt);
         const uint32_t used_mne = mne;
         int32_t action = -1;
-        if (program) {
+        if (spec2) {
+            if (ctl2_update(&ctl, n, tours, infos, A, best, global_tour, global_cost, epoch_cost, from_epoch,
+                            c->ls_evaluation_limit) != 0) { failed = 1; break; }
+            ctl.parent_cost = parent_cost;
+            action = used_action;
+        } else if (program) {
             uint64_t sumq = 0;
             for (uint32_t row = 0; row < n; ++row) sumq += orc_row_entropy_q(trails + (size_t)row * k, k, log2k);
             const uint32_t t1 = batch + 1, stag = t1 - last_improvement, age = t1 - last_restart;
@@ -860,6 +1033,11 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
             r->construction_steps = steps; r->ls_evaluations = evals;
         }
     }
+    if (spec2 && control) {
+        control->archive_size = ctl.archive.size;
+        control->feedback = ctl.feedback;
+    }
+    if (spec2) ctl2_free(&ctl);
     *global_cost_out = global_cost;
     if (trails_out) memcpy(trails_out, trails, sizeof(float) * cells);
     if (products_out) memcpy(products_out, products, sizeof(float) * cells);

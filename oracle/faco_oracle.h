@@ -147,6 +147,90 @@ typedef struct {
 int64_t orc_prepare(uint32_t n, const int32_t* xy, const orc_prep_cfg_t* cfg, uint32_t* primary,
                     uint32_t* backup, uint32_t* ls, uint32_t* initial);
 
+/* ---- the reference's 12-feature controller (feature spec 2) -------------- */
+#define ORC_ARCHIVE_CAPACITY 4u
+#define ORC_REGION_CAPACITY 16u
+#define ORC_SAMPLE_CAPACITY 64u
+#define ORC_ARCHIVE_BAND 0.02
+
+typedef struct { uint64_t first, second; } orc_fp_t;
+
+typedef struct {
+    float return_rate, ls_work;
+    uint64_t stagnant_batches, epoch_batches, restarts;
+} orc_feedback_t;
+
+/* Up to 4 reference tours: [4][n] orders and positions, costs, fingerprints. */
+typedef struct {
+    uint32_t n, size;
+    uint32_t* tours;
+    uint32_t* pos;
+    int64_t cost[ORC_ARCHIVE_CAPACITY];
+    orc_fp_t id[ORC_ARCHIVE_CAPACITY];
+} orc_archive_t;
+
+/* Everything one decision reads. */
+typedef struct {
+    uint32_t n;
+    const int32_t* xy;
+    const uint32_t* primary;      /* [n][k] */
+    uint32_t k;
+    const uint32_t* samples;      /* min(n, 64) sample nodes */
+    uint32_t sample_count;
+    const double* local_scale;    /* [n] mean of the 8 nearest lengths */
+    double epsilon;
+    const uint32_t* active_tour;  /* the parent tour (and its positions) */
+    const uint32_t* active_pos;
+    int64_t active_cost;
+    orc_fp_t active_id;
+    const orc_archive_t* archive;
+    orc_feedback_t feedback;
+    const double* trails;         /* [n][k] */
+    double default_trail, tau_min, tau_max;
+    double elapsed_ratio;
+    uint64_t solve_key;
+    uint32_t batch;
+    uint32_t experiment_mask;
+} orc_control_in_t;
+
+uint64_t orc_ctl_mix(uint64_t v);
+orc_fp_t orc_fingerprint_edge(uint32_t a, uint32_t b);
+orc_fp_t orc_fingerprint(const uint32_t* tour, uint32_t n);
+int orc_canonical_compare(const uint32_t* ta, const uint32_t* pa, const uint32_t* tb, const uint32_t* pb,
+                          uint32_t n);
+void orc_sample_nodes(uint32_t n, uint64_t instance_key, uint32_t* out);
+void orc_build_region(const uint32_t* tour, uint32_t n, const uint32_t* primary, uint32_t k, uint64_t key,
+                      uint32_t batch, uint32_t mode, uint32_t region, uint32_t* nodes);
+uint32_t orc_sampled_difference(const uint32_t* ct, const uint32_t* cp, const uint32_t* at, const uint32_t* ap,
+                                uint32_t n, const uint32_t* samples, uint32_t count);
+void orc_update_feedback(orc_feedback_t* s, int improved, double returned_fraction, double work_fraction,
+                         uint32_t ants);
+void orc_restart_feedback(orc_feedback_t* s);
+int orc_archive_update(orc_archive_t* ar, const uint32_t* global_tour, int64_t global_cost,
+                       const uint32_t* cand_tours, const int64_t* cand_costs, uint32_t m);
+uint32_t orc_archive_alternative(const orc_archive_t* ar, const uint32_t* at, const uint32_t* ap, orc_fp_t active_id,
+                                 const uint32_t* samples, uint32_t sample_count);
+/* features [12][32], regions [2][4][16]; returns the legal mask. */
+uint32_t orc_control_features(const orc_control_in_t* in, float* features, uint32_t* regions,
+                              uint32_t* alternative);
+/* Per-node scale: sum of the min(8, n-1) nearest EUC_2D lengths, each divided
+ * by that count (prepared_problem.cpp:66-86); epsilon = 1e-12 * max span. */
+void orc_local_scale(uint32_t n, const int32_t* xy, double* scale, double* epsilon);
+
+/* Decisions captured at the given 1-based batch numbers (the decision made
+ * before batch point-1), and the final controller state. */
+typedef struct {
+    uint64_t instance_key;
+    const uint32_t* points;
+    uint32_t count;
+    float* features;       /* [count][12][32] */
+    float* scores;         /* [count][32] (conditional: role scores in 0-9) */
+    uint32_t* masks;       /* [count] */
+    int32_t* actions;      /* [count] */
+    uint32_t archive_size; /* out */
+    orc_feedback_t feedback; /* out */
+} orc_control_io_t;
+
 /* ---- a whole plain-FACO colony run in engine arithmetic ------------------ */
 typedef struct {
     uint32_t ants, k, b, w, mne_target;
@@ -166,13 +250,16 @@ typedef struct {
 } orc_iter_trace_t;
 
 /* Runs `iterations` batches of one colony.  global_tour [n]; trace
- * [iterations] (may be NULL); trails_out/products_out [n][k] (may be NULL). */
+ * [iterations] (may be NULL); trails_out/products_out [n][k] (may be NULL).
+ * A program of feature spec 2 runs the reference's 12-feature controller
+ * (control_oracle.c; `control` carries the instance key, decision captures
+ * and the final controller state); spec 3 the engine's own. */
 int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const uint32_t* backup,
                    const uint32_t* ls, const uint32_t* initial, int64_t initial_cost,
                    const orc_run_cfg_t* cfg, uint64_t key, uint32_t iterations,
                    uint32_t* global_tour, int64_t* global_cost, orc_iter_trace_t* trace,
                    float* trails_out, float* products_out, const struct orc_program* program, uint32_t mask,
-                   uint32_t total_iterations, uint32_t controller_kind);
+                   uint32_t total_iterations, uint32_t controller_kind, orc_control_io_t* control);
 
 /* ---- GP controller scoring (postfix IR) --------------------------------- */
 typedef struct orc_program {

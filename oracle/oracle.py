@@ -28,13 +28,13 @@ f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 def build(force: bool = False) -> Path:
     """Compile the oracle with the host compiler (contractions off)."""
-    src = HERE / "faco_oracle.c"
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime,
-                                                                (HERE / "faco_oracle.h").stat().st_mtime):
+    sources = [HERE / "faco_oracle.c", HERE / "control_oracle.c"]
+    newest = max(p.stat().st_mtime for p in sources + [HERE / "faco_oracle.h"])
+    if force or not LIB.exists() or LIB.stat().st_mtime < newest:
         LIB.parent.mkdir(exist_ok=True)
         tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
         subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-                               str(src), "-o", str(tmp), "-lm"])
+                               *map(str, sources), "-o", str(tmp), "-lm"])
         os.replace(tmp, LIB)
     return LIB
 
@@ -90,6 +90,36 @@ class Program(C.Structure):
                 ("operand", C.c_uint8 * 63), ("constants", C.c_float * 63)]
 
 
+class Fp(C.Structure):
+    _fields_ = [("first", C.c_uint64), ("second", C.c_uint64)]
+
+
+class Feedback(C.Structure):
+    _fields_ = [("return_rate", C.c_float), ("ls_work", C.c_float), ("stagnant_batches", C.c_uint64),
+                ("epoch_batches", C.c_uint64), ("restarts", C.c_uint64)]
+
+
+class Archive(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("size", C.c_uint32), ("tours", C.c_void_p), ("pos", C.c_void_p),
+                ("cost", C.c_int64 * 4), ("id", Fp * 4)]
+
+
+class ControlIn(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("xy", C.c_void_p), ("primary", C.c_void_p), ("k", C.c_uint32),
+                ("samples", C.c_void_p), ("sample_count", C.c_uint32), ("local_scale", C.c_void_p),
+                ("epsilon", C.c_double), ("active_tour", C.c_void_p), ("active_pos", C.c_void_p),
+                ("active_cost", C.c_int64), ("active_id", Fp), ("archive", C.c_void_p), ("feedback", Feedback),
+                ("trails", C.c_void_p), ("default_trail", C.c_double), ("tau_min", C.c_double),
+                ("tau_max", C.c_double), ("elapsed_ratio", C.c_double), ("solve_key", C.c_uint64),
+                ("batch", C.c_uint32), ("experiment_mask", C.c_uint32)]
+
+
+class ControlIO(C.Structure):
+    _fields_ = [("instance_key", C.c_uint64), ("points", C.c_void_p), ("count", C.c_uint32),
+                ("features", C.c_void_p), ("scores", C.c_void_p), ("masks", C.c_void_p), ("actions", C.c_void_p),
+                ("archive_size", C.c_uint32), ("feedback", Feedback)]
+
+
 _lib = None
 _ref = None
 
@@ -127,7 +157,20 @@ def lib():
         L.orc_run_colony.restype = C.c_int
         L.orc_run_colony.argtypes = [C.c_uint32, i32p, u32p, u32p, u32p, u32p, C.c_int64, C.POINTER(RunCfg),
                                      C.c_uint64, C.c_uint32, u32p, C.POINTER(C.c_int64), C.c_void_p,
-                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                     C.c_void_p]
+        L.orc_ctl_mix.restype = C.c_uint64
+        L.orc_ctl_mix.argtypes = [C.c_uint64]
+        L.orc_fingerprint.restype = Fp
+        L.orc_fingerprint.argtypes = [u32p, C.c_uint32]
+        L.orc_sample_nodes.argtypes = [C.c_uint32, C.c_uint64, u32p]
+        L.orc_build_region.argtypes = [u32p, C.c_uint32, u32p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32,
+                                       C.c_uint32, u32p]
+        L.orc_archive_update.restype = C.c_int
+        L.orc_archive_update.argtypes = [C.POINTER(Archive), u32p, C.c_int64, u32p, i64p, C.c_uint32]
+        L.orc_control_features.restype = C.c_uint32
+        L.orc_control_features.argtypes = [C.POINTER(ControlIn), f32p, u32p, C.POINTER(C.c_uint32)]
+        L.orc_local_scale.argtypes = [C.c_uint32, i32p, f64p, C.POINTER(C.c_double)]
         L.orc_score_conditional.argtypes = [C.c_void_p, f32p, u32p, C.c_uint32, f32p, i32p]
         L.orc_control_choose_conditional.restype = C.c_int32
         L.orc_control_choose_conditional.argtypes = [C.c_void_p, f32p, C.c_uint32, f32p]
@@ -166,6 +209,19 @@ def ref():
         R.ref_score.restype = C.c_int
         R.ref_score.argtypes = [C.c_uint16, C.c_uint16, C.c_uint16, C.c_uint16, u8p, u8p, C.c_uint16, f32p,
                                 f32p, u32p, C.c_uint32, f32p, i32p]
+        R.ref_fingerprint.argtypes = [u32p, C.c_uint32, u64p]
+        R.ref_sample_nodes.argtypes = [C.c_uint32, C.c_uint64, u32p]
+        R.ref_build_region.argtypes = [u32p, C.c_uint32, u32p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32,
+                                       C.c_uint32, u32p]
+        R.ref_archive_update.restype = C.c_int
+        R.ref_archive_update.argtypes = [C.c_uint32, f64p, u32p, C.c_uint32, u32p, u32p, C.c_uint32, u32p, f64p,
+                                         u64p, C.POINTER(C.c_uint32)]
+        R.ref_action_snapshot.restype = C.c_int
+        R.ref_action_snapshot.argtypes = [C.c_uint32, f64p, u32p, C.c_uint32, u32p, C.c_uint32, f64p, C.c_double,
+                                          u32p, u32p, C.c_uint32, f64p, u32p, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.c_uint32, C.c_double, C.c_uint64, C.c_uint32,
+                                          C.c_uint32, f32p, u32p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                          f64p, C.POINTER(C.c_double)]
         R.ref_colony.restype = C.c_int
         R.ref_colony.argtypes = [C.c_uint32, f64p, u32p, C.c_uint32, u32p, C.c_uint32, u32p, C.c_uint32, u32p,
                                  C.c_double, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, C.c_double,
@@ -280,7 +336,11 @@ def prepare(xy, k, b, w, initial_ls_limit=100000):
 
 def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, retention=0.98, p_best=0.1,
                epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True, ls_mode=0,
-               program=None, mask=0xFFFFFFFF, total_iterations=None):
+               program=None, mask=0xFFFFFFFF, total_iterations=None, instance_key=0, decision_iterations=()):
+    """One colony run.  A program (or controller) of feature spec 2 runs the
+    reference's 12-feature controller; `instance_key` seeds its sample nodes
+    and `decision_iterations` (1-based) capture its decisions, returned under
+    "decisions" with the final "control_state"."""
     xy = np.ascontiguousarray(xy, dtype=np.int32)
     n = xy.shape[0]
     cfg = RunCfg(ants, k, b, w, mne, beta, retention, p_best, epoch_source_probability, ls_limit, threads, ls_mode)
@@ -290,6 +350,12 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
     trails = np.zeros(n * k, np.float32); products = np.zeros(n * k, np.float32)
     backup = np.ascontiguousarray(prep["backup"] if b else np.zeros((n, 1), np.uint32), dtype=np.uint32)
     slots, kind = controller_slots(program) if program is not None else (None, 0)
+    points = np.ascontiguousarray(decision_iterations, dtype=np.uint32)
+    dec = dict(features=np.zeros((max(points.size, 1), 12, 32), np.float32),
+               scores=np.zeros((max(points.size, 1), 32), np.float32), masks=np.zeros(max(points.size, 1), np.uint32),
+               actions=np.zeros(max(points.size, 1), np.int32))
+    io = ControlIO(instance_key, points.ctypes.data, points.size, dec["features"].ctypes.data,
+                   dec["scores"].ctypes.data, dec["masks"].ctypes.data, dec["actions"].ctypes.data)
     rc = lib().orc_run_colony(n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
                               np.ascontiguousarray(prep["ls"], dtype=np.uint32),
                               np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),
@@ -297,7 +363,7 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
                               C.cast(trace, C.c_void_p) if trace is not None else None,
                               trails.ctypes.data, products.ctypes.data,
                               C.cast(slots, C.c_void_p) if slots is not None else None, mask,
-                              total_iterations or iterations, kind)
+                              total_iterations or iterations, kind, C.addressof(io))
     if rc != 0:
         raise RuntimeError(f"oracle colony run failed ({rc})")
     rows = None
@@ -308,8 +374,17 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
                      mne_target=t.mne_target, action=t.action,
                      construction_steps=t.construction_steps, ls_evaluations=t.ls_evaluations)
                 for t in trace[:iterations]]
-    return dict(tour=tour, cost=int(cost.value), trace=rows, trails=trails.reshape(n, k),
-                products=products.reshape(n, k))
+    out = dict(tour=tour, cost=int(cost.value), trace=rows, trails=trails.reshape(n, k),
+               products=products.reshape(n, k))
+    if slots is not None and slots[0].feature_spec_id == 2:
+        fb = io.feedback
+        out["control_state"] = dict(archive_size=io.archive_size, stagnant_batches=fb.stagnant_batches,
+                                    return_rate=fb.return_rate, ls_work=fb.ls_work,
+                                    epoch_batches=fb.epoch_batches, restarts=fb.restarts)
+        out["decisions"] = [dict(iteration=int(points[i]), legal_mask=int(dec["masks"][i]),
+                                 action=int(dec["actions"][i]), features=dec["features"][i],
+                                 scores=dec["scores"][i]) for i in range(points.size)]
+    return out
 
 
 def controller_slots(controller: dict):
@@ -364,3 +439,96 @@ def score(program: dict, features: np.ndarray, masks: np.ndarray):
     scores = np.zeros((colonies, 32), np.float32); actions = np.zeros(colonies, np.int32)
     lib().orc_score(C.byref(p), features.shape[0], features, masks, colonies, scores, actions)
     return scores, actions
+
+
+# ------------------------------------------- the 12-feature controller pieces
+
+def fingerprint(tour) -> tuple[int, int]:
+    tour = np.ascontiguousarray(tour, dtype=np.uint32)
+    f = lib().orc_fingerprint(tour, tour.size)
+    return int(f.first), int(f.second)
+
+
+def sample_nodes(n: int, instance_key: int) -> np.ndarray:
+    out = np.zeros(min(n, 64), np.uint32)
+    lib().orc_sample_nodes(n, instance_key, out)
+    return out
+
+
+def build_region(tour, primary, key, batch, mode, region) -> np.ndarray:
+    tour = np.ascontiguousarray(tour, dtype=np.uint32)
+    primary = np.ascontiguousarray(primary, dtype=np.uint32)
+    out = np.zeros(16, np.uint32)
+    lib().orc_build_region(tour, tour.size, primary, primary.shape[1], key, batch, mode, region, out)
+    return out[:min(tour.size, 16)]
+
+
+def local_scale(xy):
+    xy = np.ascontiguousarray(xy, dtype=np.int32)
+    out = np.zeros(xy.shape[0], np.float64)
+    eps = C.c_double()
+    lib().orc_local_scale(xy.shape[0], xy, out, C.byref(eps))
+    return out, eps.value
+
+
+class ControlArchive:
+    """An archive seeded with entries[0] and updated once with global =
+    entries[0] and the other entries as the batch (the reference's
+    ReferenceArchive built the same way)."""
+
+    def __init__(self, xy, entries):
+        self.xy = np.ascontiguousarray(xy, dtype=np.int32)
+        n = self.xy.shape[0]
+        self.tours = np.zeros((4, n), np.uint32)
+        self.pos = np.zeros((4, n), np.uint32)
+        self.s = Archive(n, 1, self.tours.ctypes.data, self.pos.ctypes.data)
+        e0 = np.ascontiguousarray(entries[0], dtype=np.uint32)
+        self.tours[0] = e0
+        self.pos[0, e0] = np.arange(n, dtype=np.uint32)
+        self.s.cost[0] = self.length(e0)
+        f = lib().orc_fingerprint(e0, n)
+        self.s.id[0] = f
+        self.update(e0, entries[1:])
+
+    def length(self, tour) -> int:
+        return int(np.sum(euc2d_matrix(self.xy)[tour, np.roll(tour, -1)].astype(np.int64)))
+
+    def update(self, global_tour, batch):
+        n = self.xy.shape[0]
+        g = np.ascontiguousarray(global_tour, dtype=np.uint32)
+        cands = np.ascontiguousarray(np.asarray(batch, dtype=np.uint32).reshape(-1, n))
+        costs = np.array([self.length(t) for t in cands], np.int64)
+        if lib().orc_archive_update(C.byref(self.s), g, self.length(g), cands.reshape(-1) if cands.size
+                                    else np.zeros(1, np.uint32), costs if costs.size else np.zeros(1, np.int64),
+                                    cands.shape[0]) != 0:
+            raise RuntimeError("archive update failed")
+
+    def entries(self):
+        return [(self.tours[i].copy(), int(self.s.cost[i]), (int(self.s.id[i].first), int(self.s.id[i].second)))
+                for i in range(self.s.size)]
+
+
+def control_features(xy, primary, samples, scale, epsilon, active, archive: ControlArchive, feedback, trails,
+                     default_trail, tau_min, tau_max, elapsed, solve_key, batch, mask):
+    """make_action_snapshot in the oracle: features [12][32], regions
+    [2][4][16], alternative slot, legal mask."""
+    xy = np.ascontiguousarray(xy, dtype=np.int32)
+    n = xy.shape[0]
+    primary = np.ascontiguousarray(primary, dtype=np.uint32)
+    samples = np.ascontiguousarray(samples, dtype=np.uint32)
+    scale = np.ascontiguousarray(scale, dtype=np.float64)
+    active = np.ascontiguousarray(active, dtype=np.uint32)
+    apos = np.zeros(n, np.uint32)
+    apos[active] = np.arange(n, dtype=np.uint32)
+    trails = np.ascontiguousarray(trails, dtype=np.float64)
+    fb = Feedback(feedback[0], feedback[1], int(feedback[2]), int(feedback[3]), int(feedback[4]))
+    f = lib().orc_fingerprint(active, n)
+    cin = ControlIn(n, xy.ctypes.data, primary.ctypes.data, primary.shape[1], samples.ctypes.data, samples.size,
+                    scale.ctypes.data, epsilon, active.ctypes.data, apos.ctypes.data, archive.length(active), f,
+                    C.addressof(archive.s), fb, trails.ctypes.data, default_trail, tau_min, tau_max, elapsed,
+                    solve_key, batch, mask)
+    features = np.zeros((12, 32), np.float32)
+    regions = np.zeros((2, 4, 16), np.uint32)
+    alt = C.c_uint32()
+    legal = lib().orc_control_features(C.byref(cin), features.reshape(-1), regions.reshape(-1), C.byref(alt))
+    return dict(features=features, regions=regions, alternative=alt.value, legal=legal)

@@ -6,7 +6,10 @@
 // to pin the C restatement in oracle/faco_oracle.c to the reference's own code.
 // Each entry point composes the reference API the way its own tests do
 // (tests/cpp/test_cuda_faco.cpp:68-98, tests/cpp/test_fixed_faco.cpp:235-282,
-// tests/python/test_native_scoring.py:23-46).
+// tests/python/test_native_scoring.py:23-46); the controller entries compose
+// cpp/src/control_cpu.cpp and cpp/include/gp_faco/control_ops.hpp as
+// make_action_snapshot does.
+#include "gp_faco/control_cpu.hpp"
 #include "gp_faco/faco_cpu.hpp"
 #include "gp_faco/program.hpp"
 
@@ -202,6 +205,110 @@ int ref_colony(std::uint32_t n, const double* matrix, const std::uint32_t* prima
         }
         std::memcpy(tour_out, best.data(), n * sizeof(Node));
         *cost_out = gp_faco::CpuTour(best, distance).recomputed_cost();
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// ---- the 12-feature controller (cpp/src/control_cpu.cpp, control_ops.hpp) ----
+
+void ref_fingerprint(const std::uint32_t* tour, std::uint32_t n, std::uint64_t* out) {
+    std::vector<Node> positions(n);
+    for (Node i = 0; i < n; ++i) positions[tour[i]] = i;
+    const auto f = gp_faco::fingerprint({tour, positions.data(), n});
+    out[0] = f.first;
+    out[1] = f.second;
+}
+
+void ref_sample_nodes(std::uint32_t n, std::uint64_t instance_key, std::uint32_t* out) {
+    gp_faco::sample_nodes(n, instance_key, out);
+}
+
+void ref_build_region(const std::uint32_t* tour, std::uint32_t n, const std::uint32_t* primary, std::uint32_t k,
+                      std::uint64_t key, std::uint32_t batch, std::uint32_t mode, std::uint32_t region,
+                      std::uint32_t* nodes) {
+    std::vector<Node> positions(n);
+    for (Node i = 0; i < n; ++i) positions[tour[i]] = i;
+    gp_faco::build_region({tour, positions.data(), n}, primary, k, key, batch, mode, region, nodes);
+}
+
+// ReferenceArchive seeded with entries[0], updated with global = entries[0]
+// and completed = entries[1..m) (one update), then updated once more with
+// `global` and `completed`.  Writes the final entries' tours, costs and
+// fingerprints.
+int ref_archive_update(std::uint32_t n, const double* matrix, const std::uint32_t* entries, std::uint32_t m,
+                       const std::uint32_t* global, const std::uint32_t* completed, std::uint32_t c,
+                       std::uint32_t* out_tours, double* out_costs, std::uint64_t* out_ids, std::uint32_t* count) {
+    try {
+        const auto distance = matrix_distance(matrix, n);
+        const auto record = [&](const std::uint32_t* t) { return gp_faco::TourRecord(std::vector<Node>(t, t + n), distance); };
+        gp_faco::ReferenceArchive archive(record(entries));
+        std::vector<gp_faco::TourRecord> first;
+        for (std::uint32_t i = 1; i < m; ++i) first.push_back(record(entries + static_cast<std::size_t>(i) * n));
+        archive.update(record(entries), first);
+        std::vector<gp_faco::TourRecord> batch;
+        for (std::uint32_t i = 0; i < c; ++i) batch.push_back(record(completed + static_cast<std::size_t>(i) * n));
+        archive.update(record(global), batch);
+        const auto& e = archive.entries();
+        *count = static_cast<std::uint32_t>(e.size());
+        for (std::size_t i = 0; i < e.size(); ++i) {
+            std::memcpy(out_tours + i * n, e[i].order.data(), n * sizeof(Node));
+            out_costs[i] = e[i].cost;
+            out_ids[2 * i] = e[i].identity.first;
+            out_ids[2 * i + 1] = e[i].identity.second;
+        }
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+// make_action_snapshot on an archive built as in ref_archive_update (global =
+// entries[0], completed = entries[1..m)), an active tour, feedback
+// {return_rate, ls_work, stagnant, epoch_batches, restarts} and the trails of
+// a SparsePheromone(initial) evaporated to `minimum` and deposited along
+// `parent` for `rounds` rounds.  Writes features [12][32], regions [2][4][16],
+// the alternative slot, the legal mask and the trails used.
+int ref_action_snapshot(std::uint32_t n, const double* matrix, const std::uint32_t* primary, std::uint32_t k,
+                        const std::uint32_t* samples, std::uint32_t sample_count, const double* local_scale,
+                        double epsilon, const std::uint32_t* active, const std::uint32_t* entries, std::uint32_t m,
+                        const double* feedback, const std::uint32_t* parent, double initial, double retention,
+                        double minimum, double maximum, double increment, std::uint32_t rounds, double elapsed,
+                        std::uint64_t solve_key, std::uint32_t batch, std::uint32_t experiment_mask,
+                        float* features, std::uint32_t* regions, std::uint32_t* alternative, std::uint32_t* legal,
+                        double* trails_out, double* default_out) {
+    try {
+        const auto distance = matrix_distance(matrix, n);
+        const auto record = [&](const std::uint32_t* t) { return gp_faco::TourRecord(std::vector<Node>(t, t + n), distance); };
+        gp_faco::ReferenceArchive archive(record(entries));
+        std::vector<gp_faco::TourRecord> first;
+        for (std::uint32_t i = 1; i < m; ++i) first.push_back(record(entries + static_cast<std::size_t>(i) * n));
+        archive.update(record(entries), first);
+        gp_faco::SparsePheromone pheromone(rows_of(primary, n, k), initial, true);
+        for (std::uint32_t r = 0; r < rounds; ++r) {
+            pheromone.evaporate(retention, minimum);
+            for (Node i = 0; i < n; ++i) pheromone.deposit(parent[(i + n - 1) % n], parent[i], increment, maximum);
+        }
+        gp_faco::ControlStaticData problem{n, k, std::vector<Node>(primary, primary + static_cast<std::size_t>(n) * k),
+            std::vector<Node>(samples, samples + sample_count), std::vector<double>(local_scale, local_scale + n),
+            epsilon};
+        gp_faco::FeedbackState state;
+        state.return_rate = static_cast<float>(feedback[0]);
+        state.ls_work = static_cast<float>(feedback[1]);
+        state.stagnant_batches = static_cast<std::uint64_t>(feedback[2]);
+        state.epoch_batches = static_cast<std::uint64_t>(feedback[3]);
+        state.restarts = static_cast<std::uint64_t>(feedback[4]);
+        const auto snapshot = gp_faco::make_action_snapshot(problem, record(active), archive, state, pheromone,
+            {minimum, maximum}, distance, elapsed, solve_key, batch, experiment_mask);
+        std::memcpy(features, snapshot.features.data(), sizeof(float) * 12 * 32);
+        for (Node mode = 0; mode < 2; ++mode)
+            for (Node region = 0; region < 4; ++region)
+                std::memcpy(regions + (mode * 4 + region) * 16, snapshot.regions.nodes[mode][region], 16 * sizeof(Node));
+        *alternative = snapshot.alternative_slot;
+        *legal = snapshot.legal_mask;
+        std::memcpy(trails_out, pheromone.stored().data(), sizeof(double) * n * k);
+        *default_out = pheromone.default_value();
         return 0;
     } catch (const std::exception&) {
         return -1;
