@@ -65,7 +65,15 @@ class Outputs(C.Structure):
                 ("construction_steps", C.c_uint64), ("ls_evaluations", C.c_uint64),
                 ("reversed_elements", C.c_uint64), ("kernel_milliseconds", C.c_double),
                 ("solve_seconds", C.c_double), ("colony_work", C.c_void_p),
-                ("control_states", C.c_void_p)]
+                ("control_states", C.c_void_p), ("decision_iterations", C.c_void_p),
+                ("n_decisions", C.c_uint32), ("decision_features", C.c_void_p), ("decision_scores", C.c_void_p),
+                ("decision_masks", C.c_void_p), ("decision_actions", C.c_void_p)]
+
+
+# faco_control_state
+CONTROL_STATE_DTYPE = np.dtype([("restarts", "<u8"), ("stagnant_batches", "<u8"), ("epoch_batches", "<u8"),
+                                ("return_rate", "<f4"), ("ls_work", "<f4"), ("archive_size", "<u4"),
+                                ("start_region", "<u4"), ("mne_target", "<u4"), ("reserved", "<u4")])
 
 
 class Program(C.Structure):

@@ -100,6 +100,11 @@ struct InstanceView {
     const node_t* region_list;     // nodes grouped by quadrant of the bounding box
     std::uint32_t region_offsets[5];
     float mean_nn;                 // mean nearest-neighbour distance (prior features)
+    // 12-feature controller (feature spec 2)
+    const node_t* samples;         // min(n, 64) sample nodes drawn from the instance key
+    std::uint32_t sample_count;
+    const double* local_scale;     // [n] mean of the min(8, n-1) nearest lengths
+    double scale_epsilon;          // 1e-12 * max(coordinate span, 1)
 };
 
 // GP program (postfix IR; device mirror of faco_program).
@@ -135,9 +140,11 @@ struct ColonyState {
     std::int32_t action;
     unsigned long long construction_steps, ls_evaluations, reversed_elements;
     // controller state (GP-controlled evaluations)
-    std::uint32_t region;          // start region of the next iteration (4 = all nodes)
+    std::uint32_t region;          // start region of the next iteration (4 = all nodes, 5 = the controller's start list)
     std::uint32_t restarts, last_improvement, last_restart;
 };
+
+struct RefControl;
 
 // Per-colony constant view.
 struct ColonyView {
@@ -159,6 +166,11 @@ struct ColonyView {
     const Program* program;        // GP controller of this colony: 3 tree slots (null: plain FACO)
     std::uint32_t action_mask;     // legal actions
     std::uint32_t controller_kind; // 0 joint_single (slot 0), 1 conditional_three (slots 0-2 = roles)
+    // 12-feature controller (feature spec 2; null otherwise)
+    RefControl* control;
+    node_t* archive;               // [2 sides][4 slots][tour, positions][n_pad]
+    unsigned long long* ant_ids;   // [ants][2] fingerprints of the batch's tours
+    std::uint32_t* ant_p0;         // [ants] position of node 0 in each tour
 };
 
 struct TraceRow {

@@ -167,15 +167,60 @@ struct Instance {
     DeviceBuffer<faco::node_t> d_regions;
     std::uint32_t region_offsets[5] = {0, 0, 0, 0, 0};
     float mean_nn = 1.0f;
+    // 12-feature controller data (prepared_problem.cpp:66-86, control_ops.hpp:103-107)
+    DeviceBuffer<faco::node_t> d_samples;
+    DeviceBuffer<double> d_local_scale;
+    std::uint32_t sample_count = 0;
+    double scale_epsilon = 0.0;
     faco::InstanceView view() const {
         faco::InstanceView v{n, k, b, w, d_xy.get(), d_primary.get(), d_backup.get(), d_ls.get(), d_ls_dist.get(),
                              d_eta.get(), d_initial.get(), static_cast<long long>(initial_cost), d_regions.get(),
                              {0, 0, 0, 0, 0}};
         for (int r = 0; r < 5; ++r) v.region_offsets[r] = region_offsets[r];
         v.mean_nn = mean_nn;
+        v.samples = d_samples.get();
+        v.sample_count = sample_count;
+        v.local_scale = d_local_scale.get();
+        v.scale_epsilon = scale_epsilon;
         return v;
     }
 };
+
+// Sample nodes and per-node scale of the 12-feature controller: the scale of
+// a node is the mean of its min(8, n-1) nearest EUC_2D lengths, each divided
+// by that count and summed nearest first (prepared_problem.cpp:66-86);
+// epsilon = 1e-12 * max(x span, y span, 1).  The LS rows hold the nearest
+// lengths in order when they are at least that wide.
+void upload_control_data(Instance& in, const std::vector<std::int32_t>& ls_dist, cudaStream_t s) {
+    const std::uint32_t n = in.n, width = std::min<std::uint32_t>(8, n - 1);
+    std::vector<double> scale(n, 0.0);
+    std::vector<std::int32_t> row;
+    for (std::uint32_t a = 0; a < n; ++a) {
+        const std::int32_t* nearest = ls_dist.data() + static_cast<std::size_t>(a) * in.w;
+        if (in.w < width) {
+            row.clear();
+            for (std::uint32_t b = 0; b < n; ++b)
+                if (b != a)
+                    row.push_back(faco::host_euc2d(in.xy[2 * a], in.xy[2 * a + 1], in.xy[2 * b], in.xy[2 * b + 1]));
+            std::partial_sort(row.begin(), row.begin() + width, row.end());
+            nearest = row.data();
+        }
+        double sum = 0.0;
+        for (std::uint32_t j = 0; j < width; ++j) sum += static_cast<double>(nearest[j]) / width;
+        scale[a] = sum;
+    }
+    std::int64_t minx = in.xy[0], maxx = minx, miny = in.xy[1], maxy = miny;
+    for (std::uint32_t i = 0; i < n; ++i) {
+        minx = std::min<std::int64_t>(minx, in.xy[2 * i]); maxx = std::max<std::int64_t>(maxx, in.xy[2 * i]);
+        miny = std::min<std::int64_t>(miny, in.xy[2 * i + 1]); maxy = std::max<std::int64_t>(maxy, in.xy[2 * i + 1]);
+    }
+    in.scale_epsilon = 1e-12 * std::max({static_cast<double>(maxx - minx), static_cast<double>(maxy - miny), 1.0});
+    in.sample_count = std::min<std::uint32_t>(n, faco::kSamples);
+    std::vector<faco::node_t> samples(in.sample_count);
+    faco::sample_nodes(n, in.key, samples.data());
+    in.d_samples.upload(samples, s);
+    in.d_local_scale.upload(scale, s);
+}
 
 // Packed parent neighbours: successor | predecessor << 16, indexed by node.
 std::vector<std::uint32_t> parent_neighbours(const std::uint32_t* tour, std::uint32_t n) {
@@ -214,6 +259,13 @@ struct faco_engine {
     DeviceBuffer<uint2> work;
     DeviceBuffer<faco::TraceRow> trace;
     DeviceBuffer<faco::node_t> checkpoints;
+    // 12-feature controller (feature spec 2)
+    DeviceBuffer<faco::RefControl> ref_controls;
+    DeviceBuffer<faco::node_t> archives;          // per colony [2][4][2][n_pad]
+    DeviceBuffer<unsigned long long> ant_ids;     // per ant [2]
+    DeviceBuffer<std::uint32_t> ant_p0, decision_points, decision_masks;
+    DeviceBuffer<float> decision_features, decision_scores;
+    DeviceBuffer<std::int32_t> decision_actions;
     // learned edge prior
     DeviceBuffer<faco::MlpParams> prior_params;
     DeviceBuffer<faco::MlpOperands> prior_ops;
@@ -241,6 +293,8 @@ struct faco_engine {
         std::vector<faco_program> programs;     // host copy of the controller slots (snapshots)
         std::vector<std::uint32_t> kinds;
         std::uint32_t action_mask = 0xFFFFFFFFu;
+        std::uint32_t feature_spec = 0;         // 2 or 3 for controlled evaluations
+        std::vector<std::uint32_t> decision_points;
         std::vector<AntClass> classes;
         faco::ColonyParams P{};
         faco::AntLaunch L{};
@@ -419,6 +473,7 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         double nn_sum = 0.0;
         for (std::uint32_t a = 0; a < n; ++a) nn_sum += ls_dist[static_cast<std::size_t>(a) * inst->w];
         inst->mean_nn = static_cast<float>(std::max(1.0, nn_sum / n));
+        upload_control_data(*inst, ls_dist, s);
         // initial checklist 2-opt over the NN tour on the GPU (prepared_problem.cpp:159-162)
         std::vector<faco::node_t> tour16(nn.begin(), nn.end());
         const long long nn_cost = faco::host_tour_length(inst->xy, nn.data(), n);
@@ -672,6 +727,8 @@ struct Control {
     std::uint32_t n_programs = 0;
     std::uint32_t action_mask = 0xFFFFFFFFu;
     std::uint32_t total_iterations = 1;
+    const std::uint32_t* decision_points = nullptr;   // feature spec 2: decisions to capture
+    std::uint32_t n_decisions = 0;
 };
 
 // Slots and kinds of plain joint programs (one tree each).
@@ -684,25 +741,33 @@ struct JointSlots {
 };
 
 // Validation of one controller (validate_controller, cpp/src/program_cpu.cpp:11-24,
-// with this engine's feature spec 3): every used tree valid and of spec 3,
-// at most 63 nodes over the roles, and a role reads no descriptor of a
-// decision taken after it (role 0 neither the MNE level (7) nor the start
-// region (8); role 1 not the MNE level).
-void validate_controller(const faco_program* slots, std::uint32_t kind) {
+// python/gp_faco/controller.py:8-33): every used tree valid and of one
+// feature spec (2, the reference's 12 features, or 3, this engine's), at most
+// 63 nodes over the roles, and a role reads no feature of a decision taken
+// after it.  Spec 2 (ROLE_FEATURES): the restart role reads features
+// 0-4, 6, 7, the region role all but 5 (the MNE level); spec 3: role 0
+// neither the MNE level (7) nor the start region (8), role 1 not the MNE level.
+// Returns the feature spec.
+std::uint32_t validate_controller(const faco_program* slots, std::uint32_t kind) {
     require(kind <= 1, "unknown controller kind");
     std::uint32_t total = 0;
+    const std::uint32_t spec = slots[0].feature_spec_id;
+    require(spec == 2 || spec == 3, "controllers use feature spec 2 or 3");
     for (std::uint32_t role = 0; role < (kind ? 3u : 1u); ++role) {
         const faco_program& p = slots[role];
         if (faco_validate_program(&p) != FACO_OK) throw Error(FACO_EINVAL, g_error);
-        require(p.feature_spec_id == 3, "controllers use feature spec 3");
+        require(p.feature_spec_id == spec, "the trees of a controller use one feature spec");
         total += p.length;
         for (std::uint32_t i = 0; kind && i < p.length; ++i) {
             const std::uint32_t f = p.operand[i];
-            require(!(p.opcode[i] == 0 && ((role == 0 && (f == 7 || f == 8)) || (role == 1 && f == 7))),
-                    "a role tree reads the descriptor of a later decision");
+            if (p.opcode[i] != 0) continue;
+            const bool later = spec == 2 ? (role == 0 && (f == 5 || f >= 8)) || (role == 1 && f == 5)
+                                         : (role == 0 && (f == 7 || f == 8)) || (role == 1 && f == 7);
+            require(!later, "a role tree reads the features of a later decision");
         }
     }
     require(total <= 63, "a controller has more than 63 nodes");
+    return spec;
 }
 
 void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, uint32_t count,
@@ -749,18 +814,43 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     e->ant_tours.resize(ant_total);
     e->ant_costs.resize(static_cast<std::size_t>(A) * count);
     e->ant_ccosts.resize(static_cast<std::size_t>(A) * count);
-    std::uint32_t replicas = 1;
+    std::uint32_t replicas = 1, spec = 0;
     if (control.programs) {
         require(control.n_programs >= 1 && count % control.n_programs == 0,
                 "colonies must be a whole number of replicas per program");
         require(control.action_mask != 0, "the action mask leaves no legal action");
         require(control.kinds != nullptr, "controller kinds missing");
-        for (std::uint32_t i = 0; i < control.n_programs; ++i)
-            validate_controller(control.programs + 3ull * i, control.kinds[i]);
+        for (std::uint32_t i = 0; i < control.n_programs; ++i) {
+            const std::uint32_t si = validate_controller(control.programs + 3ull * i, control.kinds[i]);
+            require(spec == 0 || si == spec, "the controllers of one evaluation use one feature spec");
+            spec = si;
+        }
+        if (spec == 2) {
+            // the first batch has no alternative reference (batch_engine.cu:599-600)
+            require((control.action_mask & 0xFFFFu) != 0, "the action mask keeps no action of mode 0");
+            require(A <= faco::kCtlMaxAnts, "the 12-feature controller takes at most 1024 ants per colony");
+        }
         replicas = count / control.n_programs;
         static_assert(sizeof(faco::Program) == sizeof(faco_program), "program layout");
         e->programs.upload(reinterpret_cast<const faco::Program*>(control.programs), 3ull * control.n_programs,
                            e->stream);
+    }
+    require(control.n_decisions == 0 || spec == 2, "decision captures need controllers of feature spec 2");
+    if (spec == 2) {
+        e->ref_controls.resize(count);
+        e->archives.resize(16ull * node_total);
+        e->ant_ids.resize(2ull * A * count);
+        e->ant_p0.resize(static_cast<std::size_t>(A) * count);
+    }
+    v.feature_spec = spec;
+    v.decision_points.assign(control.decision_points, control.decision_points + control.n_decisions);
+    if (control.n_decisions) {
+        e->decision_points.upload(v.decision_points, s);
+        const std::size_t slots = static_cast<std::size_t>(control.n_decisions) * count;
+        e->decision_features.resize(slots * 12 * 32);
+        e->decision_scores.resize(slots * 32);
+        e->decision_masks.resize(slots);
+        e->decision_actions.resize(slots);
     }
     e->ant_counts.resize(3ull * A * count);
     e->states.resize(count);
@@ -786,6 +876,12 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
         cv.action_mask = control.action_mask;
         cv.controller_kind = control.programs ? control.kinds[c / replicas] : 0u;
         cv.ant_counts = e->ant_counts.get() + 3ull * c * A;
+        if (spec == 2) {
+            cv.control = e->ref_controls.get() + c;
+            cv.archive = e->archives.get() + 16ull * node_off;
+            cv.ant_ids = e->ant_ids.get() + 2ull * A * c;
+            cv.ant_p0 = e->ant_p0.get() + static_cast<std::size_t>(A) * c;
+        }
         tau_off += (static_cast<std::size_t>(in.n) * in.k + 3) & ~std::size_t{3};
         node_off += cv.n_pad;
         ant_off += static_cast<std::size_t>(A) * cv.n_pad;
@@ -832,6 +928,13 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.P.controlled = control.programs != nullptr;
     v.P.total_iterations = std::max<std::uint32_t>(1, control.total_iterations);
     v.P.log2k = faco::host_log2(static_cast<float>(k_common));
+    v.P.ref_control = spec == 2;
+    v.P.ls_limit = e->settings.ls_evaluation_limit;
+    if (control.n_decisions) {
+        v.P.capture = faco::DecisionCapture{e->decision_points.get(), control.n_decisions, e->decision_features.get(),
+                                            e->decision_scores.get(), e->decision_masks.get(),
+                                            e->decision_actions.get()};
+    }
     v.P.p_root = std::pow(e->settings.p_best, 1.0 / static_cast<double>(k_common));
     v.L = faco::AntLaunch{};
     v.L.instances = e->d_instances.get();
@@ -842,7 +945,8 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.L.ls_mode = e->settings.ls_mode;
     v.L.error = e->error.get();
     e->reset_error();
-    faco::colony_init_kernel<<<count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(), e->states.get(), v.P);
+    faco::colony_init_kernel<<<count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(), e->states.get(), v.P,
+                                                   count);
     cuda_check(cudaGetLastError(), "init launch");
     while (e->branch_streams.size() + 1 < v.classes.size()) {
         cudaStream_t bs;
@@ -891,6 +995,21 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
     e->global.download(global.data(), v.node_total, s);
     std::vector<faco::ColonyState> states(v.count);
     e->states.download(states.data(), v.count, s);
+    std::vector<faco::RefControl> refs;
+    if (v.feature_spec == 2) {
+        refs.resize(v.count);
+        e->ref_controls.download(refs.data(), v.count, s);
+    }
+    if (!v.decision_points.empty()) {
+        require(out->n_decisions == v.decision_points.size() && out->decision_features && out->decision_scores &&
+                    out->decision_masks && out->decision_actions,
+                "decision outputs missing");
+        const std::size_t slots = v.decision_points.size() * v.count;
+        e->decision_features.download(out->decision_features, slots * 12 * 32, s);
+        e->decision_scores.download(out->decision_scores, slots * 32, s);
+        e->decision_masks.download(out->decision_masks, slots, s);
+        e->decision_actions.download(reinterpret_cast<std::int32_t*>(out->decision_actions), slots, s);
+    }
     if (out->trace && v.trace_cap) {
         static_assert(sizeof(faco::TraceRow) == sizeof(faco_trace_row), "trace row layout");
         e->trace.download(reinterpret_cast<faco::TraceRow*>(out->trace),
@@ -952,11 +1071,23 @@ void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimensio
             out->colony_work[3 * c + 2] = states[c].reversed_elements;
         }
         if (out->control_states) {
-            std::uint32_t* row = out->control_states + 4 * std::size_t(c);
-            row[0] = states[c].restarts;
-            row[1] = states[c].iteration - states[c].last_improvement;
-            row[2] = states[c].region;
-            row[3] = states[c].mne_target;
+            faco_control_state& row = out->control_states[c];
+            row = faco_control_state{};
+            if (v.feature_spec == 2) {
+                const faco::RefControl& r = refs[c];
+                row.restarts = r.restarts;
+                row.stagnant_batches = r.stagnant_batches;
+                row.epoch_batches = r.epoch_batches;
+                row.return_rate = r.return_rate;
+                row.ls_work = r.ls_work;
+                row.archive_size = r.archive_size;
+            } else {
+                row.restarts = states[c].restarts;
+                row.stagnant_batches = states[c].iteration - states[c].last_improvement;
+                row.epoch_batches = states[c].iteration - states[c].last_restart;
+            }
+            row.start_region = states[c].region;
+            row.mne_target = states[c].mne_target;
         }
         steps += states[c].construction_steps;
         evals += states[c].ls_evaluations;
@@ -987,14 +1118,14 @@ namespace {
 // kept.  The Philox streams are keyed by the iteration counter kept in the
 // colony states, so a restored evaluation continues bit for bit.
 constexpr char kSnapshotMagic[8] = {'F', 'A', 'C', 'O', 'S', 'N', 'P', '1'};
-constexpr std::uint32_t kSnapshotVersion = 1;
+constexpr std::uint32_t kSnapshotVersion = 2;
 static_assert(sizeof(faco::ColonyState) == 104, "snapshot layout (the Python reader's ColonyState size)");
 
 struct SnapshotHeader {
     char magic[8];
     std::uint32_t version, count, ants, k_common;
     std::uint32_t mne_target, n_programs, action_mask, total_iterations;
-    std::uint32_t controlled, done, reserved0, reserved1;
+    std::uint32_t controlled, done, feature_spec, reserved1;
     std::uint64_t settings_digest, tau_total, node_total;
 };
 
@@ -1079,6 +1210,7 @@ int faco_snapshot(faco_engine* e, void* buffer, uint64_t capacity, uint64_t* byt
         h.total_iterations = v.P.total_iterations;
         h.controlled = v.P.controlled;
         h.done = v.done;
+        h.feature_spec = v.feature_spec;
         h.settings_digest = settings_digest(e->settings, e->ants);
         h.tau_total = v.tau_total;
         h.node_total = v.node_total;
@@ -1101,6 +1233,12 @@ int faco_snapshot(faco_engine* e, void* buffer, uint64_t capacity, uint64_t* byt
             const auto nbr = fetch(e->parent_nbr, v.node_total, s);
             const auto epoch = fetch(e->epoch, v.node_total, s);
             const auto global = fetch(e->global, v.node_total, s);
+            std::vector<faco::RefControl> refs;
+            std::vector<faco::node_t> archives;
+            if (v.feature_spec == 2) {
+                refs = fetch(e->ref_controls, v.count, s);
+                archives = fetch(e->archives, 16 * v.node_total, s);
+            }
             cuda_check(cudaStreamSynchronize(s), "snapshot download");
             w.put(states.data(), states.size() * sizeof(faco::ColonyState));
             w.put(trails.data(), trails.size() * sizeof(float));
@@ -1110,9 +1248,13 @@ int faco_snapshot(faco_engine* e, void* buffer, uint64_t capacity, uint64_t* byt
             w.put(nbr.data(), nbr.size() * sizeof(std::uint32_t));
             w.put(epoch.data(), epoch.size() * sizeof(faco::node_t));
             w.put(global.data(), global.size() * sizeof(faco::node_t));
+            w.put(refs.data(), refs.size() * sizeof(faco::RefControl));
+            w.put(archives.data(), archives.size() * sizeof(faco::node_t));
         } else {
             w.used += v.count * sizeof(faco::ColonyState) + 3 * v.tau_total * sizeof(float) +
                       v.node_total * (3 * sizeof(faco::node_t) + sizeof(std::uint32_t));
+            if (v.feature_spec == 2)
+                w.used += v.count * sizeof(faco::RefControl) + 16 * v.node_total * sizeof(faco::node_t);
         }
         const std::uint64_t total = w.used + sizeof(std::uint64_t);
         *bytes = total;
@@ -1169,6 +1311,10 @@ int faco_restore(faco_engine* e, const void* buffer, uint64_t bytes, uint32_t tr
         const unsigned char* nbr = take(h.node_total * sizeof(std::uint32_t));
         const unsigned char* epoch = take(h.node_total * sizeof(faco::node_t));
         const unsigned char* global = take(h.node_total * sizeof(faco::node_t));
+        require(h.feature_spec == 0 || h.feature_spec == 2 || h.feature_spec == 3, "snapshot feature spec unknown");
+        const bool ref = h.feature_spec == 2;
+        const unsigned char* refs = ref ? take(h.count * sizeof(faco::RefControl)) : nullptr;
+        const unsigned char* archives = ref ? take(16 * h.node_total * sizeof(faco::node_t)) : nullptr;
         require(off + sizeof sum == bytes, "snapshot has trailing bytes");
         Control control;
         if (h.n_programs) {
@@ -1196,6 +1342,11 @@ int faco_restore(faco_engine* e, const void* buffer, uint64_t bytes, uint32_t tr
             put(e->parent_nbr.get(), nbr, h.node_total * sizeof(std::uint32_t));
             put(e->epoch.get(), epoch, h.node_total * sizeof(faco::node_t));
             put(e->global.get(), global, h.node_total * sizeof(faco::node_t));
+            require(v.feature_spec == h.feature_spec, "snapshot controller spec differs");
+            if (ref) {
+                put(e->ref_controls.get(), refs, h.count * sizeof(faco::RefControl));
+                put(e->archives.get(), archives, 16 * h.node_total * sizeof(faco::node_t));
+            }
             cuda_check(cudaStreamSynchronize(s), "snapshot upload");
             v.done = h.done;
         } catch (...) {
@@ -1293,7 +1444,15 @@ int evaluate_impl(faco_engine* e, const uint64_t* keys, const uint64_t* seeds, u
                     "checkpoints must be strictly increasing");
         }
         require(n_checkpoints == 0 || out->checkpoint_tours, "checkpoint output missing");
+        for (std::uint32_t i = 0; i < out->n_decisions; ++i) {
+            require(out->decision_iterations, "decision iterations missing");
+            const std::uint32_t p = out->decision_iterations[i];
+            require(p >= 1 && p <= T && (i == 0 || p > out->decision_iterations[i - 1]),
+                    "decision iterations must be strictly increasing batch numbers within the budget");
+        }
         control.total_iterations = T;
+        control.decision_points = out->decision_iterations;
+        control.n_decisions = out->n_decisions;
         begin_evaluation(e, keys, seeds, count, mne_target, out->trace ? T : 0, control);
         auto& v = e->eval;
         try {

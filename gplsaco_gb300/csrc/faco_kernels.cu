@@ -135,7 +135,9 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
     } else {
         // ---------------- focused construction ----------------
         std::uint32_t current;
-        if (kEngine) current = region_start(key, batch, ant, in_ptr, region);
+        if (kEngine) current = region == 5 ? list_start(key, batch, ant, cv.control->start_nodes,
+                                                        cv.control->start_count)
+                                           : region_start(key, batch, ant, in_ptr, region);
         else if (MODE == kModeVisits) current = L.task_visits[(size_t)task * n];
         else current = L.task_starts[task];
         if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n] = (node_t)current;
@@ -392,39 +394,6 @@ __device__ __forceinline__ void trail_limits(long long cost, double retention, d
     tmin = (float)mn;
 }
 
-__global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
-                                   ColonyParams P) {
-    const std::uint32_t c = blockIdx.x;
-    const ColonyView cv = colonies[c];
-    const InstanceView in = instances[cv.instance];
-    const std::uint32_t n = in.n, k = in.k;
-    __shared__ float s_tmax;
-    if (threadIdx.x == 0) {
-        ColonyState st{};
-        st.epoch_cost = st.global_cost = st.parent_cost = st.iteration_best_cost = in.initial_cost;
-        trail_limits(in.initial_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
-        st.default_trail = st.tau_max;
-        st.mne_target = P.mne_target;
-        st.action = -1;
-        st.region = 4;
-        states[c] = st;
-        s_tmax = st.tau_max;
-    }
-    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const node_t v = in.initial[i];
-        cv.parent[i] = cv.epoch[i] = cv.global[i] = v;
-        cv.parent_nbr[v] = (std::uint32_t)in.initial[i + 1 == n ? 0 : i + 1] |
-                           ((std::uint32_t)in.initial[i == 0 ? n - 1 : i - 1] << 16);
-    }
-    __syncthreads();
-    const float tmax = s_tmax;
-    for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
-        cv.trails[i] = tmax;
-        cv.eta[i] = in.eta[i];
-        cv.products[i] = tmax * in.eta[i];
-    }
-}
-
 // MMAS evaporate/deposit on FP32 trails (cuda/colony_state.cuh:210-229):
 // tau <- max(tau_min, tau * retention); a directed candidate entry (from, to)
 // on the parent tour also gains min(tau_max, tau + 1/parent_cost); products
@@ -571,6 +540,530 @@ __device__ __forceinline__ std::uint32_t choose_conditional(const Program* trees
 
 __device__ __forceinline__ float clamp01(double v) { return (float)(v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v); }
 
+// ---------------------------------------------------------------------------
+// The reference's 12-feature controller (feature spec 2): per batch, after
+// the trail update, the ants' fingerprints, the archive of distinct
+// near-best tours and the feedback (update_control, control_state.cuh:
+// 124-245), then the decision for the next batch -- alternative reference,
+// 8 start regions, 12 x 32 features, scoring, and the action (MNE target,
+// start list, restart from the alternative; build_control_features and
+// apply_control_action, :247-364).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double unit_clip(double v) { return v < 0.0 ? 0.0 : v > 1.0 ? 1.0 : v; }
+
+// A tour in device memory: its order, its positions (may be null) and the
+// position of node 0.
+struct TourRef {
+    const node_t* tour;
+    const node_t* pos;
+    std::uint32_t p0;
+};
+
+__device__ __forceinline__ node_t* archive_tour(const ColonyView& cv, std::uint32_t side, std::uint32_t slot) {
+    return cv.archive + (size_t)((side * kArchive + slot) * 2u) * cv.n_pad;
+}
+__device__ __forceinline__ TourRef archive_ref(const ColonyView& cv, std::uint32_t side, std::uint32_t slot) {
+    const node_t* t = archive_tour(cv, side, slot);
+    return {t, t + cv.n_pad, t[cv.n_pad]};
+}
+
+// canonical_compare (control_ops.hpp:61-74) by one warp: both tours read
+// from node 0 towards its smaller neighbour; -1, 0 or 1.
+__device__ int warp_canonical_compare(TourRef a, TourRef b, std::uint32_t n, std::uint32_t lane) {
+    const bool fa = a.tour[a.p0 + 1 == n ? 0 : a.p0 + 1] < a.tour[a.p0 == 0 ? n - 1 : a.p0 - 1];
+    const bool fb = b.tour[b.p0 + 1 == n ? 0 : b.p0 + 1] < b.tour[b.p0 == 0 ? n - 1 : b.p0 - 1];
+    for (std::uint32_t base = 1; base < n; base += 32) {
+        const std::uint32_t i = base + lane;
+        std::uint32_t va = 0, vb = 0;
+        if (i < n) {
+            va = a.tour[fa ? (a.p0 + i) % n : (a.p0 + n - i) % n];
+            vb = b.tour[fb ? (b.p0 + i) % n : (b.p0 + n - i) % n];
+        }
+        const unsigned m = __ballot_sync(kFull, va != vb);
+        if (m) return __shfl_sync(kFull, va < vb ? -1 : 1, __ffs(m) - 1);
+    }
+    return 0;
+}
+
+__device__ std::uint32_t warp_find_zero(const node_t* tour, std::uint32_t n, std::uint32_t lane) {
+    for (std::uint32_t base = 0; base < n; base += 32) {
+        const unsigned m = __ballot_sync(kFull, base + lane < n && tour[base + lane] == 0);
+        if (m) return base + __ffs(m) - 1;
+    }
+    return 0;
+}
+
+// XOR of the n edge fingerprints (fingerprint_ants, control_state.cuh:45-64)
+// and the position of node 0, by one warp.
+__device__ Fingerprint warp_fingerprint(const node_t* tour, std::uint32_t n, std::uint32_t lane, std::uint32_t& p0) {
+    unsigned long long f1 = 0, f2 = 0;
+    std::uint32_t z = 0xffffffffu;
+    for (std::uint32_t i = lane; i < n; i += 32) {
+        const std::uint32_t a = tour[i];
+        const Fingerprint e = fingerprint_edge(a, tour[i + 1 == n ? 0 : i + 1]);
+        f1 ^= e.first;
+        f2 ^= e.second;
+        if (a == 0) z = i;
+    }
+    for (int o = 16; o; o >>= 1) {
+        f1 ^= __shfl_xor_sync(kFull, f1, o);
+        f2 ^= __shfl_xor_sync(kFull, f2, o);
+        z = min(z, __shfl_xor_sync(kFull, z, o));
+    }
+    p0 = z;
+    return {f1, f2};
+}
+
+struct CandidateView {
+    const ColonyView& cv;
+    const RefControl& ctl;
+    __device__ long long cost(std::uint32_t c) const {
+        return c < kArchive ? ctl.archive_cost[c] : cv.ant_costs[c - kArchive];
+    }
+    __device__ Fingerprint id(std::uint32_t c) const {
+        if (c < kArchive) return ctl.archive_id[c];
+        const unsigned long long* p = cv.ant_ids + 2ull * (c - kArchive);
+        return {p[0], p[1]};
+    }
+    __device__ TourRef ref(std::uint32_t c) const {
+        if (c < kArchive) return archive_ref(cv, ctl.side, c);
+        return {cv.ant_tours + (size_t)(c - kArchive) * cv.n_pad, nullptr, cv.ant_p0[c - kArchive]};
+    }
+};
+
+constexpr std::uint32_t kCtlWords = (kArchive + kCtlMaxAnts + 31) / 32;
+
+// Archive selection by warp 0 (update_control's slot loop): the global best
+// first, then up to 3 distinct tours of the old archive and the batch within
+// 2 % of the global cost, each the least by (cost, fingerprint, canonical
+// order, candidate index).  Candidates 0-3 are archive slots, 4 + a ant a.
+__device__ std::uint32_t ref_archive_select(const CandidateView& v, const ColonyState& st, std::uint32_t A,
+                                            bool improved, std::uint32_t n, std::uint32_t lane,
+                                            std::uint32_t* excluded, std::uint32_t* chosen) {
+    const std::uint32_t total = kArchive + A;
+    for (std::uint32_t w = lane; w < (total + 31) / 32; w += 32) excluded[w] = 0;
+    __syncwarp();
+    const double limit = (double)st.global_cost * (1 + kArchiveBand);
+    auto is_excluded = [&](std::uint32_t c) { return (excluded[c >> 5] >> (c & 31u)) & 1u; };
+    auto eligible = [&](std::uint32_t c) {
+        if (c < kArchive && c >= v.ctl.archive_size) return false;
+        return (double)v.cost(c) <= limit && !is_excluded(c);
+    };
+    std::uint32_t count = 0;
+    auto add = [&](std::uint32_t w) {
+        if (lane == 0) {
+            chosen[count] = w;
+            excluded[w >> 5] |= 1u << (w & 31u);
+        }
+        ++count;
+        __syncwarp();
+        const Fingerprint idw = v.id(w);
+        const TourRef rw = v.ref(w);
+        for (std::uint32_t base = 0; base < total; base += 32) {
+            const std::uint32_t c = base + lane;
+            unsigned m = __ballot_sync(kFull, c < total && !is_excluded(c) && fp_equal(v.id(c), idw));
+            while (m) {
+                const std::uint32_t j = base + __ffs(m) - 1;
+                m &= m - 1;
+                if (warp_canonical_compare(v.ref(j), rw, n, lane) == 0 && lane == 0)
+                    excluded[j >> 5] |= 1u << (j & 31u);
+                __syncwarp();
+            }
+        }
+        __syncwarp();
+    };
+    add(improved ? kArchive + st.iteration_best : 0u);
+    for (std::uint32_t slot = 1; slot < kArchive; ++slot) {
+        std::uint32_t best = 0xffffffffu;
+        long long bc = 0;
+        Fingerprint bi{0, 0};
+        for (std::uint32_t c = lane; c < total; c += 32) {
+            if (!eligible(c)) continue;
+            const long long cc = v.cost(c);
+            const Fingerprint ci = v.id(c);
+            if (best == 0xffffffffu || cc < bc || (cc == bc && fp_less(ci, bi))) { best = c; bc = cc; bi = ci; }
+        }
+        for (int o = 16; o; o >>= 1) {
+            const std::uint32_t ob = __shfl_xor_sync(kFull, best, o);
+            const long long oc = __shfl_xor_sync(kFull, bc, o);
+            const Fingerprint oi{__shfl_xor_sync(kFull, bi.first, o), __shfl_xor_sync(kFull, bi.second, o)};
+            const bool take = ob != 0xffffffffu &&
+                              (best == 0xffffffffu || oc < bc ||
+                               (oc == bc && (fp_less(oi, bi) || (fp_equal(oi, bi) && ob < best))));
+            if (take) { best = ob; bc = oc; bi = oi; }
+        }
+        if (best == 0xffffffffu) break;
+        // equal cost and fingerprint with another tour: canonical order decides
+        for (std::uint32_t base = 0; base < total; base += 32) {
+            const std::uint32_t c = base + lane;
+            unsigned m = __ballot_sync(kFull, c < total && c != best && eligible(c) && v.cost(c) == bc &&
+                                                  fp_equal(v.id(c), bi));
+            while (m) {
+                const std::uint32_t j = base + __ffs(m) - 1;
+                m &= m - 1;
+                if (warp_canonical_compare(v.ref(j), v.ref(best), n, lane) < 0) best = j;
+            }
+        }
+        add(best);
+    }
+    return count;
+}
+
+struct RefShared {
+    float feat[12][32];
+    float scores[32];
+    node_t regions[8][kRegionNodes];
+    std::uint32_t excluded[kCtlWords];
+    std::uint32_t chosen[kArchive];
+    long long chosen_cost[kArchive];
+    Fingerprint chosen_id[kArchive];
+    std::uint32_t count, alternative, mask, action, largest;
+    float gap[2], difference;
+};
+
+// update_control for one colony (after reduce/select and the trail update).
+__device__ void ref_update(const ColonyView& cv, const InstanceView& in, const ColonyState& st,
+                           const ColonyParams& P, RefShared& sh) {
+    RefControl& ctl = *cv.control;
+    const std::uint32_t n = in.n, A = P.ants;
+    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (std::uint32_t a = warp; a < A; a += warps) {
+        std::uint32_t p0;
+        const Fingerprint f = warp_fingerprint(cv.ant_tours + (size_t)a * cv.n_pad, n, lane, p0);
+        if (lane == 0) {
+            cv.ant_ids[2 * a] = f.first;
+            cv.ant_ids[2 * a + 1] = f.second;
+            cv.ant_p0[a] = p0;
+        }
+    }
+    __syncthreads();
+    const bool improved = st.global_cost < ctl.tracked_global;
+    if (warp == 0) {
+        const CandidateView v{cv, ctl};
+        const std::uint32_t count = ref_archive_select(v, st, A, improved, n, lane, sh.excluded, sh.chosen);
+        if (lane == 0) {
+            sh.count = count;
+            for (std::uint32_t i = 0; i < count; ++i) {
+                sh.chosen_cost[i] = v.cost(sh.chosen[i]);
+                sh.chosen_id[i] = v.id(sh.chosen[i]);
+            }
+            // feedback (update_feedback, control_ops.hpp:177-188)
+            double returned = 0, work = 0;
+            for (std::uint32_t a = 0; a < A; ++a) {
+                returned += (cv.ant_ids[2 * a] == ctl.active_id.first && cv.ant_ids[2 * a + 1] == ctl.active_id.second)
+                                ? 1.0 : 0.0;
+                if (P.ls_limit) work += (double)cv.ant_counts[3 * a + 1] / (double)P.ls_limit;
+            }
+            const float rf = (float)unit_clip(returned / (double)A), wf = (float)unit_clip(work / (double)A);
+            ctl.return_rate += (rf - ctl.return_rate) * 0.0625f;
+            ctl.ls_work += (wf - ctl.ls_work) * 0.0625f;
+            if (improved) ctl.stagnant_batches = 0;
+            else if (ctl.stagnant_batches != ~0ull) ++ctl.stagnant_batches;
+            if (ctl.epoch_batches != ~0ull) ++ctl.epoch_batches;
+            const unsigned long long* best = cv.ant_ids + 2ull * st.iteration_best;
+            if (st.epoch_cost < ctl.tracked_epoch) ctl.epoch_id = {best[0], best[1]};
+            ctl.active_id = st.source_is_epoch ? ctl.epoch_id : Fingerprint{best[0], best[1]};
+            ctl.tracked_global = st.global_cost;
+            ctl.tracked_epoch = st.epoch_cost;
+        }
+    }
+    __syncthreads();
+    // chosen tours into the other half of the archive buffer
+    const std::uint32_t side = ctl.side, next = side ^ 1u, count = sh.count;
+    const CandidateView v{cv, ctl};
+    for (std::uint32_t i = threadIdx.x; i < count * n; i += blockDim.x) {
+        const std::uint32_t slot = i / n, p = i % n;
+        const node_t node = v.ref(sh.chosen[slot]).tour[p];
+        node_t* dst = archive_tour(cv, next, slot);
+        dst[p] = node;
+        dst[cv.n_pad + node] = (node_t)p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (std::uint32_t i = 0; i < kArchive; ++i) {
+            ctl.archive_cost[i] = i < count ? sh.chosen_cost[i] : 0;
+            ctl.archive_id[i] = i < count ? sh.chosen_id[i] : Fingerprint{0, 0};
+        }
+        ctl.archive_size = count;
+        ctl.side = next;
+    }
+    __syncthreads();
+}
+
+// The decision before batch `batch` (build_control_features, score and
+// apply_control_action).  Called by the whole block; st is shared.
+__device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyState& st, const ColonyParams& P,
+                           std::uint32_t colony, std::uint32_t colony_count, std::uint32_t batch, RefShared& sh) {
+    RefControl& ctl = *cv.control;
+    const std::uint32_t n = in.n, k = in.k;
+    const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    const std::uint32_t side = ctl.side, size = ctl.archive_size;
+    if (warp == 0) {
+        // alternative reference: the archive tour other than the active one
+        // that differs most from it on the sampled nodes (control_cpu.cpp:46-63)
+        const TourRef parent{cv.parent, nullptr, warp_find_zero(cv.parent, n, lane)};
+        std::uint32_t alt = kArchive, largest = 0;
+        for (std::uint32_t i = 0; i < size; ++i) {
+            const TourRef ri = archive_ref(cv, side, i);
+            if (fp_equal(ctl.archive_id[i], ctl.active_id) && warp_canonical_compare(ri, parent, n, lane) == 0)
+                continue;
+            std::uint32_t missing = 0;
+            for (std::uint32_t j = lane; j < in.sample_count; j += 32) {
+                const std::uint32_t x = in.samples[j], px = ri.pos[x];
+                const std::uint32_t cs = ri.tour[px + 1 == n ? 0 : px + 1], cp = ri.tour[px == 0 ? n - 1 : px - 1];
+                const std::uint32_t nb = cv.parent_nbr[x], ps = nb & 0xffffu, pp = nb >> 16;
+                missing += (cs != ps && cs != pp) + (cp != ps && cp != pp);
+            }
+            for (int o = 16; o; o >>= 1) missing += __shfl_xor_sync(kFull, missing, o);
+            bool better_tie = false;
+            if (alt != kArchive && missing == largest) {
+                const long long ci = ctl.archive_cost[i], ca = ctl.archive_cost[alt];
+                const Fingerprint fi = ctl.archive_id[i], fa = ctl.archive_id[alt];
+                better_tie = ci < ca || (ci == ca && (fp_less(fi, fa) ||
+                                                      (fp_equal(fi, fa) &&
+                                                       warp_canonical_compare(ri, archive_ref(cv, side, alt), n,
+                                                                              lane) < 0)));
+            }
+            if (alt == kArchive || missing > largest || better_tie) { alt = i; largest = missing; }
+        }
+        if (lane == 0) {
+            sh.alternative = alt;
+            sh.largest = largest;
+            sh.gap[0] = (float)unit_clip(((double)st.parent_cost / (double)st.global_cost - 1) / kArchiveBand);
+            sh.gap[1] = alt < kArchive ? (float)unit_clip(((double)ctl.archive_cost[alt] / (double)st.global_cost - 1) /
+                                                          kArchiveBand)
+                                       : 0.0f;
+            sh.difference = alt < kArchive ? (float)largest / (float)(2 * in.sample_count) : 0.0f;
+            sh.mask = cv.action_mask & (alt < kArchive ? 0xFFFFFFFFu : 0xFFFFu);
+        }
+    }
+    __syncthreads();
+    const std::uint32_t alt = sh.alternative, count = n < kRegionNodes ? n : kRegionNodes;
+    const double elapsed = (double)((unsigned long long)batch * P.ants) /
+                           (double)((unsigned long long)P.total_iterations * P.ants);
+    for (std::uint32_t w = warp; w < 8; w += warps) {
+        // start region (mode, region) and its 4 features (region_features,
+        // control_ops.hpp:192-214), contributions per node, summed in node order
+        const std::uint32_t mode = w >> 2, region = w & 3u;
+        const bool valid = mode == 0 || alt < kArchive;
+        node_t* nodes = sh.regions[w];
+        const TourRef ref = mode == 0 ? TourRef{cv.parent, nullptr, 0} : archive_ref(cv, side, alt < kArchive ? alt : 0);
+        if (lane == 0) {
+            for (std::uint32_t i = 0; i < kRegionNodes; ++i) nodes[i] = 0;
+            if (valid) build_region(ref.tour, n, in.primary, k, cv.key, batch, mode, region, nodes);
+        }
+        __syncwarp();
+        float regional[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (valid) {
+            double v0 = 0.0, v2 = 0.0, v3 = 0.0;
+            std::uint32_t v1 = 0, v4 = 0;
+            if (lane < count) {
+                const std::uint32_t x = nodes[lane];
+                std::uint32_t prev, next;
+                if (mode == 0) {
+                    const std::uint32_t nb = cv.parent_nbr[x];
+                    next = nb & 0xffffu;
+                    prev = nb >> 16;
+                } else {
+                    const std::uint32_t px = ref.pos[x];
+                    next = ref.tour[px + 1 == n ? 0 : px + 1];
+                    prev = ref.tour[px == 0 ? n - 1 : px - 1];
+                }
+                const double scale = in.local_scale[x] < in.scale_epsilon ? in.scale_epsilon : in.local_scale[x];
+                v0 = unit_clip(((0.5 * (double)euc2d(in.xy[x], in.xy[prev]) + 0.5 * (double)euc2d(in.xy[x], in.xy[next])) /
+                                    scale - 1) / 3);
+                const std::uint32_t nbs[2] = {prev, next};
+                double strength[2];
+                for (int s = 0; s < 2; ++s) {
+                    for (std::uint32_t j = 0; j < size; ++j) {
+                        const TourRef aj = archive_ref(cv, side, j);
+                        const std::uint32_t pj = aj.pos[x];
+                        const std::uint32_t sj = aj.tour[pj + 1 == n ? 0 : pj + 1], qj = aj.tour[pj == 0 ? n - 1 : pj - 1];
+                        v1 += sj != nbs[s] && qj != nbs[s];
+                    }
+                    double tau = (double)st.default_trail;
+                    for (std::uint32_t j = 0; j < k; ++j)
+                        if (in.primary[(size_t)x * k + j] == nbs[s]) { tau = (double)cv.trails[(size_t)x * k + j]; break; }
+                    const double lo = (double)st.tau_min, hi = (double)st.tau_max;
+                    strength[s] = lo == hi ? 1.0 : unit_clip((tau - lo) / (hi - lo));
+                    v4 += !has_node(nodes, count, nbs[s]);
+                }
+                v2 = strength[0];
+                v3 = strength[1];
+            }
+            double excess = 0, disagreement = 0, strength = 0, dispersion = 0;
+            for (std::uint32_t i = 0; i < count; ++i) {
+                excess += __shfl_sync(kFull, v0, i);
+                disagreement += (double)__shfl_sync(kFull, v1, i);
+                strength += __shfl_sync(kFull, v2, i);
+                strength += __shfl_sync(kFull, v3, i);
+                dispersion += (double)__shfl_sync(kFull, v4, i);
+            }
+            regional[0] = (float)(excess / count);
+            regional[1] = (float)(disagreement / (double)(2 * count * size));
+            regional[2] = (float)(strength / (double)(2 * count));
+            regional[3] = (float)(dispersion / (double)(2 * count));
+        }
+        if (lane < 4) {
+            const std::uint32_t level = lane, a = mode * 16 + region * 4 + level;
+            const unsigned long long stag = ctl.stagnant_batches;
+            sh.feat[0][a] = (float)unit_clip(elapsed);
+            sh.feat[1][a] = (float)(stag < 32 ? (double)stag / 32.0 : 1.0);
+            sh.feat[2][a] = ctl.return_rate;
+            sh.feat[3][a] = ctl.ls_work;
+            sh.feat[4][a] = (float)mode;
+            sh.feat[5][a] = (float)(level + 1) * 0.25f;
+            sh.feat[6][a] = sh.gap[mode];
+            sh.feat[7][a] = mode ? sh.difference : 0.0f;
+            for (int f = 0; f < 4; ++f) sh.feat[8 + f][a] = regional[f];
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const std::uint32_t mask = sh.mask;
+        std::uint32_t a;
+        if (cv.controller_kind == 1) {
+            sh.scores[lane] = 0.0f;
+            __syncwarp();
+            a = choose_conditional(cv.program, [&](int i, std::uint32_t act) { return sh.feat[i][act]; }, mask, lane,
+                                   sh.scores);
+        } else {
+            const float value = eval_program(*cv.program, [&](int i) { return sh.feat[i][lane]; });
+            sh.scores[lane] = value;
+            a = choose_action(value, (mask >> lane) & 1u, lane);
+        }
+        __syncwarp();
+        const std::uint32_t chosen = a < 32 ? a : 0;
+        const DecisionCapture& cap = P.capture;
+        for (std::uint32_t i = 0; i < cap.count; ++i) {
+            if (cap.points[i] != batch + 1) continue;
+            const size_t slot = (size_t)i * colony_count + colony;
+            for (std::uint32_t f = 0; f < 12; ++f) cap.features[(slot * 12 + f) * 32 + lane] = sh.feat[f][lane];
+            cap.scores[slot * 32 + lane] = sh.scores[lane];
+            if (lane == 0) {
+                cap.masks[slot] = mask;
+                cap.actions[slot] = (std::int32_t)chosen;
+            }
+        }
+        if (lane == 0) {
+            sh.action = chosen;
+            st.action = (std::int32_t)chosen;
+            st.mne_target = 2u << (chosen & 3u);
+            st.region = 5;
+            ctl.alternative = alt;
+            ctl.legal_mask = mask;
+            ctl.start_count = count;
+            const node_t* list = sh.regions[(chosen >> 4) * 4 + ((chosen >> 2) & 3u)];
+            for (std::uint32_t i = 0; i < kRegionNodes; ++i) ctl.start_nodes[i] = list[i];
+            if (chosen >= 16) {
+                // restart from the alternative reference (control_state.cuh:302-336)
+                st.epoch_cost = st.parent_cost = ctl.archive_cost[alt];
+                trail_limits(st.epoch_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
+                st.default_trail = st.tau_max;
+                st.source_is_epoch = 0;
+                st.iteration_best = 0;
+                ctl.tracked_epoch = st.epoch_cost;
+                ctl.active_id = ctl.epoch_id = ctl.archive_id[alt];
+                ctl.return_rate = ctl.ls_work = 0.0f;
+                ctl.epoch_batches = 0;
+                if (ctl.restarts != ~0ull) ++ctl.restarts;
+            }
+        }
+    }
+    __syncthreads();
+    if (sh.action >= 16) {
+        const node_t* tour = archive_tour(cv, side, alt);
+        for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) cv.parent[i] = cv.epoch[i] = tour[i];
+        __syncthreads();
+        for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+            cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
+                                          ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
+        const float tmax = st.tau_max;
+        for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
+            cv.trails[i] = tmax;
+            cv.products[i] = tmax * cv.eta[i];
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
+                                   ColonyParams P, std::uint32_t colony_count) {
+    const std::uint32_t c = blockIdx.x;
+    const ColonyView cv = colonies[c];
+    const InstanceView in = instances[cv.instance];
+    const std::uint32_t n = in.n, k = in.k;
+    __shared__ float s_tmax;
+    __shared__ ColonyState s_st;
+    if (threadIdx.x == 0) {
+        ColonyState st{};
+        st.epoch_cost = st.global_cost = st.parent_cost = st.iteration_best_cost = in.initial_cost;
+        trail_limits(in.initial_cost, P.retention, P.p_root, k, st.tau_min, st.tau_max);
+        st.default_trail = st.tau_max;
+        st.mne_target = P.mne_target;
+        st.action = -1;
+        st.region = 4;
+        states[c] = st;
+        s_st = st;
+        s_tmax = st.tau_max;
+    }
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const node_t v = in.initial[i];
+        cv.parent[i] = cv.epoch[i] = cv.global[i] = v;
+        cv.parent_nbr[v] = (std::uint32_t)in.initial[i + 1 == n ? 0 : i + 1] |
+                           ((std::uint32_t)in.initial[i == 0 ? n - 1 : i - 1] << 16);
+    }
+    __syncthreads();
+    const float tmax = s_tmax;
+    for (std::uint32_t i = threadIdx.x; i < n * k; i += blockDim.x) {
+        cv.trails[i] = tmax;
+        cv.eta[i] = in.eta[i];
+        cv.products[i] = tmax * in.eta[i];
+    }
+    if (P.ref_control && cv.control) {
+        // the archive holds the initial tour (initialize_control,
+        // control_state.cuh:21-43); then the decision before batch 0
+        __shared__ RefShared s_ref;
+        node_t* a0 = archive_tour(cv, 0, 0);
+        for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            a0[i] = in.initial[i];
+            a0[cv.n_pad + in.initial[i]] = (node_t)i;
+        }
+        if (threadIdx.x < 32) {
+            std::uint32_t p0;
+            const Fingerprint f = warp_fingerprint(in.initial, n, threadIdx.x, p0);
+            if (threadIdx.x == 0) {
+                RefControl ctl{};
+                ctl.archive_size = 1;
+                ctl.archive_cost[0] = in.initial_cost;
+                ctl.archive_id[0] = f;
+                ctl.active_id = ctl.epoch_id = f;
+                ctl.tracked_global = ctl.tracked_epoch = in.initial_cost;
+                ctl.alternative = kArchive;
+                *cv.control = ctl;
+            }
+        }
+        __syncthreads();
+        ref_decide(cv, in, s_st, P, c, colony_count, 0, s_ref);
+        if (threadIdx.x == 0) states[c] = s_st;
+    }
+}
+
+__device__ __forceinline__ void write_trace(TraceRow& row, const ColonyState& st, std::uint32_t mne,
+                                            std::int32_t action, unsigned long long steps, unsigned long long evals) {
+    row.iteration_best_cost = st.iteration_best_cost;
+    row.global_cost = st.global_cost;
+    row.parent_cost = st.parent_cost;
+    row.iteration_best = st.iteration_best;
+    row.source_is_epoch = st.source_is_epoch;
+    row.tau_min = st.tau_min;
+    row.tau_max = st.tau_max;
+    row.mne_target = mne;
+    row.action = action;
+    row.construction_steps = steps;
+    row.ls_evaluations = evals;
+}
+
 // Fused reduce_and_select + update_pheromone for one colony, then (GP-controlled
 // evaluations) the controller decision for the next iteration.
 __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* instances,
@@ -662,7 +1155,18 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
     trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, cv.eta, cv.trails,
                  cv.products, threadIdx.x, blockDim.x);
     std::int32_t action = -1;
-    if (P.controlled && cv.program) {
+    if (P.ref_control) {
+        // the 12-feature controller: the trace row holds the action this
+        // batch ran with; archive and feedback; the next batch's decision
+        __shared__ RefShared s_ref;
+        __syncthreads();
+        if (threadIdx.x == 0 && trace && s_st.iteration < trace_cap)
+            write_trace(trace[(size_t)s_st.iteration * colony_count + c], s_st, s_used_mne, s_st.action, s_steps,
+                        s_evals);
+        ref_update(cv, in, s_st, P, s_ref);
+        if (s_st.iteration + 1 < P.total_iterations)
+            ref_decide(cv, in, s_st, P, c, colony_count, s_st.iteration + 1, s_ref);
+    } else if (P.controlled && cv.program) {
         // mean normalised entropy of the trail rows (exact integer sum)
         __syncthreads();
         unsigned long long q = 0;
@@ -734,20 +1238,8 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
     __syncthreads();
     if (threadIdx.x == 0) {
         ColonyState st = s_st;
-        if (trace && st.iteration < trace_cap) {
-            TraceRow& row = trace[(size_t)st.iteration * colony_count + c];
-            row.iteration_best_cost = st.iteration_best_cost;
-            row.global_cost = st.global_cost;
-            row.parent_cost = st.parent_cost;
-            row.iteration_best = st.iteration_best;
-            row.source_is_epoch = st.source_is_epoch;
-            row.tau_min = st.tau_min;
-            row.tau_max = st.tau_max;
-            row.mne_target = s_used_mne;
-            row.action = action;
-            row.construction_steps = s_steps;
-            row.ls_evaluations = s_evals;
-        }
+        if (trace && st.iteration < trace_cap && !P.ref_control)
+            write_trace(trace[(size_t)st.iteration * colony_count + c], st, s_used_mne, action, s_steps, s_evals);
         ++st.iteration;
         states[c] = st;
     }

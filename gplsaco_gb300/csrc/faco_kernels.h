@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "faco_ant.cuh"
+#include "faco_control.cuh"
 
 namespace faco {
 
@@ -23,6 +24,9 @@ struct ColonyParams {
     std::uint32_t controlled;        // GP controllers choose MNE, start region and restarts
     std::uint32_t total_iterations;  // T of the evaluation (iteration-fraction feature)
     float log2k;                     // log2(k) by the engine's own log2
+    std::uint32_t ref_control;       // 1: the 12-feature controller (feature spec 2)
+    unsigned long long ls_limit;     // LS evaluation budget per ant (LS-work feedback)
+    DecisionCapture capture;         // decisions to record (count 0: none)
 };
 
 // Candidate rows of registration on the GPU (faco_knn.cu): per node its
@@ -39,7 +43,7 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
                               std::uint32_t smem_bytes, cudaStream_t stream);
 
 __global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
-                                   ColonyParams P);
+                                   ColonyParams P, std::uint32_t colony_count);
 __global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,
                                      ColonyState* states, ColonyParams P, TraceRow* trace,
                                      std::uint32_t colony_count, std::uint32_t trace_cap);

@@ -95,6 +95,7 @@ class FacoBatchEngine:
         self.settings = settings
         self.ants = settings.ants or faco_ants(dimension)
         self._sizes: dict[int, int] = {}
+        self._spec = 0          # feature spec of the active stepwise evaluation (0: plain FACO)
         self._lock = threading.Lock()
 
     def close(self) -> None:
@@ -146,12 +147,15 @@ class FacoBatchEngine:
 
     def evaluate_program_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, program,
                                      preparation_mode="cached", experiment_mask=0xFFFFFFFF, *,
-                                     checkpoint_iterations=(), initial_mne=8, trace=False) -> dict:
+                                     checkpoint_iterations=(), initial_mne=8, trace=False,
+                                     decision_iterations=()) -> dict:
         """evaluate_program_evaluations (bindings.cpp:721-757): every colony is
-        driven by one GP controller program (feature spec 3)."""
+        driven by one GP controller program -- feature spec 2 (the
+        reference's 12 features) or 3 (this engine's).  decision_iterations
+        (spec 2) records the decisions before the given 1-based batches."""
         return self._programs(_u64_array(instance_keys, "instance_keys"), _u64_array(seeds, "seeds"),
                               evaluation_limit_per_colony, [program], experiment_mask, checkpoint_iterations,
-                              initial_mne, trace, preparation_mode)
+                              initial_mne, trace, preparation_mode, decisions=decision_iterations)
 
     def evaluate_controller_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, controller,
                                         experiment_mask=0xFFFFFFFF, *, decision_iterations=()) -> dict:
@@ -160,7 +164,9 @@ class FacoBatchEngine:
         bindings.cpp:58-73) -- a bare program, or {controller_version: 1,
         representation, controller_id, trees}.  A joint_single controller is
         its one tree; a conditional_three controller's role trees pick restart,
-        start region and MNE level in turn (faco_evaluate_controllers)."""
+        start region and MNE level in turn (faco_evaluate_controllers).
+        decision_iterations (feature spec 2) records the decisions before the
+        given 1-based batches under "decisions"."""
         if not isinstance(controller, dict):
             raise ValueError("controller must be a dict")
         if "opcode" in controller:
@@ -177,16 +183,13 @@ class FacoBatchEngine:
             if len(trees) != (3 if kind == "conditional_three" else 1):
                 raise ValueError("wrong number of role trees for the controller representation")
             if kind == "conditional_three":
-                if decision_iterations:
-                    raise ValueError("decision recording is not supported by this engine")
                 return self._controllers(_u64_array(instance_keys, "instance_keys"), _u64_array(seeds, "seeds"),
-                                         evaluation_limit_per_colony, [controller], experiment_mask)
+                                         evaluation_limit_per_colony, [controller], experiment_mask,
+                                         decision_iterations)
             program = trees[0]
-        if decision_iterations:
-            raise ValueError("decision recording is not supported by this engine")
         return self._programs(_u64_array(instance_keys, "instance_keys"), _u64_array(seeds, "seeds"),
                               evaluation_limit_per_colony, [program], experiment_mask, (), 8, False,
-                              "cached_charged")
+                              "cached_charged", decisions=decision_iterations)
 
     def evaluate_population_evaluations(self, instance_keys, seeds, evaluation_limit_per_colony, programs,
                                         experiment_mask=0xFFFFFFFF, *, factorial_policy=None,
@@ -240,26 +243,26 @@ class FacoBatchEngine:
             out.append(part)
         return out
 
-    def _controllers(self, keys, seeds, limit, controllers, experiment_mask) -> dict:
+    def _controllers(self, keys, seeds, limit, controllers, experiment_mask, decisions=()) -> dict:
         arr, kinds = controller_arrays(controllers)
         mask = _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF)
-        return self._evaluate(keys, seeds, limit, 8, "cached_charged", (), False, False, (arr, kinds), mask)
+        return self._evaluate(keys, seeds, limit, 8, "cached_charged", (), False, False, (arr, kinds), mask,
+                              decisions)
 
     def _programs(self, keys, seeds, limit, programs, experiment_mask, checkpoint_iterations, initial_mne, trace,
-                  preparation_mode, profile_events_only=False) -> dict:
+                  preparation_mode, profile_events_only=False, decisions=()) -> dict:
         if not isinstance(programs, (list, tuple)) or not programs:
             raise ValueError("programs must be a non-empty list of IR dicts")
         mask = _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF)
         mne = _exact_int(initial_mne, "initial_mne", 1, 2**32 - 1)
         arr = (_lib.Program * len(programs))(*[program_to_c(p) for p in programs])
-        for p in arr:
-            if p.feature_spec_id != 3:
-                raise ValueError("controller programs use feature spec 3")
+        if any(p.feature_spec_id not in (2, 3) for p in arr) or len({p.feature_spec_id for p in arr}) != 1:
+            raise ValueError("controller programs use one feature spec, 2 or 3")
         return self._evaluate(keys, seeds, limit, mne, preparation_mode, checkpoint_iterations, profile_events_only,
-                              trace, arr, mask)
+                              trace, arr, mask, decisions)
 
     def _evaluate(self, instance_keys, seeds, evaluation_limit_per_colony, mne, preparation_mode,
-                  checkpoint_iterations, profile_events_only, trace, programs, mask) -> dict:
+                  checkpoint_iterations, profile_events_only, trace, programs, mask, decisions=()) -> dict:
         keys = _u64_array(instance_keys, "instance_keys")
         seeds = _u64_array(seeds, "seeds")
         if keys.size != seeds.size:
@@ -270,6 +273,7 @@ class FacoBatchEngine:
         if type(profile_events_only) is not bool or type(trace) is not bool:
             raise ValueError("flags must be bool")
         cps = np.asarray([_exact_int(c, "checkpoint") for c in checkpoint_iterations], dtype=np.uint64)
+        points = np.asarray([_exact_int(d, "decision iteration", 1, 2**32 - 1) for d in decisions], dtype=np.uint32)
         count = keys.size
         D = self.dimension
         iterations = limit // self.ants if self.ants else 0
@@ -278,10 +282,22 @@ class FacoBatchEngine:
         trace_rows = np.zeros((iterations, count), _lib.TRACE_DTYPE) if trace else None
         cp_tours = np.zeros((cps.size, count, D), np.uint32) if cps.size else None
         work = np.zeros((count, 3), np.uint64)
-        control = np.zeros((count, 4), np.uint32)
+        control = np.zeros(count, _lib.CONTROL_STATE_DTYPE)
         out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), _lib.ptr(cp_tours))
         out.colony_work = work.ctypes.data
         out.control_states = control.ctypes.data
+        dec = None
+        if points.size:
+            dec = dict(features=np.zeros((points.size, count, 12, 32), np.float32),
+                       scores=np.zeros((points.size, count, 32), np.float32),
+                       masks=np.zeros((points.size, count), np.uint32),
+                       actions=np.zeros((points.size, count), np.int32))
+            out.decision_iterations = points.ctypes.data
+            out.n_decisions = points.size
+            out.decision_features = dec["features"].ctypes.data
+            out.decision_scores = dec["scores"].ctypes.data
+            out.decision_masks = dec["masks"].ctypes.data
+            out.decision_actions = dec["actions"].ctypes.data
         if not self._lock.acquire(blocking=False):
             raise RuntimeError("only one active evaluation per engine")
         try:
@@ -324,7 +340,10 @@ class FacoBatchEngine:
             "preparation_mode": preparation_mode,
         }
         if programs is not None:
-            result["control_states"] = control_state_dicts(control)
+            spec, kinds = _feature_spec(programs)
+            result["control_states"] = control_state_dicts(control, spec)
+            if dec is not None:
+                result["decisions"] = decision_rows(points, dec, kinds, count)
         if cps.size:
             result["checkpoints"] = [
                 {"iterations": int(cps[i]),
@@ -344,6 +363,7 @@ class FacoBatchEngine:
         _exact_int(trace_iterations, "trace_iterations", 0, 2**32 - 1)
         _lib.check(self._L.faco_begin(self._handle, keys.ctypes.data, seeds.ctypes.data, keys.size, mne,
                                       trace_iterations))
+        self._spec = 0
         self._active = (keys.copy(), trace_iterations, 0)
 
     def step(self, iterations: int) -> None:
@@ -370,17 +390,19 @@ class FacoBatchEngine:
         costs = np.zeros(count, np.int64)
         trace_rows = np.zeros((min(cap, done), count), _lib.TRACE_DTYPE) if cap else None
         work = np.zeros((count, 3), np.uint64)
-        control = np.zeros((count, 4), np.uint32)
+        control = np.zeros(count, _lib.CONTROL_STATE_DTYPE)
         out = _lib.Outputs(tours.ctypes.data, costs.ctypes.data, _lib.ptr(trace_rows), None)
         out.colony_work = work.ctypes.data
         out.control_states = control.ctypes.data
         self._active = None
         _lib.check(self._L.faco_finish(self._handle, C.byref(out)))
-        return {"tours": [tours[c, :self._sizes[int(keys[c])]] for c in range(count)], "costs": costs,
-                "completed_batches": int(out.completed_batches),
-                "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
-                "reversed_elements": int(out.reversed_elements), "colony_work": work, "trace": trace_rows,
-                "control_states": control_state_dicts(control)}
+        res = {"tours": [tours[c, :self._sizes[int(keys[c])]] for c in range(count)], "costs": costs,
+               "completed_batches": int(out.completed_batches),
+               "construction_steps": int(out.construction_steps), "ls_evaluations": int(out.ls_evaluations),
+               "reversed_elements": int(out.reversed_elements), "colony_work": work, "trace": trace_rows}
+        if self._spec:
+            res["control_states"] = control_state_dicts(control, self._spec)
+        return res
 
     def begin_programs(self, instance_keys, seeds, programs, experiment_mask=0xFFFFFFFF, *, initial_mne=8,
                        total_iterations, trace_iterations: int = 0) -> None:
@@ -391,6 +413,7 @@ class FacoBatchEngine:
         if keys.size != seeds.size:
             raise ValueError("instance_keys and seeds differ in length")
         arr = self._program_array(programs)
+        self._spec = arr[0].feature_spec_id
         _lib.check(self._L.faco_begin_programs(self._handle, keys.ctypes.data, seeds.ctypes.data, keys.size,
                                                C.cast(arr, C.c_void_p), len(arr),
                                                _exact_int(experiment_mask, "experiment_mask", 1, 0xFFFFFFFF),
@@ -415,6 +438,7 @@ class FacoBatchEngine:
         _lib.check(self._L.faco_restore(self._handle, data, len(data),
                                         _exact_int(trace_iterations, "trace_iterations", 0, 2**32 - 1)))
         info = state.describe()
+        self._spec = info["feature_spec"] if info["controlled"] else 0
         self._active = (np.asarray(info["instance_keys"], np.uint64), trace_iterations, info["completed_batches"])
 
     def _stepwise_output(self, res: dict, limit: int) -> dict:
@@ -428,7 +452,8 @@ class FacoBatchEngine:
                 "completed_batches": res["completed_batches"],
                 "completed_construction_steps": res["construction_steps"],
                 "completed_ls_evaluations": res["ls_evaluations"], "reversed_elements": res["reversed_elements"],
-                "colony_work": res["colony_work"]}
+                "colony_work": res["colony_work"],
+                **({"control_states": res["control_states"]} if "control_states" in res else {})}
 
     def _batches(self, evaluations, name: str) -> int:
         value = _exact_int(evaluations, name)
@@ -489,9 +514,8 @@ class FacoBatchEngine:
         if not isinstance(programs, (list, tuple)) or not programs:
             raise ValueError("programs must be a non-empty list of IR dicts")
         arr = (_lib.Program * len(programs))(*[program_to_c(p) for p in programs])
-        for p in arr:
-            if p.feature_spec_id != 3:
-                raise ValueError("controller programs use feature spec 3")
+        if any(p.feature_spec_id not in (2, 3) for p in arr) or len({p.feature_spec_id for p in arr}) != 1:
+            raise ValueError("controller programs use one feature spec, 2 or 3")
         return arr
 
     # ---- learned edge prior on the active stepwise evaluation ---------------
@@ -531,7 +555,7 @@ class FacoBatchEngine:
 _SNAPSHOT_HEADER = np.dtype([
     ("magic", "S8"), ("version", "<u4"), ("count", "<u4"), ("ants", "<u4"), ("k_common", "<u4"),
     ("mne_target", "<u4"), ("n_programs", "<u4"), ("action_mask", "<u4"), ("total_iterations", "<u4"),
-    ("controlled", "<u4"), ("done", "<u4"), ("reserved0", "<u4"), ("reserved1", "<u4"),
+    ("controlled", "<u4"), ("done", "<u4"), ("feature_spec", "<u4"), ("reserved1", "<u4"),
     ("settings_digest", "<u8"), ("tau_total", "<u8"), ("node_total", "<u8")])
 _COLONY_STATE_BYTES = 104      # sizeof(ColonyState); global_cost at byte 8
 
@@ -566,7 +590,7 @@ class CountedState:
                 "instance_keys": keys.tolist(), "seeds": seeds.tolist(), "global_costs": costs,
                 "controlled": bool(h["controlled"]), "programs": int(h["n_programs"]),
                 "mne_target": int(h["mne_target"]), "total_iterations": int(h["total_iterations"]),
-                "bytes": len(self._data)}
+                "feature_spec": int(h["feature_spec"]), "bytes": len(self._data)}
 
 
 class FixedFacoGpu:
@@ -631,13 +655,58 @@ def program_to_c(program: dict) -> _lib.Program:
     return p
 
 
-def control_state_dicts(rows) -> list[dict]:
+def _feature_spec(programs):
+    """(feature spec, kinds) of the program array or (slots, kinds) pair."""
+    if isinstance(programs, tuple):
+        arr, kinds = programs
+        return arr[0].feature_spec_id, [int(k) for k in kinds]
+    return programs[0].feature_spec_id, [0] * len(programs)
+
+
+def control_state_dicts(rows, spec=3) -> list[dict]:
     """Per-colony controller feedback after the last batch (the
-    control_states list of bindings.cpp:395-407, for the feature-spec-3
-    controller): restarts, batches since the last global improvement, and
-    the start region (4 = all nodes) and MNE target of the next batch."""
-    return [{"restarts": int(r[0]), "stagnant_batches": int(r[1]), "start_region": int(r[2]),
-             "mne_target": int(r[3])} for r in rows]
+    control_states list of bindings.cpp:395-407).  Feature spec 2: the
+    reference's fields (archive size, stagnant batches, return rate, LS work,
+    batches since the last restart, restarts); spec 3: restarts, batches since
+    the last global improvement, and the start region (4 = all nodes) and MNE
+    target of the next batch."""
+    if spec == 2:
+        return [{"archive_size": int(r["archive_size"]), "stagnant_batches": int(r["stagnant_batches"]),
+                 "return_rate": float(r["return_rate"]), "ls_work": float(r["ls_work"]),
+                 "epoch_batches": int(r["epoch_batches"]), "restarts": int(r["restarts"])} for r in rows]
+    return [{"restarts": int(r["restarts"]), "stagnant_batches": int(r["stagnant_batches"]),
+             "start_region": int(r["start_region"]), "mne_target": int(r["mne_target"])} for r in rows]
+
+
+def controller_stages(scores, mask: int, action: int) -> list[dict]:
+    """The three role decisions of a conditional controller (bindings.cpp:76-91)."""
+    stages, prefix = [], 0
+    for role, (width, stride, offset) in enumerate(((2, 16, 0), (4, 4, 2), (4, 1, 6))):
+        legal = [bool((mask >> (prefix + i * stride)) & ((1 << stride) - 1)) for i in range(width)]
+        selected = (action - prefix) // stride
+        stages.append({"scores": [float(x) for x in scores[offset:offset + width]], "legal": legal,
+                       "selected": selected})
+        prefix += selected * stride
+    return stages
+
+
+def decision_rows(points, dec, kinds, count) -> list[dict]:
+    """Captured decisions as the reference returns them (bindings.cpp:323-346):
+    one row per (iteration, colony) with its legal mask, action, 12 x 32
+    features and 32 scores (conditional controllers: the role stages)."""
+    rows = []
+    per = count // len(kinds)
+    for i, point in enumerate(points):
+        for c in range(count):
+            row = {"iteration": int(point), "colony": c, "legal_mask": int(dec["masks"][i, c]),
+                   "action": int(dec["actions"][i, c]),
+                   "features": [dec["features"][i, c, f].tolist() for f in range(12)]}
+            if kinds[c // per] == 1:
+                row["stages"] = controller_stages(dec["scores"][i, c], row["legal_mask"], row["action"])
+            else:
+                row["scores"] = [float(x) if np.isfinite(x) else None for x in dec["scores"][i, c]]
+            rows.append(row)
+    return rows
 
 
 def controller_arrays(controllers):

@@ -109,6 +109,22 @@ typedef struct faco_trace_row {
     uint64_t ls_evaluations;
 } faco_trace_row;
 
+/* Controller feedback of one colony after its last batch (the control_states
+ * rows of bindings.cpp:395-407).  Feature spec 2 fills every field; spec 3
+ * the restarts, stagnant batches, start region and MNE target. */
+typedef struct faco_control_state {
+    uint64_t restarts;
+    uint64_t stagnant_batches;  /* batches since the last global improvement */
+    uint64_t epoch_batches;     /* batches since the last restart (spec 2)    */
+    float return_rate;          /* spec 2: EMA of ants returning the parent   */
+    float ls_work;              /* spec 2: EMA of the LS budget used          */
+    uint32_t archive_size;      /* spec 2: reference tours held (1-4)         */
+    uint32_t start_region;      /* start region of the next batch (spec 3: 0-3, 4 = all
+                                   nodes; spec 2: 5 = the controller's start list) */
+    uint32_t mne_target;        /* MNE target of the next batch               */
+    uint32_t reserved;
+} faco_control_state;
+
 typedef struct faco_outputs {
     uint32_t* tours;          /* [count][dimension] global-best tours (u32)       */
     int64_t* costs;           /* [count] integer EUC_2D lengths                   */
@@ -122,11 +138,19 @@ typedef struct faco_outputs {
     double solve_seconds;
     uint64_t* colony_work;      /* [count][3] per colony: construction steps, LS
                                    evaluations, reversed elements; may be NULL */
-    uint32_t* control_states;   /* [count][4] per colony after the last batch
-                                   (the controller feedback of bindings.cpp:395-407):
-                                   restarts, stagnant batches (since the last
-                                   global improvement), start region of the next
-                                   batch (4 = all nodes), its MNE target; may be NULL */
+    faco_control_state* control_states; /* [count], may be NULL */
+    /* Decision captures of feature-spec-2 controllers (decision_iterations,
+     * bindings.cpp:323-346): for each 1-based batch number p in
+     * decision_iterations (strictly increasing, <= the batches run) the
+     * decision taken before batch p-1 -- its 12 x 32 features, the 32
+     * scores (conditional controllers: role scores in slots 0-9), the legal
+     * mask and the action -- per colony.  n_decisions 0: none. */
+    const uint32_t* decision_iterations;
+    uint32_t n_decisions;
+    float* decision_features;   /* [n_decisions][count][12][32] */
+    float* decision_scores;     /* [n_decisions][count][32]     */
+    uint32_t* decision_masks;   /* [n_decisions][count]         */
+    int32_t* decision_actions;  /* [n_decisions][count]         */
 } faco_outputs;
 
 /* evaluate_faco_evaluations(keys, seeds, evaluation_limit_per_colony, mne,
@@ -141,14 +165,26 @@ int faco_evaluate(faco_engine* engine, const uint64_t* instance_keys, const uint
 /* evaluate_program_evaluations / evaluate_population_evaluations
  * (bindings.cpp:721-757,776-817; engine cuda/batch_engine.cu:379-437,
  * per-batch control :884-950): colony c is driven by programs[c / (count /
- * n_programs)], a postfix program of feature spec 3 that scores the 32
- * actions of its colony after every iteration from 7 colony features
- * (iteration fraction, stagnation, mean/best gap, trail-row entropy,
- * restarts, LS gain, reference-tour age) and 3 action descriptors; the first
- * best legal action (action_mask) sets the next MNE target 2<<(a&3), the
- * start region (a>>2)&3 and, for a >= 16, a restart from the global best with
- * trails reset to tau_max.  initial_mne is the target of the first
- * iteration.  Traces record the target used and the action chosen. */
+ * n_programs)].  All programs of one call share one feature spec:
+ *
+ * spec 2, the reference's 12-feature controller (control_state.cuh:45-364,
+ * control_cpu.cpp:72-118): before every batch the 32 actions (mode x start
+ * region x MNE level) are scored on elapsed fraction, stagnation, return
+ * rate, LS work, mode, level, reference gap, sampled difference and four
+ * features of the action's 16-node start region; the best legal action sets
+ * the MNE target 2<<(a&3) and the start nodes, and a >= 16 restarts from
+ * the alternative archive tour.  Actions >= 16 are legal only while the
+ * archive holds an alternative; action_mask & 0xffff must be non-zero.
+ * Traces record the target and action each batch ran with.
+ *
+ * spec 3, this engine's compact controller: after every iteration the
+ * actions are scored from 7 colony features (iteration fraction,
+ * stagnation, mean/best gap, trail-row entropy, restarts, LS gain,
+ * reference-tour age) and 3 action descriptors; the action sets the next MNE
+ * target 2<<(a&3), the start quadrant (a>>2)&3 and, for a >= 16, a restart
+ * from the global best with trails reset to tau_max.  initial_mne is the
+ * target of the first iteration.  Traces record the target used and the
+ * action chosen after the iteration. */
 int faco_evaluate_programs(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds,
                            uint32_t count, uint64_t evaluation_limit_per_colony, const struct faco_program* programs,
                            uint32_t n_programs, uint32_t action_mask, uint32_t initial_mne,
