@@ -391,10 +391,13 @@ POP_N, POP_SEED, POP_PROGRAMS, POP_ITERATIONS = 500, 2, 128, 1000
 POP_METRIC = "GP individuals evaluated/sec (N=500, 32 ants, 1000 iterations each)"
 
 
-def population_programs() -> list:
+def population_programs(spec: int = 3) -> list:
+    """128 random controller programs: feature spec 3 (the colony features of
+    the GP evaluation batch) or 2 (the reference's 12-feature controller)."""
     from gplsaco_gb300.programs import random_program
     rng = np.random.default_rng(POP_SEED)
-    return [random_program(rng, extended=True, features=10, feature_spec_id=3) for _ in range(POP_PROGRAMS)]
+    return [random_program(rng, extended=True, features=10 if spec == 3 else 12, feature_spec_id=spec)
+            for _ in range(POP_PROGRAMS)]
 
 
 def population_workload() -> Workload:
@@ -403,7 +406,7 @@ def population_workload() -> Workload:
                     np.ones(1, np.uint64), 32, 16, 64, 20)
 
 
-def population_cpu(threads: int, colonies: int, iterations: int) -> float:
+def population_cpu(threads: int, colonies: int, iterations: int, spec: int = 3) -> float:
     """Elapsed seconds of `colonies` controller-driven colonies (programs in
     order) of `iterations` iterations on the oracle port, one per thread."""
     from concurrent.futures import ThreadPoolExecutor
@@ -411,13 +414,14 @@ def population_cpu(threads: int, colonies: int, iterations: int) -> float:
     from oracle import oracle
     oracle.lib()
     wl = population_workload()
-    programs = population_programs()
+    programs = population_programs(spec)
     prep = oracle.prepare(wl.xys[0], wl.k, wl.b, wl.w)
 
     def one(c):
         oracle.run_colony(wl.xys[0], prep, ants=wl.ants, k=wl.k, b=wl.b, w=wl.w, mne=wl.mne, iterations=iterations,
                           key=oracle.lib().orc_colony_key(1, 1), retention=wl.retention, threads=1,
-                          want_trace=False, program=programs[c % len(programs)], total_iterations=POP_ITERATIONS)
+                          want_trace=False, program=programs[c % len(programs)], total_iterations=POP_ITERATIONS,
+                          instance_key=1)
 
     start = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as pool:
@@ -425,12 +429,12 @@ def population_cpu(threads: int, colonies: int, iterations: int) -> float:
     return time.perf_counter() - start
 
 
-def population_cpu_line(colonies_per_thread: int = 2) -> dict:
+def population_cpu_line(colonies_per_thread: int = 2, spec: int = 3) -> dict:
     """Whole 1000-iteration controller-driven runs of the first programs on
     the oracle port, one colony per host thread at a time."""
     threads = os.cpu_count() or 1
     colonies = min(POP_PROGRAMS, colonies_per_thread * threads)
-    elapsed = population_cpu(threads, colonies, POP_ITERATIONS)
+    elapsed = population_cpu(threads, colonies, POP_ITERATIONS, spec)
     value = colonies / elapsed
     return {"value": value, "unit": "individuals/s", "cores": threads, "kind": "port",
             "sample": f"{colonies} of the {POP_PROGRAMS} programs, whole {POP_ITERATIONS}-iteration colony runs, "
@@ -438,7 +442,7 @@ def population_cpu_line(colonies_per_thread: int = 2) -> dict:
 
 
 def run_population_reference(args) -> None:
-    base = population_cpu_line()
+    base = population_cpu_line(spec=args.controller)
     line = {"impl": "reference", "metric": POP_METRIC, "value": base["value"], "unit": "individuals/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
@@ -457,7 +461,7 @@ def run_population(args, rank: int, world: int) -> None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     wl = population_workload()
-    programs = population_programs()
+    programs = population_programs(args.controller)
     settings = g.FixedFacoSettings(ants=wl.ants, primary_width=wl.k, backup_width=wl.b, ls_width=wl.w,
                                    retention=wl.retention)
     engine = g.FacoBatchEngine(POP_N, 1, settings, population_size=POP_PROGRAMS, device=local)
@@ -490,14 +494,17 @@ def run_population(args, rank: int, world: int) -> None:
         return
     value = args.steps * POP_PROGRAMS * world / (elapsed_ms / 1e3)
     e2e = args.steps * POP_PROGRAMS / float(np.sum(wall))
-    base = population_cpu_line() if args.cpu_baseline else None
+    base = population_cpu_line(spec=args.controller) if args.cpu_baseline else None
+    controller = ("feature spec 3: 7 colony features + 3 action descriptors" if args.controller == 3 else
+                  "feature spec 2: the reference's 12-feature controller with its tour archive")
     line = {
         "metric": POP_METRIC, "value": value, "unit": "individuals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": {"workload": "GP evaluation batch: 1 uniform N=500 instance (seed 2), 128 random controller "
-                               "programs (feature spec 3, depth <= 6), one colony each, 32 ants, k=16, 1000 "
+                               "programs (depth <= 6), one colony each, 32 ants, k=16, 1000 "
                                "iterations; a step is one evaluate_population_evaluations call",
+                   "controller": controller,
                    "l2": "each step runs 1000 iterations; the panel's working set (~30 MB) is L2-resident by design"},
         "e2e": {"value": e2e, "unit": "individuals/s", "h2d_bytes_per_step": float(keys.nbytes + seeds.nbytes),
                 "d2h_bytes_per_step": float(POP_PROGRAMS * (POP_N * 4 + 8)),
@@ -505,7 +512,7 @@ def run_population(args, rank: int, world: int) -> None:
         "roofline": None,
         "cpu_baseline": base,
         "clocks": clocks.summary(),
-        "gpu_launches": (1 + 2 * POP_ITERATIONS) * args.steps,
+        "gpu_launches": (1 + (3 if args.controller == 2 else 2) * POP_ITERATIONS) * args.steps,
     }
     print(json.dumps(line), flush=True)
 
@@ -540,6 +547,9 @@ def main():
     ap.add_argument("--workload", default="throughput",
                     choices=["throughput", "uneven", "large", "gp-population", "time-to-gap"],
                     help="time-to-gap: learned-prior vs plain FACO wall-clock to a 1%% mean gap (N=1000/2000)")
+    ap.add_argument("--controller", type=int, default=3, choices=[2, 3],
+                    help="gp-population: feature spec of the programs (3: the batch's colony features; "
+                         "2: the reference's 12-feature controller)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -64,34 +64,59 @@ __host__ __device__ __forceinline__ bool has_node(const T* nodes, std::uint32_t 
     return false;
 }
 
-// Start region (mode, region) of one batch around a reference tour:
-// regions 0-1 are 16 consecutive tour nodes from a random position, region 2
-// a breadth-first walk over the primary candidate rows from a random node,
-// region 3 (and any shortfall of 2) distinct uniform nodes.
-__device__ inline void build_region(const node_t* tour, std::uint32_t n, const node_t* primary, std::uint32_t k,
-                                    unsigned long long key, std::uint32_t batch, std::uint32_t mode,
-                                    std::uint32_t region, node_t* nodes) {
+// Start region (mode, region) of one batch around a reference tour, built by
+// one warp (every lane draws the same random sequence): regions 0-1 are 16
+// consecutive tour nodes from a random position, region 2 a breadth-first
+// walk over the primary candidate rows from a random node (a row's new nodes
+// taken in row order), region 3 (and any shortfall of 2) distinct uniform
+// nodes -- the rank-th node outside the set is the least fixed point of
+// x = rank + |{e in set : e <= x}|.  nodes[16] in shared memory; k <= 32.
+__device__ inline void warp_build_region(const node_t* tour, std::uint32_t n, const node_t* primary,
+                                         std::uint32_t k, unsigned long long key, std::uint32_t batch,
+                                         std::uint32_t mode, std::uint32_t region, node_t* nodes,
+                                         std::uint32_t lane) {
     const std::uint32_t count = n < kRegionNodes ? n : kRegionNodes;
     CtlRandom r{ctl_mix(key ^ 0xbb67ae8584caa73bULL ^ ctl_mix((unsigned long long)batch ^ 0x3c6ef372fe94f82bULL) ^
                         ctl_mix((unsigned long long)(mode * 4 + region + 1) ^ 0xa54ff53a5f1d36f1ULL)),
                 0};
-    std::uint32_t used = 0;
     if (region < 2) {
         const std::uint32_t start = r.bounded(n);
-        for (std::uint32_t i = 0; i < count; ++i) nodes[i] = tour[(start + i) % n];
+        if (lane < kRegionNodes) nodes[lane] = lane < count ? tour[(start + lane) % n] : (node_t)0;
+        __syncwarp();
         return;
     }
+    if (lane < kRegionNodes) nodes[lane] = 0;
+    __syncwarp();
+    std::uint32_t used = 0;
     if (region == 2) {
-        nodes[used++] = (node_t)r.bounded(n);
-        for (std::uint32_t head = 0; head < used && used < count; ++head)
-            for (std::uint32_t j = 0; j < k && used < count; ++j) {
-                const std::uint32_t v = primary[(size_t)nodes[head] * k + j];
-                if (v < n && !has_node(nodes, used, v)) nodes[used++] = (node_t)v;
-            }
+        const std::uint32_t first = r.bounded(n);
+        if (lane == 0) nodes[0] = (node_t)first;
+        used = 1;
+        __syncwarp();
+        for (std::uint32_t head = 0; head < used && used < count; ++head) {
+            const std::uint32_t v = lane < k ? primary[(size_t)nodes[head] * k + lane] : n;
+            const bool fresh = v < n && !has_node(nodes, used, v);
+            const unsigned ok = __ballot_sync(0xffffffffu, fresh);
+            const std::uint32_t take = min((std::uint32_t)__popc(ok), count - used);
+            const std::uint32_t rank = __popc(ok & ((1u << lane) - 1u));
+            __syncwarp();
+            if (fresh && rank < take) nodes[used + rank] = (node_t)v;
+            used += take;
+            __syncwarp();
+        }
     }
     while (used < count) {
-        const std::uint32_t v = remaining_node(r.bounded(n - used), nodes, used);
-        nodes[used++] = (node_t)v;
+        const std::uint32_t rank = r.bounded(n - used);
+        const std::uint32_t e = lane < used ? (std::uint32_t)nodes[lane] : 0xffffffffu;
+        std::uint32_t x = rank;
+        for (;;) {
+            const std::uint32_t next = rank + __popc(__ballot_sync(0xffffffffu, e <= x));
+            if (next == x) break;
+            x = next;
+        }
+        if (lane == 0) nodes[used] = (node_t)x;
+        ++used;
+        __syncwarp();
     }
 }
 
@@ -129,6 +154,7 @@ struct RefControl {
     std::uint32_t archive_size, side;   // archive entries; which half of the double buffer holds them
     std::uint32_t alternative, legal_mask;
     std::uint32_t start_count, reserved;
+    std::uint32_t archive_p0[kArchive];   // position of node 0 in each archive tour
     node_t start_nodes[kRegionNodes];
 };
 

@@ -574,13 +574,23 @@ void enqueue_ants(faco_engine* e, cudaStream_t st) {
     for (std::size_t i = 1; i < branches; ++i) cuda_check(cudaStreamWaitEvent(st, e->branch_events[i], 0), "join wait");
 }
 
-void enqueue_iteration(faco_engine* e, cudaStream_t st) {
+// The colony update of one iteration (with the 12-feature controller, the
+// ants' fingerprints first, one warp per ant).
+void enqueue_update(faco_engine* e, cudaStream_t st) {
     auto& v = e->eval;
-    enqueue_ants(e, st);
+    if (v.P.ref_control) {
+        const std::uint32_t warps = v.count * v.P.ants;
+        faco::fingerprint_kernel<<<(warps + 7) / 8, 256, 0, st>>>(e->colonies.get(), v.P.ants, v.count);
+    }
     faco::colony_update_kernel<<<v.count, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
                                                          v.P, v.trace_cap ? e->trace.get() : nullptr, v.count,
                                                          v.trace_cap);
     cuda_check(cudaGetLastError(), "update launch");
+}
+
+void enqueue_iteration(faco_engine* e, cudaStream_t st) {
+    enqueue_ants(e, st);
+    enqueue_update(e, st);
 }
 
 // Kernel variant of a size class: the global-memory workspace (tour and
@@ -1118,7 +1128,7 @@ namespace {
 // kept.  The Philox streams are keyed by the iteration counter kept in the
 // colony states, so a restored evaluation continues bit for bit.
 constexpr char kSnapshotMagic[8] = {'F', 'A', 'C', 'O', 'S', 'N', 'P', '1'};
-constexpr std::uint32_t kSnapshotVersion = 2;
+constexpr std::uint32_t kSnapshotVersion = 3;
 static_assert(sizeof(faco::ColonyState) == 104, "snapshot layout (the Python reader's ColonyState size)");
 
 struct SnapshotHeader {
@@ -1391,11 +1401,7 @@ int faco_step_timed(faco_engine* e, uint32_t iterations, double* ant_ms, double*
             cuda_check(cudaEventRecord(ev[3 * i], s), "event");
             enqueue_ants(e, s);
             cuda_check(cudaEventRecord(ev[3 * i + 1], s), "event");
-            faco::colony_update_kernel<<<v.count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(),
-                                                               e->states.get(), v.P,
-                                                               v.trace_cap ? e->trace.get() : nullptr, v.count,
-                                                               v.trace_cap);
-            cuda_check(cudaGetLastError(), "update launch");
+            enqueue_update(e, s);
             cuda_check(cudaEventRecord(ev[3 * i + 2], s), "event");
         }
         cuda_check(cudaStreamSynchronize(s), "timed step");

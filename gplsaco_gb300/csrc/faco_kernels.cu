@@ -562,33 +562,32 @@ struct TourRef {
 __device__ __forceinline__ node_t* archive_tour(const ColonyView& cv, std::uint32_t side, std::uint32_t slot) {
     return cv.archive + (size_t)((side * kArchive + slot) * 2u) * cv.n_pad;
 }
-__device__ __forceinline__ TourRef archive_ref(const ColonyView& cv, std::uint32_t side, std::uint32_t slot) {
-    const node_t* t = archive_tour(cv, side, slot);
-    return {t, t + cv.n_pad, t[cv.n_pad]};
-}
 
 // canonical_compare (control_ops.hpp:61-74) by one warp: both tours read
-// from node 0 towards its smaller neighbour; -1, 0 or 1.
+// from node 0 towards its smaller neighbour; -1, 0 or 1.  Each lane loads 16
+// elements of both tours before the first vote, so the loads overlap.
+__device__ __forceinline__ std::uint32_t canonical_index(std::uint32_t p0, bool forward, std::uint32_t i,
+                                                         std::uint32_t n) {
+    std::uint32_t x = forward ? p0 + i : p0 + n - i;   // < 2n
+    return x >= n ? x - n : x;
+}
 __device__ int warp_canonical_compare(TourRef a, TourRef b, std::uint32_t n, std::uint32_t lane) {
+    constexpr std::uint32_t kUnroll = 16;
     const bool fa = a.tour[a.p0 + 1 == n ? 0 : a.p0 + 1] < a.tour[a.p0 == 0 ? n - 1 : a.p0 - 1];
     const bool fb = b.tour[b.p0 + 1 == n ? 0 : b.p0 + 1] < b.tour[b.p0 == 0 ? n - 1 : b.p0 - 1];
-    for (std::uint32_t base = 1; base < n; base += 32) {
-        const std::uint32_t i = base + lane;
-        std::uint32_t va = 0, vb = 0;
-        if (i < n) {
-            va = a.tour[fa ? (a.p0 + i) % n : (a.p0 + n - i) % n];
-            vb = b.tour[fb ? (b.p0 + i) % n : (b.p0 + n - i) % n];
+    for (std::uint32_t base = 1; base < n; base += 32 * kUnroll) {
+        std::uint32_t va[kUnroll], vb[kUnroll];
+#pragma unroll
+        for (std::uint32_t u = 0; u < kUnroll; ++u) {
+            const std::uint32_t i = base + u * 32 + lane;
+            va[u] = i < n ? a.tour[canonical_index(a.p0, fa, i, n)] : 0u;
+            vb[u] = i < n ? b.tour[canonical_index(b.p0, fb, i, n)] : 0u;
         }
-        const unsigned m = __ballot_sync(kFull, va != vb);
-        if (m) return __shfl_sync(kFull, va < vb ? -1 : 1, __ffs(m) - 1);
-    }
-    return 0;
-}
-
-__device__ std::uint32_t warp_find_zero(const node_t* tour, std::uint32_t n, std::uint32_t lane) {
-    for (std::uint32_t base = 0; base < n; base += 32) {
-        const unsigned m = __ballot_sync(kFull, base + lane < n && tour[base + lane] == 0);
-        if (m) return base + __ffs(m) - 1;
+#pragma unroll
+        for (std::uint32_t u = 0; u < kUnroll; ++u) {
+            const unsigned m = __ballot_sync(kFull, va[u] != vb[u]);
+            if (m) return __shfl_sync(kFull, va[u] < vb[u] ? -1 : 1, __ffs(m) - 1);
+        }
     }
     return 0;
 }
@@ -598,12 +597,23 @@ __device__ std::uint32_t warp_find_zero(const node_t* tour, std::uint32_t n, std
 __device__ Fingerprint warp_fingerprint(const node_t* tour, std::uint32_t n, std::uint32_t lane, std::uint32_t& p0) {
     unsigned long long f1 = 0, f2 = 0;
     std::uint32_t z = 0xffffffffu;
-    for (std::uint32_t i = lane; i < n; i += 32) {
-        const std::uint32_t a = tour[i];
-        const Fingerprint e = fingerprint_edge(a, tour[i + 1 == n ? 0 : i + 1]);
-        f1 ^= e.first;
-        f2 ^= e.second;
-        if (a == 0) z = i;
+    for (std::uint32_t base = 0; base < n; base += 128) {
+        std::uint32_t a[4], b[4];
+#pragma unroll
+        for (std::uint32_t u = 0; u < 4; ++u) {
+            const std::uint32_t i = base + u * 32 + lane;
+            a[u] = i < n ? tour[i] : 0u;
+            b[u] = i < n ? tour[i + 1 == n ? 0 : i + 1] : 0u;
+        }
+#pragma unroll
+        for (std::uint32_t u = 0; u < 4; ++u) {
+            const std::uint32_t i = base + u * 32 + lane;
+            if (i >= n) continue;
+            const Fingerprint e = fingerprint_edge(a[u], b[u]);
+            f1 ^= e.first;
+            f2 ^= e.second;
+            if (a[u] == 0) z = i;
+        }
     }
     for (int o = 16; o; o >>= 1) {
         f1 ^= __shfl_xor_sync(kFull, f1, o);
@@ -614,40 +624,51 @@ __device__ Fingerprint warp_fingerprint(const node_t* tour, std::uint32_t n, std
     return {f1, f2};
 }
 
+// Candidates of the archive selection: 0-3 the archive slots, 4 + a ant a.
+// Archive fields come from the shared copy of the controller state; the
+// ants' costs, fingerprints and node-0 positions from shared memory when the
+// colony has at most kStageAnts ants, else from global memory.
+constexpr std::uint32_t kStageAnts = 128;
 struct CandidateView {
     const ColonyView& cv;
     const RefControl& ctl;
-    __device__ long long cost(std::uint32_t c) const {
-        return c < kArchive ? ctl.archive_cost[c] : cv.ant_costs[c - kArchive];
-    }
-    __device__ Fingerprint id(std::uint32_t c) const {
-        if (c < kArchive) return ctl.archive_id[c];
-        const unsigned long long* p = cv.ant_ids + 2ull * (c - kArchive);
-        return {p[0], p[1]};
-    }
+    const long long* costs;
+    const Fingerprint* ids;
+    const std::uint32_t* p0s;
+    __device__ long long cost(std::uint32_t c) const { return c < kArchive ? ctl.archive_cost[c] : costs[c - kArchive]; }
+    __device__ Fingerprint id(std::uint32_t c) const { return c < kArchive ? ctl.archive_id[c] : ids[c - kArchive]; }
     __device__ TourRef ref(std::uint32_t c) const {
-        if (c < kArchive) return archive_ref(cv, ctl.side, c);
-        return {cv.ant_tours + (size_t)(c - kArchive) * cv.n_pad, nullptr, cv.ant_p0[c - kArchive]};
+        if (c < kArchive) {
+            const node_t* t = archive_tour(cv, ctl.side, c);
+            return {t, t + cv.n_pad, ctl.archive_p0[c]};
+        }
+        return {cv.ant_tours + (size_t)(c - kArchive) * cv.n_pad, nullptr, p0s[c - kArchive]};
     }
 };
 
 constexpr std::uint32_t kCtlWords = (kArchive + kCtlMaxAnts + 31) / 32;
 
+// The archive band as an integer: an integer cost c exceeds the double
+// global_cost * (1 + band) exactly when c exceeds its floor.
+__device__ __forceinline__ long long band_limit(long long global_cost) {
+    return (long long)floor((double)global_cost * (1 + kArchiveBand));
+}
+
 // Archive selection by warp 0 (update_control's slot loop): the global best
 // first, then up to 3 distinct tours of the old archive and the batch within
 // 2 % of the global cost, each the least by (cost, fingerprint, canonical
-// order, candidate index).  Candidates 0-3 are archive slots, 4 + a ant a.
+// order, candidate index).
 __device__ std::uint32_t ref_archive_select(const CandidateView& v, const ColonyState& st, std::uint32_t A,
                                             bool improved, std::uint32_t n, std::uint32_t lane,
                                             std::uint32_t* excluded, std::uint32_t* chosen) {
     const std::uint32_t total = kArchive + A;
     for (std::uint32_t w = lane; w < (total + 31) / 32; w += 32) excluded[w] = 0;
     __syncwarp();
-    const double limit = (double)st.global_cost * (1 + kArchiveBand);
+    const long long limit = band_limit(st.global_cost);
     auto is_excluded = [&](std::uint32_t c) { return (excluded[c >> 5] >> (c & 31u)) & 1u; };
     auto eligible = [&](std::uint32_t c) {
         if (c < kArchive && c >= v.ctl.archive_size) return false;
-        return (double)v.cost(c) <= limit && !is_excluded(c);
+        return v.cost(c) <= limit && !is_excluded(c);
     };
     std::uint32_t count = 0;
     auto add = [&](std::uint32_t w) {
@@ -709,80 +730,181 @@ __device__ std::uint32_t ref_archive_select(const CandidateView& v, const Colony
     return count;
 }
 
+// The same selection when every pair of candidates with equal fingerprints
+// holds the same tour (rep[c]: the first valid candidate with c's cost and
+// fingerprint): a group of identical tours acts as its first member, and the
+// least by (cost, fingerprint, index) needs no tour comparison.
+__device__ std::uint32_t ref_archive_select_groups(const CandidateView& v, const ColonyState& st, std::uint32_t A,
+                                                   bool improved, std::uint32_t lane, const std::uint16_t* rep,
+                                                   std::uint32_t* excluded, std::uint32_t* chosen) {
+    const std::uint32_t total = kArchive + A;
+    for (std::uint32_t w = lane; w < (total + 31) / 32; w += 32) excluded[w] = 0;
+    __syncwarp();
+    const long long limit = band_limit(st.global_cost);
+    const std::uint32_t first = improved ? kArchive + st.iteration_best : 0u;
+    if (lane == 0) {
+        chosen[0] = first;
+        excluded[rep[first] >> 5] |= 1u << (rep[first] & 31u);
+    }
+    __syncwarp();
+    std::uint32_t count = 1;
+    for (std::uint32_t slot = 1; slot < kArchive; ++slot) {
+        std::uint32_t best = 0xffffffffu;
+        long long bc = 0;
+        Fingerprint bi{0, 0};
+        for (std::uint32_t c = lane; c < total; c += 32) {
+            if (rep[c] != c || ((excluded[c >> 5] >> (c & 31u)) & 1u)) continue;
+            const long long cc = v.cost(c);
+            if (cc > limit) continue;
+            const Fingerprint ci = v.id(c);
+            if (best == 0xffffffffu || cc < bc || (cc == bc && fp_less(ci, bi))) { best = c; bc = cc; bi = ci; }
+        }
+        for (int o = 16; o; o >>= 1) {
+            const std::uint32_t ob = __shfl_xor_sync(kFull, best, o);
+            const long long oc = __shfl_xor_sync(kFull, bc, o);
+            const Fingerprint oi{__shfl_xor_sync(kFull, bi.first, o), __shfl_xor_sync(kFull, bi.second, o)};
+            const bool take = ob != 0xffffffffu &&
+                              (best == 0xffffffffu || oc < bc ||
+                               (oc == bc && (fp_less(oi, bi) || (fp_equal(oi, bi) && ob < best))));
+            if (take) { best = ob; bc = oc; bi = oi; }
+        }
+        if (best == 0xffffffffu) break;
+        if (lane == 0) {
+            chosen[count] = best;
+            excluded[best >> 5] |= 1u << (best & 31u);
+        }
+        ++count;
+        __syncwarp();
+    }
+    return count;
+}
+
 struct RefShared {
+    RefControl ctl;                       // the colony's controller state while the kernel runs
     float feat[12][32];
     float scores[32];
     node_t regions[8][kRegionNodes];
+    long long ant_cost[kStageAnts];
+    Fingerprint ant_id[kStageAnts];
+    std::uint32_t ant_p0[kStageAnts];
+    std::uint16_t rep[kArchive + kCtlMaxAnts];
+    std::uint32_t collision;
     std::uint32_t excluded[kCtlWords];
-    std::uint32_t chosen[kArchive];
+    std::uint32_t chosen[kArchive], next_p0[kArchive];
     long long chosen_cost[kArchive];
     Fingerprint chosen_id[kArchive];
     std::uint32_t count, alternative, mask, action, largest;
-    float gap[2], difference;
+    float gap[2], difference, elapsed, stagnation;
 };
 
-// update_control for one colony (after reduce/select and the trail update).
+__device__ __forceinline__ CandidateView candidates(const ColonyView& cv, const RefShared& sh, std::uint32_t A) {
+    const bool staged = A <= kStageAnts;
+    return {cv, sh.ctl, staged ? sh.ant_cost : cv.ant_costs,
+            staged ? sh.ant_id : reinterpret_cast<const Fingerprint*>(cv.ant_ids), staged ? sh.ant_p0 : cv.ant_p0};
+}
+
+// update_control for one colony (after reduce/select and the trail update);
+// sh.ctl holds the controller state.
 __device__ void ref_update(const ColonyView& cv, const InstanceView& in, const ColonyState& st,
                            const ColonyParams& P, RefShared& sh) {
-    RefControl& ctl = *cv.control;
+    RefControl& ctl = sh.ctl;
     const std::uint32_t n = in.n, A = P.ants;
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-    for (std::uint32_t a = warp; a < A; a += warps) {
-        std::uint32_t p0;
-        const Fingerprint f = warp_fingerprint(cv.ant_tours + (size_t)a * cv.n_pad, n, lane, p0);
-        if (lane == 0) {
-            cv.ant_ids[2 * a] = f.first;
-            cv.ant_ids[2 * a + 1] = f.second;
-            cv.ant_p0[a] = p0;
+    const bool staged = A <= kStageAnts;
+    // the ants' fingerprints come from fingerprint_kernel
+    if (staged)
+        for (std::uint32_t a = threadIdx.x; a < A; a += blockDim.x) {
+            sh.ant_cost[a] = cv.ant_costs[a];
+            sh.ant_id[a] = {cv.ant_ids[2 * a], cv.ant_ids[2 * a + 1]};
+            sh.ant_p0[a] = cv.ant_p0[a];
         }
-    }
+    if (threadIdx.x == 0) sh.collision = 0;
     __syncthreads();
     const bool improved = st.global_cost < ctl.tracked_global;
+    const CandidateView v = candidates(cv, sh, A);
+    const std::uint32_t total = kArchive + A;
+    // groups of equal (cost, fingerprint); a fingerprint shared across costs,
+    // or by two different tours, sends the selection to the general path
+    for (std::uint32_t c = threadIdx.x; c < total; c += blockDim.x) {
+        std::uint16_t r = 0xffffu;
+        if (c >= kArchive || c < ctl.archive_size) {
+            r = (std::uint16_t)c;
+            const Fingerprint fc = v.id(c);
+            const long long cc = v.cost(c);
+            for (std::uint32_t q = 0; q < c; ++q) {
+                if (q < kArchive && q >= ctl.archive_size) continue;
+                if (!fp_equal(v.id(q), fc)) continue;
+                if (v.cost(q) == cc) { r = (std::uint16_t)q; break; }
+                sh.collision = 1;
+            }
+        }
+        sh.rep[c] = r;
+    }
+    __syncthreads();
+    for (std::uint32_t c = warp; c < total; c += warps) {
+        const std::uint32_t r = sh.rep[c];
+        if (r != 0xffffu && r != c && warp_canonical_compare(v.ref(c), v.ref(r), n, lane) != 0 && lane == 0)
+            sh.collision = 1;
+    }
+    __syncthreads();
     if (warp == 0) {
-        const CandidateView v{cv, ctl};
-        const std::uint32_t count = ref_archive_select(v, st, A, improved, n, lane, sh.excluded, sh.chosen);
+        const std::uint32_t count =
+            sh.collision ? ref_archive_select(v, st, A, improved, n, lane, sh.excluded, sh.chosen)
+                         : ref_archive_select_groups(v, st, A, improved, lane, sh.rep, sh.excluded, sh.chosen);
         if (lane == 0) {
             sh.count = count;
             for (std::uint32_t i = 0; i < count; ++i) {
                 sh.chosen_cost[i] = v.cost(sh.chosen[i]);
                 sh.chosen_id[i] = v.id(sh.chosen[i]);
             }
-            // feedback (update_feedback, control_ops.hpp:177-188)
-            double returned = 0, work = 0;
-            for (std::uint32_t a = 0; a < A; ++a) {
-                returned += (cv.ant_ids[2 * a] == ctl.active_id.first && cv.ant_ids[2 * a + 1] == ctl.active_id.second)
-                                ? 1.0 : 0.0;
-                if (P.ls_limit) work += (double)cv.ant_counts[3 * a + 1] / (double)P.ls_limit;
+        }
+    } else if (warp == 1) {
+        // feedback (update_feedback, control_ops.hpp:177-188), beside the
+        // selection: the LS work fractions summed in ant order
+        std::uint32_t returned = 0;
+        double work = 0;
+        for (std::uint32_t base = 0; base < A; base += 32) {
+            const std::uint32_t a = base + lane;
+            bool back = false;
+            double wa = 0.0;
+            if (a < A) {
+                back = fp_equal(v.id(kArchive + a), ctl.active_id);
+                if (P.ls_limit) wa = (double)cv.ant_counts[3 * a + 1] / (double)P.ls_limit;
             }
-            const float rf = (float)unit_clip(returned / (double)A), wf = (float)unit_clip(work / (double)A);
+            returned += __popc(__ballot_sync(kFull, back));
+            for (std::uint32_t j = 0; j < 32 && base + j < A; ++j) work += __shfl_sync(kFull, wa, j);
+        }
+        if (lane == 0) {
+            const float rf = (float)unit_clip((double)returned / (double)A), wf = (float)unit_clip(work / (double)A);
             ctl.return_rate += (rf - ctl.return_rate) * 0.0625f;
             ctl.ls_work += (wf - ctl.ls_work) * 0.0625f;
             if (improved) ctl.stagnant_batches = 0;
             else if (ctl.stagnant_batches != ~0ull) ++ctl.stagnant_batches;
             if (ctl.epoch_batches != ~0ull) ++ctl.epoch_batches;
-            const unsigned long long* best = cv.ant_ids + 2ull * st.iteration_best;
-            if (st.epoch_cost < ctl.tracked_epoch) ctl.epoch_id = {best[0], best[1]};
-            ctl.active_id = st.source_is_epoch ? ctl.epoch_id : Fingerprint{best[0], best[1]};
+            const Fingerprint best = v.id(kArchive + st.iteration_best);
+            if (st.epoch_cost < ctl.tracked_epoch) ctl.epoch_id = best;
+            ctl.active_id = st.source_is_epoch ? ctl.epoch_id : best;
             ctl.tracked_global = st.global_cost;
             ctl.tracked_epoch = st.epoch_cost;
         }
     }
     __syncthreads();
     // chosen tours into the other half of the archive buffer
-    const std::uint32_t side = ctl.side, next = side ^ 1u, count = sh.count;
-    const CandidateView v{cv, ctl};
+    const std::uint32_t next = ctl.side ^ 1u, count = sh.count;
     for (std::uint32_t i = threadIdx.x; i < count * n; i += blockDim.x) {
         const std::uint32_t slot = i / n, p = i % n;
         const node_t node = v.ref(sh.chosen[slot]).tour[p];
         node_t* dst = archive_tour(cv, next, slot);
         dst[p] = node;
         dst[cv.n_pad + node] = (node_t)p;
+        if (node == 0) sh.next_p0[slot] = p;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (std::uint32_t i = 0; i < kArchive; ++i) {
             ctl.archive_cost[i] = i < count ? sh.chosen_cost[i] : 0;
             ctl.archive_id[i] = i < count ? sh.chosen_id[i] : Fingerprint{0, 0};
+            ctl.archive_p0[i] = i < count ? sh.next_p0[i] : 0u;
         }
         ctl.archive_size = count;
         ctl.side = next;
@@ -791,40 +913,63 @@ __device__ void ref_update(const ColonyView& cv, const InstanceView& in, const C
 }
 
 // The decision before batch `batch` (build_control_features, score and
-// apply_control_action).  Called by the whole block; st is shared.
+// apply_control_action).  Called by the whole block; st and sh.ctl shared.
 __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyState& st, const ColonyParams& P,
-                           std::uint32_t colony, std::uint32_t colony_count, std::uint32_t batch, RefShared& sh) {
-    RefControl& ctl = *cv.control;
+                           std::uint32_t colony, std::uint32_t colony_count, std::uint32_t batch,
+                           std::uint32_t parent_p0, RefShared& sh) {
+    RefControl& ctl = sh.ctl;
     const std::uint32_t n = in.n, k = in.k;
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
     const std::uint32_t side = ctl.side, size = ctl.archive_size;
     if (warp == 0) {
         // alternative reference: the archive tour other than the active one
-        // that differs most from it on the sampled nodes (control_cpu.cpp:46-63)
-        const TourRef parent{cv.parent, nullptr, warp_find_zero(cv.parent, n, lane)};
+        // that differs most from it on the sampled nodes (control_cpu.cpp:46-63);
+        // each lane takes samples lane and lane + 32 of every archive tour
+        const TourRef parent{cv.parent, nullptr, parent_p0};
+        std::uint32_t x[2], ps[2], pp[2], missing[kArchive] = {0, 0, 0, 0};
+        bool have[2];
+        for (std::uint32_t h = 0; h < 2; ++h) {
+            have[h] = lane + 32 * h < in.sample_count;
+            x[h] = have[h] ? in.samples[lane + 32 * h] : 0u;
+        }
+        std::uint32_t pos[kArchive][2];
+        for (std::uint32_t h = 0; h < 2; ++h) {
+            const std::uint32_t nb = have[h] ? cv.parent_nbr[x[h]] : 0u;
+            ps[h] = nb & 0xffffu;
+            pp[h] = nb >> 16;
+#pragma unroll
+            for (std::uint32_t i = 0; i < kArchive; ++i)
+                pos[i][h] = have[h] && i < size ? archive_tour(cv, side, i)[cv.n_pad + x[h]] : 0u;
+        }
+#pragma unroll
+        for (std::uint32_t i = 0; i < kArchive; ++i) {
+            if (i >= size) continue;
+            const node_t* t = archive_tour(cv, side, i);
+            for (std::uint32_t h = 0; h < 2; ++h) {
+                if (!have[h]) continue;
+                const std::uint32_t px = pos[i][h];
+                const std::uint32_t cs = t[px + 1 == n ? 0 : px + 1], cp = t[px == 0 ? n - 1 : px - 1];
+                missing[i] += (cs != ps[h] && cs != pp[h]) + (cp != ps[h] && cp != pp[h]);
+            }
+        }
+#pragma unroll
+        for (std::uint32_t i = 0; i < kArchive; ++i)
+            for (int o = 16; o; o >>= 1) missing[i] += __shfl_xor_sync(kFull, missing[i], o);
         std::uint32_t alt = kArchive, largest = 0;
         for (std::uint32_t i = 0; i < size; ++i) {
-            const TourRef ri = archive_ref(cv, side, i);
+            const TourRef ri{archive_tour(cv, side, i), archive_tour(cv, side, i) + cv.n_pad, ctl.archive_p0[i]};
             if (fp_equal(ctl.archive_id[i], ctl.active_id) && warp_canonical_compare(ri, parent, n, lane) == 0)
                 continue;
-            std::uint32_t missing = 0;
-            for (std::uint32_t j = lane; j < in.sample_count; j += 32) {
-                const std::uint32_t x = in.samples[j], px = ri.pos[x];
-                const std::uint32_t cs = ri.tour[px + 1 == n ? 0 : px + 1], cp = ri.tour[px == 0 ? n - 1 : px - 1];
-                const std::uint32_t nb = cv.parent_nbr[x], ps = nb & 0xffffu, pp = nb >> 16;
-                missing += (cs != ps && cs != pp) + (cp != ps && cp != pp);
-            }
-            for (int o = 16; o; o >>= 1) missing += __shfl_xor_sync(kFull, missing, o);
             bool better_tie = false;
-            if (alt != kArchive && missing == largest) {
+            if (alt != kArchive && missing[i] == largest) {
                 const long long ci = ctl.archive_cost[i], ca = ctl.archive_cost[alt];
                 const Fingerprint fi = ctl.archive_id[i], fa = ctl.archive_id[alt];
+                const TourRef ra{archive_tour(cv, side, alt), archive_tour(cv, side, alt) + cv.n_pad,
+                                 ctl.archive_p0[alt]};
                 better_tie = ci < ca || (ci == ca && (fp_less(fi, fa) ||
-                                                      (fp_equal(fi, fa) &&
-                                                       warp_canonical_compare(ri, archive_ref(cv, side, alt), n,
-                                                                              lane) < 0)));
+                                                      (fp_equal(fi, fa) && warp_canonical_compare(ri, ra, n, lane) < 0)));
             }
-            if (alt == kArchive || missing > largest || better_tie) { alt = i; largest = missing; }
+            if (alt == kArchive || missing[i] > largest || better_tie) { alt = i; largest = missing[i]; }
         }
         if (lane == 0) {
             sh.alternative = alt;
@@ -835,80 +980,95 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
                                        : 0.0f;
             sh.difference = alt < kArchive ? (float)largest / (float)(2 * in.sample_count) : 0.0f;
             sh.mask = cv.action_mask & (alt < kArchive ? 0xFFFFFFFFu : 0xFFFFu);
+            sh.elapsed = (float)unit_clip((double)((unsigned long long)batch * P.ants) /
+                                          (double)((unsigned long long)P.total_iterations * P.ants));
+            const unsigned long long stag = ctl.stagnant_batches;
+            sh.stagnation = (float)(stag < 32 ? (double)stag / 32.0 : 1.0);
         }
     }
     __syncthreads();
     const std::uint32_t alt = sh.alternative, count = n < kRegionNodes ? n : kRegionNodes;
-    const double elapsed = (double)((unsigned long long)batch * P.ants) /
-                           (double)((unsigned long long)P.total_iterations * P.ants);
     for (std::uint32_t w = warp; w < 8; w += warps) {
         // start region (mode, region) and its 4 features (region_features,
-        // control_ops.hpp:192-214), contributions per node, summed in node order
+        // control_ops.hpp:192-214); lane 2i + s takes node i and its
+        // predecessor (s = 0) or successor (s = 1); sums in node order
         const std::uint32_t mode = w >> 2, region = w & 3u;
         const bool valid = mode == 0 || alt < kArchive;
         node_t* nodes = sh.regions[w];
-        const TourRef ref = mode == 0 ? TourRef{cv.parent, nullptr, 0} : archive_ref(cv, side, alt < kArchive ? alt : 0);
-        if (lane == 0) {
-            for (std::uint32_t i = 0; i < kRegionNodes; ++i) nodes[i] = 0;
-            if (valid) build_region(ref.tour, n, in.primary, k, cv.key, batch, mode, region, nodes);
+        const node_t* rtour = mode == 0 ? cv.parent : archive_tour(cv, side, alt < kArchive ? alt : 0);
+        if (valid) {
+            warp_build_region(rtour, n, in.primary, k, cv.key, batch, mode, region, nodes, lane);
+        } else {
+            if (lane < kRegionNodes) nodes[lane] = 0;
+            __syncwarp();
         }
-        __syncwarp();
         float regional[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (valid) {
-            double v0 = 0.0, v2 = 0.0, v3 = 0.0;
-            std::uint32_t v1 = 0, v4 = 0;
-            if (lane < count) {
-                const std::uint32_t x = nodes[lane];
-                std::uint32_t prev, next;
+            const std::uint32_t i = lane >> 1, s = lane & 1u;
+            const bool active = i < count;
+            double half = 0.0, strength_v = 0.0;
+            std::uint32_t dis = 0, disp = 0;
+            std::uint32_t xn = 0, y = 0;
+            if (active) {
+                xn = nodes[i];
                 if (mode == 0) {
-                    const std::uint32_t nb = cv.parent_nbr[x];
-                    next = nb & 0xffffu;
-                    prev = nb >> 16;
+                    const std::uint32_t nb = cv.parent_nbr[xn];
+                    y = s ? nb & 0xffffu : nb >> 16;
                 } else {
-                    const std::uint32_t px = ref.pos[x];
-                    next = ref.tour[px + 1 == n ? 0 : px + 1];
-                    prev = ref.tour[px == 0 ? n - 1 : px - 1];
+                    const std::uint32_t px = rtour[cv.n_pad + xn];
+                    y = s ? rtour[px + 1 == n ? 0 : px + 1] : rtour[px == 0 ? n - 1 : px - 1];
                 }
-                const double scale = in.local_scale[x] < in.scale_epsilon ? in.scale_epsilon : in.local_scale[x];
-                v0 = unit_clip(((0.5 * (double)euc2d(in.xy[x], in.xy[prev]) + 0.5 * (double)euc2d(in.xy[x], in.xy[next])) /
-                                    scale - 1) / 3);
-                const std::uint32_t nbs[2] = {prev, next};
-                double strength[2];
-                for (int s = 0; s < 2; ++s) {
-                    for (std::uint32_t j = 0; j < size; ++j) {
-                        const TourRef aj = archive_ref(cv, side, j);
-                        const std::uint32_t pj = aj.pos[x];
-                        const std::uint32_t sj = aj.tour[pj + 1 == n ? 0 : pj + 1], qj = aj.tour[pj == 0 ? n - 1 : pj - 1];
-                        v1 += sj != nbs[s] && qj != nbs[s];
-                    }
-                    double tau = (double)st.default_trail;
-                    for (std::uint32_t j = 0; j < k; ++j)
-                        if (in.primary[(size_t)x * k + j] == nbs[s]) { tau = (double)cv.trails[(size_t)x * k + j]; break; }
-                    const double lo = (double)st.tau_min, hi = (double)st.tau_max;
-                    strength[s] = lo == hi ? 1.0 : unit_clip((tau - lo) / (hi - lo));
-                    v4 += !has_node(nodes, count, nbs[s]);
+                std::uint32_t pj[kArchive];
+#pragma unroll
+                for (std::uint32_t j = 0; j < kArchive; ++j) pj[j] = j < size ? archive_tour(cv, side, j)[cv.n_pad + xn] : 0u;
+                const int2 a = in.xy[xn], b = in.xy[y];
+                half = 0.5 * (double)euc2d(a, b);
+                float tau = st.default_trail;
+                for (std::uint32_t t = 0; t < k; ++t)
+                    if (in.primary[(size_t)xn * k + t] == y) { tau = cv.trails[(size_t)xn * k + t]; break; }
+#pragma unroll
+                for (std::uint32_t j = 0; j < kArchive; ++j) {
+                    if (j >= size) continue;
+                    const node_t* t = archive_tour(cv, side, j);
+                    const std::uint32_t sj = t[pj[j] + 1 == n ? 0 : pj[j] + 1], qj = t[pj[j] == 0 ? n - 1 : pj[j] - 1];
+                    dis += sj != y && qj != y;
                 }
-                v2 = strength[0];
-                v3 = strength[1];
+                const double lo = (double)st.tau_min, hi = (double)st.tau_max;
+                strength_v = lo == hi ? 1.0 : unit_clip(((double)tau - lo) / (hi - lo));
+                disp = !has_node(nodes, count, y);
             }
-            double excess = 0, disagreement = 0, strength = 0, dispersion = 0;
-            for (std::uint32_t i = 0; i < count; ++i) {
-                excess += __shfl_sync(kFull, v0, i);
-                disagreement += (double)__shfl_sync(kFull, v1, i);
-                strength += __shfl_sync(kFull, v2, i);
-                strength += __shfl_sync(kFull, v3, i);
-                dispersion += (double)__shfl_sync(kFull, v4, i);
+            const double other = __shfl_down_sync(kFull, half, 1);
+            double ex = 0.0;
+            if (active && s == 0) {
+                const double scale = in.local_scale[xn] < in.scale_epsilon ? in.scale_epsilon : in.local_scale[xn];
+                ex = unit_clip(((half + other) / scale - 1) / 3);
             }
-            regional[0] = (float)(excess / count);
-            regional[1] = (float)(disagreement / (double)(2 * count * size));
-            regional[2] = (float)(strength / (double)(2 * count));
-            regional[3] = (float)(dispersion / (double)(2 * count));
+            double excess = 0, strength = 0;
+            for (std::uint32_t q = 0; q < count; ++q) {
+                excess += __shfl_sync(kFull, ex, 2 * q);
+                strength += __shfl_sync(kFull, strength_v, 2 * q);
+                strength += __shfl_sync(kFull, strength_v, 2 * q + 1);
+            }
+            for (int o = 16; o; o >>= 1) {
+                dis += __shfl_xor_sync(kFull, dis, o);
+                disp += __shfl_xor_sync(kFull, disp, o);
+            }
+            // a ratio of small integers rounds to the same float directly as
+            // through double; division by 16 or 32 is an exact scaling
+            if (count == kRegionNodes) {
+                regional[0] = (float)(excess * (1.0 / kRegionNodes));
+                regional[2] = (float)(strength * (0.5 / kRegionNodes));
+            } else {
+                regional[0] = (float)(excess / count);
+                regional[2] = (float)(strength / (double)(2 * count));
+            }
+            regional[1] = __fdiv_rn((float)dis, (float)(2 * count * size));
+            regional[3] = __fdiv_rn((float)disp, (float)(2 * count));
         }
         if (lane < 4) {
             const std::uint32_t level = lane, a = mode * 16 + region * 4 + level;
-            const unsigned long long stag = ctl.stagnant_batches;
-            sh.feat[0][a] = (float)unit_clip(elapsed);
-            sh.feat[1][a] = (float)(stag < 32 ? (double)stag / 32.0 : 1.0);
+            sh.feat[0][a] = sh.elapsed;
+            sh.feat[1][a] = sh.stagnation;
             sh.feat[2][a] = ctl.return_rate;
             sh.feat[3][a] = ctl.ls_work;
             sh.feat[4][a] = (float)mode;
@@ -953,8 +1113,6 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
             ctl.alternative = alt;
             ctl.legal_mask = mask;
             ctl.start_count = count;
-            const node_t* list = sh.regions[(chosen >> 4) * 4 + ((chosen >> 2) & 3u)];
-            for (std::uint32_t i = 0; i < kRegionNodes; ++i) ctl.start_nodes[i] = list[i];
             if (chosen >= 16) {
                 // restart from the alternative reference (control_state.cuh:302-336)
                 st.epoch_cost = st.parent_cost = ctl.archive_cost[alt];
@@ -969,6 +1127,8 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
                 if (ctl.restarts != ~0ull) ++ctl.restarts;
             }
         }
+        if (lane < kRegionNodes)
+            ctl.start_nodes[lane] = sh.regions[(chosen >> 4) * 4 + ((chosen >> 2) & 3u)][lane];
     }
     __syncthreads();
     if (sh.action >= 16) {
@@ -985,6 +1145,23 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
         }
     }
     __syncthreads();
+}
+
+// Fingerprints (and node-0 positions) of every ant's tour of a batch, one
+// warp per ant over all colonies (fingerprint_ants, control_state.cuh:45-64).
+__global__ void __launch_bounds__(256) fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants,
+                                                          std::uint32_t colony_count) {
+    const std::uint32_t job = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (job >= ants * colony_count) return;
+    const std::uint32_t colony = job / ants, ant = job % ants;
+    const ColonyView& cv = colonies[colony];
+    std::uint32_t p0;
+    const Fingerprint f = warp_fingerprint(cv.ant_tours + (size_t)ant * cv.n_pad, cv.n, lane, p0);
+    if (lane == 0) {
+        cv.ant_ids[2 * ant] = f.first;
+        cv.ant_ids[2 * ant + 1] = f.second;
+        cv.ant_p0[ant] = p0;
+    }
 }
 
 __global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
@@ -1029,23 +1206,29 @@ __global__ void colony_init_kernel(const InstanceView* instances, const ColonyVi
             a0[i] = in.initial[i];
             a0[cv.n_pad + in.initial[i]] = (node_t)i;
         }
+        __shared__ std::uint32_t s_p0;
         if (threadIdx.x < 32) {
             std::uint32_t p0;
             const Fingerprint f = warp_fingerprint(in.initial, n, threadIdx.x, p0);
             if (threadIdx.x == 0) {
+                s_p0 = p0;
                 RefControl ctl{};
                 ctl.archive_size = 1;
                 ctl.archive_cost[0] = in.initial_cost;
                 ctl.archive_id[0] = f;
+                ctl.archive_p0[0] = p0;
                 ctl.active_id = ctl.epoch_id = f;
                 ctl.tracked_global = ctl.tracked_epoch = in.initial_cost;
                 ctl.alternative = kArchive;
-                *cv.control = ctl;
+                s_ref.ctl = ctl;
             }
         }
         __syncthreads();
-        ref_decide(cv, in, s_st, P, c, colony_count, 0, s_ref);
-        if (threadIdx.x == 0) states[c] = s_st;
+        ref_decide(cv, in, s_st, P, c, colony_count, 0, s_p0, s_ref);
+        if (threadIdx.x == 0) {
+            states[c] = s_st;
+            *cv.control = s_ref.ctl;
+        }
     }
 }
 
@@ -1081,7 +1264,7 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
     __shared__ float s_tmin, s_tmax, s_inc, s_feat[7];
     __shared__ long long s_sum_final, s_sum_cons, s_best_cost;
     __shared__ unsigned long long s_steps, s_evals;
-    __shared__ std::uint32_t s_used_mne;
+    __shared__ std::uint32_t s_used_mne, s_parent_p0;
 
     // iteration best: first strict minimum over ants (costs are >= 0); work counters
     unsigned long long best = ~0ull, steps = 0, evals = 0, moved = 0, sum_final = 0, sum_cons = 0;
@@ -1145,7 +1328,9 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
         const node_t v = best_tour[i];
         if (ie) cv.epoch[i] = v;
         if (ig) cv.global[i] = v;
-        cv.parent[i] = fe ? cv.epoch[i] : v;
+        const node_t p = fe ? cv.epoch[i] : v;
+        cv.parent[i] = p;
+        if (p == 0) s_parent_p0 = i;
     }
     __syncthreads();
     for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x)
@@ -1159,13 +1344,17 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
         // the 12-feature controller: the trace row holds the action this
         // batch ran with; archive and feedback; the next batch's decision
         __shared__ RefShared s_ref;
+        if (threadIdx.x == 0) {
+            s_ref.ctl = *cv.control;
+            if (trace && s_st.iteration < trace_cap)
+                write_trace(trace[(size_t)s_st.iteration * colony_count + c], s_st, s_used_mne, s_st.action, s_steps,
+                            s_evals);
+        }
         __syncthreads();
-        if (threadIdx.x == 0 && trace && s_st.iteration < trace_cap)
-            write_trace(trace[(size_t)s_st.iteration * colony_count + c], s_st, s_used_mne, s_st.action, s_steps,
-                        s_evals);
         ref_update(cv, in, s_st, P, s_ref);
         if (s_st.iteration + 1 < P.total_iterations)
-            ref_decide(cv, in, s_st, P, c, colony_count, s_st.iteration + 1, s_ref);
+            ref_decide(cv, in, s_st, P, c, colony_count, s_st.iteration + 1, s_parent_p0, s_ref);
+        if (threadIdx.x == 0) *cv.control = s_ref.ctl;
     } else if (P.controlled && cv.program) {
         // mean normalised entropy of the trail rows (exact integer sum)
         __syncthreads();

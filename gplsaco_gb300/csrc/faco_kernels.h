@@ -44,6 +44,7 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
 
 __global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
                                    ColonyParams P, std::uint32_t colony_count);
+__global__ void fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants, std::uint32_t colony_count);
 __global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,
                                      ColonyState* states, ColonyParams P, TraceRow* trace,
                                      std::uint32_t colony_count, std::uint32_t trace_cap);
