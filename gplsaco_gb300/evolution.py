@@ -12,7 +12,9 @@ directly on the postfix IR (DEAP is not a dependency here), and adds
 `evolve`, which evaluates each generation as one population batch on the
 engine (FacoBatchEngine.evaluate_population_evaluations).
 
-Programs are IR dicts of feature spec 3 (the engine's controller features).
+Programs are IR dicts of feature spec 3 (the engine's compact controller)
+or, with EvolutionSettings(feature_spec_id=2), of the reference's 12-feature
+controller.
 """
 from __future__ import annotations
 
@@ -25,7 +27,7 @@ import numpy as np
 
 from .programs import EXTENDED_OPS, REFERENCE_OPS
 
-FEATURES = 10                     # feature spec 3: 7 colony features + 3 action descriptors
+FEATURES = {2: 12, 3: 10}         # terminals of feature spec 2 (the reference's) and 3 (7 + 3 descriptors)
 
 
 @dataclass(frozen=True)
@@ -43,17 +45,19 @@ class EvolutionSettings:
     mutation_depth_min: int = 0
     mutation_depth_max: int = 2
     extended: bool = False        # the extended grammar (numeric spec 2) instead of the reference's
+    feature_spec_id: int = 3      # 2: the reference's 12-feature controller; 3: the engine's
 
     def __post_init__(self) -> None:
         ints = {k: v for k, v in asdict(self).items()
-                if k not in ("crossover_probability", "mutation_probability", "extended")}
+                if k not in ("crossover_probability", "mutation_probability", "extended", "feature_spec_id")}
         if any(type(v) is not int for v in ints.values()):
             raise ValueError("evolution counts and tree limits must be integers")
         if not (2 <= self.population and 1 <= self.generations and 0 <= self.elites < self.population
                 and 1 <= self.tournament_size
                 and 0 <= self.initial_depth_min <= self.initial_depth_max <= self.max_depth <= 5
                 and 0 <= self.mutation_depth_min <= self.mutation_depth_max <= self.max_depth
-                and 1 <= self.max_nodes <= 63 and type(self.extended) is bool):
+                and 1 <= self.max_nodes <= 63 and type(self.extended) is bool
+                and type(self.feature_spec_id) is int and self.feature_spec_id in FEATURES):
             raise ValueError("evolution settings out of range")
         for p in (self.crossover_probability, self.mutation_probability):
             if type(p) not in (int, float) or not math.isfinite(p) or not 0 <= p <= 1:
@@ -96,24 +100,25 @@ def _height(tree, ops) -> int:
     return stack[0]
 
 
-def _grow(rng: random.Random, depth: int, height: int, ops: dict, full: bool, min_depth: int = 0) -> list:
+def _grow(rng: random.Random, depth: int, height: int, ops: dict, full: bool, min_depth: int = 0,
+          features: int = FEATURES[3]) -> list:
     """DEAP's genFull / genGrow: a leaf at the target height, or (grow only,
     from `min_depth` on) with the terminal ratio; terminals are the features
     and one ephemeral constant uniform in [-1, 1] (FP32)."""
-    terminals = FEATURES + 1
+    terminals = features + 1
     if depth == height or (not full and depth >= min_depth and rng.random() < terminals / (terminals + len(ops))):
         pick = rng.randrange(terminals)
-        if pick == FEATURES:
+        if pick == features:
             return [(1, struct.unpack("<f", struct.pack("<f", rng.uniform(-1.0, 1.0)))[0])]
         return [(0, pick)]
     op = rng.choice(sorted(ops))
     out = []
     for _ in range(ops[op]):
-        out += _grow(rng, depth + 1, height, ops, full, min_depth)
+        out += _grow(rng, depth + 1, height, ops, full, min_depth, features)
     return out + [(op, None)]
 
 
-def to_ir(tree, extended: bool) -> dict:
+def to_ir(tree, extended: bool, feature_spec_id: int = 3) -> dict:
     constants = [c for op, c in tree if op == 1]
     operands, ci = [], 0
     for op, arg in tree:
@@ -122,7 +127,7 @@ def to_ir(tree, extended: bool) -> dict:
             ci += 1
         else:
             operands.append(0 if arg is None else arg)
-    return dict(ir_version=1, numeric_spec_id=2 if extended else 1, feature_spec_id=3,
+    return dict(ir_version=1, numeric_spec_id=2 if extended else 1, feature_spec_id=feature_spec_id,
                 opcode=[op for op, _ in tree], operand=operands,
                 constant_bits=[struct.unpack("<I", struct.pack("<f", c))[0] for c in constants])
 
@@ -176,7 +181,8 @@ class Evolution:
         i = self.rng.randrange(len(tree))
         s = _subtree_start(tree, i, self.ops)
         height = self.rng.randint(self.settings.mutation_depth_min, self.settings.mutation_depth_max)
-        return tree[:s] + _grow(self.rng, 0, height, self.ops, True) + tree[i + 1:]
+        return tree[:s] + _grow(self.rng, 0, height, self.ops, True,
+                                features=FEATURES[self.settings.feature_spec_id]) + tree[i + 1:]
 
     def _limited(self, children, parents):
         """Static limit: an offspring over the depth or size limit is replaced
@@ -200,7 +206,8 @@ class Evolution:
             # genHalfAndHalf: full or grow with equal odds, height in [min, max]
             height = self.rng.randint(s.initial_depth_min, s.initial_depth_max)
             full = self.rng.random() < 0.5
-            self.population.append(_grow(self.rng, 0, height, init_ops, full, s.initial_depth_min))
+            self.population.append(_grow(self.rng, 0, height, init_ops, full, s.initial_depth_min,
+                                         FEATURES[s.feature_spec_id]))
         self._reset_ids()
 
     def _reset_ids(self) -> None:
@@ -208,7 +215,7 @@ class Evolution:
         self.fitness = [None] * len(self.population)
 
     def programs(self) -> list[dict]:
-        return [to_ir(tree, self.settings.extended) for tree in self.population]
+        return [to_ir(tree, self.settings.extended, self.settings.feature_spec_id) for tree in self.population]
 
     def begin_panel(self, panel_id: str) -> None:
         if not self.population or self.panel_id is not None or not panel_id:
@@ -239,7 +246,7 @@ class Evolution:
             raise ValueError("this generation is already archived")
         best = min(range(len(self.population)), key=self._rank)
         result = {"generation": self.generation, "panel_id": self.panel_id,
-                  "program": to_ir(self.population[best], self.settings.extended),
+                  "program": to_ir(self.population[best], self.settings.extended, self.settings.feature_spec_id),
                   "fitness": self.fitness[best] if math.isfinite(self.fitness[best]) else None}
         self.winners.append(result)
         return result

@@ -502,10 +502,12 @@ def test_snapshot_resume_continues_bit_for_bit(api):
         e.close()
 
 
-def test_gp_evolution_on_the_engine(api):
+@pytest.mark.parametrize("spec", [3, 2])
+def test_gp_evolution_on_the_engine(api, spec):
     """A short evolution (8 programs, 3 generations) evaluated as population
     batches on the engine: every generation's programs run, the elites carry
-    the best fitness forward (same panel and seeds, so re-evaluation is exact)."""
+    the best fitness forward (same panel and seeds, so re-evaluation is exact)
+    -- with the engine's controller features and the reference's 12."""
     from gplsaco_gb300 import evolution as ev
     n, ants = 60, 8
     xy = _cases.uniform_instance(n, seed=321)
@@ -514,7 +516,8 @@ def test_gp_evolution_on_the_engine(api):
     info = engine.register_problem(5, xy.astype(np.float64))
     keys, seeds = np.full(2, 5, np.uint64), np.array([1, 2], np.uint64)
     refs = np.full(2, float(info["initial_cost"]))
-    evo = ev.evolve(engine, keys, seeds, refs, 6, ev.EvolutionSettings(population=8, generations=3, elites=2), 9)
+    evo = ev.evolve(engine, keys, seeds, refs, 6,
+                    ev.EvolutionSettings(population=8, generations=3, elites=2, feature_spec_id=spec), 9)
     fitness = [w["fitness"] for w in evo.winners]
     assert len(fitness) == 3 and all(0 < f <= 1.0 for f in fitness)
     assert fitness[1] <= fitness[0] and fitness[2] <= fitness[1]
