@@ -38,7 +38,8 @@ class Settings(C.Structure):
                 ("ls_width", C.c_uint32), ("beta", C.c_double), ("retention", C.c_double),
                 ("p_best", C.c_double), ("epoch_source_probability", C.c_double),
                 ("ls_evaluation_limit", C.c_uint64), ("initial_ls_evaluation_limit", C.c_uint64),
-                ("ls_mode", C.c_uint32), ("autotune", C.c_uint32), ("workspace", C.c_uint32)]
+                ("ls_mode", C.c_uint32), ("autotune", C.c_uint32), ("workspace", C.c_uint32),
+                ("force_fingerprint_collisions", C.c_uint32)]
 
 
 class Registration(C.Structure):

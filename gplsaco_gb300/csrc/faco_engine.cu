@@ -362,6 +362,7 @@ void faco_default_settings(faco_settings* s) {
     s->ls_mode = FACO_LS_TWO_OPT;
     s->autotune = 1;
     s->workspace = FACO_WORKSPACE_AUTO;
+    s->force_fingerprint_collisions = 0;
 }
 
 int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_settings* settings, int device,
@@ -379,6 +380,7 @@ int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_setting
         require(c.primary_width <= 32 && c.ls_width <= 32, "primary and LS widths are limited to 32 (one warp)");
         require(c.ls_mode == FACO_LS_TWO_OPT || c.ls_mode == FACO_LS_TWO_OPT_OR_OPT, "unknown local-search mode");
         require(c.workspace <= FACO_WORKSPACE_GLOBAL, "unknown ant workspace placement");
+        require(c.force_fingerprint_collisions <= 1, "force_fingerprint_collisions must be 0 or 1");
         auto e = std::make_unique<faco_engine>();
         e->settings = c;
         e->dimension = dimension;
@@ -580,7 +582,8 @@ void enqueue_update(faco_engine* e, cudaStream_t st) {
     auto& v = e->eval;
     if (v.P.ref_control) {
         const std::uint32_t warps = v.count * v.P.ants;
-        faco::fingerprint_kernel<<<(warps + 7) / 8, 256, 0, st>>>(e->colonies.get(), v.P.ants, v.count);
+        faco::fingerprint_kernel<<<(warps + 7) / 8, 256, 0, st>>>(e->colonies.get(), v.P.ants, v.count,
+                                                                 v.P.zero_fingerprints);
     }
     faco::colony_update_kernel<<<v.count, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
                                                          v.P, v.trace_cap ? e->trace.get() : nullptr, v.count,
@@ -939,6 +942,7 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.P.total_iterations = std::max<std::uint32_t>(1, control.total_iterations);
     v.P.log2k = faco::host_log2(static_cast<float>(k_common));
     v.P.ref_control = spec == 2;
+    v.P.zero_fingerprints = e->settings.force_fingerprint_collisions;
     v.P.ls_limit = e->settings.ls_evaluation_limit;
     if (control.n_decisions) {
         v.P.capture = faco::DecisionCapture{e->decision_points.get(), control.n_decisions, e->decision_features.get(),
@@ -1148,7 +1152,8 @@ std::uint64_t fnv1a(const void* data, std::size_t bytes, std::uint64_t h = 14695
 // Everything in the settings that changes the search after registration.
 std::uint64_t settings_digest(const faco_settings& c, std::uint32_t ants) {
     std::uint64_t h = fnv1a(&ants, sizeof ants);
-    const std::uint32_t u[4] = {c.primary_width, c.backup_width, c.ls_width, c.ls_mode};
+    const std::uint32_t u[5] = {c.primary_width, c.backup_width, c.ls_width, c.ls_mode,
+                                c.force_fingerprint_collisions};
     const double d[4] = {c.beta, c.retention, c.p_best, c.epoch_source_probability};
     h = fnv1a(u, sizeof u, h);
     h = fnv1a(d, sizeof d, h);

@@ -1148,9 +1148,10 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
 }
 
 // Fingerprints (and node-0 positions) of every ant's tour of a batch, one
-// warp per ant over all colonies (fingerprint_ants, control_state.cuh:45-64).
+// warp per ant over all colonies (fingerprint_ants, control_state.cuh:45-64);
+// `zero` forces every fingerprint to 0 (the collision diagnostic).
 __global__ void __launch_bounds__(256) fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants,
-                                                          std::uint32_t colony_count) {
+                                                          std::uint32_t colony_count, std::uint32_t zero) {
     const std::uint32_t job = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (job >= ants * colony_count) return;
     const std::uint32_t colony = job / ants, ant = job % ants;
@@ -1158,8 +1159,8 @@ __global__ void __launch_bounds__(256) fingerprint_kernel(const ColonyView* colo
     std::uint32_t p0;
     const Fingerprint f = warp_fingerprint(cv.ant_tours + (size_t)ant * cv.n_pad, cv.n, lane, p0);
     if (lane == 0) {
-        cv.ant_ids[2 * ant] = f.first;
-        cv.ant_ids[2 * ant + 1] = f.second;
+        cv.ant_ids[2 * ant] = zero ? 0ull : f.first;
+        cv.ant_ids[2 * ant + 1] = zero ? 0ull : f.second;
         cv.ant_p0[ant] = p0;
     }
 }
@@ -1209,7 +1210,8 @@ __global__ void colony_init_kernel(const InstanceView* instances, const ColonyVi
         __shared__ std::uint32_t s_p0;
         if (threadIdx.x < 32) {
             std::uint32_t p0;
-            const Fingerprint f = warp_fingerprint(in.initial, n, threadIdx.x, p0);
+            Fingerprint f = warp_fingerprint(in.initial, n, threadIdx.x, p0);
+            if (P.zero_fingerprints) f = Fingerprint{0, 0};
             if (threadIdx.x == 0) {
                 s_p0 = p0;
                 RefControl ctl{};

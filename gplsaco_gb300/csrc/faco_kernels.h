@@ -25,6 +25,7 @@ struct ColonyParams {
     std::uint32_t total_iterations;  // T of the evaluation (iteration-fraction feature)
     float log2k;                     // log2(k) by the engine's own log2
     std::uint32_t ref_control;       // 1: the 12-feature controller (feature spec 2)
+    std::uint32_t zero_fingerprints; // diagnostic: every tour fingerprint 0 (forced collisions)
     unsigned long long ls_limit;     // LS evaluation budget per ant (LS-work feedback)
     DecisionCapture capture;         // decisions to record (count 0: none)
 };
@@ -44,7 +45,8 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
 
 __global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
                                    ColonyParams P, std::uint32_t colony_count);
-__global__ void fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants, std::uint32_t colony_count);
+__global__ void fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants, std::uint32_t colony_count,
+                                   std::uint32_t zero);
 __global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,
                                      ColonyState* states, ColonyParams P, TraceRow* trace,
                                      std::uint32_t colony_count, std::uint32_t trace_cap);

@@ -43,11 +43,13 @@ class FixedFacoSettings:
     ls_mode: int = _lib.FACO_LS_TWO_OPT
     autotune: int = 1
     workspace: int = 0      # 0 auto, 1 shared memory, 2 global memory (ant tour/inverse placement)
+    force_fingerprint_collisions: int = 0   # diagnostic: all 12-feature-controller fingerprints 0
 
     def to_c(self) -> _lib.Settings:
         s = _lib.Settings()
         for name in ("ants", "primary_width", "backup_width", "ls_width", "ls_evaluation_limit",
-                     "initial_ls_evaluation_limit", "ls_mode", "autotune", "workspace"):
+                     "initial_ls_evaluation_limit", "ls_mode", "autotune", "workspace",
+                     "force_fingerprint_collisions"):
             setattr(s, name, _exact_int(getattr(self, name), name))
         for name in ("beta", "retention", "p_best", "epoch_source_probability"):
             value = getattr(self, name)

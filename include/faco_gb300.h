@@ -53,6 +53,9 @@ typedef struct faco_settings {
     uint32_t ls_mode; /* FACO_LS_* */
     uint32_t autotune; /* 1: pick ants per block (and workspace placement) per size class by timing */
     uint32_t workspace; /* FACO_WORKSPACE_*: where an ant keeps its tour and inverse */
+    uint32_t force_fingerprint_collisions; /* diagnostic (batch_engine.hpp:66): every tour fingerprint
+                                              of the 12-feature controller is 0, so its archive
+                                              compares whole tours; 0 in production */
 } faco_settings;
 
 void faco_default_settings(faco_settings* s);

@@ -218,13 +218,16 @@ int orc_archive_update(orc_archive_t* ar, const uint32_t* global_tour, int64_t g
         const uint32_t* t = cand_tours + (size_t)a * n;
         uint32_t* p = cand_pos + (size_t)a * n;
         for (uint32_t i = 0; i < n; ++i) p[t[i]] = i;
-        pool_entry_t e = {t, p, cand_costs[a], orc_fingerprint(t, n), count};
+        const orc_fp_t zero = {0, 0};
+        pool_entry_t e = {t, p, cand_costs[a], ar->zero_ids ? zero : orc_fingerprint(t, n), count};
         pool[count] = e;
     }
     g_sort_n = n;
     qsort(pool, total, sizeof(pool_entry_t), pool_cmp);
     pool_entry_t chosen[ORC_ARCHIVE_CAPACITY];
-    const pool_entry_t g = {global_tour, gpos, global_cost, orc_fingerprint(global_tour, n), 0};
+    const orc_fp_t zero_id = {0, 0};
+    const pool_entry_t g = {global_tour, gpos, global_cost,
+                            ar->zero_ids ? zero_id : orc_fingerprint(global_tour, n), 0};
     chosen[0] = g;
     uint32_t used = 1;
     const double limit = (double)global_cost * (1 + ORC_ARCHIVE_BAND);

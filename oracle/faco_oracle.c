@@ -755,7 +755,7 @@ typedef struct {
 } ctl2_t;
 
 static int ctl2_init(ctl2_t* t, uint32_t n, const int32_t* xy, const uint32_t* primary, uint32_t k,
-                     const uint32_t* initial, int64_t initial_cost, uint64_t instance_key) {
+                     const uint32_t* initial, int64_t initial_cost, uint64_t instance_key, uint32_t zero) {
     (void)primary;
     t->local_scale = (double*)malloc(sizeof(double) * n);
     t->trails64 = (double*)malloc(sizeof(double) * (size_t)n * k);
@@ -770,7 +770,8 @@ static int ctl2_init(ctl2_t* t, uint32_t n, const int32_t* xy, const uint32_t* p
     memcpy(t->archive.tours, initial, sizeof(uint32_t) * n);
     for (uint32_t i = 0; i < n; ++i) t->archive.pos[initial[i]] = i;
     t->archive.cost[0] = initial_cost;
-    t->archive.id[0] = orc_fingerprint(initial, n);
+    t->archive.zero_ids = zero;
+    t->archive.id[0] = zero ? (orc_fp_t){0, 0} : orc_fingerprint(initial, n);
     t->active_id = t->epoch_id = t->archive.id[0];
     t->tracked_global = t->tracked_epoch = t->parent_cost = initial_cost;
     return 0;
@@ -831,7 +832,7 @@ static int ctl2_update(ctl2_t* t, uint32_t n, const uint32_t* tours, const orc_a
         if (!t->ids || !t->costs) return -1;
     }
     for (uint32_t a = 0; a < A; ++a) {
-        t->ids[a] = orc_fingerprint(tours + (size_t)a * n, n);
+        t->ids[a] = t->archive.zero_ids ? (orc_fp_t){0, 0} : orc_fingerprint(tours + (size_t)a * n, n);
         t->costs[a] = infos[a].final_cost;
     }
     const int improved = global_cost < t->tracked_global;
@@ -905,7 +906,8 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     uint32_t start_list[ORC_REGION_CAPACITY], start_count = 0;
     int32_t used_action = -1;
     uint32_t cursor = 0;
-    if (spec2 && ctl2_init(&ctl, n, xy, primary, k, initial, initial_cost, control ? control->instance_key : 0) != 0)
+    if (spec2 && ctl2_init(&ctl, n, xy, primary, k, initial, initial_cost, control ? control->instance_key : 0,
+                           control ? control->force_collisions : 0) != 0)
         return -1;
     for (uint32_t batch = 0; batch < iterations; ++batch) {
         if (spec2) {

@@ -167,6 +167,7 @@ typedef struct {
     uint32_t* pos;
     int64_t cost[ORC_ARCHIVE_CAPACITY];
     orc_fp_t id[ORC_ARCHIVE_CAPACITY];
+    uint32_t zero_ids;    /* forced collisions: every fingerprint is 0 */
 } orc_archive_t;
 
 /* Everything one decision reads. */
@@ -229,6 +230,7 @@ typedef struct {
     int32_t* actions;      /* [count] */
     uint32_t archive_size; /* out */
     orc_feedback_t feedback; /* out */
+    uint32_t force_collisions; /* every tour fingerprint 0 (batch_engine.hpp:66) */
 } orc_control_io_t;
 
 /* ---- a whole plain-FACO colony run in engine arithmetic ------------------ */

@@ -101,7 +101,7 @@ class Feedback(C.Structure):
 
 class Archive(C.Structure):
     _fields_ = [("n", C.c_uint32), ("size", C.c_uint32), ("tours", C.c_void_p), ("pos", C.c_void_p),
-                ("cost", C.c_int64 * 4), ("id", Fp * 4)]
+                ("cost", C.c_int64 * 4), ("id", Fp * 4), ("zero_ids", C.c_uint32)]
 
 
 class ControlIn(C.Structure):
@@ -117,7 +117,7 @@ class ControlIn(C.Structure):
 class ControlIO(C.Structure):
     _fields_ = [("instance_key", C.c_uint64), ("points", C.c_void_p), ("count", C.c_uint32),
                 ("features", C.c_void_p), ("scores", C.c_void_p), ("masks", C.c_void_p), ("actions", C.c_void_p),
-                ("archive_size", C.c_uint32), ("feedback", Feedback)]
+                ("archive_size", C.c_uint32), ("feedback", Feedback), ("force_collisions", C.c_uint32)]
 
 
 _lib = None
@@ -336,7 +336,8 @@ def prepare(xy, k, b, w, initial_ls_limit=100000):
 
 def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, retention=0.98, p_best=0.1,
                epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True, ls_mode=0,
-               program=None, mask=0xFFFFFFFF, total_iterations=None, instance_key=0, decision_iterations=()):
+               program=None, mask=0xFFFFFFFF, total_iterations=None, instance_key=0, decision_iterations=(),
+               force_collisions=False):
     """One colony run.  A program (or controller) of feature spec 2 runs the
     reference's 12-feature controller; `instance_key` seeds its sample nodes
     and `decision_iterations` (1-based) capture its decisions, returned under
@@ -356,6 +357,7 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
                actions=np.zeros(max(points.size, 1), np.int32))
     io = ControlIO(instance_key, points.ctypes.data, points.size, dec["features"].ctypes.data,
                    dec["scores"].ctypes.data, dec["masks"].ctypes.data, dec["actions"].ctypes.data)
+    io.force_collisions = int(bool(force_collisions))
     rc = lib().orc_run_colony(n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
                               np.ascontiguousarray(prep["ls"], dtype=np.uint32),
                               np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),

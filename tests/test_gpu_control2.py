@@ -151,3 +151,36 @@ def test_spec2_snapshot_resume_and_refusals(api):
         a.evaluate_program_evaluations(keys, seeds, ants * 4, program, decision_iterations=[2, 2])
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("grid", [False, True])
+def test_spec2_forced_fingerprint_collisions_match_oracle(api, oracle, grid):
+    """With every fingerprint forced to 0 (batch_engine.hpp:66) the archive
+    orders and de-duplicates tours by full canonical comparison -- the path
+    real runs take only on a fingerprint collision.  On a 12 x 12 grid many
+    distinct tours share a length.  Tours, traces, feedback and decisions
+    equal the oracle's forced run."""
+    n, ants, iterations = 60, 8, 12
+    rng = np.random.default_rng(91 + grid)
+    xy = (rng.integers(0, 12, (n, 2)) if grid else _cases.uniform_instance(n, seed=5)).astype(np.int32)
+    settings = _settings(api, ants, force_fingerprint_collisions=1)
+    engine = api.FacoBatchEngine(n, 2, settings)
+    engine.register_problem(9, xy.astype(np.float64))
+    prep = oracle.prepare(xy, 16, 43, 20)
+    keys, seeds = np.full(2, 9, np.uint64), np.array([5, 6], np.uint64)
+    points = [1, 4, 8, 12]
+    for program in (_programs.random_program(rng, features=12, feature_spec_id=2), _always_restart()):
+        res = engine.evaluate_program_evaluations(keys, seeds, ants * iterations, program, trace=True,
+                                                  decision_iterations=points)
+        for c in range(2):
+            key = oracle.lib().orc_colony_key(int(seeds[c]), 9)
+            ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=43, w=20, mne=8, iterations=iterations, key=key,
+                                    retention=0.9, program=program, total_iterations=iterations, instance_key=9,
+                                    decision_iterations=points, force_collisions=True)
+            _check_colony(res, c, ref, iterations, ("forced", grid, c))
+            for d, want in enumerate(ref["decisions"]):
+                got = res["decisions"][d * 2 + c]
+                assert got["legal_mask"] == want["legal_mask"] and got["action"] == want["action"]
+                assert np.array_equal(np.asarray(got["features"], np.float32).view(np.uint32),
+                                      want["features"].view(np.uint32))
+    engine.close()
