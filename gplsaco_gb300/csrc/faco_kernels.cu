@@ -147,9 +147,18 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         const std::uint32_t k = in.k, b = in.b;
         const unsigned long long loop_cap = 2ull * n + 2;
         unsigned long long guard = 0;
+        // the construction draws of 32 consecutive steps at a time, lane i
+        // holding step draw_base + i (the same counters as one draw per step)
+        std::uint32_t draw_base = 0x80000000u, draw_hi = 0, draw_lo = 0;   // steps < 2^16: first step refreshes
         while (r.mne < target && r.steps + 1 < n) {
             if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
             const std::uint32_t step = r.steps + 1;
+            if (kEngine && step - draw_base >= 32u) {
+                draw_base = step;
+                const uint4v rb = philox4x32(step + lane, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+                draw_hi = rb.x;
+                draw_lo = rb.y;
+            }
             // loads that depend only on `current`, issued first
             const std::uint32_t pnbr = __ldg(parent_nbr + current);
             std::uint32_t cand = n;
@@ -166,9 +175,8 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                 double u_given = 0.0;
                 float uf;
                 if (kEngine) {
-                    const uint4v rb = philox4x32(step, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
-                    rhi = rb.x;
-                    rlo = rb.y;
+                    rhi = __shfl_sync(kFull, draw_hi, step - draw_base);
+                    rlo = __shfl_sync(kFull, draw_lo, step - draw_base);
                     uf = __uint2float_rn(rhi) * 0x1p-32f;
                 } else {
                     u_given = L.task_uniforms[(size_t)task * n + step];
