@@ -150,6 +150,11 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         // the construction draws of 32 consecutive steps at a time, lane i
         // holding step draw_base + i (the same counters as one draw per step)
         std::uint32_t draw_base = 0x80000000u, draw_hi = 0, draw_lo = 0;   // steps < 2^16: first step refreshes
+        // the candidate row of the likely next node, loaded one step ahead:
+        // once trails converge an ant mostly walks the parent tour, so the
+        // next node is the parent neighbour of `current` not yet visited
+        std::uint32_t next_node = n, next_pnbr = 0, next_cand = n;
+        float next_p = 0.0f;
         while (r.mne < target && r.steps + 1 < n) {
             if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
             const std::uint32_t step = r.steps + 1;
@@ -160,12 +165,29 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                 draw_lo = rb.y;
             }
             // loads that depend only on `current`, issued first
-            const std::uint32_t pnbr = __ldg(parent_nbr + current);
-            std::uint32_t cand = n;
+            std::uint32_t pnbr, cand = n;
             float p = 0.0f;
-            if (MODE != kModeVisits && lane < k) {
-                cand = __ldg(in.primary + (size_t)current * k + lane);
-                p = __ldg(products + (size_t)current * k + lane);
+            if (kEngine && current == next_node) {
+                pnbr = next_pnbr;
+                cand = next_cand;
+                p = next_p;
+            } else {
+                pnbr = __ldg(parent_nbr + current);
+                if (MODE != kModeVisits && lane < k) {
+                    cand = __ldg(in.primary + (size_t)current * k + lane);
+                    p = __ldg(products + (size_t)current * k + lane);
+                }
+            }
+            if (kEngine) {
+                const std::uint32_t ps = pnbr & 0xffffu;
+                next_node = test_bit(s.visited, ps) ? pnbr >> 16 : ps;
+                next_pnbr = __ldg(parent_nbr + next_node);
+                next_cand = n;
+                next_p = 0.0f;
+                if (lane < k) {
+                    next_cand = __ldg(in.primary + (size_t)next_node * k + lane);
+                    next_p = __ldg(products + (size_t)next_node * k + lane);
+                }
             }
             std::uint32_t selected = n;
             if (MODE == kModeVisits) {
