@@ -44,6 +44,7 @@ CPU_COLONIES_PER_THREAD = 16
 # (profiles/ant_kernel_plain_faco_n1000.md, launches 105-106: 15.09 / 15.29 MB
 # read, 0 written).  Reported for the default workload only.
 ANT_TRAFFIC_BYTES_PER_LAUNCH = 15.19e6
+STEADY_ITERATION = 400   # the converged-colony window of the throughput workload
 
 
 @dataclass
@@ -301,14 +302,13 @@ def run_gb300(args, rank: int, world: int) -> None:
     # ---- device throughput: inputs resident, L2 flushed before every step ----
     # the panel first runs `precondition` iterations so that the timed steps see
     # converged trails (construction steps per tour grow as they converge)
+    kernel_steps = 3
     engine.begin(keys, seeds, wl.mne)
     engine.step(wl.precondition + args.warmup)
     torch.cuda.synchronize()
-    step_ms = []
-    with ClockSampler(local) as clocks:
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
+
+    def timed_steps() -> list:
+        out = []
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
@@ -317,14 +317,40 @@ def run_gb300(args, rank: int, world: int) -> None:
             engine.step(1)
             b.record(stream)
             b.synchronize()
-            step_ms.append(a.elapsed_time(b))
+            out.append(a.elapsed_time(b))
+        return out
+
+    with ClockSampler(local) as clocks:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        step_ms = timed_steps()
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
     # per-kernel split of a few more steps (ant kernel = the dominant kernel)
-    kernel_steps = 3
     ant_ms, upd_ms = engine.step_timed(kernel_steps)
     totals = engine.finish()
+    steady = None
+    if wl.name == "throughput":
+        # the same steps once the colonies have converged (construction walks
+        # the parent tour: more steps and LS evaluations per tour), in a second
+        # evaluation from the initial tours with per-iteration traces
+        first = wl.precondition + args.warmup
+        engine.begin(keys, seeds, wl.mne, trace_iterations=STEADY_ITERATION + args.steps)
+        engine.step(STEADY_ITERATION)
+        torch.cuda.synchronize()
+        steady_ms = timed_steps()
+        trace = engine.finish()["trace"]
+        window, early = trace[STEADY_ITERATION:], trace[first:first + args.steps]
+        per_tour = float(wl.colonies * wl.ants * args.steps)
+        steady = {"value": world * per_tour / (max_over_ranks(float(np.sum(steady_ms)), world, "cuda") / 1e3),
+                  "ms_per_step": float(np.mean(steady_ms)), "timed_iterations_start_at": STEADY_ITERATION,
+                  "per_tour": {"construction_steps": float(window["construction_steps"].sum()) / per_tour,
+                               "ls_evaluations": float(window["ls_evaluations"].sum()) / per_tour},
+                  "per_tour_in_the_value_window": {
+                      "construction_steps": float(early["construction_steps"].sum()) / per_tour,
+                      "ls_evaluations": float(early["ls_evaluations"].sum()) / per_tour}}
     iters = totals["completed_batches"]
     work = totals["colony_work"].astype(np.float64)
     fe_total = iters * wl.colonies * wl.ants
@@ -383,6 +409,8 @@ def run_gb300(args, rank: int, world: int) -> None:
         "clocks": clocks.summary(),
         "gpu_launches": (classes + 1) * args.steps,
     }
+    if steady is not None:
+        line["steady_state"] = steady
     print(json.dumps(line), flush=True)
 
 
