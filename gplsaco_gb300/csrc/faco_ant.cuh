@@ -168,30 +168,36 @@ struct AntResult {
 };
 
 // Moves `node` right after `target` (CpuTour::relocate): shifts the closed
-// interval between their positions by one, register-staged per 32-element
-// chunk so that every read of a chunk precedes its writes.
+// interval between their positions by one, register-staged per 64-element
+// chunk (two elements per lane) so that every read of a chunk precedes its
+// writes; chunks run away from the vacated end.
 __device__ __forceinline__ void relocate_shift(const AntSmem& s, std::uint32_t lane, std::uint32_t tpos,
                                                std::uint32_t npos, std::uint32_t node) {
     if (tpos < npos) {
         // new[tpos+1] = node, new[i] = old[i-1] for i in (tpos+1, npos]
-        for (int base = (int)npos; base >= (int)tpos + 1; base -= 32) {
-            const int i = base - (int)lane;
-            std::uint32_t v = 0;
-            const bool act = i >= (int)tpos + 1;
-            if (act) v = i == (int)tpos + 1 ? node : s.tour[i - 1];
+        const int lo = (int)tpos + 1;
+        for (int base = (int)npos; base >= lo; base -= 64) {
+            const int i0 = base - (int)lane, i1 = i0 - 32;
+            std::uint32_t v0 = 0, v1 = 0;
+            const bool a0 = i0 >= lo, a1 = i1 >= lo;
+            if (a0) v0 = i0 == lo ? node : s.tour[i0 - 1];
+            if (a1) v1 = i1 == lo ? node : s.tour[i1 - 1];
             __syncwarp();
-            if (act) { s.tour[i] = (node_t)v; s.pos[v] = (node_t)i; }
+            if (a0) { s.tour[i0] = (node_t)v0; s.pos[v0] = (node_t)i0; }
+            if (a1) { s.tour[i1] = (node_t)v1; s.pos[v1] = (node_t)i1; }
             __syncwarp();
         }
     } else {
         // new[i] = old[i+1] for i in [npos, tpos), new[tpos] = node
-        for (std::uint32_t base = npos; base <= tpos; base += 32) {
-            const std::uint32_t i = base + lane;
-            std::uint32_t v = 0;
-            const bool act = i <= tpos;
-            if (act) v = i == tpos ? node : s.tour[i + 1];
+        for (std::uint32_t base = npos; base <= tpos; base += 64) {
+            const std::uint32_t i0 = base + lane, i1 = i0 + 32;
+            std::uint32_t v0 = 0, v1 = 0;
+            const bool a0 = i0 <= tpos, a1 = i1 <= tpos;
+            if (a0) v0 = i0 == tpos ? node : s.tour[i0 + 1];
+            if (a1) v1 = i1 == tpos ? node : s.tour[i1 + 1];
             __syncwarp();
-            if (act) { s.tour[i] = (node_t)v; s.pos[v] = (node_t)i; }
+            if (a0) { s.tour[i0] = (node_t)v0; s.pos[v0] = (node_t)i0; }
+            if (a1) { s.tour[i1] = (node_t)v1; s.pos[v1] = (node_t)i1; }
             __syncwarp();
         }
     }
