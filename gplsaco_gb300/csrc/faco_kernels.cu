@@ -4,7 +4,10 @@
 //   colony_init_kernel      reset_colony + initialize_products
 //                           (cuda/colony_state.cuh:72-110)
 //   colony_update_kernel    reduce_and_select + update_pheromone fused, one
-//                           block per colony (cuda/colony_state.cuh:148-229)
+//                           block per colony (cuda/colony_state.cuh:148-229),
+//                           with the controllers' per-batch work
+//   fingerprint_kernel      tour fingerprints for the 12-feature controller,
+//                           one warp per ant (cuda/control_state.cuh:45-64)
 //   pheromone_step_kernel   the trail update alone (parity hook)
 //   score_kernel            GP controller scoring, warp per colony
 //                           (cuda/gp_score.cuh:64-102)
