@@ -556,7 +556,9 @@ def run_time_to_gap(args) -> None:
             "value_one_colony_per_instance": res["ratio"],
             "unit": "prior/plain wall-clock", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
             "config": {"workload": "16 instances (N=1000/2000, uniform/clustered, seeds 100-115), 32 ants, "
-                                   "k=20, MNE 8, 2-opt; reference = best of 2 plain runs of 1500 iterations",
+                                   "k=20, 2-opt; reference = best of 2 plain runs of 1500 iterations (MNE 8)",
+                       "tuning": "both arms tuned on 8 validation instances by wall-clock to the target: plain "
+                                 "over MNE targets, the prior over model, floor, exponent, refresh and MNE",
                        "budget": "equal: two colonies per instance in both arms (plain: seeds 1, 2; prior: seed 1 "
                                  "plain as the per-instance fallback + seed 2 with the prior), best of the two; "
                                  "value_one_colony_per_instance charges the prior for a plain warm-up run that "

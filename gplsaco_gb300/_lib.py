@@ -28,6 +28,7 @@ EXPORTED = (
     "faco_ant_diagnostic", "faco_pheromone_step", "faco_begin", "faco_step", "faco_step_timed", "faco_finish",
     "faco_engine_stream", "faco_evaluate_programs", "faco_mlp_param_count", "faco_mlp_forward", "faco_mlp_gradient",
     "faco_mlp_train", "faco_edge_data", "faco_prior_set", "faco_prior_refresh", "faco_current_costs",
+    "faco_set_mne_targets",
     "faco_pheromone_step_noalloc", "faco_begin_programs", "faco_snapshot", "faco_restore",
     "faco_evaluate_controllers", "faco_validate_controller", "faco_score_controllers",
 )
@@ -150,6 +151,7 @@ def load():
     L.faco_prior_set.argtypes = [vp, vp, C.c_float, C.c_int, vp]
     L.faco_prior_refresh.argtypes = [vp]
     L.faco_current_costs.argtypes = [vp, vp, C.POINTER(C.c_uint32)]
+    L.faco_set_mne_targets.argtypes = [vp, vp, C.c_uint32]
     L.faco_begin.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32]
     L.faco_step.argtypes = [vp, C.c_uint32]
     L.faco_step_timed.argtypes = [vp, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]

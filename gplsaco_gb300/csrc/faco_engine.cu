@@ -1945,10 +1945,14 @@ int faco_mlp_gradient(const float* params, const uint16_t* x, const float* y, ui
         DeviceBuffer<float> dy, dl(1);
         dy.upload(y, count, s);
         G.resize(1);
-        cuda_check(cudaMemsetAsync(G.get(), 0, sizeof(faco::MlpParams), s), "memset");
         cuda_check(cudaMemsetAsync(dl.get(), 0, sizeof(float), s), "memset");
-        faco::mlp_grad_kernel<<<mlp_blocks((count + 63) / 64), 128, 0, s>>>(P.get(), O.get(), dx.get(), dy.get(),
-                                                                          count, 1.0f / count, G.get(), dl.get());
+        const std::uint32_t blocks = mlp_blocks((count + 63) / 64);
+        DeviceBuffer<faco::MlpParams> partials(blocks);
+        DeviceBuffer<float> loss_partials(blocks);
+        faco::mlp_grad_kernel<<<blocks, 128, 0, s>>>(P.get(), O.get(), dx.get(), dy.get(), count, 1.0f / count,
+                                                     partials.get(), loss_partials.get());
+        faco::mlp_grad_reduce_kernel<<<20, 256, 0, s>>>(partials.get(), loss_partials.get(), blocks, G.get(),
+                                                        dl.get());
         cuda_check(cudaGetLastError(), "mlp gradient");
         G.download(reinterpret_cast<faco::MlpParams*>(grad), 1, s);
         dl.download(loss, 1, s);
@@ -1974,14 +1978,19 @@ int faco_mlp_train(float* params, const uint16_t* x, const float* y, uint32_t co
         cuda_check(cudaMemsetAsync(dl.get(), 0, sizeof(float) * epochs, s), "memset");
         const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
         std::uint64_t step = 0;
+        const std::uint32_t max_blocks = mlp_blocks((std::min(batch, count) + 63) / 64);
+        DeviceBuffer<faco::MlpParams> partials(max_blocks);
+        DeviceBuffer<float> loss_partials(max_blocks);
         for (std::uint32_t ep = 0; ep < epochs; ++ep) {
             for (std::uint32_t first = 0; first < count; first += batch) {
                 const std::uint32_t size = std::min(batch, count - first);
+                const std::uint32_t blocks = mlp_blocks((size + 63) / 64);
                 ++step;
-                cuda_check(cudaMemsetAsync(G.get(), 0, sizeof(faco::MlpParams), s), "memset");
-                faco::mlp_grad_kernel<<<mlp_blocks((size + 63) / 64), 128, 0, s>>>(
+                faco::mlp_grad_kernel<<<blocks, 128, 0, s>>>(
                     P.get(), O.get(), dx.get() + static_cast<std::size_t>(first) * faco::kMlpIn, dy.get() + first,
-                    size, 1.0f / size, G.get(), dl.get() + ep);
+                    size, 1.0f / size, partials.get(), loss_partials.get());
+                faco::mlp_grad_reduce_kernel<<<20, 256, 0, s>>>(partials.get(), loss_partials.get(), blocks, G.get(),
+                                                                dl.get() + ep);
                 const float b1 = 1.0f - std::pow(beta1, static_cast<float>(step));
                 const float b2 = 1.0f - std::pow(beta2, static_cast<float>(step));
                 faco::adam_kernel<<<20, 256, 0, s>>>(P.get(), G.get(), M.get(), V.get(), lr, beta1, beta2, eps, b1, b2);
@@ -2105,6 +2114,25 @@ int faco_current_costs(faco_engine* e, int64_t* costs, uint32_t* iterations) {
         cuda_check(cudaStreamSynchronize(e->stream), "costs");
         for (std::uint32_t c = 0; c < v.count; ++c) costs[c] = st[c].global_cost;
         if (iterations) *iterations = st[0].iteration;
+    });
+}
+
+int faco_set_mne_targets(faco_engine* e, const uint32_t* targets, uint32_t count) {
+    return guarded([&] {
+        require(e && targets, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        require(!v.P.controlled, "controlled evaluations choose their MNE targets by action");
+        require(count == v.count, "one target per colony");
+        for (std::uint32_t c = 0; c < count; ++c) require(targets[c] >= 1, "MNE targets must be positive");
+        std::vector<faco::ColonyState> st(v.count);
+        e->states.download(st.data(), v.count, e->stream);
+        cuda_check(cudaStreamSynchronize(e->stream), "states");
+        for (std::uint32_t c = 0; c < count; ++c) st[c].mne_target = targets[c];
+        e->states.upload(st, e->stream);
+        cuda_check(cudaStreamSynchronize(e->stream), "states");
     });
 }
 

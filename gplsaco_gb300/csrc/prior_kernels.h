@@ -14,7 +14,9 @@ namespace faco {
 __global__ void mlp_forward_kernel(const MlpParams* P, const MlpOperands* O, const __nv_bfloat16* x, std::uint32_t E,
                                    float* prob, unsigned* error);
 __global__ void mlp_grad_kernel(const MlpParams* P, const MlpOperands* O, const __nv_bfloat16* x, const float* y,
-                                std::uint32_t E, float inv_count, MlpParams* grad, float* loss);
+                                std::uint32_t E, float inv_count, MlpParams* partials, float* loss_partials);
+__global__ void mlp_grad_reduce_kernel(const MlpParams* partials, const float* loss_partials, std::uint32_t blocks,
+                                       MlpParams* grad, float* loss);
 __global__ void adam_kernel(MlpParams* P, const MlpParams* grad, MlpParams* m, MlpParams* v, float lr, float beta1,
                             float beta2, float eps, float bias1, float bias2);
 __global__ void refresh_operands_kernel(const MlpParams* P, MlpOperands* O);

@@ -50,12 +50,18 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const MlpParams* P, co
         [&](std::uint32_t row, float z) { prob[row] = sigmoid(z); });
 }
 
-// Binary cross-entropy gradients of the mean loss over `scale_count` edges,
-// accumulated (atomically) into grad (an MlpParams-shaped FP32 array); the
-// summed loss goes to *loss.  Blocks stride over 64-edge chunks.
+// Binary cross-entropy gradients of the mean loss over `scale_count` edges.
+// Blocks stride over 64-edge chunks; block b writes its partial gradient to
+// partials[b] and its summed loss to loss_partials[b] (every entry written by
+// one thread, the warps' shares of the vectors summed in warp order), and
+// mlp_grad_reduce_kernel adds the partials in block order -- the same bits on
+// every run.
 __global__ void __launch_bounds__(128) mlp_grad_kernel(const MlpParams* P, const MlpOperands* O,
                                                        const __nv_bfloat16* x, const float* y, std::uint32_t E,
-                                                       float inv_count, MlpParams* grad, float* loss) {
+                                                       float inv_count, MlpParams* partials, float* loss_partials) {
+    MlpParams* grad = partials + blockIdx.x;
+    __shared__ float s_vec[4][3][kMlpHidden];
+    __shared__ float s_scalar[4][2];
     __shared__ SharedOperands s;
     __shared__ __align__(16) __nv_bfloat16 xs[kChunk * kMlpIn];
     __shared__ __align__(16) __nv_bfloat16 h1s[kChunk * kMlpHidden];
@@ -160,20 +166,21 @@ __global__ void __launch_bounds__(128) mlp_grad_kernel(const MlpParams* P, const
         }
         __syncthreads();
     }
-    // flush: weight matrices (each warp owns 16 rows), then the vectors
+    // flush: weight matrices (each warp owns 16 rows, each thread its
+    // entries), then the vectors
     const int o = warp * 16 + g;
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         const int col = nt * 8 + 2 * q;
-        atomicAdd(&grad->w2[o * kMlpHidden + col], gw2[nt][0]);
-        atomicAdd(&grad->w2[o * kMlpHidden + col + 1], gw2[nt][1]);
-        atomicAdd(&grad->w2[(o + 8) * kMlpHidden + col], gw2[nt][2]);
-        atomicAdd(&grad->w2[(o + 8) * kMlpHidden + col + 1], gw2[nt][3]);
+        grad->w2[o * kMlpHidden + col] = gw2[nt][0];
+        grad->w2[o * kMlpHidden + col + 1] = gw2[nt][1];
+        grad->w2[(o + 8) * kMlpHidden + col] = gw2[nt][2];
+        grad->w2[(o + 8) * kMlpHidden + col + 1] = gw2[nt][3];
     }
-    atomicAdd(&grad->w1[o * kMlpIn + 2 * q], gw1[0]);
-    atomicAdd(&grad->w1[o * kMlpIn + 2 * q + 1], gw1[1]);
-    atomicAdd(&grad->w1[(o + 8) * kMlpIn + 2 * q], gw1[2]);
-    atomicAdd(&grad->w1[(o + 8) * kMlpIn + 2 * q + 1], gw1[3]);
+    grad->w1[o * kMlpIn + 2 * q] = gw1[0];
+    grad->w1[o * kMlpIn + 2 * q + 1] = gw1[1];
+    grad->w1[(o + 8) * kMlpIn + 2 * q] = gw1[2];
+    grad->w1[(o + 8) * kMlpIn + 2 * q + 1] = gw1[3];
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
         // reduce over the 8 row groups (lanes with equal q)
@@ -189,9 +196,9 @@ __global__ void __launch_bounds__(128) mlp_grad_kernel(const MlpParams* P, const
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
                 const int c = nt * 8 + 2 * q + j;
-                atomicAdd(&grad->b1[c], gb1[2 * nt + j]);
-                atomicAdd(&grad->b2[c], gb2[2 * nt + j]);
-                atomicAdd(&grad->w3[c], gw3[2 * nt + j]);
+                s_vec[warp][0][c] = gb1[2 * nt + j];
+                s_vec[warp][1][c] = gb2[2 * nt + j];
+                s_vec[warp][2][c] = gw3[2 * nt + j];
             }
     }
     for (int off = 16; off; off >>= 1) {
@@ -199,8 +206,48 @@ __global__ void __launch_bounds__(128) mlp_grad_kernel(const MlpParams* P, const
         lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
     }
     if (lane == 0) {
-        atomicAdd(&grad->b3, gb3);
-        atomicAdd(loss, lsum);
+        s_scalar[warp][0] = gb3;
+        s_scalar[warp][1] = lsum;
+    }
+    __syncthreads();
+    if (threadIdx.x < kMlpHidden) {
+        const int c = threadIdx.x;
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+        for (int w = 0; w < 4; ++w) {
+            v0 += s_vec[w][0][c];
+            v1 += s_vec[w][1][c];
+            v2 += s_vec[w][2][c];
+        }
+        grad->b1[c] = v0;
+        grad->b2[c] = v1;
+        grad->w3[c] = v2;
+    }
+    if (threadIdx.x == 0) {
+        float v0 = 0.f, v1 = 0.f;
+        for (int w = 0; w < 4; ++w) {
+            v0 += s_scalar[w][0];
+            v1 += s_scalar[w][1];
+        }
+        grad->b3 = v0;
+        grad->pad[0] = grad->pad[1] = grad->pad[2] = 0.f;
+        loss_partials[blockIdx.x] = v1;
+    }
+}
+
+// grad = the block partials summed in block order; *loss += their losses.
+__global__ void mlp_grad_reduce_kernel(const MlpParams* partials, const float* loss_partials, std::uint32_t blocks,
+                                       MlpParams* grad, float* loss) {
+    const float* src = reinterpret_cast<const float*>(partials);
+    float* dst = reinterpret_cast<float*>(grad);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpParamCount; i += gridDim.x * blockDim.x) {
+        float sum = 0.f;
+        for (std::uint32_t b = 0; b < blocks; ++b) sum += src[(size_t)b * kMlpParamCount + i];
+        dst[i] = sum;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        float sum = 0.f;
+        for (std::uint32_t b = 0; b < blocks; ++b) sum += loss_partials[b];
+        *loss += sum;
     }
 }
 

@@ -548,6 +548,13 @@ class FacoBatchEngine:
         _lib.check(self._L.faco_current_costs(self._handle, costs.ctypes.data, C.byref(it)))
         return costs, int(it.value)
 
+    def set_mne_targets(self, targets) -> None:
+        """Per-colony MNE targets of the active plain stepwise evaluation from
+        the next batch on (one per colony, each >= 1)."""
+        t = np.ascontiguousarray([_exact_int(int(v) if isinstance(v, np.integer) else v, "MNE target", 1,
+                                             2**32 - 1) for v in targets], dtype=np.uint32)
+        _lib.check(self._L.faco_set_mne_targets(self._handle, t.ctypes.data, t.size))
+
     @property
     def stream_ptr(self) -> int:
         """The engine's cudaStream_t as an integer (torch.cuda.ExternalStream)."""

@@ -32,7 +32,7 @@ class GapConfig:
     ls_width: int = 20
     retention: float = 0.98
     mne: int = 8
-    chunk: int = 10                 # iterations between cost reads (and prior refreshes)
+    chunk: int = 10                 # iterations between cost reads
     iterations: int = 400           # timed budget per method
     reference_iterations: int = 1500
     reference_seeds: int = 2
@@ -41,14 +41,19 @@ class GapConfig:
     gamma: int = 1
     target_gap: float = 0.01
     extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
-    # (model, floor, gamma, chunk) candidates, tuned on validation instances
-    # (seeds 200-214) by wall-clock time to the target gap.  "full" sees all seven
-    # features; "geometry" only the geometric ones (trail level and
-    # best-tour membership masked), so it does not pull ants back onto the
-    # parent tour's edges.
-    tune_grid: tuple = (("full", 0.05, 1, 10), ("full", 0.5, 1, 10), ("geometry", 0.05, 1, 10),
-                        ("geometry", 0.2, 1, 10), ("geometry", 0.5, 1, 10), ("geometry", 0.05, 2, 10),
-                        ("geometry", 0.2, 2, 10))
+    # Both arms are tuned on validation instances (seeds 200-214) by wall-clock
+    # time to the target gap: plain FACO over MNE targets, the prior over
+    # (model, floor, gamma, refresh, MNE).  "full" sees all seven features;
+    # "geometry" only the geometric ones (trail level and best-tour membership
+    # masked), so it does not pull ants back onto the parent tour's edges --
+    # and, its inputs being static, needs no refresh.  refresh: iterations
+    # between recomputations of the prior (0: never).  A sharp prior makes
+    # ants walk the parent tour longer before their MNE-th new edge, so the
+    # prior's best MNE target can differ from plain FACO's.
+    mne_grid: tuple = (8, 6, 5, 4)
+    tune_grid: tuple = (("full", 0.5, 1, 10, 8), ("geometry", 0.2, 1, 0, 8), ("geometry", 0.2, 1, 0, 6),
+                        ("geometry", 0.05, 2, 0, 8), ("geometry", 0.05, 2, 0, 6), ("geometry", 0.05, 2, 0, 5),
+                        ("geometry", 0.05, 2, 0, 4), ("geometry", 0.2, 2, 0, 6))
     train_pool: int = 32
     train_snapshot: int = 25
     train_iterations: int = 300
@@ -108,13 +113,13 @@ def reference_lengths(cfg: GapConfig, xys: list, device: int = 0) -> np.ndarray:
 
 
 def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0,
-            floor: float | None = None, gamma: int | None = None, chunk: int | None = None):
+            floor: float | None = None, gamma: int | None = None, refresh: int = 10, mne: int | None = None):
     """One method on all evaluation instances (one colony each, seed 1).
     Returns rows (iteration, seconds, mean gap, costs), the fallback mask and
     the work per ant-iteration (construction steps, LS evaluations)."""
     floor = cfg.floor if floor is None else floor
     gamma = cfg.gamma if gamma is None else gamma
-    chunk = cfg.chunk if chunk is None else chunk
+    chunk = cfg.chunk
     dim = max(len(xy) for xy in xys)
     engine = FacoBatchEngine(dim, len(xys), _settings(cfg), device=device)
     for i, xy in enumerate(xys):
@@ -123,7 +128,7 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     seeds = np.ones(len(xys), np.uint64)
     rows = []
     enabled = np.ones(len(xys), np.uint8)
-    engine.begin(keys, seeds, cfg.mne)
+    engine.begin(keys, seeds, cfg.mne if mne is None else mne)
     costs, _ = engine.current_costs(len(xys))
     t0 = time.perf_counter()
     if params is not None:
@@ -139,7 +144,7 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
                 now, _ = engine.current_costs(len(xys))
                 enabled = (now <= plain_warmup_costs).astype(np.uint8)
                 engine.prior_set(None, enabled, floor, gamma)
-            else:
+            elif refresh and done % refresh == 0:
                 engine.prior_refresh()
         costs, _ = engine.current_costs(len(xys))
         rows.append((done, time.perf_counter() - t0, float(np.mean((costs - refs) / refs)), costs.copy()))
@@ -170,22 +175,26 @@ def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
 
 
 def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: int = 0, floor: float | None = None,
-             gamma: int | None = None, chunk: int | None = None):
+             gamma: int | None = None, refresh: int = 10, prior_mne: int | None = None, mne: int | None = None):
     """Two colonies per instance, the instance's length the better of the
     two.  params None: both plain (seeds 1 and 2).  Otherwise colony 2 runs
-    with the prior and colony 1 stays plain -- the per-instance fallback is
-    the concurrent plain colony, with no warm-up run to charge.  Returns rows
-    (iteration, seconds, mean gap, best costs) and the work per ant-iteration."""
+    with the prior (at MNE target prior_mne) and colony 1 stays plain -- the
+    per-instance fallback is the concurrent plain colony, with no warm-up run
+    to charge.  Returns rows (iteration, seconds, mean gap, best costs) and
+    the work per ant-iteration."""
     floor = cfg.floor if floor is None else floor
     gamma = cfg.gamma if gamma is None else gamma
-    chunk = cfg.chunk if chunk is None else chunk
+    chunk = cfg.chunk
     count = 2 * len(xys)
     engine = FacoBatchEngine(max(len(xy) for xy in xys), count, _settings(cfg), device=device)
     for i, xy in enumerate(xys):
         engine.register_problem(1 + i, xy.astype(np.float64))
     keys = np.repeat(np.arange(1, len(xys) + 1, dtype=np.uint64), 2)
     seeds = np.tile(np.array([1, 2], np.uint64), len(xys))
-    engine.begin(keys, seeds, cfg.mne)
+    plain_mne = cfg.mne if mne is None else mne
+    engine.begin(keys, seeds, plain_mne)
+    if params is not None and prior_mne is not None and prior_mne != plain_mne:
+        engine.set_mne_targets(np.tile(np.array([plain_mne, prior_mne], np.uint32), len(xys)))
     costs, _ = engine.current_costs(count)
     t0 = time.perf_counter()
     if params is not None:
@@ -201,7 +210,7 @@ def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: i
     while done < cfg.iterations:
         engine.step(chunk)
         done += chunk
-        if params is not None:
+        if params is not None and refresh and done % refresh == 0:
             engine.prior_refresh()
         costs, _ = engine.current_costs(count)
         rows.append(row(done, costs))
@@ -232,33 +241,47 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     geo_params, geo_losses = geometry_model(x, y, cfg)
     log(f"geometry-model losses {np.round(geo_losses, 4).tolist()}")
     models = {"full": params, "geometry": geo_params}
-    # tune (floor, gamma, refresh chunk) on validation instances, by iterations to the target
+    # tune (model, floor, gamma, refresh interval) on validation instances, by wall-clock to the target
     val = [_xy(kind, n, seed + 100) for kind, n, seed in cfg.eval_instances[::2]]
     val_refs = reference_lengths(cfg, val, device)
-    val_plain, _, val_work = gap_run(cfg, val, val_refs, None, None, device)
-    val_warm = next(r for r in val_plain if r[0] == cfg.warmup)
-    t_val, _ = first_time_below(val_plain, cfg.target_gap)
+    plain_tuning = []
+    for mne in cfg.mne_grid:
+        rows, _, work = gap_run(cfg, val, val_refs, None, None, device, mne=mne)
+        t, it = first_time_below(rows, cfg.target_gap)
+        plain_tuning.append({"mne": mne, "final_gap": rows[-1][2], "iterations_to_target": it,
+                             "seconds_to_target": t, "rows": rows, **work})
+    plain_best = min(plain_tuning, key=lambda r: (r["seconds_to_target"] is None, r["seconds_to_target"] or 0.0,
+                                                  r["final_gap"]))
+    plain_mne = plain_best["mne"]
+    val_warm = next(r for r in plain_best["rows"] if r[0] == cfg.warmup)
+    t_val = plain_best["seconds_to_target"]
+    val_work = {k: plain_best[k] for k in ("construction_steps", "ls_evaluations", "ms_per_iteration")}
+    for r in plain_tuning:
+        del r["rows"]
     tuning = []
-    for model, floor, gamma, chunk in cfg.tune_grid:
-        rows, _, work = gap_run(cfg, val, val_refs, models[model], val_warm[3], device, floor, gamma, chunk)
+    for model, floor, gamma, refresh, mne in cfg.tune_grid:
+        rows, _, work = gap_run(cfg, val, val_refs, models[model], val_warm[3], device, floor, gamma, refresh, mne)
         t, it = first_time_below(rows, cfg.target_gap, extra_seconds=val_warm[1])
-        tuning.append({"model": model, "floor": floor, "gamma": gamma, "refresh_every": chunk,
+        tuning.append({"model": model, "floor": floor, "gamma": gamma, "refresh_every": refresh, "mne": mne,
                        "final_gap": rows[-1][2], "iterations_to_target": it, "seconds_to_target": t, **work})
     best_row = min(tuning, key=lambda r: (r["seconds_to_target"] is None, r["seconds_to_target"] or 0.0,
                                           r["final_gap"]))
     best = (best_row["floor"], best_row["gamma"], best_row["refresh_every"])
-    best_model = best_row["model"]
-    log(f"validation plain: {t_val} s, {val_work}; tuning {tuning} -> {best_model} {best}")
+    best_model, prior_mne = best_row["model"], best_row["mne"]
+    log(f"validation plain: MNE {plain_mne}, {t_val} s, {val_work}; tuning {tuning} -> {best_model} {best} "
+        f"MNE {prior_mne}")
     xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
     refs = reference_lengths(cfg, xys, device)
-    plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device)
+    plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device, mne=plain_mne)
     warm = next(r for r in plain_rows if r[0] == cfg.warmup)
-    prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, models[best_model], warm[3], device, *best)
+    prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, models[best_model], warm[3], device, *best,
+                                              mne=prior_mne)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
     # equal resources: two colonies per instance in both arms
-    pair_plain, pair_plain_work = pair_run(cfg, xys, refs, None, device)
-    pair_prior, pair_prior_work = pair_run(cfg, xys, refs, models[best_model], device, *best)
+    pair_plain, pair_plain_work = pair_run(cfg, xys, refs, None, device, mne=plain_mne)
+    pair_prior, pair_prior_work = pair_run(cfg, xys, refs, models[best_model], device, *best, prior_mne=prior_mne,
+                                           mne=plain_mne)
 
     def targets(rows_a, rows_b):
         out = {}
@@ -274,7 +297,9 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         "ratio": (t_prior / t_plain) if (t_prior is not None and t_plain) else None,
         "prior_charged_warmup_seconds": warm[1],
         "prior_enabled_after_warmup": int(enabled.sum()), "instances": len(xys),
-        "prior_setting": {"model": best_model, "floor": best[0], "gamma": best[1], "refresh_every": best[2]},
+        "prior_setting": {"model": best_model, "floor": best[0], "gamma": best[1], "refresh_every": best[2],
+                          "mne": prior_mne},
+        "plain_setting": {"mne": plain_mne}, "plain_tuning": plain_tuning,
         "plain_work": plain_work, "prior_work": prior_work,
         "validation_plain": {"seconds_to_target": t_val, **val_work}, "tuning": tuning,
         "other_targets": {

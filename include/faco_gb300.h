@@ -338,6 +338,10 @@ int faco_prior_set(faco_engine* engine, const float* params, float floor, int ga
 int faco_prior_refresh(faco_engine* engine);
 /* Current global-best lengths of the colonies (synchronises). */
 int faco_current_costs(faco_engine* engine, int64_t* costs, uint32_t* iterations);
+/* Per-colony MNE targets (maximum new edges per ant) of the active plain
+ * stepwise evaluation from the next batch on, targets[count] >= 1
+ * (synchronises).  GP-controlled evaluations choose their targets by action. */
+int faco_set_mne_targets(faco_engine* engine, const uint32_t* targets, uint32_t count);
 
 /* One MMAS evaporate/deposit step (cuda/colony_state.cuh:210-229) on FP32
  * trails [n][k] along `parent`; refreshes products = trails * eta. */

@@ -63,6 +63,13 @@ def test_training_reduces_loss(prior):
     assert losses[-1] < 0.5 * losses[0]
     acc = np.mean((prior.forward(trained, bits) > 0.5) == (y > 0.5))
     assert acc > 0.9
+    # the gradient is reduced in a fixed order: training is reproducible bit for bit
+    again, again_losses = prior.train(params, bits, y, epochs=8, batch=4096, lr=3e-3)
+    assert np.array_equal(np.asarray(again).view(np.uint32), np.asarray(trained).view(np.uint32))
+    assert np.array_equal(np.asarray(again_losses), np.asarray(losses))
+    g1, l1 = prior.gradient(params, bits, y)
+    g2, l2 = prior.gradient(params, bits, y)
+    assert np.array_equal(np.asarray(g1).view(np.uint32), np.asarray(g2).view(np.uint32)) and l1 == l2
 
 
 def test_edge_data_and_fallback(prior):
