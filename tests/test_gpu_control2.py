@@ -184,3 +184,38 @@ def test_spec2_forced_fingerprint_collisions_match_oracle(api, oracle, grid):
                 assert np.array_equal(np.asarray(got["features"], np.float32).view(np.uint32),
                                       want["features"].view(np.uint32))
     engine.close()
+
+
+@pytest.mark.parametrize("workspace", [0, 2])
+def test_spec2_uneven_batch_and_global_workspace(api, oracle, workspace):
+    """The 12-feature controller on an uneven batch (instances of different
+    sizes in one evaluation, each colony with its own archive and regions),
+    with the ants' tours in shared memory and in the global workspace: every
+    colony equals its own oracle run."""
+    sizes = [150, 420, 2100]
+    ants, iterations = 8, 6
+    rng = np.random.default_rng(31)
+    program = _programs.random_program(rng, features=12, feature_spec_id=2)
+    engine = api.FacoBatchEngine(max(sizes), 3, _settings(api, ants, workspace=workspace))
+    preps = {}
+    for i, n in enumerate(sizes):
+        xy = _cases.uniform_instance(n, seed=40 + i)
+        engine.register_problem(70 + i, xy.astype(np.float64))
+        preps[70 + i] = (xy, oracle.prepare(xy, 16, 64, 20))
+    keys = np.array([72, 70, 71], np.uint64)
+    seeds = np.array([3, 4, 5], np.uint64)
+    res = engine.evaluate_program_evaluations(keys, seeds, ants * iterations, program, trace=True,
+                                              decision_iterations=[2, iterations])
+    for c in range(3):
+        xy, prep = preps[int(keys[c])]
+        key = oracle.lib().orc_colony_key(int(seeds[c]), int(keys[c]))
+        ref = oracle.run_colony(xy, prep, ants=ants, k=16, b=64, w=20, mne=8, iterations=iterations, key=key,
+                                retention=0.9, program=program, total_iterations=iterations,
+                                instance_key=int(keys[c]), decision_iterations=[2, iterations])
+        _check_colony(res, c, ref, iterations, ("uneven", workspace, c))
+        for d, want in enumerate(ref["decisions"]):
+            got = res["decisions"][d * 3 + c]
+            assert got["action"] == want["action"]
+            assert np.array_equal(np.asarray(got["features"], np.float32).view(np.uint32),
+                                  want["features"].view(np.uint32))
+    engine.close()
