@@ -3,9 +3,12 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload throughput|uneven|large|gp-population|time-to-gap]
 
-A step is one ACO iteration of the whole panel: every ant of every colony
+A step is one replay of the engine's per-evaluation CUDA graph: 16 ACO
+iterations of the whole panel, in each of which every ant of every colony
 constructs a tour from its colony's parent and runs its local search, then
-each colony reduces, selects and updates its trails.  Default workload
+each colony reduces, selects and updates its trails (the colonies run as
+independent chains inside the graph, so one chain's slowest ants overlap
+the other chains' iterations).  Default workload
 (throughput): 16 instances of N=1000 integer coordinates uniform in
 [0,10^6]^2 x 16 seeds = 256 colonies, 32 ants each, k=16, backup 64, LS
 width 20, MNE 8, 2-opt, retention 0.98.  Other workloads:
@@ -45,6 +48,7 @@ CPU_COLONIES_PER_THREAD = 16
 # read, 0 written).  Reported for the default workload only.
 ANT_TRAFFIC_BYTES_PER_LAUNCH = 15.19e6
 STEADY_ITERATION = 400   # the converged-colony window of the throughput workload
+ITERATIONS_PER_STEP = 16  # a step: one replay of the engine's per-evaluation CUDA graph
 
 
 @dataclass
@@ -99,7 +103,8 @@ def make_workload(name: str, rank: int = 0) -> Workload:
             "uneven", "ant-tours+LS/sec (uneven batch, N~U[200,1000])",
             "plain FACO, 256 clustered instances (4-16 Gaussian clusters, sigma 2-8% of [0,10^6], 20% uniform "
             "noise), N ~ U[200,1000], one colony each, 16 ants, k=16, backup 64, LS width 20, MNE 8, 2-opt, "
-            "retention 0.98; size-class ant launches as parallel graph branches, warps per block autotuned",
+            "retention 0.98; colony chains of one size class each as parallel graph branches, warps per block "
+            "autotuned",
             instances.uneven_batch(256, (200, 1000)), np.arange(256),
             np.full(256, 1 + 1000 * rank, np.uint64), 16, 16, 64, 20, e2e_iterations=500)
     if name == "large":
@@ -300,11 +305,19 @@ def run_gb300(args, rank: int, world: int) -> None:
     classes = size_classes(wl.sizes())
 
     # ---- device throughput: inputs resident, L2 flushed before every step ----
-    # the panel first runs `precondition` iterations so that the timed steps see
-    # converged trails (construction steps per tour grow as they converge)
+    # a step is one replay of the evaluation's CUDA graph (`graph_iterations`
+    # iterations, the colony chains overlapping inside it); the panel first
+    # runs `precondition` iterations, the last W steps of them the untimed
+    # warm-up, so that the timed steps start at iteration `precondition`
     kernel_steps = 3
     engine.begin(keys, seeds, wl.mne)
-    engine.step(wl.precondition + args.warmup)
+    plan = engine.launch_plan()
+    per_step = plan["graph_iterations"]
+    assert per_step == ITERATIONS_PER_STEP, plan
+    first = max(wl.precondition, per_step * args.warmup)
+    engine.step(first - per_step * args.warmup)
+    for _ in range(args.warmup):
+        engine.step(per_step)
     torch.cuda.synchronize()
 
     def timed_steps() -> list:
@@ -314,7 +327,7 @@ def run_gb300(args, rank: int, world: int) -> None:
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            engine.step(1)
+            engine.step(per_step)
             b.record(stream)
             b.synchronize()
             out.append(a.elapsed_time(b))
@@ -336,14 +349,13 @@ def run_gb300(args, rank: int, world: int) -> None:
         # the same steps once the colonies have converged (construction walks
         # the parent tour: more steps and LS evaluations per tour), in a second
         # evaluation from the initial tours with per-iteration traces
-        first = wl.precondition + args.warmup
-        engine.begin(keys, seeds, wl.mne, trace_iterations=STEADY_ITERATION + args.steps)
+        engine.begin(keys, seeds, wl.mne, trace_iterations=STEADY_ITERATION + per_step * args.steps)
         engine.step(STEADY_ITERATION)
         torch.cuda.synchronize()
         steady_ms = timed_steps()
         trace = engine.finish()["trace"]
-        window, early = trace[STEADY_ITERATION:], trace[first:first + args.steps]
-        per_tour = float(wl.colonies * wl.ants * args.steps)
+        window, early = trace[STEADY_ITERATION:], trace[first:first + per_step * args.steps]
+        per_tour = float(wl.colonies * wl.ants * per_step * args.steps)
         steady = {"value": world * per_tour / (max_over_ranks(float(np.sum(steady_ms)), world, "cuda") / 1e3),
                   "ms_per_step": float(np.mean(steady_ms)), "timed_iterations_start_at": STEADY_ITERATION,
                   "per_tour": {"construction_steps": float(window["construction_steps"].sum()) / per_tour,
@@ -355,7 +367,7 @@ def run_gb300(args, rank: int, world: int) -> None:
     work = totals["colony_work"].astype(np.float64)
     fe_total = iters * wl.colonies * wl.ants
     elapsed_ms = max_over_ranks(float(np.sum(step_ms)), world, "cuda")
-    fe_timed = args.steps * wl.colonies * wl.ants * world
+    fe_timed = args.steps * per_step * wl.colonies * wl.ants * world
     value = fe_timed / (elapsed_ms / 1e3)
 
     # ---- end to end through the public API: host keys/seeds in, tours out;
@@ -388,7 +400,9 @@ def run_gb300(args, rank: int, world: int) -> None:
         "config": {"workload": wl.description, "colonies": wl.colonies, "ants": wl.ants,
                    "n_range": [int(wl.sizes().min()), int(wl.sizes().max())],
                    "l2": "flushed before every timed step (258 MB write)",
-                   "timed_iterations_start_at": wl.precondition + args.warmup,
+                   "iterations_per_step": per_step,
+                   "timed_iterations": [first, first + per_step * args.steps],
+                   "colony_chains": plan["chains"],
                    "registration_seconds": registration_s, "size_classes": classes},
         "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d / e2e_iters,
                 "d2h_bytes_per_step": d2h / e2e_iters, "iterations": e2e_iters,
@@ -407,7 +421,7 @@ def run_gb300(args, rank: int, world: int) -> None:
                      "ant_kernel_ms": ant_ms / kernel_steps, "update_kernel_ms": upd_ms / kernel_steps},
         "cpu_baseline": base,
         "clocks": clocks.summary(),
-        "gpu_launches": (classes + 1) * args.steps,
+        "gpu_launches": plan["launches_per_iteration"] * per_step * args.steps,
     }
     if steady is not None:
         line["steady_state"] = steady
@@ -517,6 +531,7 @@ def run_population(args, rank: int, world: int) -> None:
             torch.distributed.barrier()
     assert len(res) == POP_PROGRAMS and all(len(r["items"][0]["tour"]) == POP_N for r in res)
     elapsed_ms = max_over_ranks(float(np.sum(dev_ms)), world, "cuda")
+    plan = engine.launch_plan()
     engine.close()
     if rank != 0:
         return
@@ -532,7 +547,7 @@ def run_population(args, rank: int, world: int) -> None:
         "config": {"workload": "GP evaluation batch: 1 uniform N=500 instance (seed 2), 128 random controller "
                                "programs (depth <= 6), one colony each, 32 ants, k=16, 1000 "
                                "iterations; a step is one evaluate_population_evaluations call",
-                   "controller": controller,
+                   "controller": controller, "colony_chains": plan["chains"],
                    "l2": "each step runs 1000 iterations; the panel's working set (~30 MB) is L2-resident by design"},
         "e2e": {"value": e2e, "unit": "individuals/s", "h2d_bytes_per_step": float(keys.nbytes + seeds.nbytes),
                 "d2h_bytes_per_step": float(POP_PROGRAMS * (POP_N * 4 + 8)),
@@ -540,7 +555,7 @@ def run_population(args, rank: int, world: int) -> None:
         "roofline": None,
         "cpu_baseline": base,
         "clocks": clocks.summary(),
-        "gpu_launches": (1 + (3 if args.controller == 2 else 2) * POP_ITERATIONS) * args.steps,
+        "gpu_launches": (1 + plan["launches_per_iteration"] * POP_ITERATIONS) * args.steps,
     }
     print(json.dumps(line), flush=True)
 

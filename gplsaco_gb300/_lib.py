@@ -28,7 +28,7 @@ EXPORTED = (
     "faco_ant_diagnostic", "faco_pheromone_step", "faco_begin", "faco_step", "faco_step_timed", "faco_finish",
     "faco_engine_stream", "faco_evaluate_programs", "faco_mlp_param_count", "faco_mlp_forward", "faco_mlp_gradient",
     "faco_mlp_train", "faco_edge_data", "faco_prior_set", "faco_prior_refresh", "faco_current_costs",
-    "faco_set_mne_targets",
+    "faco_set_mne_targets", "faco_get_launch_plan",
     "faco_pheromone_step_noalloc", "faco_begin_programs", "faco_snapshot", "faco_restore",
     "faco_evaluate_controllers", "faco_validate_controller", "faco_score_controllers",
 )
@@ -40,7 +40,12 @@ class Settings(C.Structure):
                 ("p_best", C.c_double), ("epoch_source_probability", C.c_double),
                 ("ls_evaluation_limit", C.c_uint64), ("initial_ls_evaluation_limit", C.c_uint64),
                 ("ls_mode", C.c_uint32), ("autotune", C.c_uint32), ("workspace", C.c_uint32),
-                ("force_fingerprint_collisions", C.c_uint32)]
+                ("force_fingerprint_collisions", C.c_uint32), ("chains", C.c_uint32)]
+
+
+class LaunchPlan(C.Structure):
+    _fields_ = [("size_classes", C.c_uint32), ("chains", C.c_uint32), ("graph_iterations", C.c_uint32),
+                ("launches_per_iteration", C.c_uint32)]
 
 
 class Registration(C.Structure):
@@ -155,6 +160,7 @@ def load():
     L.faco_begin.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32]
     L.faco_step.argtypes = [vp, C.c_uint32]
     L.faco_step_timed.argtypes = [vp, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.faco_get_launch_plan.argtypes = [vp, C.POINTER(LaunchPlan)]
     L.faco_finish.argtypes = [vp, C.POINTER(Outputs)]
     L.faco_engine_stream.argtypes = [vp]
     L.faco_engine_stream.restype = vp

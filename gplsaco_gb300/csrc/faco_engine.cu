@@ -34,6 +34,9 @@ thread_local std::string g_error;
 
 // Iterations captured per CUDA graph (replayed until the budget is spent).
 constexpr std::uint32_t kGraphIterations = 16;
+// Automatic chain count: one chain per kColoniesPerChain colonies, at most kMaxChains.
+constexpr std::uint32_t kColoniesPerChain = 32;
+constexpr std::uint32_t kMaxChains = 8;
 
 struct Error : std::runtime_error {
     int code;
@@ -257,6 +260,7 @@ struct faco_engine {
     DeviceBuffer<faco::ColonyState> states;
     DeviceBuffer<faco::ColonyView> colonies;
     DeviceBuffer<uint2> work;
+    DeviceBuffer<std::uint32_t> chain_colonies;
     DeviceBuffer<faco::TraceRow> trace;
     DeviceBuffer<faco::node_t> checkpoints;
     // 12-feature controller (feature spec 2)
@@ -284,6 +288,16 @@ struct faco_engine {
         int mode = faco::kModeEngine;   // or kModeEngineGlobal (tour/inverse in global memory)
         faco::AntLaunch L{};
     };
+    // A chain: a subset of the colonies of one size class, whose iterations
+    // depend only on one another.  In the evaluation's graph each chain runs
+    // its own sequence of ant launches and updates, so one chain's slowest
+    // ants overlap the other chains' work instead of idling the GPU at every
+    // iteration.
+    struct Chain {
+        std::uint32_t first = 0, count = 0;   // colonies chain_colonies[first, first + count)
+        std::uint32_t cls = 0, first_job = 0, blocks = 0;   // its ant launch: class, jobs
+        faco::AntLaunch L{};
+    };
     struct EvalState {
         bool active = false;
         std::uint32_t count = 0, n_max = 0, trace_cap = 0, done = 0;
@@ -296,6 +310,7 @@ struct faco_engine {
         std::uint32_t feature_spec = 0;         // 2 or 3 for controlled evaluations
         std::vector<std::uint32_t> decision_points;
         std::vector<AntClass> classes;
+        std::vector<Chain> chains;
         faco::ColonyParams P{};
         faco::AntLaunch L{};
         cudaGraph_t graph = nullptr;
@@ -381,6 +396,7 @@ int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_setting
         require(c.ls_mode == FACO_LS_TWO_OPT || c.ls_mode == FACO_LS_TWO_OPT_OR_OPT, "unknown local-search mode");
         require(c.workspace <= FACO_WORKSPACE_GLOBAL, "unknown ant workspace placement");
         require(c.force_fingerprint_collisions <= 1, "force_fingerprint_collisions must be 0 or 1");
+        require(c.chains <= 64, "chains must be in [0, 64]");
         auto e = std::make_unique<faco_engine>();
         e->settings = c;
         e->dimension = dimension;
@@ -576,24 +592,82 @@ void enqueue_ants(faco_engine* e, cudaStream_t st) {
     for (std::size_t i = 1; i < branches; ++i) cuda_check(cudaStreamWaitEvent(st, e->branch_events[i], 0), "join wait");
 }
 
-// The colony update of one iteration (with the 12-feature controller, the
-// ants' fingerprints first, one warp per ant).
-void enqueue_update(faco_engine* e, cudaStream_t st) {
+// The colony update of one iteration for `colonies` colonies (those of
+// `list`, or all when null); with the 12-feature controller the ants'
+// fingerprints first, one warp per ant.
+void enqueue_update(faco_engine* e, cudaStream_t st, const std::uint32_t* list, std::uint32_t colonies) {
     auto& v = e->eval;
     if (v.P.ref_control) {
-        const std::uint32_t warps = v.count * v.P.ants;
-        faco::fingerprint_kernel<<<(warps + 7) / 8, 256, 0, st>>>(e->colonies.get(), v.P.ants, v.count,
+        const std::uint32_t warps = colonies * v.P.ants;
+        faco::fingerprint_kernel<<<(warps + 7) / 8, 256, 0, st>>>(e->colonies.get(), list, v.P.ants, colonies,
                                                                  v.P.zero_fingerprints);
     }
-    faco::colony_update_kernel<<<v.count, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
-                                                         v.P, v.trace_cap ? e->trace.get() : nullptr, v.count,
-                                                         v.trace_cap);
+    faco::colony_update_kernel<<<colonies, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
+                                                          v.P, v.trace_cap ? e->trace.get() : nullptr, list,
+                                                          v.count, v.trace_cap);
     cuda_check(cudaGetLastError(), "update launch");
 }
+
+void enqueue_update(faco_engine* e, cudaStream_t st) { enqueue_update(e, st, nullptr, e->eval.count); }
 
 void enqueue_iteration(faco_engine* e, cudaStream_t st) {
     enqueue_ants(e, st);
     enqueue_update(e, st);
+}
+
+// One iteration of chain `g`: its ant launch, then its colonies' update,
+// both on `st`.
+void enqueue_chain_iteration(faco_engine* e, std::size_t g, cudaStream_t st) {
+    auto& v = e->eval;
+    const auto& ch = v.chains[g];
+    const auto& c = v.classes[ch.cls];
+    cuda_check(faco::launch_ant_kernel(c.mode, ch.L, ch.blocks, c.warps, c.smem, st), "ant launch");
+    enqueue_update(e, st, e->chain_colonies.get() + ch.first, ch.count);
+}
+
+// Streams and events for `branches` parallel graph branches besides `st`.
+void ensure_branches(faco_engine* e, std::size_t branches) {
+    while (e->branch_streams.size() < branches) {
+        cudaStream_t bs;
+        cuda_check(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "branch stream");
+        e->branch_streams.push_back(bs);
+    }
+    while (e->branch_events.size() < branches + 2) {
+        cudaEvent_t ev;
+        cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "branch event");
+        e->branch_events.push_back(ev);
+    }
+}
+
+// `iterations` iterations of every colony; with more than one chain, each
+// chain's iterations run on their own stream, forked from and joined back
+// into `st` (independent branches when captured into a graph).
+void enqueue_iterations(faco_engine* e, cudaStream_t st, std::uint32_t iterations) {
+    auto& v = e->eval;
+    const std::size_t chains = v.chains.size();
+    if (chains <= 1) {
+        for (std::uint32_t i = 0; i < iterations; ++i) enqueue_iteration(e, st);
+        return;
+    }
+    cuda_check(cudaEventRecord(e->branch_events[0], st), "fork");
+    for (std::size_t g = 1; g < chains; ++g)
+        cuda_check(cudaStreamWaitEvent(e->branch_streams[g - 1], e->branch_events[0], 0), "fork wait");
+    for (std::uint32_t i = 0; i < iterations; ++i)
+        for (std::size_t g = 0; g < chains; ++g) enqueue_chain_iteration(e, g, g == 0 ? st : e->branch_streams[g - 1]);
+    for (std::size_t g = 1; g < chains; ++g) {
+        cuda_check(cudaEventRecord(e->branch_events[g], e->branch_streams[g - 1]), "join");
+        cuda_check(cudaStreamWaitEvent(st, e->branch_events[g], 0), "join wait");
+    }
+}
+
+// The evaluation's graph: kGraphIterations iterations, replayed.
+void capture_graph(faco_engine* e, cudaStream_t st) {
+    auto& v = e->eval;
+    destroy_graph(e);
+    cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    enqueue_iterations(e, st, kGraphIterations);
+    cuda_check(cudaStreamEndCapture(st, &v.graph), "end capture");
+    cuda_check(cudaGraphInstantiate(&v.exec, v.graph, 0), "graph instantiate");
 }
 
 // Kernel variant of a size class: the global-memory workspace (tour and
@@ -715,6 +789,36 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
         cl.smem = class_smem(cl.mode, cl.n_max, cl.warps);
         all.insert(all.end(), jobs.begin(), jobs.end());
     }
+    // chains: each size class split into pieces in proportion to its
+    // colony count (G pieces over all classes), its colonies dealt
+    // round-robin (largest instances first) so that the pieces are alike;
+    // each chain's jobs are a second copy of the work table
+    const std::uint32_t count = v.count;
+    const std::uint32_t G = std::min(c.chains ? c.chains : std::clamp(count / kColoniesPerChain, 1u, kMaxChains), count);
+    v.chains.clear();
+    if (G > 1) {
+        std::vector<std::uint32_t> list;
+        for (std::size_t i = 0; i < members.size(); ++i) {
+            const std::uint32_t m = static_cast<std::uint32_t>(members[i].size());
+            const std::uint32_t pieces = std::clamp((G * m + count / 2) / count, 1u, m);
+            for (std::uint32_t j = 0; j < pieces; ++j) {
+                std::vector<std::uint32_t> piece;
+                for (std::uint32_t t = j; t < m; t += pieces) piece.push_back(members[i][t]);
+                const auto jobs = jobs_for(piece, v.classes[i].warps);
+                faco_engine::Chain ch;
+                ch.first = static_cast<std::uint32_t>(list.size());
+                ch.count = static_cast<std::uint32_t>(piece.size());
+                ch.cls = static_cast<std::uint32_t>(i);
+                ch.first_job = static_cast<std::uint32_t>(all.size());
+                ch.blocks = static_cast<std::uint32_t>(jobs.size());
+                v.chains.push_back(ch);
+                all.insert(all.end(), jobs.begin(), jobs.end());
+                list.insert(list.end(), piece.begin(), piece.end());
+            }
+        }
+        if (v.chains.size() == 1) v.chains.clear();
+        else e->chain_colonies.upload(list, s);
+    }
     e->work.upload(all, s);
     // the dynamic shared-memory limit is a property of each kernel variant,
     // shared by every class that uses it: it must admit the largest one
@@ -724,6 +828,7 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
         auto& m = smem_max[cl.mode == faco::kModeEngineGlobal ? 1 : 0];
         m = std::max(m, cl.smem);
     }
+    for (auto& ch : v.chains) ch.L = launch_of(ch.first_job, v.classes[ch.cls].warps, v.classes[ch.cls].n_max);
     if (smem_max[0]) cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem_max[0]), "cudaFuncSetAttribute");
     if (smem_max[1])
         cuda_check(faco::prepare_ant_kernel(faco::kModeEngineGlobal, smem_max[1]), "cudaFuncSetAttribute");
@@ -962,23 +1067,10 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     faco::colony_init_kernel<<<count, 256, 0, s>>>(e->d_instances.get(), e->colonies.get(), e->states.get(), v.P,
                                                    count);
     cuda_check(cudaGetLastError(), "init launch");
-    while (e->branch_streams.size() + 1 < v.classes.size()) {
-        cudaStream_t bs;
-        cuda_check(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "branch stream");
-        e->branch_streams.push_back(bs);
-    }
-    while (e->branch_events.size() < v.classes.size() + 1) {
-        cudaEvent_t ev;
-        cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "branch event");
-        e->branch_events.push_back(ev);
-    }
     build_work_tables(e, members, class_ids);
+    ensure_branches(e, std::max(v.classes.size(), v.chains.size()));
     // one graph of kGraphIterations iterations, replayed; the batch index is device state
-    destroy_graph(e);
-    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
-    for (std::uint32_t i = 0; i < kGraphIterations; ++i) enqueue_iteration(e, s);
-    cuda_check(cudaStreamEndCapture(s, &v.graph), "end capture");
-    cuda_check(cudaGraphInstantiate(&v.exec, v.graph, 0), "graph instantiate");
+    capture_graph(e, s);
     v.done = 0;
     v.active = true;
 }
@@ -991,7 +1083,7 @@ void step_evaluation(faco_engine* e, std::uint32_t iterations) {
         cuda_check(cudaGraphLaunch(v.exec, e->stream), "graph launch");
         left -= kGraphIterations;
     }
-    for (; left; --left) enqueue_iteration(e, e->stream);
+    if (left) enqueue_iterations(e, e->stream, left);
     v.done += iterations;
 }
 
@@ -1422,6 +1514,21 @@ int faco_step_timed(faco_engine* e, uint32_t iterations, double* ant_ms, double*
         v.done += iterations;
         *ant_ms = a;
         *update_ms = u;
+    });
+}
+
+int faco_get_launch_plan(faco_engine* e, faco_launch_plan* plan) {
+    return guarded([&] {
+        require(e && plan, "null argument");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        const auto& v = e->eval;
+        const std::uint32_t per_update = v.P.ref_control ? 2u : 1u;   // fingerprints + update
+        const auto chains = static_cast<std::uint32_t>(v.chains.size());
+        plan->size_classes = static_cast<std::uint32_t>(v.classes.size());
+        plan->chains = chains;
+        plan->graph_iterations = kGraphIterations;
+        plan->launches_per_iteration = chains ? chains * (1 + per_update) : plan->size_classes + per_update;
     });
 }
 

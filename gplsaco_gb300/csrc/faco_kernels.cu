@@ -1181,13 +1181,16 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
 }
 
 // Fingerprints (and node-0 positions) of every ant's tour of a batch, one
-// warp per ant over all colonies (fingerprint_ants, control_state.cuh:45-64);
-// `zero` forces every fingerprint to 0 (the collision diagnostic).
-__global__ void __launch_bounds__(256) fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants,
-                                                          std::uint32_t colony_count, std::uint32_t zero) {
+// warp per ant over the colonies of `list` (all colonies when null)
+// (fingerprint_ants, control_state.cuh:45-64); `zero` forces every
+// fingerprint to 0 (the collision diagnostic).
+__global__ void __launch_bounds__(256) fingerprint_kernel(const ColonyView* colonies, const std::uint32_t* list,
+                                                          std::uint32_t ants, std::uint32_t colony_count,
+                                                          std::uint32_t zero) {
     const std::uint32_t job = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (job >= ants * colony_count) return;
-    const std::uint32_t colony = job / ants, ant = job % ants;
+    const std::uint32_t slot = job / ants, ant = job % ants;
+    const std::uint32_t colony = list ? list[slot] : slot;
     const ColonyView& cv = colonies[colony];
     std::uint32_t p0;
     const Fingerprint f = warp_fingerprint(cv.ant_tours + (size_t)ant * cv.n_pad, cv.n, lane, p0);
@@ -1283,12 +1286,15 @@ __device__ __forceinline__ void write_trace(TraceRow& row, const ColonyState& st
 }
 
 // Fused reduce_and_select + update_pheromone for one colony, then (GP-controlled
-// evaluations) the controller decision for the next iteration.
+// evaluations) the controller decision for the next iteration.  Block b
+// updates colony list[b] (colony b when `list` is null); `colony_count` is
+// the evaluation's colony count.
 __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* instances,
                                                             const ColonyView* colonies, ColonyState* states,
                                                             ColonyParams P, TraceRow* trace,
+                                                            const std::uint32_t* list,
                                                             std::uint32_t colony_count, std::uint32_t trace_cap) {
-    const std::uint32_t c = blockIdx.x;
+    const std::uint32_t c = list ? list[blockIdx.x] : blockIdx.x;
     const ColonyView cv = colonies[c];
     const InstanceView in = instances[cv.instance];
     const std::uint32_t n = in.n, k = in.k, A = P.ants;

@@ -45,11 +45,12 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
 
 __global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
                                    ColonyParams P, std::uint32_t colony_count);
-__global__ void fingerprint_kernel(const ColonyView* colonies, std::uint32_t ants, std::uint32_t colony_count,
-                                   std::uint32_t zero);
+__global__ void fingerprint_kernel(const ColonyView* colonies, const std::uint32_t* list, std::uint32_t ants,
+                                   std::uint32_t colony_count, std::uint32_t zero);
 __global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,
                                      ColonyState* states, ColonyParams P, TraceRow* trace,
-                                     std::uint32_t colony_count, std::uint32_t trace_cap);
+                                     const std::uint32_t* list, std::uint32_t colony_count,
+                                     std::uint32_t trace_cap);
 __global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
                                       const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
                                       const float* eta, float* trails, float* products);

@@ -44,12 +44,13 @@ class FixedFacoSettings:
     autotune: int = 1
     workspace: int = 0      # 0 auto, 1 shared memory, 2 global memory (ant tour/inverse placement)
     force_fingerprint_collisions: int = 0   # diagnostic: all 12-feature-controller fingerprints 0
+    chains: int = 0         # independent colony chains per graph (0 auto); results do not depend on it
 
     def to_c(self) -> _lib.Settings:
         s = _lib.Settings()
         for name in ("ants", "primary_width", "backup_width", "ls_width", "ls_evaluation_limit",
                      "initial_ls_evaluation_limit", "ls_mode", "autotune", "workspace",
-                     "force_fingerprint_collisions"):
+                     "force_fingerprint_collisions", "chains"):
             setattr(s, name, _exact_int(getattr(self, name), name))
         for name in ("beta", "retention", "p_best", "epoch_source_probability"):
             value = getattr(self, name)
@@ -384,6 +385,13 @@ class FacoBatchEngine:
         keys, cap, done = self._active
         self._active = (keys, cap, done + iterations)
         return ant_ms.value, update_ms.value
+
+    def launch_plan(self) -> dict:
+        """The active (or most recent) evaluation's size classes, colony
+        chains, iterations per graph replay and kernel launches per iteration."""
+        plan = _lib.LaunchPlan()
+        _lib.check(self._L.faco_get_launch_plan(self._handle, C.byref(plan)))
+        return {name: int(getattr(plan, name)) for name, _ in plan._fields_}
 
     def finish(self) -> dict:
         keys, cap, done = self._active

@@ -56,6 +56,8 @@ typedef struct faco_settings {
     uint32_t force_fingerprint_collisions; /* diagnostic (batch_engine.hpp:66): every tour fingerprint
                                               of the 12-feature controller is 0, so its archive
                                               compares whole tours; 0 in production */
+    uint32_t chains; /* independent colony chains in the evaluation's graph (0: one per 32
+                        colonies, at most 8); results do not depend on it */
 } faco_settings;
 
 void faco_default_settings(faco_settings* s);
@@ -229,6 +231,18 @@ int faco_step(faco_engine* engine, uint32_t iterations);
 int faco_step_timed(faco_engine* engine, uint32_t iterations, double* ant_milliseconds,
                     double* update_milliseconds);
 int faco_finish(faco_engine* engine, faco_outputs* out);
+/* The launch plan of the active or most recent evaluation (no counterpart
+ * in the reference; zeros before the first): its size classes, its colony chains (independent branches of
+ * the graph; 0 when the colonies run as one), the iterations captured per
+ * graph (faco_step of that many iterations replays the graph once) and the
+ * kernel launches per iteration. */
+typedef struct faco_launch_plan {
+    uint32_t size_classes;
+    uint32_t chains;
+    uint32_t graph_iterations;
+    uint32_t launches_per_iteration;
+} faco_launch_plan;
+int faco_get_launch_plan(faco_engine* engine, faco_launch_plan* plan);
 /* The engine's cudaStream_t (for events recorded by the caller). */
 void* faco_engine_stream(faco_engine* engine);
 

@@ -670,3 +670,45 @@ def test_conditional_controllers_match_oracle(api, oracle, n, ants, iterations):
                                                  controllers[0], 0xFFFF0FFF)
     assert [it["cost"] for it in one["items"]] == [it["cost"] for it in res[0]["items"]]
     engine.close()
+
+
+@pytest.mark.parametrize("chains", [2, 3, 5])
+def test_colony_chains_change_nothing(api, oracle, chains):
+    """Colonies split into independent chains in the evaluation's graph
+    (iterations of different chains overlap) give the results of the
+    unchained run bit for bit: tours, costs and every trace row, over two
+    graph replays and a remainder; plain FACO on an uneven batch and the
+    12-feature controller with decision captures."""
+    sizes = [200, 537, 1000, 311]
+    ants, iterations = 8, 37
+    xys = [_cases.uniform_instance(n, seed=200 + i) for i, n in enumerate(sizes)]
+    keys = np.array([1003, 1000, 1002, 1001, 1002, 1000, 1003], np.uint64)
+    seeds = np.arange(11, 18, dtype=np.uint64)
+    program = _programs.random_program(np.random.default_rng(5), features=12, feature_spec_id=2)
+    runs = {}
+    for ch in (1, chains):
+        settings = api.FixedFacoSettings(ants=ants, primary_width=16, backup_width=64, ls_width=20, retention=0.9,
+                                         chains=ch)
+        engine = api.FacoBatchEngine(1000, keys.size, settings)
+        for i, xy in enumerate(xys):
+            engine.register_problem(1000 + i, xy.astype(np.float64))
+        plain = engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8, trace=True)
+        controlled = engine.evaluate_program_evaluations(keys, seeds, ants * iterations, program, trace=True,
+                                                         decision_iterations=[1, 20, iterations])
+        runs[ch] = (plain, controlled)
+        engine.close()
+    for a, b in zip(runs[1], runs[chains]):
+        assert [it["tour"] for it in a["items"]] == [it["tour"] for it in b["items"]]
+        assert [it["cost"] for it in a["items"]] == [it["cost"] for it in b["items"]]
+        assert np.array_equal(a["trace"], b["trace"])
+    da, db = runs[1][1]["decisions"], runs[chains][1]["decisions"]
+    assert len(da) == len(db) == 3 * keys.size
+    for x, y in zip(da, db):
+        assert x["action"] == y["action"]
+        assert np.array_equal(np.asarray(x["features"], np.float32).view(np.uint32),
+                              np.asarray(y["features"], np.float32).view(np.uint32))
+    xy = xys[2]
+    key = oracle.lib().orc_colony_key(int(seeds[2]), int(keys[2]))
+    ref = oracle.run_colony(xy, oracle.prepare(xy, 16, 64, 20), ants=ants, k=16, b=64, w=20, mne=8,
+                            iterations=iterations, key=key, retention=0.9)
+    assert runs[chains][0]["items"][2]["cost"] == ref["cost"]
