@@ -153,7 +153,7 @@ def load():
     L.faco_mlp_gradient.argtypes = [vp, vp, vp, C.c_uint32, vp, vp]
     L.faco_mlp_train.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, vp]
     L.faco_edge_data.argtypes = [vp, vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]
-    L.faco_prior_set.argtypes = [vp, vp, C.c_float, C.c_int, vp]
+    L.faco_prior_set.argtypes = [vp, vp, C.c_float, C.c_int, vp, C.c_uint32]
     L.faco_prior_refresh.argtypes = [vp]
     L.faco_current_costs.argtypes = [vp, vp, C.POINTER(C.c_uint32)]
     L.faco_set_mne_targets.argtypes = [vp, vp, C.c_uint32]

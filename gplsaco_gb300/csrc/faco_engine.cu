@@ -274,6 +274,7 @@ struct faco_engine {
     DeviceBuffer<faco::MlpParams> prior_params;
     DeviceBuffer<faco::MlpOperands> prior_ops;
     DeviceBuffer<std::uint8_t> prior_enabled;
+    DeviceBuffer<std::uint32_t> prior_modes;   // per colony: 1 = the prior re-ranks departures only
     float prior_floor = 0.05f;
     int prior_gamma = 1;
     bool prior_loaded = false;
@@ -1049,6 +1050,9 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.P.ref_control = spec == 2;
     v.P.zero_fingerprints = e->settings.force_fingerprint_collisions;
     v.P.ls_limit = e->settings.ls_evaluation_limit;
+    e->prior_modes.resize(count);
+    cuda_check(cudaMemsetAsync(e->prior_modes.get(), 0, count * sizeof(std::uint32_t), s), "memset");
+    v.P.prior_rows = e->prior_modes.get();
     if (control.n_decisions) {
         v.P.capture = faco::DecisionCapture{e->decision_points.get(), control.n_decisions, e->decision_features.get(),
                                             e->decision_scores.get(), e->decision_masks.get(),
@@ -2175,9 +2179,13 @@ static void apply_prior(faco_engine* e) {
         e->prior_ops.get(), e->prior_floor, e->prior_gamma, e->prior_gnbr.get(), e->prior_offsets.get(),
         e->error.get());
     cuda_check(cudaGetLastError(), "prior apply");
+    faco::prior_rows_kernel<<<v.count, 256, 0, e->stream>>>(e->d_instances.get(), e->colonies.get(),
+                                                            e->prior_modes.get());
+    cuda_check(cudaGetLastError(), "prior rows");
 }
 
-int faco_prior_set(faco_engine* e, const float* params, float floor, int gamma, const uint8_t* enabled) {
+int faco_prior_set(faco_engine* e, const float* params, float floor, int gamma, const uint8_t* enabled,
+                   uint32_t departures) {
     return guarded([&] {
         require(e && enabled, "null argument");
         std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
@@ -2194,7 +2202,11 @@ int faco_prior_set(faco_engine* e, const float* params, float floor, int gamma, 
         require(gamma == 1 || gamma == 2, "the prior exponent must be 1 or 2");
         e->prior_floor = floor;
         e->prior_gamma = gamma;
+        require(departures <= 1, "departures must be 0 or 1");
         e->prior_enabled.upload(enabled, v.count, e->stream);
+        std::vector<std::uint32_t> modes(v.count);
+        for (std::uint32_t c = 0; c < v.count; ++c) modes[c] = enabled[c] && departures ? 1u : 0u;
+        e->prior_modes.upload(modes, e->stream);
         apply_prior(e);
     });
 }

@@ -468,6 +468,36 @@ __device__ __forceinline__ void trail_update(std::uint32_t n, std::uint32_t k, c
     }
 }
 
+// Products of a colony whose prior re-ranks departures only: per node row,
+// the parent-tour entries keep the instance heuristic (products = trail *
+// eta), and the other entries take the prior's heuristic scaled so that
+// their total weight equals the plain total, sum(trail * eta) over the
+// non-parent entries.  An ant then leaves the parent tour as often as a
+// plain ant does, and the prior only decides where it goes.  Rows over
+// [first, n) with the given stride; trails are already updated.
+__device__ __forceinline__ void departure_rows(const InstanceView& in, const ColonyView& cv, std::uint32_t first,
+                                               std::uint32_t stride) {
+    const std::uint32_t n = in.n, k = in.k;
+    for (std::uint32_t i = first; i < n; i += stride) {
+        const std::uint32_t nb = cv.parent_nbr[i], succ = nb & 0xffffu, pred = nb >> 16;
+        const std::size_t row = (std::size_t)i * k;
+        float plain = 0.0f, prior = 0.0f;
+        for (std::uint32_t j = 0; j < k; ++j) {
+            const std::uint32_t node = in.primary[row + j];
+            if (node == succ || node == pred) continue;
+            const float t = cv.trails[row + j];
+            plain += t * in.eta[row + j];
+            prior += t * cv.eta[row + j];
+        }
+        const float scale = prior > 0.0f ? plain / prior : 1.0f;
+        for (std::uint32_t j = 0; j < k; ++j) {
+            const std::uint32_t node = in.primary[row + j];
+            const float t = cv.trails[row + j];
+            cv.products[row + j] = node == succ || node == pred ? t * in.eta[row + j] : t * cv.eta[row + j] * scale;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // GP controller pieces (the engine's feature spec 3; the same arithmetic is
 // restated on the CPU beside the oracle colony run).
@@ -1180,6 +1210,16 @@ __device__ void ref_decide(const ColonyView& cv, const InstanceView& in, ColonyS
     __syncthreads();
 }
 
+// Departure-only prior products (departure_rows) of the colonies whose mode
+// is 1, one block per colony: run after the prior's heuristic is applied.
+__global__ void __launch_bounds__(256) prior_rows_kernel(const InstanceView* instances, const ColonyView* colonies,
+                                                         const std::uint32_t* modes) {
+    const std::uint32_t c = blockIdx.x;
+    if (!modes[c]) return;
+    const ColonyView cv = colonies[c];
+    departure_rows(instances[cv.instance], cv, threadIdx.x, blockDim.x);
+}
+
 // Fingerprints (and node-0 positions) of every ant's tour of a batch, one
 // warp per ant over the colonies of `list` (all colonies when null)
 // (fingerprint_ants, control_state.cuh:45-64); `zero` forces every
@@ -1380,6 +1420,10 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
     __syncthreads();
     trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, cv.eta, cv.trails,
                  cv.products, threadIdx.x, blockDim.x);
+    if (P.prior_rows && P.prior_rows[c]) {
+        __syncthreads();
+        departure_rows(in, cv, threadIdx.x, blockDim.x);
+    }
     std::int32_t action = -1;
     if (P.ref_control) {
         // the 12-feature controller: the trace row holds the action this

@@ -28,6 +28,7 @@ struct ColonyParams {
     std::uint32_t zero_fingerprints; // diagnostic: every tour fingerprint 0 (forced collisions)
     unsigned long long ls_limit;     // LS evaluation budget per ant (LS-work feedback)
     DecisionCapture capture;         // decisions to record (count 0: none)
+    const std::uint32_t* prior_rows; // per colony: 1 = the prior re-ranks departures only (device; may be null)
 };
 
 // Candidate rows of registration on the GPU (faco_knn.cu): per node its
@@ -45,6 +46,8 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
 
 __global__ void colony_init_kernel(const InstanceView* instances, const ColonyView* colonies, ColonyState* states,
                                    ColonyParams P, std::uint32_t colony_count);
+__global__ void prior_rows_kernel(const InstanceView* instances, const ColonyView* colonies,
+                                  const std::uint32_t* modes);
 __global__ void fingerprint_kernel(const ColonyView* colonies, const std::uint32_t* list, std::uint32_t ants,
                                    std::uint32_t colony_count, std::uint32_t zero);
 __global__ void colony_update_kernel(const InstanceView* instances, const ColonyView* colonies,

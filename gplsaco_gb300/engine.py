@@ -539,13 +539,18 @@ class FacoBatchEngine:
         _lib.check(self._L.faco_edge_data(self._handle, _lib.ptr(x), _lib.ptr(y), rows.value, C.byref(rows)))
         return x, y
 
-    def prior_set(self, params, enabled, floor: float = 0.05, gamma: int = 1) -> None:
+    def prior_set(self, params, enabled, floor: float = 0.05, gamma: int = 1, departures: bool = False) -> None:
         """Reweights eta by (floor + p)^gamma on colonies with enabled[c]; the
-        others use the plain heuristic.  params None keeps the loaded network."""
+        others use the plain heuristic.  params None keeps the loaded network.
+        departures: the prior only re-ranks the departures from the parent
+        tour (parent-tour entries keep the plain heuristic, the others keep
+        the plain total weight per node)."""
         enabled = np.ascontiguousarray(enabled, np.uint8)
         p = None if params is None else np.ascontiguousarray(params, np.float32)
+        if type(departures) is not bool:
+            raise ValueError("departures must be a bool")
         _lib.check(self._L.faco_prior_set(self._handle, _lib.ptr(p), float(floor), _exact_int(gamma, "gamma", 1, 2),
-                                          enabled.ctypes.data))
+                                          enabled.ctypes.data, int(departures)))
 
     def prior_refresh(self) -> None:
         _lib.check(self._L.faco_prior_refresh(self._handle))

@@ -43,17 +43,23 @@ class GapConfig:
     extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
     # Both arms are tuned on validation instances (seeds 200-214) by wall-clock
     # time to the target gap: plain FACO over MNE targets, the prior over
-    # (model, floor, gamma, refresh, MNE).  "full" sees all seven features;
+    # (model, floor, gamma, refresh, MNE, departures).  "full" sees all seven features;
     # "geometry" only the geometric ones (trail level and best-tour membership
     # masked), so it does not pull ants back onto the parent tour's edges --
     # and, its inputs being static, needs no refresh.  refresh: iterations
     # between recomputations of the prior (0: never).  A sharp prior makes
     # ants walk the parent tour longer before their MNE-th new edge, so the
-    # prior's best MNE target can differ from plain FACO's.
+    # prior's best MNE target can differ from plain FACO's.  departures: the
+    # prior only re-ranks the departures from the parent tour (the parent's
+    # entries keep the plain heuristic, the others the plain total weight per
+    # node), so prior ants leave the parent tour as often as plain ants.
     mne_grid: tuple = (8, 6, 5, 4)
-    tune_grid: tuple = (("full", 0.5, 1, 10, 8), ("geometry", 0.2, 1, 0, 8), ("geometry", 0.2, 1, 0, 6),
-                        ("geometry", 0.05, 2, 0, 8), ("geometry", 0.05, 2, 0, 6), ("geometry", 0.05, 2, 0, 5),
-                        ("geometry", 0.05, 2, 0, 4), ("geometry", 0.2, 2, 0, 6))
+    tune_grid: tuple = (("full", 0.5, 1, 10, 8, False), ("geometry", 0.2, 1, 0, 8, False),
+                        ("geometry", 0.05, 2, 0, 8, False), ("geometry", 0.05, 2, 0, 6, False),
+                        ("geometry", 0.05, 2, 0, 5, False), ("geometry", 0.2, 2, 0, 6, False),
+                        ("geometry", 0.05, 2, 0, 8, True), ("geometry", 0.05, 2, 0, 6, True),
+                        ("geometry", 0.05, 2, 0, 5, True), ("geometry", 0.05, 1, 0, 5, True),
+                        ("full", 0.05, 2, 10, 5, True), ("full", 0.05, 2, 10, 6, True))
     train_pool: int = 32
     train_snapshot: int = 25
     train_iterations: int = 300
@@ -113,7 +119,8 @@ def reference_lengths(cfg: GapConfig, xys: list, device: int = 0) -> np.ndarray:
 
 
 def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0,
-            floor: float | None = None, gamma: int | None = None, refresh: int = 10, mne: int | None = None):
+            floor: float | None = None, gamma: int | None = None, refresh: int = 10, mne: int | None = None,
+            departures: bool = False):
     """One method on all evaluation instances (one colony each, seed 1).
     Returns rows (iteration, seconds, mean gap, costs), the fallback mask and
     the work per ant-iteration (construction steps, LS evaluations)."""
@@ -132,7 +139,7 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     costs, _ = engine.current_costs(len(xys))
     t0 = time.perf_counter()
     if params is not None:
-        engine.prior_set(params, enabled, floor, gamma)
+        engine.prior_set(params, enabled, floor, gamma, departures)
     rows.append((0, 0.0, float(np.mean((costs - refs) / refs)), costs.copy()))
     done = 0
     while done < cfg.iterations:
@@ -143,7 +150,7 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
             if done == cfg.warmup and plain_warmup_costs is not None:
                 now, _ = engine.current_costs(len(xys))
                 enabled = (now <= plain_warmup_costs).astype(np.uint8)
-                engine.prior_set(None, enabled, floor, gamma)
+                engine.prior_set(None, enabled, floor, gamma, departures)
             elif refresh and done % refresh == 0:
                 engine.prior_refresh()
         costs, _ = engine.current_costs(len(xys))
@@ -175,7 +182,8 @@ def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
 
 
 def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: int = 0, floor: float | None = None,
-             gamma: int | None = None, refresh: int = 10, prior_mne: int | None = None, mne: int | None = None):
+             gamma: int | None = None, refresh: int = 10, prior_mne: int | None = None, mne: int | None = None,
+             departures: bool = False):
     """Two colonies per instance, the instance's length the better of the
     two.  params None: both plain (seeds 1 and 2).  Otherwise colony 2 runs
     with the prior (at MNE target prior_mne) and colony 1 stays plain -- the
@@ -198,7 +206,7 @@ def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: i
     costs, _ = engine.current_costs(count)
     t0 = time.perf_counter()
     if params is not None:
-        engine.prior_set(params, np.tile(np.array([0, 1], np.uint8), len(xys)), floor, gamma)
+        engine.prior_set(params, np.tile(np.array([0, 1], np.uint8), len(xys)), floor, gamma, departures)
 
     def row(it, costs):
         best = costs.reshape(len(xys), 2).min(axis=1)
@@ -259,29 +267,31 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     for r in plain_tuning:
         del r["rows"]
     tuning = []
-    for model, floor, gamma, refresh, mne in cfg.tune_grid:
-        rows, _, work = gap_run(cfg, val, val_refs, models[model], val_warm[3], device, floor, gamma, refresh, mne)
+    for model, floor, gamma, refresh, mne, departures in cfg.tune_grid:
+        rows, _, work = gap_run(cfg, val, val_refs, models[model], val_warm[3], device, floor, gamma, refresh, mne,
+                                departures)
         t, it = first_time_below(rows, cfg.target_gap, extra_seconds=val_warm[1])
         tuning.append({"model": model, "floor": floor, "gamma": gamma, "refresh_every": refresh, "mne": mne,
-                       "final_gap": rows[-1][2], "iterations_to_target": it, "seconds_to_target": t, **work})
+                       "departures": departures, "final_gap": rows[-1][2], "iterations_to_target": it,
+                       "seconds_to_target": t, **work})
     best_row = min(tuning, key=lambda r: (r["seconds_to_target"] is None, r["seconds_to_target"] or 0.0,
                                           r["final_gap"]))
     best = (best_row["floor"], best_row["gamma"], best_row["refresh_every"])
-    best_model, prior_mne = best_row["model"], best_row["mne"]
+    best_model, prior_mne, departures = best_row["model"], best_row["mne"], best_row["departures"]
     log(f"validation plain: MNE {plain_mne}, {t_val} s, {val_work}; tuning {tuning} -> {best_model} {best} "
-        f"MNE {prior_mne}")
+        f"MNE {prior_mne} departures {departures}")
     xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
     refs = reference_lengths(cfg, xys, device)
     plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device, mne=plain_mne)
     warm = next(r for r in plain_rows if r[0] == cfg.warmup)
     prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, models[best_model], warm[3], device, *best,
-                                              mne=prior_mne)
+                                              mne=prior_mne, departures=departures)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
     # equal resources: two colonies per instance in both arms
     pair_plain, pair_plain_work = pair_run(cfg, xys, refs, None, device, mne=plain_mne)
     pair_prior, pair_prior_work = pair_run(cfg, xys, refs, models[best_model], device, *best, prior_mne=prior_mne,
-                                           mne=plain_mne)
+                                           mne=plain_mne, departures=departures)
 
     def targets(rows_a, rows_b):
         out = {}
@@ -298,7 +308,7 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         "prior_charged_warmup_seconds": warm[1],
         "prior_enabled_after_warmup": int(enabled.sum()), "instances": len(xys),
         "prior_setting": {"model": best_model, "floor": best[0], "gamma": best[1], "refresh_every": best[2],
-                          "mne": prior_mne},
+                          "mne": prior_mne, "departures": departures},
         "plain_setting": {"mne": plain_mne}, "plain_tuning": plain_tuning,
         "plain_work": plain_work, "prior_work": prior_work,
         "validation_plain": {"seconds_to_target": t_val, **val_work}, "tuning": tuning,

@@ -346,8 +346,13 @@ int faco_edge_data(faco_engine* engine, uint16_t* x, float* y, uint64_t capacity
  * keep the loaded ones): eta' = eta * (floor + p)^gamma (gamma 1 or 2),
  * products refreshed; floor > 0 so that no candidate is removed.  Colonies
  * with enabled[c] == 0 get the plain heuristic back (the per-instance
- * fallback). */
-int faco_prior_set(faco_engine* engine, const float* params, float floor, int gamma, const uint8_t* enabled);
+ * fallback).  departures = 1: the prior re-ranks only the departures from
+ * the parent tour -- per node, parent-tour entries keep the plain heuristic
+ * and the other entries' prior weights are scaled to the plain total, so an
+ * ant leaves the parent tour as often as a plain ant (every batch, after
+ * the trail update). */
+int faco_prior_set(faco_engine* engine, const float* params, float floor, int gamma, const uint8_t* enabled,
+                   uint32_t departures);
 /* Recomputes the prior from the colonies' current trails and best tours. */
 int faco_prior_refresh(faco_engine* engine);
 /* Current global-best lengths of the colonies (synchronises). */

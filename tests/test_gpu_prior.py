@@ -121,3 +121,46 @@ def test_edge_data_and_fallback(prior):
         assert np.array_equal(np.sort(t), np.arange(n))
         assert int(np.sum(m[t, np.roll(t, -1)])) == int(res["costs"][c])
     engine.close()
+
+
+def test_departures_prior(prior):
+    """The departures-only prior: disabled on every colony it is plain FACO
+    bit for bit; enabled (with and without departures) it gives valid
+    tours with exact lengths; a non-bool flag is refused."""
+    import gplsaco_gb300 as g
+    from oracle import oracle
+    n, ants, iterations = 400, 8, 12
+    xy = _cases.uniform_instance(n, seed=21)
+    settings = g.FixedFacoSettings(ants=ants, primary_width=20, retention=0.98)
+    keys = np.array([7, 7], np.uint64)
+    seeds = np.array([1, 2], np.uint64)
+    engine = g.FacoBatchEngine(n, 2, settings)
+    engine.register_problem(7, xy.astype(np.float64))
+    plain = engine.evaluate_faco_evaluations(keys, seeds, ants * iterations, 8)
+    params = prior.init_params(seed=4)
+    engine.begin(keys, seeds, 8)
+    engine.prior_set(params, np.zeros(2, np.uint8), 0.05, 2, departures=True)
+    engine.step(iterations)
+    res = engine.finish()
+    assert [int(c) for c in res["costs"]] == [it["cost"] for it in plain["items"]]
+    steps = {}
+    for departures in (False, True):
+        engine.begin(keys, seeds, 8)
+        engine.prior_set(params, np.ones(2, np.uint8), 0.05, 2, departures=departures)
+        engine.step(iterations)
+        res = engine.finish()
+        m = oracle.euc2d_matrix(xy)
+        for c in range(2):
+            t = np.asarray(res["tours"][c], np.int64)
+            assert np.array_equal(np.sort(t), np.arange(n))
+            assert int(np.sum(m[t, np.roll(t, -1)])) == int(res["costs"][c])
+        steps[departures] = res["construction_steps"]
+    with pytest.raises(ValueError):
+        engine.begin(keys, seeds, 8)
+        try:
+            engine.prior_set(params, np.ones(2, np.uint8), 0.05, 2, departures=1)
+        finally:
+            engine.finish()
+    engine.close()
+    assert steps[True] > 0 and steps[False] > 0
+    print("construction steps, prior / departures-only prior:", steps[False], steps[True])
