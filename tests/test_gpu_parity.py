@@ -672,13 +672,15 @@ def test_conditional_controllers_match_oracle(api, oracle, n, ants, iterations):
     engine.close()
 
 
-@pytest.mark.parametrize("chains", [2, 3, 5])
-def test_colony_chains_change_nothing(api, oracle, chains):
+@pytest.mark.parametrize("chains,workspace", [(2, 0), (3, 2), (5, 0)])
+def test_colony_chains_change_nothing(api, oracle, chains, workspace):
     """Colonies split into independent chains in the evaluation's graph
     (iterations of different chains overlap) give the results of the
     unchained run bit for bit: tours, costs and every trace row, over two
     graph replays and a remainder; plain FACO on an uneven batch and the
-    12-feature controller with decision captures."""
+    12-feature controller with decision captures; tours in shared memory and
+    in the global workspace (one slot per colony and ant, so concurrent
+    chains never share one)."""
     sizes = [200, 537, 1000, 311]
     ants, iterations = 8, 37
     xys = [_cases.uniform_instance(n, seed=200 + i) for i, n in enumerate(sizes)]
@@ -688,7 +690,7 @@ def test_colony_chains_change_nothing(api, oracle, chains):
     runs = {}
     for ch in (1, chains):
         settings = api.FixedFacoSettings(ants=ants, primary_width=16, backup_width=64, ls_width=20, retention=0.9,
-                                         chains=ch)
+                                         chains=ch, workspace=workspace)
         engine = api.FacoBatchEngine(1000, keys.size, settings)
         for i, xy in enumerate(xys):
             engine.register_problem(1000 + i, xy.astype(np.float64))
