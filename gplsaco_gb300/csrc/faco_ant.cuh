@@ -203,6 +203,102 @@ __device__ __forceinline__ void relocate_shift(const AntSmem& s, std::uint32_t l
     }
 }
 
+// Reverses tour[lo..hi] (inclusive, lo <= hi, no wrap) with the inverse.
+__device__ __forceinline__ void reverse_range(const AntSmem& s, std::uint32_t lane, std::uint32_t lo,
+                                              std::uint32_t hi) {
+    const std::uint32_t count = hi - lo + 1;
+    for (std::uint32_t o = lane; o < count / 2; o += 32) {
+        const std::uint32_t l = lo + o, r = hi - o;
+        const node_t a = s.tour[l], b = s.tour[r];
+        s.tour[l] = b; s.tour[r] = a;
+        s.pos[b] = (node_t)l; s.pos[a] = (node_t)r;
+    }
+    __syncwarp();
+}
+
+// A run of relocations deferred during construction.  Once trails converge
+// an ant mostly follows parent edges: after it takes a node x from its place
+// to after the current node, its next nodes are x's old tour neighbours,
+// taken one at a time from the same place -- each relocation shifting the
+// whole span between the two places again.  A run starts at a relocation:
+// it keeps the tour as it is before the node moves (`ph`, the node y_1 at
+// p, the current node at t) and the number m of nodes taken since
+// (y_j = ph[p + dir (j-1)], j = 1..m), and reads the relocated tour through
+// a position map; apply() rewrites the span once, by the single shift when
+// m == 1, else with two or three reversals.  The tour it reads equals the one the
+// relocations one by one would have left (CpuTour::relocate,
+// cpp/src/faco_cpu.cpp:82-112):
+//   p < t: the taken nodes sit at [t-m+1, t] in order, the span between
+//          them and their source moved left by m;
+//   p > t: the taken nodes sit at [t+1, t+m] in order, the span moved
+//          right by m.
+// An ant defers its relocations on instances of more than kDeferAllFrom
+// nodes, and on the others after kDeferFromStep construction steps (early,
+// short walks rarely continue a run: there a deferred single relocation
+// costs more than an immediate one; measured at N=1000 and N=5000-10000).
+constexpr std::uint32_t kDeferFromStep = 24;
+constexpr std::uint32_t kDeferAllFrom = 2048;
+
+struct RelocationRun {
+    std::uint32_t m = 0;   // 0: no run
+    std::uint32_t p = 0, t = 0;
+    int dir = 1;           // +1: sources taken rightwards; -1: leftwards (either while m == 1)
+
+    // node at position i of the relocated tour
+    __device__ __forceinline__ std::uint32_t read(const AntSmem& s, std::uint32_t i) const {
+        if (p < t) {
+            const std::uint32_t first = t - m + 1;
+            if (i >= first && i <= t) return s.tour[dir > 0 ? p + (i - first) : p - (i - first)];
+            const std::uint32_t lo = dir > 0 ? p : p - m + 1;
+            if (i >= lo && i < first) return s.tour[i + m];
+        } else {
+            const std::uint32_t last = t + m;
+            if (i > t && i <= last) return s.tour[dir > 0 ? p + (i - t - 1) : p - (i - t - 1)];
+            const std::uint32_t hi = dir > 0 ? p + m - 1 : p;
+            if (i > last && i <= hi) return s.tour[i - m];
+        }
+        return s.tour[i];
+    }
+    // position of the current node (the last one taken)
+    __device__ __forceinline__ std::uint32_t current_pos() const { return p < t ? t : t + m; }
+    // Direction in which a node at position q of ph continues the run (the
+    // next source, p + dir m), or 0: not next to the sources, past a tour
+    // end, or out of the span between the sources and the taken nodes.
+    __device__ __forceinline__ int continues(std::uint32_t q) const {
+        if (q + m == p && (p < t || q > t) && (m == 1 || dir < 0)) return -1;
+        if (q == p + m && (p > t || q < t) && (m == 1 || dir > 0)) return 1;
+        return 0;
+    }
+    // position of that node in the relocated tour
+    __device__ __forceinline__ std::uint32_t source_pos(int d) const {
+        return (p < t) == (d < 0) ? (d < 0 ? p - m : p + m) : p;
+    }
+    // Rewrites the span so that the tour holds the relocated order; the run
+    // ends.  `last` is the node taken last (the ant's current node).
+    __device__ void apply(const AntSmem& s, std::uint32_t lane, std::uint32_t last) {
+        if (m == 1) {
+            relocate_shift(s, lane, t, p, last);   // reads before its first write, after a warp barrier
+            m = 0;
+            return;
+        }
+        __syncwarp();
+        if (p < t) {
+            // [sources | span] -> [span | taken in order]
+            const std::uint32_t lo = dir > 0 ? p : p - m + 1, span = t - lo + 1 - m;
+            reverse_range(s, lane, lo, t);
+            if (span > 1) reverse_range(s, lane, lo, lo + span - 1);
+            if (dir > 0) reverse_range(s, lane, t - m + 1, t);
+        } else {
+            // [span | sources] -> [taken in order | span]
+            const std::uint32_t hi = dir > 0 ? p + m - 1 : p, span = hi - t - m;
+            reverse_range(s, lane, t + 1, hi);
+            if (dir > 0) reverse_range(s, lane, t + 1, t + m);
+            if (span > 1) reverse_range(s, lane, t + m + 1, hi);
+        }
+        m = 0;
+    }
+};
+
 // flip_without_cost (cpp/src/faco_cpu.cpp:114-135) as disjoint swap pairs.
 // Returns the number of elements in the reversed segment.
 __device__ __forceinline__ std::uint32_t flip(const AntSmem& s, std::uint32_t n, std::uint32_t lane,

@@ -661,12 +661,21 @@ void enqueue_iterations(faco_engine* e, cudaStream_t st, std::uint32_t iteration
     }
 }
 
-// The evaluation's graph: kGraphIterations iterations, replayed.
+// The evaluation's graph: kGraphIterations iterations, replayed.  A failed
+// enqueue ends the capture (discarding the partial graph) before the error
+// propagates, so the stream is usable again.
 void capture_graph(faco_engine* e, cudaStream_t st) {
     auto& v = e->eval;
     destroy_graph(e);
     cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-    enqueue_iterations(e, st, kGraphIterations);
+    try {
+        enqueue_iterations(e, st, kGraphIterations);
+    } catch (...) {
+        cudaGraph_t partial = nullptr;
+        if (cudaStreamEndCapture(st, &partial) == cudaSuccess && partial) cudaGraphDestroy(partial);
+        cudaGetLastError();
+        throw;
+    }
     cuda_check(cudaStreamEndCapture(st, &v.graph), "end capture");
     cuda_check(cudaGraphInstantiate(&v.exec, v.graph, 0), "graph instantiate");
 }

@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         // next node is the parent neighbour of `current` not yet visited
         std::uint32_t next_node = n, next_pnbr = 0, next_cand = n;
         float next_p = 0.0f;
+        RelocationRun run;
         while (r.mne < target && r.steps + 1 < n) {
             if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
             const std::uint32_t step = r.steps + 1;
@@ -290,10 +291,37 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                 break;
             }
             if (L.out_selected && lane == 0) L.out_selected[(size_t)task * n + step] = (node_t)selected;
-            const std::uint32_t npos = s.pos[selected], tpos = s.pos[current];
-            const std::uint32_t previous = s.tour[npos == 0 ? n - 1 : npos - 1];
-            const std::uint32_t after = s.tour[npos + 1 == n ? 0 : npos + 1];
-            const std::uint32_t target_after = s.tour[tpos + 1 == n ? 0 : tpos + 1];
+            // positions and tour neighbours, read through the deferred run
+            // when `selected` continues it, else from the rewritten tour
+            std::uint32_t npos = s.pos[selected], tpos = n, previous = n, after = n, target_after = n;
+            int run_dir = 0;
+            bool start_run = false;
+            if (run.m) {
+                // the inverse is that of the tour before the run (unchanged during it)
+                run_dir = run.continues(npos);
+                if (run_dir) {
+                    npos = run.source_pos(run_dir);
+                    tpos = run.current_pos();
+                    target_after = run.read(s, tpos + 1 == n ? 0 : tpos + 1);
+                    if (target_after == selected) run_dir = 0;
+                }
+                if (run_dir) {
+                    previous = run.read(s, npos == 0 ? n - 1 : npos - 1);
+                    after = run.read(s, npos + 1 == n ? 0 : npos + 1);
+                } else {
+                    run.apply(s, lane, current);
+                    npos = s.pos[selected];
+                }
+            }
+            if (!run_dir) {
+                tpos = s.pos[current];
+                previous = s.tour[npos == 0 ? n - 1 : npos - 1];
+                after = s.tour[npos + 1 == n ? 0 : npos + 1];
+                target_after = s.tour[tpos + 1 == n ? 0 : tpos + 1];
+                // relocations are deferred on large instances, and on the
+                // others once the walk is long (converged trails)
+                start_run = n > kDeferAllFrom || r.steps >= kDeferFromStep;
+            }
             ++r.steps;
             __syncwarp();
             if (lane == 0) s.visited[selected >> 5] |= 1u << (selected & 31u);
@@ -312,7 +340,19 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                     term = lane < 3 ? -d : d;
                 }
                 cost += __reduce_add_sync(kFull, term);
-                relocate_shift(s, lane, tpos, npos, selected);
+                if (run_dir) {
+                    // the run takes one more node
+                    run.dir = run_dir;
+                    ++run.m;
+                } else if (start_run) {
+                    // a deferred run, of this relocation alone so far
+                    run.p = npos;
+                    run.t = tpos;
+                    run.m = 1;
+                    run.dir = 1;
+                } else {
+                    relocate_shift(s, lane, tpos, npos, selected);
+                }
                 r.moved += tpos < npos ? npos - tpos : tpos - npos + 1;
             }
             if ((pnbr & 0xffffu) != selected && (pnbr >> 16) != selected) {
@@ -324,6 +364,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
             current = selected;
             __syncwarp();
         }
+        if (run.m) run.apply(s, lane, current);
         r.construction_cost = cost;
         if (L.out_construction)
             for (std::uint32_t i = lane; i < n; i += 32) L.out_construction[(size_t)task * n + i] = s.tour[i];

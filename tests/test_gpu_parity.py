@@ -147,12 +147,15 @@ def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=
 @pytest.mark.parametrize("n,ants,iterations,variant,ls_mode,workspace", [
     (7, 4, 8, 0, 0, 0), (17, 8, 8, 1, 0, 0), (100, 32, 20, 2, 0, 0), (500, 16, 6, 3, 0, 0), (1000, 32, 4, 0, 0, 0),
     (17, 8, 8, 1, 1, 0), (100, 32, 20, 2, 1, 0), (1000, 32, 4, 0, 1, 0),
-    (7, 4, 8, 0, 0, 2), (100, 32, 20, 2, 0, 2), (500, 16, 6, 3, 1, 2), (1000, 32, 4, 0, 0, 2)])
+    (7, 4, 8, 0, 0, 2), (100, 32, 20, 2, 0, 2), (500, 16, 6, 3, 1, 2), (1000, 32, 4, 0, 0, 2),
+    (1000, 16, 40, 3, 0, 0), (2600, 8, 3, 3, 0, 0), (2600, 8, 3, 1, 1, 2)])
 def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode, workspace):
     """Whole plain-FACO runs: registration rows and initial tour, every
     iteration's best/global/parent costs and trail bounds, the final global
     tour and the FP32 trails agree bit-for-bit with the oracle -- with the
-    ants' tours in shared memory and in the global-memory workspace."""
+    ants' tours in shared memory and in the global-memory workspace, and
+    with the relocations deferred into runs (long walks once trails
+    converge; every relocation above 2048 nodes)."""
     k = 2 if variant % 2 else 16
     b = 1 if variant % 2 else 64
     retention = (0.25, 0.5, 0.75, 0.98)[variant]
