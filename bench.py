@@ -42,11 +42,12 @@ sys.path.insert(0, str(ROOT))
 
 L2_BYTES = 129 * 2**20
 CPU_COLONIES_PER_THREAD = 16
-# DRAM bytes (read + write) of one steady-state ant_kernel<engine> launch of
+# DRAM bytes (read + write) of one whole-panel ant_kernel<engine> launch of
 # the default panel, from ncu dram__bytes_read.sum + dram__bytes_write.sum
-# (profiles/ant_kernel_plain_faco_n1000.md, launches 105-106: 15.09 / 15.29 MB
-# read, 0 written).  Reported for the default workload only.
-ANT_TRAFFIC_BYTES_PER_LAUNCH = 15.19e6
+# (profiles/ant_kernel_plain_faco_n1000.md: the step_timed launch after
+# `--steps 2 --warmup 3`, iteration ~133: 20.46 MB read, 0.08 MB written).
+# Reported for the default workload only.
+ANT_TRAFFIC_BYTES_PER_LAUNCH = 20.54e6
 STEADY_ITERATION = 400   # the converged-colony window of the throughput workload
 ITERATIONS_PER_STEP = 16  # a step: one replay of the engine's per-evaluation CUDA graph
 
