@@ -405,8 +405,9 @@ def run_gb300(args, rank: int, world: int) -> None:
                    "timed_iterations": [first, first + per_step * args.steps],
                    "colony_chains": plan["chains"],
                    "registration_seconds": registration_s, "size_classes": classes},
-        "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d / e2e_iters,
-                "d2h_bytes_per_step": d2h / e2e_iters, "iterations": e2e_iters,
+        "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d * per_step / e2e_iters,
+                "d2h_bytes_per_step": d2h * per_step / e2e_iters, "iterations": e2e_iters,
+                "bytes_per_call": {"h2d": h2d, "d2h": d2h},
                 "call": "FacoBatchEngine.evaluate_faco_evaluations (C ABI faco_evaluate), host keys/seeds in, "
                         "host tours/costs out"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
