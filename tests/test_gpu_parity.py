@@ -701,6 +701,13 @@ def test_colony_chains_change_nothing(api, oracle, chains, workspace):
         controlled = engine.evaluate_program_evaluations(keys, seeds, ants * iterations, program, trace=True,
                                                          decision_iterations=[1, 20, iterations])
         runs[ch] = (plain, controlled)
+        plan = engine.launch_plan()            # of the last (12-feature controlled) evaluation
+        assert plan["size_classes"] == 3 and plan["graph_iterations"] == 16
+        if ch == 1:
+            assert plan["chains"] == 0 and plan["launches_per_iteration"] == 3 + 2
+        else:
+            # every class split into at least one chain, at most one chain per colony
+            assert 3 <= plan["chains"] <= keys.size and plan["launches_per_iteration"] == 3 * plan["chains"]
         engine.close()
     for a, b in zip(runs[1], runs[chains]):
         assert [it["tour"] for it in a["items"]] == [it["tour"] for it in b["items"]]
