@@ -35,7 +35,7 @@ thread_local std::string g_error;
 // Iterations captured per CUDA graph (replayed until the budget is spent).
 constexpr std::uint32_t kGraphIterations = 16;
 // Automatic chain count: one chain per kColoniesPerChain colonies, at most kMaxChains.
-constexpr std::uint32_t kColoniesPerChain = 32;
+constexpr std::uint32_t kColoniesPerChain = 16;
 constexpr std::uint32_t kMaxChains = 8;
 
 struct Error : std::runtime_error {

@@ -56,7 +56,7 @@ typedef struct faco_settings {
     uint32_t force_fingerprint_collisions; /* diagnostic (batch_engine.hpp:66): every tour fingerprint
                                               of the 12-feature controller is 0, so its archive
                                               compares whole tours; 0 in production */
-    uint32_t chains; /* independent colony chains in the evaluation's graph (0: one per 32
+    uint32_t chains; /* independent colony chains in the evaluation's graph (0: one per 16
                         colonies, at most 8); results do not depend on it */
 } faco_settings;
 
