@@ -28,6 +28,7 @@ EXPORTED = (
     "faco_ant_diagnostic", "faco_pheromone_step", "faco_begin", "faco_step", "faco_step_timed", "faco_finish",
     "faco_engine_stream", "faco_evaluate_programs", "faco_mlp_param_count", "faco_mlp_forward", "faco_mlp_gradient",
     "faco_mlp_train", "faco_edge_data", "faco_prior_set", "faco_prior_refresh", "faco_current_costs",
+    "faco_colony_rows",
     "faco_set_mne_targets", "faco_get_launch_plan",
     "faco_pheromone_step_noalloc", "faco_begin_programs", "faco_snapshot", "faco_restore",
     "faco_evaluate_controllers", "faco_validate_controller", "faco_score_controllers",
@@ -156,6 +157,7 @@ def load():
     L.faco_prior_set.argtypes = [vp, vp, C.c_float, C.c_int, vp, C.c_uint32]
     L.faco_prior_refresh.argtypes = [vp]
     L.faco_current_costs.argtypes = [vp, vp, C.POINTER(C.c_uint32)]
+    L.faco_colony_rows.argtypes = [vp, C.c_uint32, vp, vp, vp, C.c_uint64]
     L.faco_set_mne_targets.argtypes = [vp, vp, C.c_uint32]
     L.faco_begin.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32]
     L.faco_step.argtypes = [vp, C.c_uint32]

@@ -2163,6 +2163,31 @@ int faco_edge_data(faco_engine* e, uint16_t* x_out, float* y_out, uint64_t capac
     });
 }
 
+int faco_colony_rows(faco_engine* e, uint32_t colony, float* trails, float* eta, float* products,
+                     uint64_t capacity) {
+    return guarded([&] {
+        require(e != nullptr, "null engine");
+        std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
+        if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
+        auto& v = e->eval;
+        require(v.active, "no active evaluation");
+        require(colony < v.count, "colony index out of range");
+        std::size_t offset = 0;
+        for (std::uint32_t c = 0; c < colony; ++c)
+            offset += (static_cast<std::size_t>(v.sizes[c]) * e->instances.at(v.keys[c])->k + 3) & ~std::size_t{3};
+        const std::size_t cells = static_cast<std::size_t>(v.sizes[colony]) * e->instances.at(v.keys[colony])->k;
+        require((!trails && !eta && !products) || capacity >= cells, "output capacity too small");
+        cudaStream_t s = e->stream;
+        const std::pair<const DeviceBuffer<float>*, float*> rows[3] = {
+            {&e->trails, trails}, {&e->colony_eta, eta}, {&e->products, products}};
+        for (const auto& r : rows)
+            if (r.second)
+                cuda_check(cudaMemcpyAsync(r.second, r.first->get() + offset, cells * sizeof(float),
+                                           cudaMemcpyDeviceToHost, s), "colony rows");
+        cuda_check(cudaStreamSynchronize(s), "colony rows");
+    });
+}
+
 static void apply_prior(faco_engine* e) {
     auto& v = e->eval;
     std::vector<std::uint32_t> offsets(v.count);
@@ -2287,6 +2312,7 @@ int faco_pheromone_step_noalloc(uint32_t n, uint32_t k, const uint32_t* primary,
             cuda_check(cudaPointerGetAttributes(&a, p), "cudaPointerGetAttributes");
             if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
                 throw Error(FACO_EINVAL, "faco_pheromone_step_noalloc takes device pointers only");
+            // managed memory is reachable from every device, wherever it was allocated
             if (a.type == cudaMemoryTypeDevice && a.device != device)
                 throw Error(FACO_EINVAL, "a buffer lives on another device than the current one");
         }

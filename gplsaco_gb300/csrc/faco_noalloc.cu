@@ -11,7 +11,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "noalloc_kernels.h"
 
@@ -92,30 +91,24 @@ __global__ void noalloc_update_kernel(std::uint32_t n, std::uint32_t k, const st
     }
 }
 
-constexpr int kMaxDevices = 64;
-
-// Address of the scratch on the current device, looked up once per device.
+// Address of the scratch in the current context, looked up on every call:
+// cudaGetSymbolAddress allocates nothing, and a cached address would dangle
+// after a cudaDeviceReset or under another context of the same device.
 cudaError_t scratch_address(PheromoneScratch** out) {
-    static std::mutex lock;
-    static PheromoneScratch* address[kMaxDevices] = {};
-    int device = 0;
-    cudaError_t err = cudaGetDevice(&device);
+    void* p = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress(&p, g_pheromone_scratch);
     if (err != cudaSuccess) return err;
-    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> guard(lock);
-    if (!address[device]) {
-        void* p = nullptr;
-        err = cudaGetSymbolAddress(&p, g_pheromone_scratch);
-        if (err != cudaSuccess) return err;
-        address[device] = static_cast<PheromoneScratch*>(p);
-    }
-    *out = address[device];
+    *out = static_cast<PheromoneScratch*>(p);
     return cudaSuccess;
 }
 
-std::uint32_t grid_for(std::uint64_t items) {
+// Grid-stride launches: at most 16 blocks of 256 threads per SM of the
+// current device (enough to cover the latency of the streaming loops), at
+// least one block.
+std::uint32_t grid_for(std::uint64_t items, int sms) {
+    const std::uint64_t cap = 16ull * static_cast<std::uint64_t>(sms > 0 ? sms : 1);
     const std::uint64_t blocks = (items + 255) / 256;
-    return static_cast<std::uint32_t>(blocks < 1 ? 1 : (blocks > 152 * 16 ? 152 * 16 : blocks));
+    return static_cast<std::uint32_t>(blocks < 1 ? 1 : (blocks > cap ? cap : blocks));
 }
 
 }  // namespace
@@ -127,19 +120,23 @@ cudaError_t pheromone_step_noalloc(std::uint32_t n, std::uint32_t k, const std::
     PheromoneScratch* s = nullptr;
     cudaError_t err = scratch_address(&s);
     if (err != cudaSuccess) return err;
+    int device = 0, sms = 0;
+    err = cudaGetDevice(&device);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (err != cudaSuccess) return err;
     err = cudaMemsetAsync(s->seen, 0, ((n + 31) / 32) * sizeof(std::uint32_t), stream);
     if (err == cudaSuccess) err = cudaMemsetAsync(&s->error, 0, sizeof(std::uint32_t), stream);
     if (err != cudaSuccess) return err;
     const std::uint64_t cells = static_cast<std::uint64_t>(n) * k;
-    noalloc_prepare_kernel<<<grid_for(cells > n ? cells : n), 256, 0, stream>>>(n, k, primary, parent, s);
+    noalloc_prepare_kernel<<<grid_for(cells > n ? cells : n, sms), 256, 0, stream>>>(n, k, primary, parent, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     const auto aligned = [](const void* p) { return (reinterpret_cast<std::uintptr_t>(p) & 15u) == 0; };
     if ((k & 3u) == 0 && aligned(primary) && aligned(eta) && aligned(trails) && aligned(products))
-        noalloc_update_kernel<true><<<grid_for(cells / 4), 256, 0, stream>>>(
+        noalloc_update_kernel<true><<<grid_for(cells / 4, sms), 256, 0, stream>>>(
             n, k, primary, retention, minimum, maximum, increment, eta, trails, products, s);
     else
-        noalloc_update_kernel<false><<<grid_for(cells), 256, 0, stream>>>(
+        noalloc_update_kernel<false><<<grid_for(cells, sms), 256, 0, stream>>>(
             n, k, primary, retention, minimum, maximum, increment, eta, trails, products, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;

@@ -555,6 +555,18 @@ class FacoBatchEngine:
     def prior_refresh(self) -> None:
         _lib.check(self._L.faco_prior_refresh(self._handle))
 
+    def colony_rows(self, colony: int) -> dict:
+        """One colony's trails, heuristic (eta, the prior's when it is set)
+        and products, [n, k] float32 each, after the work queued so far."""
+        keys = self._active[0]
+        c = _exact_int(colony, "colony", 0, keys.size - 1)
+        n = self._sizes[int(keys[c])]
+        k = min(self.settings.primary_width, n - 1)
+        out = {name: np.zeros((n, k), np.float32) for name in ("trails", "eta", "products")}
+        _lib.check(self._L.faco_colony_rows(self._handle, c, out["trails"].ctypes.data, out["eta"].ctypes.data,
+                                            out["products"].ctypes.data, n * k))
+        return out
+
     def current_costs(self, count: int):
         costs = np.zeros(count, np.int64)
         it = C.c_uint32()

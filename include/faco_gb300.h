@@ -355,6 +355,15 @@ int faco_prior_set(faco_engine* engine, const float* params, float floor, int ga
                    uint32_t departures);
 /* Recomputes the prior from the colonies' current trails and best tours. */
 int faco_prior_refresh(faco_engine* engine);
+/* During a stepwise evaluation: one colony's trails, heuristic (the
+ * instance's eta, or the prior-reweighted one) and products, [n][k] FP32
+ * each, copied out after the work queued so far (synchronises).  Any output
+ * may be NULL; `capacity` is the entries each non-NULL output holds.  The
+ * parity hook of the reference's trail trace (FixedFacoTrace,
+ * cpp/include/gp_faco/fixed_faco_gpu.hpp:23-33, which records the trails
+ * before and after each batch). */
+int faco_colony_rows(faco_engine* engine, uint32_t colony, float* trails, float* eta, float* products,
+                     uint64_t capacity);
 /* Current global-best lengths of the colonies (synchronises). */
 int faco_current_costs(faco_engine* engine, int64_t* costs, uint32_t* iterations);
 /* Per-colony MNE targets (maximum new edges per ant) of the active plain
@@ -393,13 +402,13 @@ int faco_pheromone_step(uint32_t n, uint32_t k, const uint32_t* primary, const u
  * candidate id is found on the device and returns FACO_EINVAL with trails
  * and products untouched.
  *
- * The first call on each device looks the scratch address up
- * (cudaGetSymbolAddress) and keeps it; make that first call before any
- * stream capture on that device.  Calls must not overlap: two calls in
- * flight at once on one device (from two host threads of one process) race
- * on the single scratch and corrupt each other's result.  Calls from one
- * thread never overlap, since each returns only after its work is
- * complete. */
+ * Every call looks the scratch address up for the current device
+ * (cudaGetSymbolAddress, which allocates nothing), so a cudaDeviceReset or
+ * another context between calls is harmless.  Calls must not overlap: two
+ * calls in flight at once on one device (from two host threads of one
+ * process) race on the single scratch and corrupt each other's result.
+ * Calls from one thread never overlap, since each returns only after its
+ * work is complete. */
 int faco_pheromone_step_noalloc(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
                                 float retention, float minimum, float maximum, float increment, const float* eta,
                                 float* trails, float* products, void* stream);

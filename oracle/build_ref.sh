@@ -3,9 +3,11 @@
 # (cpp/src/faco_cpu.cpp, program_cpu.cpp, control_cpu.cpp, prepared_problem.cpp
 # and sparse_graph.cpp of LinHuanli/GPLSACO, read in place, never copied) plus
 # oracle/ref_shim.cpp.  Test infrastructure only.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The reference checkout is the argument, else $GPLSACO_REFERENCE, else the
+# location this recipe was written against (/root/reference).
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${GPLSACO_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 if [ ! -f "$REF/cpp/src/faco_cpu.cpp" ]; then
     echo "reference sources not found under $REF; oracle/_ref not built" >&2

@@ -454,6 +454,56 @@ void orc_pheromone32(uint32_t n, uint32_t k, const uint32_t* primary, const uint
 }
 
 /* ---------------------------------------------------------------------- */
+/* Learned edge prior (no reference counterpart; it reweights the         */
+/* heuristic of initialize_products, colony_state.cuh:91-110, and of      */
+/* SparsePheromone::product_cache, faco_cpu.cpp:351-363).                 */
+/*   eta'[e] = eta[e] * f, f = floor + p[e], squared when gamma == 2,      */
+/* in FP32 with one rounding per operation.  p is the network's            */
+/* probability for the candidate entry; floor > 0, so no weight is zero.   */
+/* ---------------------------------------------------------------------- */
+void orc_prior_eta(size_t cells, const float* eta, const float* prob, float floor, int gamma, float* out) {
+    for (size_t e = 0; e < cells; ++e) {
+        const float f = floor + prob[e];
+        out[e] = eta[e] * (gamma == 2 ? f * f : f);
+    }
+}
+
+/* Products of a colony whose prior re-ranks only the departures from the  */
+/* parent tour: per node i, the entries of i's two parent-tour neighbours   */
+/* keep the plain heuristic (trail * eta), and the others take the prior's  */
+/* (trail * eta') scaled by plain / prior, the two totals summed in         */
+/* candidate order over those other entries (scale 1 when the prior total   */
+/* is 0), so that their total weight stays the plain one.                   */
+void orc_departure_rows(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
+                        const float* trails, const float* eta, const float* prior_eta, float* products) {
+    uint32_t* succ = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint32_t* pred = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    for (uint32_t p = 0; p < n; ++p) {
+        succ[parent[p]] = parent[p + 1 == n ? 0 : p + 1];
+        pred[parent[p]] = parent[p == 0 ? n - 1 : p - 1];
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        const size_t row = (size_t)i * k;
+        float plain = 0.0f, prior = 0.0f;
+        for (uint32_t j = 0; j < k; ++j) {
+            const uint32_t node = primary[row + j];
+            if (node == succ[i] || node == pred[i]) continue;
+            const float t = trails[row + j];
+            plain += t * eta[row + j];
+            prior += t * prior_eta[row + j];
+        }
+        const float scale = prior > 0.0f ? plain / prior : 1.0f;
+        for (uint32_t j = 0; j < k; ++j) {
+            const uint32_t node = primary[row + j];
+            const float t = trails[row + j];
+            products[row + j] = node == succ[i] || node == pred[i] ? t * eta[row + j] : t * prior_eta[row + j] * scale;
+        }
+    }
+    free(succ);
+    free(pred);
+}
+
+/* ---------------------------------------------------------------------- */
 /* Random stream.  Philox4x32 with 10 rounds as published by Salmon,       */
 /* Moraes, Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3"    */
 /* (SC'11).  The counter layout is this engine's own:                     */
@@ -868,10 +918,28 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    int64_t* global_cost_out, orc_iter_trace_t* trace, float* trails_out,
                    float* products_out, const orc_program_t* program, uint32_t mask,
                    uint32_t total_iterations, uint32_t controller_kind, orc_control_io_t* control) {
+    return orc_run_colony_prior(n, xy, primary, backup, ls, initial, initial_cost, c, key, iterations, global_tour,
+                                global_cost_out, trace, trails_out, products_out, program, mask, total_iterations,
+                                controller_kind, control, NULL);
+}
+
+/* The colony run with a learned prior: before batch prior->at[r] the colony */
+/* heuristic becomes prior->etas[r] ([n][k]; the instance's eta to fall back */
+/* to plain FACO) and the products are recomputed from the current trails,   */
+/* by the departure rule when prior->departures[r] is set, which then also   */
+/* follows every trail update.  Entries apply in order; NULL: plain FACO.    */
+int orc_run_colony_prior(uint32_t n, const int32_t* xy, const uint32_t* primary, const uint32_t* backup,
+                         const uint32_t* ls, const uint32_t* initial, int64_t initial_cost,
+                         const orc_run_cfg_t* c, uint64_t key, uint32_t iterations, uint32_t* global_tour,
+                         int64_t* global_cost_out, orc_iter_trace_t* trace, float* trails_out,
+                         float* products_out, const orc_program_t* program, uint32_t mask,
+                         uint32_t total_iterations, uint32_t controller_kind, orc_control_io_t* control,
+                         const orc_prior_schedule_t* prior) {
     const orc_dist_t d = {n, xy, NULL};
     const uint32_t k = c->k, A = c->ants;
     const size_t cells = (size_t)n * k;
     float* eta = (float*)malloc(sizeof(float) * cells);
+    float* ceta = (float*)malloc(sizeof(float) * cells);   /* the colony's heuristic */
     float* trails = (float*)malloc(sizeof(float) * cells);
     float* products = (float*)malloc(sizeof(float) * cells);
     uint32_t* parent = (uint32_t*)malloc(sizeof(uint32_t) * n);
@@ -879,12 +947,14 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     uint32_t* tours = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n * A);
     uint32_t* region_list = (uint32_t*)malloc(sizeof(uint32_t) * n);
     orc_ant_info_t* infos = (orc_ant_info_t*)malloc(sizeof(orc_ant_info_t) * A);
-    if (!eta || !trails || !products || !parent || !epoch || !tours || !infos || !region_list) return -1;
+    if (!eta || !ceta || !trails || !products || !parent || !epoch || !tours || !infos || !region_list) return -1;
     for (size_t i = 0; i < cells; ++i) {
         const uint32_t to = primary[i];
         const double dist = to < n ? (double)orc_distance(&d, (uint32_t)(i / k), to) : 0.0;
         eta[i] = to >= n ? 0.0f : (float)(dist > 0 ? (c->beta == 1.0 ? 1.0 / dist : 1.0 / pow(dist, c->beta)) : 1.0);
     }
+    memcpy(ceta, eta, sizeof(float) * cells);
+    uint32_t prior_next = 0, departures = 0;
     uint32_t region_offsets[5] = {0, 0, 0, 0, 0};
     orc_regions(n, xy, region_offsets, region_list);
     const double p_root = pow(c->p_best, 1.0 / (double)k);
@@ -892,7 +962,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     double tmin, tmax;
     orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
     float dflt = (float)tmax;
-    for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * eta[i]; }
+    for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * ceta[i]; }
     memcpy(parent, initial, sizeof(uint32_t) * n);
     memcpy(epoch, initial, sizeof(uint32_t) * n);
     memcpy(global_tour, initial, sizeof(uint32_t) * n);
@@ -910,6 +980,13 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                            control ? control->force_collisions : 0) != 0)
         return -1;
     for (uint32_t batch = 0; batch < iterations; ++batch) {
+        while (prior && prior_next < prior->count && prior->at[prior_next] == batch) {
+            memcpy(ceta, prior->etas + (size_t)prior_next * cells, sizeof(float) * cells);
+            departures = prior->departures[prior_next];
+            for (size_t i = 0; i < cells; ++i) products[i] = trails[i] * ceta[i];
+            if (departures) orc_departure_rows(n, k, primary, parent, trails, eta, ceta, products);
+            ++prior_next;
+        }
         if (spec2) {
             /* decision before the batch (batch_engine.cu:884-950) */
             float f[12 * 32], scores[32];
@@ -943,7 +1020,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                 orc_restart_feedback(&ctl.feedback);
                 memcpy(parent, ar->tours + (size_t)alt * n, sizeof(uint32_t) * n);
                 memcpy(epoch, ar->tours + (size_t)alt * n, sizeof(uint32_t) * n);
-                for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * eta[i]; }
+                for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * ceta[i]; }
             }
         }
 #ifdef _OPENMP
@@ -990,7 +1067,8 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
         int64_t parent_cost = from_epoch ? epoch_cost : cost;
         memcpy(parent, from_epoch ? epoch : best_tour, sizeof(uint32_t) * n);
         orc_pheromone32(n, k, primary, parent, (float)c->retention, (float)tmin, (float)tmax,
-                        (float)(1.0 / (double)parent_cost), eta, trails, products, &dflt);
+                        (float)(1.0 / (double)parent_cost), ceta, trails, products, &dflt);
+        if (departures) orc_departure_rows(n, k, primary, parent, trails, eta, ceta, products);
         const uint32_t used_mne = mne;
         int32_t action = -1;
         if (spec2) {
@@ -1022,7 +1100,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                 epoch_cost = global_cost;
                 parent_cost = global_cost;
                 orc_trail_limits(k, p_root, c->retention, (double)epoch_cost, &tmin, &tmax);
-                for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * eta[i]; }
+                for (size_t i = 0; i < cells; ++i) { trails[i] = (float)tmax; products[i] = trails[i] * ceta[i]; }
                 dflt = (float)tmax;
             }
         }
@@ -1043,7 +1121,7 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
     *global_cost_out = global_cost;
     if (trails_out) memcpy(trails_out, trails, sizeof(float) * cells);
     if (products_out) memcpy(products_out, products, sizeof(float) * cells);
-    free(eta); free(trails); free(products); free(parent); free(epoch); free(tours); free(infos); free(region_list);
+    free(eta); free(ceta); free(trails); free(products); free(parent); free(epoch); free(tours); free(infos); free(region_list);
     return failed ? -2 : 0;
 }
 

@@ -263,6 +263,24 @@ int orc_run_colony(uint32_t n, const int32_t* xy, const uint32_t* primary, const
                    float* trails_out, float* products_out, const struct orc_program* program, uint32_t mask,
                    uint32_t total_iterations, uint32_t controller_kind, orc_control_io_t* control);
 
+/* ---- learned edge prior (no reference counterpart) ---------------------- */
+typedef struct orc_prior_schedule {
+    uint32_t count;              /* entries, in batch order */
+    const uint32_t* at;          /* [count] batch before which the entry applies */
+    const float* etas;           /* [count][n*k] colony heuristic from then on */
+    const uint32_t* departures;  /* [count] 1: products by the departure rule */
+} orc_prior_schedule_t;
+void orc_prior_eta(size_t cells, const float* eta, const float* prob, float floor, int gamma, float* out);
+void orc_departure_rows(uint32_t n, uint32_t k, const uint32_t* primary, const uint32_t* parent,
+                        const float* trails, const float* eta, const float* prior_eta, float* products);
+int orc_run_colony_prior(uint32_t n, const int32_t* xy, const uint32_t* primary, const uint32_t* backup,
+                         const uint32_t* ls, const uint32_t* initial, int64_t initial_cost,
+                         const orc_run_cfg_t* cfg, uint64_t key, uint32_t iterations,
+                         uint32_t* global_tour, int64_t* global_cost, orc_iter_trace_t* trace,
+                         float* trails_out, float* products_out, const struct orc_program* program, uint32_t mask,
+                         uint32_t total_iterations, uint32_t controller_kind, orc_control_io_t* control,
+                         const orc_prior_schedule_t* prior);
+
 /* ---- GP controller scoring (postfix IR) --------------------------------- */
 typedef struct orc_program {
     uint16_t ir_version, numeric_spec_id, feature_spec_id, length, constants_count;

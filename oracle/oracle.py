@@ -90,6 +90,10 @@ class Program(C.Structure):
                 ("operand", C.c_uint8 * 63), ("constants", C.c_float * 63)]
 
 
+class PriorSchedule(C.Structure):
+    _fields_ = [("count", C.c_uint32), ("at", C.c_void_p), ("etas", C.c_void_p), ("departures", C.c_void_p)]
+
+
 class Fp(C.Structure):
     _fields_ = [("first", C.c_uint64), ("second", C.c_uint64)]
 
@@ -159,6 +163,10 @@ def lib():
                                      C.c_uint64, C.c_uint32, u32p, C.POINTER(C.c_int64), C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                      C.c_void_p]
+        L.orc_run_colony_prior.restype = C.c_int
+        L.orc_run_colony_prior.argtypes = L.orc_run_colony.argtypes + [C.POINTER(PriorSchedule)]
+        L.orc_prior_eta.argtypes = [C.c_size_t, f32p, f32p, C.c_float, C.c_int, f32p]
+        L.orc_departure_rows.argtypes = [C.c_uint32, C.c_uint32, u32p, u32p, f32p, f32p, f32p, f32p]
         L.orc_ctl_mix.restype = C.c_uint64
         L.orc_ctl_mix.argtypes = [C.c_uint64]
         L.orc_fingerprint.restype = Fp
@@ -324,6 +332,36 @@ def ant(parent, ls_rows, mne_target, cap, *, xy=None, matrix=None, visit=None, u
                 start=info.start_node)
 
 
+def heuristic(xy, primary, beta=1.0) -> np.ndarray:
+    """The instance heuristic eta = 1/d^beta (1 at d = 0) as FP32 [n, k],
+    the value the colony run starts from."""
+    d = euc2d_matrix(xy)[np.arange(len(xy))[:, None], np.asarray(primary, np.int64)].astype(np.float64)
+    with np.errstate(divide="ignore"):
+        v = 1.0 / d if beta == 1.0 else 1.0 / np.power(d, beta)
+    return np.where(d > 0, v, 1.0).astype(np.float32)
+
+
+def prior_eta(eta, prob, floor, gamma) -> np.ndarray:
+    """eta * (floor + p)^gamma in FP32, one rounding per operation."""
+    eta = np.ascontiguousarray(eta, np.float32)
+    prob = np.ascontiguousarray(prob, np.float32).reshape(eta.shape)
+    out = np.zeros_like(eta)
+    lib().orc_prior_eta(eta.size, eta.reshape(-1), prob.reshape(-1), np.float32(floor), int(gamma), out.reshape(-1))
+    return out
+
+
+def departure_rows(primary, parent, trails, eta, prior_eta_rows) -> np.ndarray:
+    """Products of a colony whose prior re-ranks departures only."""
+    primary = np.ascontiguousarray(primary, np.uint32)
+    n, k = primary.shape
+    out = np.zeros((n, k), np.float32)
+    lib().orc_departure_rows(n, k, primary, np.ascontiguousarray(parent, np.uint32),
+                             np.ascontiguousarray(trails, np.float32).reshape(-1),
+                             np.ascontiguousarray(eta, np.float32).reshape(-1),
+                             np.ascontiguousarray(prior_eta_rows, np.float32).reshape(-1), out.reshape(-1))
+    return out
+
+
 def prepare(xy, k, b, w, initial_ls_limit=100000):
     xy = np.ascontiguousarray(xy, dtype=np.int32)
     n = xy.shape[0]
@@ -337,11 +375,14 @@ def prepare(xy, k, b, w, initial_ls_limit=100000):
 def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, retention=0.98, p_best=0.1,
                epoch_source_probability=0.01, ls_limit=100000, threads=1, want_trace=True, ls_mode=0,
                program=None, mask=0xFFFFFFFF, total_iterations=None, instance_key=0, decision_iterations=(),
-               force_collisions=False):
+               force_collisions=False, prior=None):
     """One colony run.  A program (or controller) of feature spec 2 runs the
     reference's 12-feature controller; `instance_key` seeds its sample nodes
     and `decision_iterations` (1-based) capture its decisions, returned under
-    "decisions" with the final "control_state"."""
+    "decisions" with the final "control_state".  `prior`: a learned-prior
+    schedule, entries (batch, eta [n, k] float32, departures) in batch order
+    -- from that batch on the colony's heuristic is eta (the instance's own
+    eta for plain FACO), products by the departure rule when departures."""
     xy = np.ascontiguousarray(xy, dtype=np.int32)
     n = xy.shape[0]
     cfg = RunCfg(ants, k, b, w, mne, beta, retention, p_best, epoch_source_probability, ls_limit, threads, ls_mode)
@@ -358,14 +399,24 @@ def run_colony(xy, prep, *, ants, k, b, w, mne, iterations, key, beta=1.0, reten
     io = ControlIO(instance_key, points.ctypes.data, points.size, dec["features"].ctypes.data,
                    dec["scores"].ctypes.data, dec["masks"].ctypes.data, dec["actions"].ctypes.data)
     io.force_collisions = int(bool(force_collisions))
-    rc = lib().orc_run_colony(n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
-                              np.ascontiguousarray(prep["ls"], dtype=np.uint32),
-                              np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),
-                              key, iterations, tour, C.byref(cost),
-                              C.cast(trace, C.c_void_p) if trace is not None else None,
-                              trails.ctypes.data, products.ctypes.data,
-                              C.cast(slots, C.c_void_p) if slots is not None else None, mask,
-                              total_iterations or iterations, kind, C.addressof(io))
+    args = (n, xy, np.ascontiguousarray(prep["primary"], dtype=np.uint32), backup,
+            np.ascontiguousarray(prep["ls"], dtype=np.uint32),
+            np.ascontiguousarray(prep["initial"], dtype=np.uint32), prep["cost"], C.byref(cfg),
+            key, iterations, tour, C.byref(cost),
+            C.cast(trace, C.c_void_p) if trace is not None else None,
+            trails.ctypes.data, products.ctypes.data,
+            C.cast(slots, C.c_void_p) if slots is not None else None, mask,
+            total_iterations or iterations, kind, C.addressof(io))
+    if prior is None:
+        rc = lib().orc_run_colony(*args)
+    else:
+        at = np.ascontiguousarray([int(b) for b, _, _ in prior], dtype=np.uint32)
+        etas = np.ascontiguousarray(np.stack([np.asarray(e, np.float32).reshape(n * k) for _, e, _ in prior]))
+        dep = np.ascontiguousarray([1 if d else 0 for _, _, d in prior], dtype=np.uint32)
+        if np.any(np.diff(at.astype(np.int64)) < 0):
+            raise ValueError("prior schedule entries must be in batch order")
+        sched = PriorSchedule(at.size, at.ctypes.data, etas.ctypes.data, dep.ctypes.data)
+        rc = lib().orc_run_colony_prior(*args, C.byref(sched))
     if rc != 0:
         raise RuntimeError(f"oracle colony run failed ({rc})")
     rows = None

@@ -64,16 +64,25 @@ def test_no_alloc_matches_allocating_step_on_consecutive_calls(engine_lib, oracl
     lib = engine_lib
     ret, tmin, tmax, inc = float(np.float32(0.98)), float(np.float32(1e-7)), float(np.float32(2e-6)), \
         float(np.float32(1 / 7.3e7))
-    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # a caller's own non-blocking stream for the second call of each case
+    # (the first runs on the legacy default stream, NULL)
+    side = torch.cuda.Stream(device=0)
+    assert side.cuda_stream != 0
     # a large vectorised case (k % 4 == 0), then a smaller scalar one (k odd)
     # that reads the scratch after the larger call left its entries behind
     for n, k, seed in ((1000, 16, 5), (537, 7, 6)):
         primary, parent, eta, trails = _case(oracle, n, k, seed)
         dev = _Device(primary, parent, eta, trails)
+        torch.cuda.synchronize()
         ref_t, ref_p = trails, None
         for call in range(2):   # two calls in a row on the same buffers
             ref_t, ref_p = _host_step(lib, primary, parent, eta, ref_t, ret, tmin, tmax, inc)
-            assert dev.step(lib, ret, tmin, tmax, inc, stream if call else None) == 0, lib.faco_last_error()
+            if call:
+                with torch.cuda.stream(side):
+                    code = dev.step(lib, ret, tmin, tmax, inc, C.c_void_p(side.cuda_stream))
+            else:
+                code = dev.step(lib, ret, tmin, tmax, inc, None)
+            assert code == 0, lib.faco_last_error()
             got_t, got_p = dev.result()
             assert np.array_equal(got_t, ref_t) and np.array_equal(got_p, ref_p), (n, k, call)
         # and the oracle's FP32 restatement of the same two steps
