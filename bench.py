@@ -2,24 +2,32 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload throughput|uneven|large|gp-population|time-to-gap]
+                    [--no-cpu-baseline] [--no-time-to-gap] [--window-only]
 
 A step is one replay of the engine's per-evaluation CUDA graph: 16 ACO
 iterations of the whole panel, in each of which every ant of every colony
 constructs a tour from its colony's parent and runs its local search, then
 each colony reduces, selects and updates its trails (the colonies run as
 independent chains inside the graph, so one chain's slowest ants overlap
-the other chains' iterations).  Default workload
-(throughput): 16 instances of N=1000 integer coordinates uniform in
-[0,10^6]^2 x 16 seeds = 256 colonies, 32 ants each, k=16, backup 64, LS
-width 20, MNE 8, 2-opt, retention 0.98.  Other workloads:
+the other chains' iterations).  The W warm-up steps run in an evaluation of
+their own; the K timed steps are iterations 0 .. 16K of a fresh evaluation
+from the initial tours -- the same iterations the end-to-end call, the CPU
+baseline and the reference arm run.  Default workload (throughput): 16
+instances of N=1000 integer coordinates uniform in [0,10^6]^2 x 16 seeds =
+256 colonies, 32 ants each, k=16, backup 64, LS width 20, MNE 8, 2-opt,
+retention 0.98; its line also carries the converged window (iteration 400
+on) and the learned prior's time to a 1% gap against plain FACO (the
+learned-prior workload: 64 instances, N in {1000, 2000}, 32 ants, k=20).
+Other workloads:
   uneven         256 clustered instances, N ~ U[200,1000], 16 ants, k=16
                  (one colony each; size-class launches in one CUDA graph);
+                 the end-to-end call runs 500 iterations;
   large          16 clustered instances, N ~ U[5000,10000] in [0,10^7]^2,
                  5 seeds, 64 ants, k=32, 2-opt window 32 + Or-opt (<= 3);
   gp-population  one N=500 instance, 128 random GP controller programs, one
                  colony each, 32 ants, k=16, 1000 iterations per call (a step
                  is one population evaluation);
-  time-to-gap    learned-prior vs plain FACO wall-clock to a 1% mean gap.
+  time-to-gap    learned-prior vs plain FACO wall-clock to a 1% mean gap alone.
 The data are synthetic (seeded), standing in for the reference's uniform
 TSP1000 rows and its batch workloads.  With N>1 each rank runs its own
 panel (independent colonies, weak scaling, no collective on the data path).
@@ -42,14 +50,18 @@ sys.path.insert(0, str(ROOT))
 
 L2_BYTES = 129 * 2**20
 CPU_COLONIES_PER_THREAD = 16
-# DRAM bytes (read + write) of one whole-panel ant_kernel<engine> launch of
-# the default panel, from ncu dram__bytes_read.sum + dram__bytes_write.sum
-# (profiles/ant_kernel_plain_faco_n1000.md: the step_timed launch after
-# `--steps 2 --warmup 3`, iteration ~133: 20.46 MB read, 0.08 MB written).
-# Reported for the default workload only.
-ANT_TRAFFIC_BYTES_PER_LAUNCH = 20.54e6
 STEADY_ITERATION = 400   # the converged-colony window of the throughput workload
 ITERATIONS_PER_STEP = 16  # a step: one replay of the engine's per-evaluation CUDA graph
+# DRAM traffic and issue figures of the default panel from ncu, filled in from
+# a capture of this panel (none yet: the line then reports null).
+# Reported for the default workload only.
+THROUGHPUT_CAPTURE = {
+    "traffic_bytes_per_step": None,
+    "traffic_source": None,
+    "ant_issue_active_pct": None,
+    "ant_warp_instructions_per_ant_tour": None,
+    "issue_source": None,
+}
 
 
 @dataclass
@@ -69,13 +81,14 @@ class Workload:
     ls_mode: int = 0
     mne: int = 8
     retention: float = 0.98
-    precondition: int = 100          # untimed iterations before the timed steps (steady-state trails)
-    e2e_iterations: int | None = None  # iterations of the end-to-end call (None: precondition + steps)
+    e2e_iterations: int | None = None  # iterations of the end-to-end call (None: the timed window's)
     cpu_colonies_per_thread: int = CPU_COLONIES_PER_THREAD
 
     def run_iterations(self, steps: int) -> int:
-        """Iterations of the end-to-end call; the CPU sample spans the same."""
-        return self.e2e_iterations or (self.precondition + steps)
+        """Iterations of the end-to-end call; the CPU sample spans the same:
+        the timed window (steps x 16 iterations from the initial tours)
+        unless the workload names its own call length."""
+        return self.e2e_iterations or ITERATIONS_PER_STEP * steps
 
     @property
     def colonies(self) -> int:
@@ -116,7 +129,7 @@ def make_workload(name: str, rank: int = 0) -> Workload:
             "retention 0.98",
             instances.large_clustered(16), np.repeat(np.arange(16), 5),
             np.tile(np.arange(5, dtype=np.uint64), 16) + np.uint64(1000 * rank), 64, 32, 64, 32, ls_mode=1,
-            precondition=20, e2e_iterations=100, cpu_colonies_per_thread=2)
+            cpu_colonies_per_thread=2)
     raise ValueError(f"unknown workload {name}")
 
 
@@ -142,17 +155,20 @@ def size_classes(sizes) -> int:
     return len({class_of(int(n)) for n in sizes})
 
 
-def launch_bytes(wl: Workload, work: np.ndarray, iterations: int) -> float:
-    """Algorithmic bytes of one iteration (one ant launch per size class over
-    every ant): per ant parent read + tour write (8 B per node), per colony
-    the trail update (16 B per candidate entry), and the counted work --
+def step_bytes(wl: Workload, work: np.ndarray, steps: int) -> dict:
+    """Algorithmic bytes of one step (ITERATIONS_PER_STEP iterations of every
+    colony) of a window of `steps` steps, from that window's own counters:
+    per ant and iteration the parent read + tour write (8 B per node); per
+    colony and iteration the trail update (16 B per candidate entry: trail
+    read and write, product write, heuristic read); and the counted work --
     candidate id + weight per construction step (8 B x k), 20 B per LS move
-    evaluation, 16 B per moved tour element -- averaged over the iterations
-    the counters cover."""
+    evaluation, 16 B per moved tour element."""
     n = wl.sizes().astype(np.float64)
-    fixed = float(np.sum(8.0 * wl.ants * n + 16.0 * n * wl.k))
+    ants = ITERATIONS_PER_STEP * float(np.sum(8.0 * wl.ants * n))
     counted = 8.0 * wl.k * float(work[:, 0].sum()) + 20.0 * float(work[:, 1].sum()) + 16.0 * float(work[:, 2].sum())
-    return fixed + counted / iterations
+    ants += counted / steps
+    update = ITERATIONS_PER_STEP * float(np.sum(16.0 * n * wl.k))
+    return {"ant_kernel": ants, "colony_update": update, "total": ants + update}
 
 
 class ClockSampler:
@@ -270,11 +286,12 @@ def run_reference(args, rank: int) -> None:
     fe = colonies * wl.ants * iterations
     value = fe / elapsed
     line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": "ant-tours+LS/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / iterations,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * elapsed * ITERATIONS_PER_STEP / iterations,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
             "config": {"workload": f"{wl.description}; CPU: {colonies} colonies ({threads} host threads, one "
                                    f"colony each at a time), {iterations} iterations from the initial tour",
-                       "colonies": colonies, "ants": wl.ants},
+                       "colonies": colonies, "ants": wl.ants, "timed_iterations": [0, iterations]},
             "cpu_baseline": {"value": value, "unit": "ant-tours+LS/s", "cores": threads, "kind": "port",
                              "sample": f"{colonies} colonies x {iterations} iterations"},
             "e2e": {"value": value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -305,23 +322,8 @@ def run_gb300(args, rank: int, world: int) -> None:
     stream = torch.cuda.ExternalStream(engine.stream_ptr)
     classes = size_classes(wl.sizes())
 
-    # ---- device throughput: inputs resident, L2 flushed before every step ----
-    # a step is one replay of the evaluation's CUDA graph (`graph_iterations`
-    # iterations, the colony chains overlapping inside it); the panel first
-    # runs `precondition` iterations, the last W steps of them the untimed
-    # warm-up, so that the timed steps start at iteration `precondition`
-    kernel_steps = 3
-    engine.begin(keys, seeds, wl.mne)
-    plan = engine.launch_plan()
-    per_step = plan["graph_iterations"]
-    assert per_step == ITERATIONS_PER_STEP, plan
-    first = max(wl.precondition, per_step * args.warmup)
-    engine.step(first - per_step * args.warmup)
-    for _ in range(args.warmup):
-        engine.step(per_step)
-    torch.cuda.synchronize()
-
     def timed_steps() -> list:
+        """K graph replays, L2 flushed before each, CUDA events on the engine's stream."""
         out = []
         for _ in range(args.steps):
             flush.fill_(1.0)
@@ -334,6 +336,21 @@ def run_gb300(args, rank: int, world: int) -> None:
             out.append(a.elapsed_time(b))
         return out
 
+    # ---- warm-up: W steps of an evaluation of their own ----
+    engine.begin(keys, seeds, wl.mne)
+    plan = engine.launch_plan()
+    per_step = plan["graph_iterations"]
+    assert per_step == ITERATIONS_PER_STEP, plan
+    for _ in range(args.warmup):
+        engine.step(per_step)
+    engine.finish()
+    torch.cuda.synchronize()
+
+    # ---- device throughput: inputs resident, a fresh evaluation from the
+    # initial tours, the K timed steps = iterations 0 .. 16K ----
+    window = per_step * args.steps
+    engine.begin(keys, seeds, wl.mne)
+    torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         if world > 1:
             torch.distributed.barrier()
@@ -342,37 +359,49 @@ def run_gb300(args, rank: int, world: int) -> None:
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
-    # per-kernel split of a few more steps (ant kernel = the dominant kernel)
-    ant_ms, upd_ms = engine.step_timed(kernel_steps)
     totals = engine.finish()
+    assert totals["completed_batches"] == window
+    work = totals["colony_work"].astype(np.float64)        # the window's own counters
+    elapsed_ms = max_over_ranks(float(np.sum(step_ms)), world, "cuda")
+    fe_window = window * wl.colonies * wl.ants
+    value = world * fe_window / (elapsed_ms / 1e3)
+    if args.window_only:
+        engine.close()
+        if rank == 0:
+            print(json.dumps({"metric": wl.metric, "value": value, "unit": "ant-tours+LS/s", "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+                              "window_only": True, "timed_iterations": [0, window],
+                              "colony_work": work.sum(axis=0).tolist()}), flush=True)
+        return
+
+    # the same iterations again with every kernel launched alone (unchained)
+    # and timed with events: the ant kernel's and the colony update's shares
+    engine.begin(keys, seeds, wl.mne)
+    ant_ms, upd_ms = engine.step_timed(window)
+    engine.finish()
+
     steady = None
     if wl.name == "throughput":
-        # the same steps once the colonies have converged (construction walks
-        # the parent tour: more steps and LS evaluations per tour), in a second
-        # evaluation from the initial tours with per-iteration traces
-        engine.begin(keys, seeds, wl.mne, trace_iterations=STEADY_ITERATION + per_step * args.steps)
+        # converged colonies (construction walks the parent tour: more steps
+        # and LS evaluations per tour), in an evaluation with per-iteration traces
+        engine.begin(keys, seeds, wl.mne, trace_iterations=STEADY_ITERATION + window)
         engine.step(STEADY_ITERATION)
         torch.cuda.synchronize()
         steady_ms = timed_steps()
         trace = engine.finish()["trace"]
-        window, early = trace[STEADY_ITERATION:], trace[first:first + per_step * args.steps]
-        per_tour = float(wl.colonies * wl.ants * per_step * args.steps)
+        late, early = trace[STEADY_ITERATION:], trace[:window]
+        per_tour = float(fe_window)
         steady = {"value": world * per_tour / (max_over_ranks(float(np.sum(steady_ms)), world, "cuda") / 1e3),
-                  "ms_per_step": float(np.mean(steady_ms)), "timed_iterations_start_at": STEADY_ITERATION,
-                  "per_tour": {"construction_steps": float(window["construction_steps"].sum()) / per_tour,
-                               "ls_evaluations": float(window["ls_evaluations"].sum()) / per_tour},
+                  "ms_per_step": float(np.mean(steady_ms)),
+                  "timed_iterations": [STEADY_ITERATION, STEADY_ITERATION + window],
+                  "per_tour": {"construction_steps": float(late["construction_steps"].sum()) / per_tour,
+                               "ls_evaluations": float(late["ls_evaluations"].sum()) / per_tour},
                   "per_tour_in_the_value_window": {
                       "construction_steps": float(early["construction_steps"].sum()) / per_tour,
                       "ls_evaluations": float(early["ls_evaluations"].sum()) / per_tour}}
-    iters = totals["completed_batches"]
-    work = totals["colony_work"].astype(np.float64)
-    fe_total = iters * wl.colonies * wl.ants
-    elapsed_ms = max_over_ranks(float(np.sum(step_ms)), world, "cuda")
-    fe_timed = args.steps * per_step * wl.colonies * wl.ants * world
-    value = fe_timed / (elapsed_ms / 1e3)
 
-    # ---- end to end through the public API: host keys/seeds in, tours out;
-    # one solve call from the initial tours ----
+    # ---- end to end through the public API: host keys/seeds in, tours and
+    # lengths out; one solve call over the window's iterations ----
     e2e_iters = wl.run_iterations(args.steps)
     engine.evaluate_faco_evaluations(keys, seeds, wl.ants * max(1, args.warmup), wl.mne)
     torch.cuda.synchronize()
@@ -383,26 +412,46 @@ def run_gb300(args, rank: int, world: int) -> None:
     h2d = keys.nbytes + seeds.nbytes
     d2h = wl.colonies * engine.dimension * 4 + wl.colonies * 8
     assert all(len(it["tour"]) == n for it, n in zip(res["items"], wl.sizes()))
-
-    # ---- roofline of the ant kernel (per launch set = one step of all ants) ----
-    per_launch = launch_bytes(wl, work, iters)
-    achieved = per_launch / (ant_ms / kernel_steps / 1e3) / 1e9
-    peak, peak_kind = measured_peak()
     engine.close()
+
+    # ---- roofline of one step (the graph of ant launches and colony updates) ----
+    sb = step_bytes(wl, work, args.steps)
+    ms_per_step = elapsed_ms / args.steps
+    achieved = sb["total"] / (ms_per_step / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
     if rank != 0:
         return
-    base = None
-    if args.cpu_baseline:
-        base = cpu_baseline(wl, e2e_iters)
+    capture = THROUGHPUT_CAPTURE if wl.name == "throughput" else {}
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "traffic": capture.get("traffic_bytes_per_step"),
+        "traffic_source": capture.get("traffic_source"),
+        "kernel": "ant_kernel + colony_update_kernel: one graph replay (16 iterations, every colony chain)",
+        "peak_source": peak_kind,
+        "bytes_per_step": sb["total"], "bytes_per_fe": sb["total"] / (per_step * wl.colonies * wl.ants),
+        "per_fe": {"construction_steps": float(work[:, 0].sum()) / fe_window,
+                   "ls_evaluations": float(work[:, 1].sum()) / fe_window,
+                   "moved_elements": float(work[:, 2].sum()) / fe_window},
+        "ant_kernel": {"bytes_per_step": sb["ant_kernel"], "ms_per_step_unchained": ant_ms / args.steps,
+                       "share_of_unchained_time": ant_ms / (ant_ms + upd_ms),
+                       "achieved_unchained_gbs": sb["ant_kernel"] / (ant_ms / args.steps / 1e3) / 1e9},
+        "colony_update_kernel": {"bytes_per_step": sb["colony_update"], "ms_per_step_unchained": upd_ms / args.steps},
+        "issue": ({"ant_kernel_issue_active_pct": capture.get("ant_issue_active_pct"),
+                   "ant_kernel_warp_instructions_per_ant_tour": capture.get("ant_warp_instructions_per_ant_tour"),
+                   "source": capture.get("issue_source")}
+                  if capture.get("ant_issue_active_pct") else None),
+    }
+    base = cpu_baseline(wl, e2e_iters) if args.cpu_baseline else None
     line = {
         "metric": wl.metric, "value": value, "unit": "ant-tours+LS/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": {"workload": wl.description, "colonies": wl.colonies, "ants": wl.ants,
                    "n_range": [int(wl.sizes().min()), int(wl.sizes().max())],
                    "l2": "flushed before every timed step (258 MB write)",
                    "iterations_per_step": per_step,
-                   "timed_iterations": [first, first + per_step * args.steps],
+                   "timed_iterations": [0, window],
+                   "warmup": "W steps of a separate evaluation; the timed one starts from the initial tours",
                    "colony_chains": plan["chains"],
                    "registration_seconds": registration_s, "size_classes": classes},
         "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d * per_step / e2e_iters,
@@ -410,24 +459,33 @@ def run_gb300(args, rank: int, world: int) -> None:
                 "bytes_per_call": {"h2d": h2d, "d2h": d2h},
                 "call": "FacoBatchEngine.evaluate_faco_evaluations (C ABI faco_evaluate), host keys/seeds in, "
                         "host tours/costs out"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": ANT_TRAFFIC_BYTES_PER_LAUNCH if wl.name == "throughput" else None,
-                     "traffic_source": "ncu capture (profiles/ant_kernel_plain_faco_n1000.md)"
-                     if wl.name == "throughput" else None,
-                     "kernel": "ant_kernel<engine>", "peak_source": peak_kind,
-                     "bytes_per_launch": per_launch,
-                     "bytes_per_fe": per_launch / (wl.colonies * wl.ants),
-                     "per_fe": {"construction_steps": float(work[:, 0].sum()) / fe_total,
-                                "ls_evaluations": float(work[:, 1].sum()) / fe_total,
-                                "moved_elements": float(work[:, 2].sum()) / fe_total},
-                     "ant_kernel_ms": ant_ms / kernel_steps, "update_kernel_ms": upd_ms / kernel_steps},
+        "roofline": roofline,
         "cpu_baseline": base,
         "clocks": clocks.summary(),
-        "gpu_launches": plan["launches_per_iteration"] * per_step * args.steps,
+        "gpu_launches": plan["launches_per_iteration"] * window,
     }
     if steady is not None:
         line["steady_state"] = steady
+    if wl.name == "throughput" and args.time_to_gap and world == 1:
+        line["time_to_gap"] = time_to_gap_block(local)
     print(json.dumps(line), flush=True)
+
+
+def time_to_gap_block(device: int = 0) -> dict:
+    """The learned prior's wall-clock to a 1% mean gap against plain GPU FACO
+    (the learned-prior workload; both arms tuned on validation instances)."""
+    from gplsaco_gb300 import experiments
+    res = experiments.time_to_gap(device=device, log=lambda m: print(m, file=sys.stderr, flush=True))
+    out = experiments.summary(res)
+    out["workload"] = ("64 instances (seeds 100-163; N=1000 for 100-131, 2000 for 132-163; uniform for even "
+                       "seeds, clustered for odd), 32 ants, k=20, LS width 20, retention 0.98, 2-opt; budget "
+                       f"{res['budget_iterations']} iterations per method; reference length = best of 2 plain "
+                       "runs of 3000 iterations; prior trained on the engine's own runs of 32 training instances")
+    out["ratio_definition"] = ("prior/plain wall-clock to the target, equal resources: two colonies per instance "
+                               "in both arms (plain: seeds 1, 2; prior: seed 1 plain as the per-instance fallback + "
+                               "seed 2 with the prior), best of the two; ratio_one_colony_per_instance charges the "
+                               "prior for the plain warm-up run that decides its fallback")
+    return out
 
 
 # ---- GP evaluation batch: 128 controller programs on one N=500 instance ----
@@ -566,21 +624,10 @@ def run_time_to_gap(args) -> None:
     import torch
 
     torch.cuda.set_device(0)
-    from gplsaco_gb300 import experiments
-    res = experiments.time_to_gap(log=lambda m: print(m, file=sys.stderr, flush=True))
-    pair = res["two_colonies_per_instance"]["targets"][str(res["target_gap"])]
-    line = {"metric": "time to 1% mean gap, learned-prior vs plain GPU FACO (ratio)", "value": pair["ratio"],
-            "value_one_colony_per_instance": res["ratio"],
+    block = time_to_gap_block(0)
+    line = {"metric": "time to 1% mean gap, learned-prior vs plain GPU FACO (ratio)", "value": block["ratio"],
             "unit": "prior/plain wall-clock", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
-            "config": {"workload": "16 instances (N=1000/2000, uniform/clustered, seeds 100-115), 32 ants, "
-                                   "k=20, 2-opt; reference = best of 2 plain runs of 1500 iterations (MNE 8)",
-                       "tuning": "both arms tuned on 8 validation instances by wall-clock to the target: plain "
-                                 "over MNE targets, the prior over model, floor, exponent, refresh and MNE",
-                       "budget": "equal: two colonies per instance in both arms (plain: seeds 1, 2; prior: seed 1 "
-                                 "plain as the per-instance fallback + seed 2 with the prior), best of the two; "
-                                 "value_one_colony_per_instance charges the prior for a plain warm-up run that "
-                                 "decides its fallback"},
-            "time_to_gap": res}
+            "config": {"workload": block["workload"]}, "time_to_gap": block}
     print(json.dumps(line), flush=True)
 
 
@@ -591,6 +638,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-time-to-gap", dest="time_to_gap", action="store_false",
+                    help="leave the learned prior's time-to-gap block out of the throughput line")
+    ap.add_argument("--window-only", action="store_true",
+                    help="registration, warm-up and the timed window only (for kernel profiles): no unchained "
+                         "replay, converged window, end-to-end call, CPU baseline or time-to-gap")
     ap.add_argument("--workload", default="throughput",
                     choices=["throughput", "uneven", "large", "gp-population", "time-to-gap"],
                     help="time-to-gap: learned-prior vs plain FACO wall-clock to a 1%% mean gap (N=1000/2000)")

@@ -678,6 +678,8 @@ void capture_graph(faco_engine* e, cudaStream_t st) {
     }
     cuda_check(cudaStreamEndCapture(st, &v.graph), "end capture");
     cuda_check(cudaGraphInstantiate(&v.exec, v.graph, 0), "graph instantiate");
+    // upload now, so that the first replay costs what every other one does
+    cuda_check(cudaGraphUpload(v.exec, st), "graph upload");
 }
 
 // Kernel variant of a size class: the global-memory workspace (tour and

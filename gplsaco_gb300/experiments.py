@@ -33,15 +33,16 @@ class GapConfig:
     retention: float = 0.98
     mne: int = 8
     chunk: int = 10                 # iterations between cost reads
-    iterations: int = 400           # timed budget per method
-    reference_iterations: int = 1500
+    iterations: int = 400           # budget of the validation (tuning) runs
+    budget: int = 2000              # budget of the evaluation runs, per method
+    reference_iterations: int = 3000
     reference_seeds: int = 2
     warmup: int = 40                # iterations before the fallback decision
     floor: float = 0.05
     gamma: int = 1
     target_gap: float = 0.01
     extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
-    # Both arms are tuned on validation instances (seeds 200-214) by wall-clock
+    # Both arms are tuned on validation instances (seeds 200-215) by wall-clock
     # time to the target gap: plain FACO over MNE targets, the prior over
     # (model, floor, gamma, refresh, MNE, departures).  "full" sees all seven features;
     # "geometry" only the geometric ones (trail level and best-tour membership
@@ -66,11 +67,18 @@ class GapConfig:
     epochs: int = 12
     batch: int = 8192
     lr: float = 3e-3
-    eval_instances: list = field(default_factory=lambda: [
-        ("uniform", 1000, 100), ("uniform", 1000, 101), ("uniform", 1000, 102), ("uniform", 1000, 103),
-        ("clustered", 1000, 104), ("clustered", 1000, 105), ("clustered", 1000, 106), ("clustered", 1000, 107),
-        ("uniform", 2000, 108), ("uniform", 2000, 109), ("uniform", 2000, 110), ("uniform", 2000, 111),
-        ("clustered", 2000, 112), ("clustered", 2000, 113), ("clustered", 2000, 114), ("clustered", 2000, 115)])
+    # the learned-prior workload: N in {1000, 2000}, uniform and clustered,
+    # instance seeds 100-163 (evaluation) and 200-215 (validation)
+    eval_instances: list = field(default_factory=lambda: gap_instances(range(100, 164)))
+    validation_instances: list = field(default_factory=lambda: gap_instances(range(200, 216)))
+
+
+def gap_instances(seeds) -> list:
+    """(kind, n, seed) for each seed: uniform for even seeds, clustered for
+    odd ones; N = 1000 for the first half of the seeds, 2000 for the rest."""
+    seeds = list(seeds)
+    half = len(seeds) // 2
+    return [("uniform" if s % 2 == 0 else "clustered", 1000 if i < half else 2000, s) for i, s in enumerate(seeds)]
 
 
 def _settings(cfg: GapConfig) -> FixedFacoSettings:
@@ -120,7 +128,7 @@ def reference_lengths(cfg: GapConfig, xys: list, device: int = 0) -> np.ndarray:
 
 def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warmup_costs=None, device: int = 0,
             floor: float | None = None, gamma: int | None = None, refresh: int = 10, mne: int | None = None,
-            departures: bool = False):
+            departures: bool = False, iterations: int | None = None):
     """One method on all evaluation instances (one colony each, seed 1).
     Returns rows (iteration, seconds, mean gap, costs), the fallback mask and
     the work per ant-iteration (construction steps, LS evaluations)."""
@@ -142,7 +150,8 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
         engine.prior_set(params, enabled, floor, gamma, departures)
     rows.append((0, 0.0, float(np.mean((costs - refs) / refs)), costs.copy()))
     done = 0
-    while done < cfg.iterations:
+    budget = cfg.iterations if iterations is None else iterations
+    while done < budget:
         step = min(chunk, cfg.warmup - done) if done < cfg.warmup else chunk
         engine.step(step)
         done += step
@@ -183,7 +192,7 @@ def geometry_model(x: np.ndarray, y: np.ndarray, cfg: GapConfig):
 
 def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: int = 0, floor: float | None = None,
              gamma: int | None = None, refresh: int = 10, prior_mne: int | None = None, mne: int | None = None,
-             departures: bool = False):
+             departures: bool = False, iterations: int | None = None):
     """Two colonies per instance, the instance's length the better of the
     two.  params None: both plain (seeds 1 and 2).  Otherwise colony 2 runs
     with the prior (at MNE target prior_mne) and colony 1 stays plain -- the
@@ -215,7 +224,8 @@ def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: i
     rows = [row(0, costs)]
     rows[0] = (0, 0.0) + rows[0][2:]
     done = 0
-    while done < cfg.iterations:
+    budget = cfg.iterations if iterations is None else iterations
+    while done < budget:
         engine.step(chunk)
         done += chunk
         if params is not None and refresh and done % refresh == 0:
@@ -250,7 +260,7 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
     log(f"geometry-model losses {np.round(geo_losses, 4).tolist()}")
     models = {"full": params, "geometry": geo_params}
     # tune (model, floor, gamma, refresh interval) on validation instances, by wall-clock to the target
-    val = [_xy(kind, n, seed + 100) for kind, n, seed in cfg.eval_instances[::2]]
+    val = [_xy(kind, n, seed) for kind, n, seed in cfg.validation_instances]
     val_refs = reference_lengths(cfg, val, device)
     plain_tuning = []
     for mne in cfg.mne_grid:
@@ -282,16 +292,16 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
         f"MNE {prior_mne} departures {departures}")
     xys = [_xy(kind, n, seed) for kind, n, seed in cfg.eval_instances]
     refs = reference_lengths(cfg, xys, device)
-    plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device, mne=plain_mne)
+    plain_rows, _, plain_work = gap_run(cfg, xys, refs, None, None, device, mne=plain_mne, iterations=cfg.budget)
     warm = next(r for r in plain_rows if r[0] == cfg.warmup)
     prior_rows, enabled, prior_work = gap_run(cfg, xys, refs, models[best_model], warm[3], device, *best,
-                                              mne=prior_mne, departures=departures)
+                                              mne=prior_mne, departures=departures, iterations=cfg.budget)
     t_plain, it_plain = first_time_below(plain_rows, cfg.target_gap)
     t_prior, it_prior = first_time_below(prior_rows, cfg.target_gap, extra_seconds=warm[1])
     # equal resources: two colonies per instance in both arms
-    pair_plain, pair_plain_work = pair_run(cfg, xys, refs, None, device, mne=plain_mne)
+    pair_plain, pair_plain_work = pair_run(cfg, xys, refs, None, device, mne=plain_mne, iterations=cfg.budget)
     pair_prior, pair_prior_work = pair_run(cfg, xys, refs, models[best_model], device, *best, prior_mne=prior_mne,
-                                           mne=plain_mne, departures=departures)
+                                           mne=plain_mne, departures=departures, iterations=cfg.budget)
 
     def targets(rows_a, rows_b):
         out = {}
@@ -323,15 +333,43 @@ def time_to_gap(cfg: GapConfig | None = None, device: int = 0, log=print) -> dic
             "targets": targets(pair_plain, pair_prior),
             "final_gap_plain": pair_plain[-1][2], "final_gap_prior": pair_prior[-1][2],
             "plain_work": pair_plain_work, "prior_work": pair_prior_work,
-            "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(pair_plain, pair_prior)
-                       if r[0] % 50 == 0}},
-        "gap_at": {str(r[0]): [round(r[2], 5), round(p[2], 5)] for r, p in zip(plain_rows, prior_rows)
-                   if r[0] % 50 == 0},
+            "gap_at": gap_checkpoints(pair_plain, pair_prior)},
+        "gap_at": gap_checkpoints(plain_rows, prior_rows),
+        "budget_iterations": cfg.budget,
         "training_rows": int(len(y)), "training_loss": [float(v) for v in losses],
         "geometry_training_loss": [float(v) for v in geo_losses],
         "total_seconds": time.perf_counter() - t_start,
     }
     return out
+
+
+GAP_CHECKPOINTS = (0, 50, 100, 150, 200, 300, 500, 1000, 1500, 2000)
+
+
+def gap_checkpoints(rows_a, rows_b) -> dict:
+    """Mean gaps (a, b) at a few iteration counts."""
+    return {str(a[0]): [round(a[2], 5), round(b[2], 5)] for a, b in zip(rows_a, rows_b) if a[0] in GAP_CHECKPOINTS}
+
+
+def summary(res: dict) -> dict:
+    """The headline figures of time_to_gap() for one benchmark line."""
+    pair = res["two_colonies_per_instance"]
+    head = pair["targets"][str(res["target_gap"])]
+    return {
+        "ratio": head["ratio"],
+        "ratio_one_colony_per_instance": res["ratio"],
+        "target_gap": res["target_gap"],
+        "plain": {"seconds": head["plain_seconds"], "iterations": head["plain_iterations"],
+                  "ms_per_iteration": pair["plain_work"]["ms_per_iteration"],
+                  "final_gap": pair["final_gap_plain"]},
+        "prior": {"seconds": head["prior_seconds"], "iterations": head["prior_iterations"],
+                  "ms_per_iteration": pair["prior_work"]["ms_per_iteration"],
+                  "final_gap": pair["final_gap_prior"]},
+        "other_targets": {g: t["ratio"] for g, t in pair["targets"].items() if g != str(res["target_gap"])},
+        "instances": res["instances"], "budget_iterations": res.get("budget_iterations"),
+        "prior_setting": res["prior_setting"], "plain_setting": res["plain_setting"],
+        "gap_at": pair["gap_at"], "total_seconds": res["total_seconds"],
+    }
 
 
 def profile_prior_application(refreshes: int = 3, device: int = 0) -> None:
