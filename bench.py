@@ -298,10 +298,10 @@ def run_reference(args, rank: int) -> None:
     print(json.dumps(line), flush=True)
 
 
-def _engine(wl: Workload, device: int):
+def _engine(wl: Workload, device: int, follow: int = 0):
     import gplsaco_gb300 as g
     settings = g.FixedFacoSettings(ants=wl.ants, primary_width=wl.k, backup_width=wl.b, ls_width=wl.w,
-                                   retention=wl.retention, ls_mode=wl.ls_mode)
+                                   retention=wl.retention, ls_mode=wl.ls_mode, follow=follow)
     engine = g.FacoBatchEngine(int(max(len(x) for x in wl.xys)), wl.colonies, settings, device=device)
     t0 = time.perf_counter()
     for i, xy in enumerate(wl.xys):
@@ -315,7 +315,7 @@ def run_gb300(args, rank: int, world: int) -> None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     wl = make_workload(args.workload, rank)
-    engine, registration_s = _engine(wl, local)
+    engine, registration_s = _engine(wl, local, args.follow)
     keys = (wl.colony_instance + 1).astype(np.uint64)
     seeds = wl.seeds
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -452,7 +452,7 @@ def run_gb300(args, rank: int, world: int) -> None:
                    "iterations_per_step": per_step,
                    "timed_iterations": [0, window],
                    "warmup": "W steps of a separate evaluation; the timed one starts from the initial tours",
-                   "colony_chains": plan["chains"],
+                   "colony_chains": plan["chains"], "follow_batches": bool(plan["follow"]),
                    "registration_seconds": registration_s, "size_classes": classes},
         "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d * per_step / e2e_iters,
                 "d2h_bytes_per_step": d2h * per_step / e2e_iters, "iterations": e2e_iters,
@@ -467,20 +467,22 @@ def run_gb300(args, rank: int, world: int) -> None:
     if steady is not None:
         line["steady_state"] = steady
     if wl.name == "throughput" and args.time_to_gap and world == 1:
-        line["time_to_gap"] = time_to_gap_block(local)
+        line["time_to_gap"] = time_to_gap_block(local, args.follow)
     print(json.dumps(line), flush=True)
 
 
-def time_to_gap_block(device: int = 0) -> dict:
+def time_to_gap_block(device: int = 0, follow: int = 0) -> dict:
     """The learned prior's wall-clock to a 1% mean gap against plain GPU FACO
     (the learned-prior workload; both arms tuned on validation instances)."""
     from gplsaco_gb300 import experiments
-    res = experiments.time_to_gap(device=device, log=lambda m: print(m, file=sys.stderr, flush=True))
+    res = experiments.time_to_gap(experiments.GapConfig(follow=follow), device=device,
+                                  log=lambda m: print(m, file=sys.stderr, flush=True))
     out = experiments.summary(res)
     out["workload"] = ("64 instances (seeds 100-163; N=1000 for 100-131, 2000 for 132-163; uniform for even "
                        "seeds, clustered for odd), 32 ants, k=20, LS width 20, retention 0.98, 2-opt; budget "
                        f"{res['budget_iterations']} iterations per method; reference length = best of 2 plain "
                        "runs of 3000 iterations; prior trained on the engine's own runs of 32 training instances")
+    out["follow"] = {0: "auto", 1: "off", 2: "on"}[follow]
     out["ratio_definition"] = ("prior/plain wall-clock to the target, equal resources: two colonies per instance "
                                "in both arms (plain: seeds 1, 2; prior: seed 1 plain as the per-instance fallback + "
                                "seed 2 with the prior), best of the two; ratio_one_colony_per_instance charges the "
@@ -565,7 +567,7 @@ def run_population(args, rank: int, world: int) -> None:
     wl = population_workload()
     programs = population_programs(args.controller)
     settings = g.FixedFacoSettings(ants=wl.ants, primary_width=wl.k, backup_width=wl.b, ls_width=wl.w,
-                                   retention=wl.retention)
+                                   retention=wl.retention, follow=args.follow)
     engine = g.FacoBatchEngine(POP_N, 1, settings, population_size=POP_PROGRAMS, device=local)
     engine.register_problem(1, wl.xys[0].astype(np.float64))
     keys, seeds = np.ones(1, np.uint64), np.array([1 + 1000 * rank], np.uint64)
@@ -624,7 +626,7 @@ def run_time_to_gap(args) -> None:
     import torch
 
     torch.cuda.set_device(0)
-    block = time_to_gap_block(0)
+    block = time_to_gap_block(0, args.follow)
     line = {"metric": "time to 1% mean gap, learned-prior vs plain GPU FACO (ratio)", "value": block["ratio"],
             "unit": "prior/plain wall-clock", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
             "config": {"workload": block["workload"]}, "time_to_gap": block}
@@ -640,6 +642,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-time-to-gap", dest="time_to_gap", action="store_false",
                     help="leave the learned prior's time-to-gap block out of the throughput line")
+    ap.add_argument("--follow", type=int, default=0, choices=[0, 1, 2],
+                    help="parent-following construction steps in batches: 0 auto (when every ant warp fits in one "
+                         "wave of the GPU), 1 off, 2 on")
     ap.add_argument("--window-only", action="store_true",
                     help="registration, warm-up and the timed window only (for kernel profiles): no unchained "
                          "replay, converged window, end-to-end call, CPU baseline or time-to-gap")

@@ -22,6 +22,8 @@ FACO_ENOMEM = -5
 FACO_LS_TWO_OPT = 0
 FACO_LS_TWO_OPT_OR_OPT = 1
 
+FACO_FOLLOW_AUTO, FACO_FOLLOW_OFF, FACO_FOLLOW_ON = 0, 1, 2
+
 EXPORTED = (
     "faco_default_settings", "faco_last_error", "faco_engine_create", "faco_engine_destroy",
     "faco_register_problem", "faco_problem_rows", "faco_evaluate", "faco_validate_program", "faco_score",
@@ -41,12 +43,12 @@ class Settings(C.Structure):
                 ("p_best", C.c_double), ("epoch_source_probability", C.c_double),
                 ("ls_evaluation_limit", C.c_uint64), ("initial_ls_evaluation_limit", C.c_uint64),
                 ("ls_mode", C.c_uint32), ("autotune", C.c_uint32), ("workspace", C.c_uint32),
-                ("force_fingerprint_collisions", C.c_uint32), ("chains", C.c_uint32)]
+                ("force_fingerprint_collisions", C.c_uint32), ("chains", C.c_uint32), ("follow", C.c_uint32)]
 
 
 class LaunchPlan(C.Structure):
     _fields_ = [("size_classes", C.c_uint32), ("chains", C.c_uint32), ("graph_iterations", C.c_uint32),
-                ("launches_per_iteration", C.c_uint32)]
+                ("launches_per_iteration", C.c_uint32), ("follow", C.c_uint32)]
 
 
 class Registration(C.Structure):

@@ -40,10 +40,23 @@ enum AntMode : int {
     kModePrepare = 3,   // no construction; LS over the whole tour (registration)
     kModeEngineGlobal = 4,  // kModeEngine with tour/inverse in global memory and
                             // coordinates read from global (large instances)
+    kModeEngineFollow = 5,        // kModeEngine with batched parent-following steps (follow_batch)
+    kModeEngineGlobalFollow = 6,  // kModeEngineGlobal with batched parent-following steps
 };
 
 __host__ __device__ constexpr bool engine_mode(int mode) {
-    return mode == kModeEngine || mode == kModeEngineGlobal;
+    return mode == kModeEngine || mode == kModeEngineGlobal || mode == kModeEngineFollow ||
+           mode == kModeEngineGlobalFollow;
+}
+__host__ __device__ constexpr bool global_mode(int mode) {
+    return mode == kModeEngineGlobal || mode == kModeEngineGlobalFollow;
+}
+__host__ __device__ constexpr bool follow_mode(int mode) {
+    return mode == kModeEngineFollow || mode == kModeEngineGlobalFollow;
+}
+// The batched variant of an engine mode.
+__host__ __device__ constexpr int with_follow(int mode) {
+    return mode == kModeEngineGlobal ? kModeEngineGlobalFollow : mode == kModeEngine ? kModeEngineFollow : mode;
 }
 
 struct AntLaunch {
@@ -135,6 +148,7 @@ struct Checklist {
 __device__ __forceinline__ bool push_absent(const AntSmem& s, Checklist& q, std::uint32_t n, std::uint32_t v,
                                             std::uint32_t lane, std::uint32_t* log, std::uint32_t log_cap) {
     const bool absent = !test_bit(s.queued, v);
+    __syncwarp();   // every lane has read the flag before lane 0 sets it
     if (absent) {
         if (lane == 0) {
             s.queued[v >> 5] |= 1u << (v & 31u);
@@ -298,6 +312,204 @@ struct RelocationRun {
         m = 0;
     }
 };
+
+// Construction steps that follow the parent tour, evaluated 16 or 32 at a
+// time, one lane per step.  Once trails converge an ant mostly takes a
+// parent-tour neighbour of its current node (no new edge): either the node
+// after it in its tour (an identity step) or, after a jump, the old tour
+// neighbours of the node it jumped to, pulled one by one from their place
+// (a relocation run).  Both paths are known before the draws are: lane i
+// assumes the walk followed that path for i steps and decides step i's
+// roulette on its own -- candidates of its node, available unless visited
+// or earlier on the path, its own uniform -- with a serial FP32 sum and a
+// proven margin (sequential FP32 prefixes of at most 32 non-negative terms
+// are within 31 roundings of the exact ones, the threshold within 33, so
+// 2^-17 of the total separates the FP64 decision with room to spare);
+// undecided lanes end the batch.  The leading lanes whose choice is their
+// hypothesised node are then applied as one: visited bits, counters, the
+// run extended by their number (or, for identity steps, nothing else), and
+// the exact six-edge deltas of every step summed.  The tour, costs and
+// counters equal those of the steps one by one; the first lane that is not
+// taken is left to the caller's serial step.  All 32 steps are decided at
+// once, so a long walk along the parent tour costs a few steps' latency:
+// the variant for panels that leave the GPU under-filled, where an
+// iteration lasts as long as its longest walk.
+//
+// Hypotheses: with a run of m >= 2 nodes, its direction (32 lanes); with a
+// run of one node, both directions (lanes 0-15 rightwards, 16-31
+// leftwards); with no run, lanes 0-15 the parent successor of the current
+// node and 16-31 its parent predecessor -- an identity walk along the tour
+// when that node follows the current one, else the start of a run.
+// Returns the number of steps taken (0: nothing changed); `full` is set when
+// every lane of the chosen hypothesis was taken (the walk may go on).
+__device__ __forceinline__ bool on_segment(int lo, int hi, int q) { return q >= lo && q <= hi; }
+
+__device__ inline std::uint32_t follow_batch(const AntSmem& s, const int2* xy, const InstanceView& in,
+                                             const float* products, const std::uint32_t* parent_nbr, std::uint32_t n,
+                                             std::uint32_t lane, unsigned long long key, std::uint32_t batch,
+                                             std::uint32_t ant, std::uint32_t& current, AntResult& r,
+                                             long long& cost, RelocationRun& run, std::uint32_t& draw_base,
+                                             std::uint32_t& draw_hi, std::uint32_t& draw_lo, bool& full) {
+    const std::uint32_t k = in.k;
+    const std::uint32_t m0 = run.m;
+    const bool split = m0 <= 1;
+    const std::uint32_t half = split ? lane >> 4 : 0u, rel = split ? lane & 15u : lane;
+    // the draws of the next 32 steps, lane i holding step base + i (the
+    // caller's layout, which it reuses afterwards)
+    const std::uint32_t base = r.steps + 1;
+    if (base != draw_base) {
+        const uint4v rb = philox4x32(base + lane, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+        draw_base = base;
+        draw_hi = rb.x;
+        draw_lo = rb.y;
+    }
+    const std::uint32_t rhi = __shfl_sync(kFull, draw_hi, rel);
+    const float uf = __uint2float_rn(rhi) * 0x1p-32f;
+
+    // this lane's hypothesis: the node it stands on (cur) and the node it
+    // must draw (sel), with the run geometry of its step
+    bool identity = false;
+    int p = 0, t = 0, D = 1;
+    std::uint32_t t0 = 0;
+    if (m0 >= 1) {
+        p = (int)run.p;
+        t = (int)run.t;
+        D = m0 >= 2 ? run.dir : (half ? -1 : 1);
+    } else {
+        const std::uint32_t pn = __ldg(parent_nbr + current);
+        const std::uint32_t y = half ? pn >> 16 : pn & 0xffffu;
+        t0 = s.pos[current];
+        const std::uint32_t ty = s.pos[y];
+        if (ty == (t0 + 1 == n ? 0u : t0 + 1)) {
+            identity = true;
+        } else {
+            p = (int)ty;
+            t = (int)t0;
+            D = half ? -1 : 1;
+        }
+    }
+    const std::uint32_t mr = m0 + rel;   // run nodes taken before this lane's step
+    bool ok = rel + 1 < n - r.steps;     // the loop's step budget: steps + rel + 1 < n
+    std::uint32_t cur = current, sel = n;
+    int lo = 0, hi = -1;                 // path positions taken by the earlier lanes
+    if (identity) {
+        if (rel) cur = s.tour[(t0 + rel) % n];
+        sel = s.tour[(t0 + rel + 1) % n];
+    } else {
+        const int q = p + D * (int)mr;
+        ok = ok && q >= 0 && q < (int)n && (mr == 0 || (D < 0 ? (p < t || q > t) : (p > t || q < t)));
+        if (ok) {
+            sel = s.tour[q];
+            if (rel) cur = s.tour[q - D];
+        }
+        if (rel) {
+            const int a = p + D * (int)m0, b = q - D;
+            lo = a < b ? a : b;
+            hi = a < b ? b : a;
+        }
+    }
+    if (ok) {
+        const std::uint32_t pn = __ldg(parent_nbr + cur);
+        ok = (sel == (pn & 0xffffu) || sel == (pn >> 16)) && !test_bit(s.visited, sel);
+    }
+    // the run as it stands before this lane's step (m = mr): a step onto the
+    // node after the current one is an identity step, not a relocation
+    RelocationRun v;
+    v.m = mr;
+    v.p = (std::uint32_t)p;
+    v.t = (std::uint32_t)t;
+    v.dir = D;
+    if (ok && !identity) {
+        const std::uint32_t tpos = v.current_pos();
+        ok = v.read(s, tpos + 1 == n ? 0 : tpos + 1) != sel;
+    }
+    // the roulette of this lane's step: serial FP32 sums in candidate order
+    if (ok) {
+        const node_t* row = in.primary + (size_t)cur * k;
+        const float* prow = products + (size_t)cur * k;
+        unsigned avail = 0;
+        float tot = 0.0f;
+        for (std::uint32_t j = 0; j < k; ++j) {
+            const std::uint32_t x = __ldg(row + j);
+            const float w = __ldg(prow + j);
+            bool a = x < n && !test_bit(s.visited, x);
+            if (a && rel) {
+                const std::uint32_t px = s.pos[x];
+                const std::uint32_t dx = px >= t0 ? px - t0 : px + n - t0;   // tour positions after the start
+                a = identity ? !(dx >= 1 && dx <= rel) : !on_segment(lo, hi, (int)px);
+            }
+            if (a) {
+                avail |= 1u << j;
+                tot += w;
+            }
+        }
+        int choice = -1;
+        if (avail && tot >= 0x1p-100f) {
+            const float thr = uf * tot, delta = tot * 0x1p-17f;
+            float prefix = 0.0f;
+            for (std::uint32_t j = 0; j < k; ++j) {
+                if (!((avail >> j) & 1u)) continue;
+                prefix += __ldg(prow + j);
+                const float diff = prefix - thr;
+                if (diff >= -delta) {
+                    if (diff > delta) choice = (int)j;
+                    break;
+                }
+            }
+        }
+        ok = choice >= 0 && __ldg(row + choice) == sel;
+    }
+    // the leading run of taken steps
+    const unsigned okm = __ballot_sync(kFull, ok);
+    std::uint32_t f, first_lane;
+    if (split) {
+        const unsigned m_lo = okm & 0xffffu, m_hi = okm >> 16;
+        const std::uint32_t f_lo = __ffs(~m_lo) - 1, f_hi = __ffs(~m_hi) - 1;   // trailing ones, <= 16
+        first_lane = f_lo ? 0u : 16u;
+        f = f_lo ? f_lo : f_hi;
+    } else {
+        first_lane = 0;
+        f = okm == kFull ? 32u : (std::uint32_t)(__ffs(~okm) - 1);
+    }
+    full = f == (split ? 16u : 32u);
+    if (f == 0) return 0;
+    const bool taken = lane >= first_lane && lane < first_lane + f;
+    // identity lanes of the chosen half all agree on `identity`
+    const bool ident = __shfl_sync(kFull, identity ? 1 : 0, first_lane) != 0;
+    long long d = 0;
+    std::uint32_t moved = 0;
+    if (taken && !ident) {
+        // six-edge delta of CpuTour::relocate for this lane's step, its
+        // positions and tour neighbours read through the run with m = mr
+        const std::uint32_t tpos = v.current_pos(), npos = v.source_pos(D);
+        const std::uint32_t target_after = v.read(s, tpos + 1 == n ? 0 : tpos + 1);
+        const std::uint32_t previous = v.read(s, npos == 0 ? n - 1 : npos - 1);
+        const std::uint32_t after = v.read(s, npos + 1 == n ? 0 : npos + 1);
+        d = (long long)euc2d(xy[previous], xy[after]) + euc2d(xy[cur], xy[sel]) + euc2d(xy[sel], xy[target_after]) -
+            euc2d(xy[previous], xy[sel]) - euc2d(xy[sel], xy[after]) - euc2d(xy[cur], xy[target_after]);
+        moved = tpos < npos ? npos - tpos : tpos - npos + 1;
+    }
+    if (taken) atomicOr(&s.visited[sel >> 5], 1u << (sel & 31u));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(kFull, d, o);
+    moved = __reduce_add_sync(kFull, moved);
+    current = __shfl_sync(kFull, sel, first_lane + f - 1);
+    cost += d;
+    r.steps += f;
+    if (!ident) {
+        const int Dt = __shfl_sync(kFull, D, first_lane);
+        const std::uint32_t pt = (std::uint32_t)__shfl_sync(kFull, p, first_lane);
+        const std::uint32_t tt = (std::uint32_t)__shfl_sync(kFull, t, first_lane);
+        r.nonidentity += f;
+        r.moved += moved;
+        run.p = pt;
+        run.t = tt;
+        run.dir = Dt;
+        run.m = m0 + f;
+    }
+    __syncwarp();
+    return f;
+}
 
 // flip_without_cost (cpp/src/faco_cpu.cpp:114-135) as disjoint swap pairs.
 // Returns the number of elements in the reversed segment.

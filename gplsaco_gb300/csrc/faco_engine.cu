@@ -245,6 +245,7 @@ struct faco_engine {
     faco_settings settings{};
     std::uint32_t dimension = 0, capacity = 0, ants = 0;
     int device = 0;
+    int sm_count = 152;                         // multiprocessors of the device (queried at creation)
     cudaStream_t stream = nullptr;
     std::mutex busy;
     std::map<std::uint64_t, std::unique_ptr<Instance>> instances;
@@ -301,6 +302,7 @@ struct faco_engine {
     };
     struct EvalState {
         bool active = false;
+        bool follow = false;                    // the ant launches take parent-following steps in batches
         std::uint32_t count = 0, n_max = 0, trace_cap = 0, done = 0;
         std::size_t node_total = 0, tau_total = 0;
         std::vector<std::uint32_t> sizes;
@@ -395,6 +397,7 @@ int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_setting
                 "invalid FACO settings");
         require(c.primary_width <= 32 && c.ls_width <= 32, "primary and LS widths are limited to 32 (one warp)");
         require(c.ls_mode == FACO_LS_TWO_OPT || c.ls_mode == FACO_LS_TWO_OPT_OR_OPT, "unknown local-search mode");
+        require(c.follow <= FACO_FOLLOW_ON, "unknown follow setting");
         require(c.workspace <= FACO_WORKSPACE_GLOBAL, "unknown ant workspace placement");
         require(c.force_fingerprint_collisions <= 1, "force_fingerprint_collisions must be 0 or 1");
         require(c.chains <= 64, "chains must be in [0, 64]");
@@ -412,6 +415,7 @@ int faco_engine_create(uint32_t dimension, uint32_t colonies, const faco_setting
         }
         e->settings.ants = e->ants;
         cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        cuda_check(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
         cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         e->error.resize(1);
         e->reset_error();
@@ -695,7 +699,7 @@ bool may_use_shared(const faco_settings& c, std::uint32_t n_max) {
     return c.workspace != FACO_WORKSPACE_GLOBAL && faco::block_smem_bytes(n_max, 1) <= 227u * 1024u;
 }
 std::uint32_t class_smem(int mode, std::uint32_t n_max, std::uint32_t warps) {
-    return mode == faco::kModeEngineGlobal ? faco::block_smem_bytes_global(n_max, warps)
+    return faco::global_mode(mode) ? faco::block_smem_bytes_global(n_max, warps)
                                            : faco::block_smem_bytes(n_max, warps);
 }
 
@@ -832,18 +836,24 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
         else e->chain_colonies.upload(list, s);
     }
     e->work.upload(all, s);
+    // batched parent-following steps (the same results): on request, or
+    // when every ant warp of the evaluation fits in one wave of the GPU
+    const std::uint64_t ant_warps = static_cast<std::uint64_t>(v.count) * A;
+    v.follow = c.follow == FACO_FOLLOW_ON ||
+               (c.follow == FACO_FOLLOW_AUTO && ant_warps <= 32ull * static_cast<std::uint64_t>(e->sm_count));
+    if (v.follow)
+        for (auto& cl : v.classes) cl.mode = faco::with_follow(cl.mode);
     // the dynamic shared-memory limit is a property of each kernel variant,
     // shared by every class that uses it: it must admit the largest one
-    std::uint32_t smem_max[2] = {0, 0};
+    std::map<int, std::uint32_t> smem_max;
     for (auto& cl : v.classes) {
         cl.L = launch_of(cl.first_job, cl.warps, cl.n_max);
-        auto& m = smem_max[cl.mode == faco::kModeEngineGlobal ? 1 : 0];
+        auto& m = smem_max[cl.mode];
         m = std::max(m, cl.smem);
     }
     for (auto& ch : v.chains) ch.L = launch_of(ch.first_job, v.classes[ch.cls].warps, v.classes[ch.cls].n_max);
-    if (smem_max[0]) cuda_check(faco::prepare_ant_kernel(faco::kModeEngine, smem_max[0]), "cudaFuncSetAttribute");
-    if (smem_max[1])
-        cuda_check(faco::prepare_ant_kernel(faco::kModeEngineGlobal, smem_max[1]), "cudaFuncSetAttribute");
+    for (const auto& [mode, smem] : smem_max)
+        if (smem) cuda_check(faco::prepare_ant_kernel(mode, smem), "cudaFuncSetAttribute");
 }
 
 // Controller programs of a GP-controlled evaluation (null: plain FACO).
@@ -1544,6 +1554,7 @@ int faco_get_launch_plan(faco_engine* e, faco_launch_plan* plan) {
         plan->chains = chains;
         plan->graph_iterations = kGraphIterations;
         plan->launches_per_iteration = chains ? chains * (1 + per_update) : plan->size_classes + per_update;
+        plan->follow = v.follow ? 1u : 0u;
     });
 }
 

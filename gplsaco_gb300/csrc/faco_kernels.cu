@@ -50,7 +50,7 @@ __device__ __forceinline__ void load_parent(const AntSmem& s, const node_t* pare
 
 template <int MODE>
 __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_kernel(const AntLaunch L) {
-    constexpr bool kEngine = engine_mode(MODE), kGlobalWs = MODE == kModeEngineGlobal;
+    constexpr bool kEngine = engine_mode(MODE), kGlobalWs = global_mode(MODE), kFollow = follow_mode(MODE);
     extern __shared__ __align__(16) unsigned char smem[];
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     std::uint32_t colony = 0, ant = 0, task = 0;
@@ -159,8 +159,20 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
         std::uint32_t next_node = n, next_pnbr = 0, next_cand = n;
         float next_p = 0.0f;
         RelocationRun run;
+        // steps along the parent tour are taken in batches (follow_batch)
+        // until a batch stops short of its lanes; the step it stopped at is
+        // taken alone, then batches resume
+        bool follow = true;
         while (r.mne < target && r.steps + 1 < n) {
             if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
+            if (kFollow && follow) {
+                bool full = false;
+                const std::uint32_t f = follow_batch(s, xy, in, products, parent_nbr, n, lane, key, batch, ant,
+                                                     current, r, cost, run, draw_base, draw_hi, draw_lo, full);
+                follow = full;
+                if (f) continue;
+            }
+            follow = true;
             const std::uint32_t step = r.steps + 1;
             if (kEngine && step - draw_base >= 32u) {
                 draw_base = step;
@@ -355,7 +367,8 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                 }
                 r.moved += tpos < npos ? npos - tpos : tpos - npos + 1;
             }
-            if ((pnbr & 0xffffu) != selected && (pnbr >> 16) != selected) {
+            const bool new_edge = (pnbr & 0xffffu) != selected && (pnbr >> 16) != selected;
+            if (new_edge) {
                 ++r.mne;
                 push_absent(s, q, n, current, lane, log, log_cap);
                 push_absent(s, q, n, selected, lane, log, log_cap);
@@ -438,6 +451,8 @@ cudaError_t prepare_ant_kernel(int mode, std::uint32_t smem) {
         case kModeUniforms: return prepare_mode<kModeUniforms>(smem);
         case kModePrepare: return prepare_mode<kModePrepare>(smem);
         case kModeEngineGlobal: return prepare_mode<kModeEngineGlobal>(smem);
+        case kModeEngineFollow: return prepare_mode<kModeEngineFollow>(smem);
+        case kModeEngineGlobalFollow: return prepare_mode<kModeEngineGlobalFollow>(smem);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -451,6 +466,8 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
         case kModeUniforms: ant_kernel<kModeUniforms><<<grid, block, smem, stream>>>(L); break;
         case kModePrepare: ant_kernel<kModePrepare><<<grid, block, smem, stream>>>(L); break;
         case kModeEngineGlobal: ant_kernel<kModeEngineGlobal><<<grid, block, smem, stream>>>(L); break;
+        case kModeEngineFollow: ant_kernel<kModeEngineFollow><<<grid, block, smem, stream>>>(L); break;
+        case kModeEngineGlobalFollow: ant_kernel<kModeEngineGlobalFollow><<<grid, block, smem, stream>>>(L); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -45,12 +45,14 @@ class FixedFacoSettings:
     workspace: int = 0      # 0 auto, 1 shared memory, 2 global memory (ant tour/inverse placement)
     force_fingerprint_collisions: int = 0   # diagnostic: all 12-feature-controller fingerprints 0
     chains: int = 0         # independent colony chains per graph (0 auto); results do not depend on it
+    follow: int = 0         # 0 auto, 1 off, 2 on: parent-following construction steps in batches
+                            # (auto: when every ant warp fits in one wave); results do not depend on it
 
     def to_c(self) -> _lib.Settings:
         s = _lib.Settings()
         for name in ("ants", "primary_width", "backup_width", "ls_width", "ls_evaluation_limit",
                      "initial_ls_evaluation_limit", "ls_mode", "autotune", "workspace",
-                     "force_fingerprint_collisions", "chains"):
+                     "force_fingerprint_collisions", "chains", "follow"):
             setattr(s, name, _exact_int(getattr(self, name), name))
         for name in ("beta", "retention", "p_best", "epoch_source_probability"):
             value = getattr(self, name)

@@ -32,6 +32,7 @@ class GapConfig:
     ls_width: int = 20
     retention: float = 0.98
     mne: int = 8
+    follow: int = 0                 # parent-following steps in batches: 0 auto, 1 off, 2 on
     chunk: int = 10                 # iterations between cost reads
     iterations: int = 400           # budget of the validation (tuning) runs
     budget: int = 2000              # budget of the evaluation runs, per method
@@ -83,7 +84,7 @@ def gap_instances(seeds) -> list:
 
 def _settings(cfg: GapConfig) -> FixedFacoSettings:
     return FixedFacoSettings(ants=cfg.ants, primary_width=cfg.k, backup_width=64, ls_width=cfg.ls_width,
-                             retention=cfg.retention)
+                             retention=cfg.retention, follow=cfg.follow)
 
 
 def _xy(kind: str, n: int, seed: int) -> np.ndarray:

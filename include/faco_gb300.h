@@ -58,7 +58,15 @@ typedef struct faco_settings {
                                               compares whole tours; 0 in production */
     uint32_t chains; /* independent colony chains in the evaluation's graph (0: one per 16
                         colonies, at most 8); results do not depend on it */
+    uint32_t follow; /* FACO_FOLLOW_*: construction steps along the parent tour taken 16-32 at a
+                        time, one lane per step; results do not depend on it */
 } faco_settings;
+
+/* Batched parent-following steps: AUTO uses them when the evaluation's ant
+ * warps fit in one wave of the GPU (at most 32 per SM), where an iteration
+ * lasts as long as its longest walk; they cost more instructions than they
+ * save when the GPU is full. */
+enum { FACO_FOLLOW_AUTO = 0, FACO_FOLLOW_OFF = 1, FACO_FOLLOW_ON = 2 };
 
 void faco_default_settings(faco_settings* s);
 
@@ -241,6 +249,7 @@ typedef struct faco_launch_plan {
     uint32_t chains;
     uint32_t graph_iterations;
     uint32_t launches_per_iteration;
+    uint32_t follow; /* 1: the ant launches take parent-following steps in batches */
 } faco_launch_plan;
 int faco_get_launch_plan(faco_engine* engine, faco_launch_plan* plan);
 /* The engine's cudaStream_t (for events recorded by the caller). */

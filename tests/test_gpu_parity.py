@@ -138,10 +138,11 @@ def test_scores_reference_and_extended(api, oracle):
     assert got["actions"].tolist() == [0, 31, 7]
 
 
-def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000, ls_mode=0, workspace=0):
+def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=100000, ls_mode=0, workspace=0,
+              follow=0):
     return api.FixedFacoSettings(ants=ants, primary_width=k, backup_width=b, ls_width=w, retention=retention,
                                  epoch_source_probability=epoch, ls_evaluation_limit=ls_limit, ls_mode=ls_mode,
-                                 workspace=workspace)
+                                 workspace=workspace, follow=follow)
 
 
 @pytest.mark.parametrize("n,ants,iterations,variant,ls_mode,workspace", [
@@ -149,19 +150,21 @@ def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=
     (17, 8, 8, 1, 1, 0), (100, 32, 20, 2, 1, 0), (1000, 32, 4, 0, 1, 0),
     (7, 4, 8, 0, 0, 2), (100, 32, 20, 2, 0, 2), (500, 16, 6, 3, 1, 2), (1000, 32, 4, 0, 0, 2),
     (1000, 16, 40, 3, 0, 0), (2600, 8, 3, 3, 0, 0), (2600, 8, 3, 1, 1, 2)])
-def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode, workspace):
+@pytest.mark.parametrize("follow", [1, 2])
+def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode, workspace, follow):
     """Whole plain-FACO runs: registration rows and initial tour, every
     iteration's best/global/parent costs and trail bounds, the final global
     tour and the FP32 trails agree bit-for-bit with the oracle -- with the
     ants' tours in shared memory and in the global-memory workspace, and
     with the relocations deferred into runs (long walks once trails
-    converge; every relocation above 2048 nodes)."""
+    converge; every relocation above 2048 nodes), and with the steps along
+    the parent tour taken one at a time and in batches (follow 1 / 2)."""
     k = 2 if variant % 2 else 16
     b = 1 if variant % 2 else 64
     retention = (0.25, 0.5, 0.75, 0.98)[variant]
     epoch = (0.0, 0.01, 1.0, 0.3)[variant]
     xy = _cases.uniform_instance(n, seed=4703 + n)
-    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000, ls_mode, workspace)
+    settings = _settings(api, ants, k, b, 20, retention, epoch, 5000, ls_mode, workspace, follow)
     engine = api.FacoBatchEngine(n, 3, settings)
     info = engine.register_problem(n + 8999, xy.astype(np.float64))
     kk, bb, ww = min(k, n - 1), min(b, n - 1 - min(k, n - 1)), min(20, n - 1)
@@ -724,3 +727,28 @@ def test_colony_chains_change_nothing(api, oracle, chains, workspace):
     ref = oracle.run_colony(xy, oracle.prepare(xy, 16, 64, 20), ants=ants, k=16, b=64, w=20, mne=8,
                             iterations=iterations, key=key, retention=0.9)
     assert runs[chains][0]["items"][2]["cost"] == ref["cost"]
+
+
+def test_follow_batches_change_nothing(api):
+    """Converged colonies (long walks along the parent tour): the evaluation
+    with the parent-following steps taken in batches equals the one that
+    takes them one at a time, tours, lengths and every trace row."""
+    n, ants, iterations = 1000, 32, 160
+    xy = _cases.uniform_instance(n, seed=77)
+    out = {}
+    for follow in (1, 2):
+        engine = api.FacoBatchEngine(n, 4, _settings(api, ants, follow=follow))
+        engine.register_problem(3, xy.astype(np.float64))
+        keys, seeds = np.full(4, 3, np.uint64), np.array([1, 2, 3, 4], np.uint64)
+        engine.begin(keys, seeds, 8, trace_iterations=iterations)
+        assert engine.launch_plan()["follow"] == (1 if follow == 2 else 0)
+        engine.step(iterations)
+        out[follow] = engine.finish()
+        engine.close()
+    a, b = out[1], out[2]
+    assert np.array_equal(a["costs"], b["costs"])
+    assert all(np.array_equal(x, y) for x, y in zip(a["tours"], b["tours"]))
+    assert np.array_equal(a["trace"], b["trace"])
+    assert np.array_equal(a["colony_work"], b["colony_work"])
+    late = a["trace"][-16:]
+    assert float(late["construction_steps"].sum()) / (16 * 4 * ants) > 30   # walks several times the MNE target
