@@ -105,6 +105,7 @@ struct InstanceView {
     std::uint32_t sample_count;
     const double* local_scale;     // [n] mean of the min(8, n-1) nearest lengths
     double scale_epsilon;          // 1e-12 * max(coordinate span, 1)
+    const float* alpha;            // [n][k] alpha-nearness of the primary entries (prior features)
 };
 
 // GP program (postfix IR; device mirror of faco_program).

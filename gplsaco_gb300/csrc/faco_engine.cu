@@ -166,7 +166,7 @@ struct Instance {
     DeviceBuffer<int2> d_xy;
     DeviceBuffer<faco::node_t> d_primary, d_backup, d_ls, d_initial;
     DeviceBuffer<int> d_ls_dist;
-    DeviceBuffer<float> d_eta;
+    DeviceBuffer<float> d_eta, d_alpha;
     DeviceBuffer<faco::node_t> d_regions;
     std::uint32_t region_offsets[5] = {0, 0, 0, 0, 0};
     float mean_nn = 1.0f;
@@ -185,6 +185,7 @@ struct Instance {
         v.sample_count = sample_count;
         v.local_scale = d_local_scale.get();
         v.scale_epsilon = scale_epsilon;
+        v.alpha = d_alpha.get();
         return v;
     }
 };
@@ -490,6 +491,9 @@ int faco_register_problem(faco_engine* e, uint64_t instance_key, const double* x
         inst->d_ls.upload(inst->ls, s);
         inst->d_ls_dist.upload(ls_dist, s);
         inst->d_eta.upload(eta, s);
+        std::vector<float> alpha;
+        faco::host_alpha(inst->xy, n, inst->k, inst->primary, inst->b, inst->backup, inst->w, inst->ls, alpha);
+        inst->d_alpha.upload(alpha, s);
         std::vector<std::uint16_t> regions;
         faco::host_regions(inst->xy, n, inst->region_offsets, regions);
         inst->d_regions.upload(regions, s);

@@ -26,6 +26,11 @@ void host_rows_from_near(const std::vector<std::uint16_t>& near, const std::vect
 std::vector<std::uint32_t> host_nearest_neighbour_tour_near(const std::vector<std::int32_t>& xy, std::uint32_t n,
                                                             const std::vector<std::uint16_t>& near,
                                                             std::uint32_t needed);
+// Alpha-nearness (length minus the longest edge on the minimum spanning
+// tree path between the ends) of every primary candidate entry, [n][k].
+void host_alpha(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t k,
+                const std::vector<std::uint16_t>& primary, std::uint32_t b, const std::vector<std::uint16_t>& backup,
+                std::uint32_t w, const std::vector<std::uint16_t>& ls, std::vector<float>& alpha);
 void host_distance_order(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t w,
                          const std::uint32_t* rows, std::vector<std::uint16_t>& ls,
                          std::vector<std::int32_t>& ls_dist);

@@ -217,3 +217,115 @@ void host_distance_order(const std::vector<std::int32_t>& xy, std::uint32_t n, s
 }
 
 }  // namespace faco
+
+namespace faco {
+
+// Alpha-nearness of every primary candidate entry (Helsgaun, "An effective
+// implementation of the Lin-Kernighan traveling salesman heuristic", EJOR
+// 126 (2000), after Held and Karp's 1-trees): alpha(i, j) = d(i, j) -
+// beta(i, j), beta the longest edge on the path between i and j in a minimum
+// spanning tree -- the smallest bottleneck of any path between them, so the
+// same for every minimum tree.  The tree here spans the candidate graph (the
+// union of the primary, backup and LS rows, undirected); where that graph
+// has several components, entries whose ends lie in different components
+// get alpha = d(i, j).  Kruskal's algorithm over the edges sorted by (length,
+// ends), then path maxima by binary lifting from a root per component.
+void host_alpha(const std::vector<std::int32_t>& xy, std::uint32_t n, std::uint32_t k,
+                const std::vector<std::uint16_t>& primary, std::uint32_t b, const std::vector<std::uint16_t>& backup,
+                std::uint32_t w, const std::vector<std::uint16_t>& ls, std::vector<float>& alpha) {
+    struct Edge { std::int32_t d; std::uint32_t a, c; };
+    std::vector<Edge> edges;
+    edges.reserve(static_cast<std::size_t>(n) * (k + b + w));
+    auto dist = [&](std::uint32_t i, std::uint32_t j) {
+        return host_euc2d(xy[2 * i], xy[2 * i + 1], xy[2 * j], xy[2 * j + 1]);
+    };
+    auto add_rows = [&](const std::vector<std::uint16_t>& rows, std::uint32_t width) {
+        for (std::uint32_t i = 0; i < n; ++i)
+            for (std::uint32_t r = 0; r < width; ++r) {
+                const std::uint32_t j = rows[static_cast<std::size_t>(i) * width + r];
+                if (j < n && j != i) edges.push_back({dist(i, j), std::min(i, j), std::max(i, j)});
+            }
+    };
+    add_rows(primary, k);
+    add_rows(backup, b);
+    add_rows(ls, w);
+    std::sort(edges.begin(), edges.end(), [](const Edge& x, const Edge& y) {
+        return x.d != y.d ? x.d < y.d : x.a != y.a ? x.a < y.a : x.c < y.c;
+    });
+    std::vector<std::uint32_t> root(n);
+    for (std::uint32_t i = 0; i < n; ++i) root[i] = i;
+    auto find = [&](std::uint32_t v) {
+        while (root[v] != v) v = root[v] = root[root[v]];
+        return v;
+    };
+    std::vector<std::vector<std::pair<std::uint32_t, std::int32_t>>> tree(n);
+    for (const Edge& e : edges) {
+        const std::uint32_t ra = find(e.a), rc = find(e.c);
+        if (ra == rc) continue;
+        root[ra] = rc;
+        tree[e.a].push_back({e.c, e.d});
+        tree[e.c].push_back({e.a, e.d});
+    }
+    // roots, depths and the lifting tables (ancestor, longest edge to it)
+    std::uint32_t levels = 1;
+    while ((1u << levels) < n) ++levels;
+    std::vector<std::uint32_t> up(static_cast<std::size_t>(levels) * n), comp(n, n), depth(n, 0);
+    std::vector<std::int32_t> best(static_cast<std::size_t>(levels) * n, 0);
+    std::vector<std::uint32_t> queue;
+    queue.reserve(n);
+    for (std::uint32_t s = 0; s < n; ++s) {
+        if (comp[s] != n) continue;
+        comp[s] = s;
+        up[s] = s;
+        best[s] = 0;
+        queue.assign(1, s);
+        for (std::size_t h = 0; h < queue.size(); ++h) {
+            const std::uint32_t v = queue[h];
+            for (const auto& [u, d] : tree[v]) {
+                if (comp[u] != n) continue;
+                comp[u] = s;
+                depth[u] = depth[v] + 1;
+                up[u] = v;
+                best[u] = d;
+                queue.push_back(u);
+            }
+        }
+    }
+    for (std::uint32_t l = 1; l < levels; ++l)
+        for (std::uint32_t v = 0; v < n; ++v) {
+            const std::uint32_t mid = up[static_cast<std::size_t>(l - 1) * n + v];
+            up[static_cast<std::size_t>(l) * n + v] = up[static_cast<std::size_t>(l - 1) * n + mid];
+            best[static_cast<std::size_t>(l) * n + v] =
+                std::max(best[static_cast<std::size_t>(l - 1) * n + v], best[static_cast<std::size_t>(l - 1) * n + mid]);
+        }
+    auto path_max = [&](std::uint32_t a, std::uint32_t c) {
+        std::int32_t m = 0;
+        if (depth[a] < depth[c]) std::swap(a, c);
+        for (std::uint32_t l = levels; l-- > 0;)
+            if (depth[a] - depth[c] >= (1u << l)) {
+                m = std::max(m, best[static_cast<std::size_t>(l) * n + a]);
+                a = up[static_cast<std::size_t>(l) * n + a];
+            }
+        if (a == c) return m;
+        for (std::uint32_t l = levels; l-- > 0;) {
+            const std::uint32_t ua = up[static_cast<std::size_t>(l) * n + a], uc = up[static_cast<std::size_t>(l) * n + c];
+            if (ua != uc) {
+                m = std::max({m, best[static_cast<std::size_t>(l) * n + a], best[static_cast<std::size_t>(l) * n + c]});
+                a = ua;
+                c = uc;
+            }
+        }
+        return std::max({m, best[a], best[c]});
+    };
+    alpha.assign(static_cast<std::size_t>(n) * k, 0.0f);
+    for (std::uint32_t i = 0; i < n; ++i)
+        for (std::uint32_t r = 0; r < k; ++r) {
+            const std::uint32_t j = primary[static_cast<std::size_t>(i) * k + r];
+            if (j >= n) continue;
+            const std::int32_t d = dist(i, j);
+            alpha[static_cast<std::size_t>(i) * k + r] =
+                static_cast<float>(comp[i] == comp[j] ? d - path_max(i, j) : d);
+        }
+}
+
+}  // namespace faco

@@ -275,6 +275,10 @@ __global__ void adam_kernel(MlpParams* P, const MlpParams* grad, MlpParams* m, M
 //   x3 d(i,j) / d(i, k-th neighbour)
 //   x4 (tau - tau_min) / (tau_max - tau_min), clipped to [0,1]
 //   x5 1 when (i,j) is an edge of the colony's global-best tour
+//   x6 rank of i in j's own candidate row / (k-1), 1 when absent
+//   x7 min(alpha(i,j) / mean nearest-neighbour distance, 4) / 4, alpha the
+//      alpha-nearness (length minus the longest edge on the minimum
+//      spanning tree path between i and j)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void edge_features(const InstanceView& in, const ColonyView& cv, const ColonyState& st,
                                               const std::uint32_t* gnbr, std::uint32_t i, std::uint32_t r,
@@ -305,6 +309,7 @@ __device__ __forceinline__ void edge_features(const InstanceView& in, const Colo
             break;
         }
     x[6] = back;
+    x[7] = fminf(in.alpha[(size_t)i * k + r] / in.mean_nn, 4.0f) * 0.25f;
 }
 
 // Packed neighbours of the colony's global-best tour in shared memory.
@@ -335,7 +340,6 @@ __global__ void edge_features_kernel(const InstanceView* instances, const Colony
             edge_features(in, cv, st, gnbr, i, r, x);
             __nv_bfloat16* row = x_out + (base + idx) * kMlpIn;
             for (int f = 0; f < kMlpFeatures; ++f) row[f] = __float2bfloat16(x[f]);
-            row[7] = __float2bfloat16(0.0f);
         }
         if (y_out) {
             const std::uint32_t j = in.primary[idx], nb = gnbr[i];
@@ -384,7 +388,7 @@ __global__ void __launch_bounds__(128) prior_apply_kernel(const InstanceView* in
             float x[kMlpFeatures];
             edge_features(in, cv, st, gnbr, e / k, e % k, x);
             return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]),
-                              pack_bf16(x[6], 0.0f));
+                              pack_bf16(x[6], x[7]));
         },
         [&](std::uint32_t e, float z) {
             const float f = floor + sigmoid(z);
@@ -394,14 +398,14 @@ __global__ void __launch_bounds__(128) prior_apply_kernel(const InstanceView* in
         });
 }
 
-// BF16 operand copies of the masters (input columns 6, 7 stay zero).
+// BF16 operand copies of the masters.
 __global__ void refresh_operands_kernel(const MlpParams* P, MlpOperands* O) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpHidden * kMlpHidden; i += gridDim.x * blockDim.x) {
         const int r = i / kMlpHidden, c = i % kMlpHidden;
         O->w2[i] = __float2bfloat16(P->w2[i]);
         O->w2t[c * kMlpHidden + r] = __float2bfloat16(P->w2[i]);
         if (i < kMlpHidden * kMlpIn)
-            O->w1[i] = __float2bfloat16((i % kMlpIn) < kMlpFeatures ? P->w1[i] : 0.0f);
+            O->w1[i] = __float2bfloat16(P->w1[i]);
     }
 }
 

@@ -1,11 +1,11 @@
-// prior_mlp.cuh -- the learned edge prior: a 6 -> 64 -> 64 -> 1 MLP scored
-// per candidate edge (7 features), BF16 operands with FP32 accumulation on the tensor
+// prior_mlp.cuh -- the learned edge prior: an 8 -> 64 -> 64 -> 1 MLP scored
+// per candidate edge (8 features), BF16 operands with FP32 accumulation on the tensor
 // cores (mma.sync m16n8k16), forward and backward.
 //
 // The reference has no learned prior (its only prior is an external LKH
 // candidate export, python/gp_faco/candidate_prior.py:20-36); this is the
 // engine's own component.  Layout of one warp tile: 16 edges (rows); layer 1
-// K = 16 (7 features + zero padding), layers 2 and the input gradient K = 64;
+// K = 16 (8 features + zero padding), layers 2 and the input gradient K = 64;
 // the weight gradients use the edges as the K dimension, staged through
 // shared memory by the block (4 warps = 64 edges per chunk).
 #pragma once
@@ -16,13 +16,13 @@
 
 namespace faco {
 
-constexpr int kMlpIn = 8;       // feature slots per edge (7 used + 1 zero)
-constexpr int kMlpFeatures = 7;
+constexpr int kMlpIn = 8;       // feature slots per edge
+constexpr int kMlpFeatures = 8;
 constexpr int kMlpHidden = 64;
 
 // FP32 master parameters (4,673 used values) and their BF16 operand copies.
 struct MlpParams {
-    float w1[kMlpHidden * kMlpIn];      // [out][in], columns 6,7 zero
+    float w1[kMlpHidden * kMlpIn];      // [out][in]
     float b1[kMlpHidden];
     float w2[kMlpHidden * kMlpHidden];  // [out][in]
     float b2[kMlpHidden];

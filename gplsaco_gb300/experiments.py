@@ -45,7 +45,7 @@ class GapConfig:
     extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
     # Both arms are tuned on validation instances (seeds 200-215) by wall-clock
     # time to the target gap: plain FACO over MNE targets, the prior over
-    # (model, floor, gamma, refresh, MNE, departures).  "full" sees all seven features;
+    # (model, floor, gamma, refresh, MNE, departures).  "full" sees all eight features;
     # "geometry" only the geometric ones (trail level and best-tour membership
     # masked), so it does not pull ants back onto the parent tour's edges --
     # and, its inputs being static, needs no refresh.  refresh: iterations
@@ -55,10 +55,13 @@ class GapConfig:
     # prior only re-ranks the departures from the parent tour (the parent's
     # entries keep the plain heuristic, the others the plain total weight per
     # node), so prior ants leave the parent tour as often as plain ants.
-    mne_grid: tuple = (8, 6, 5, 4)
+    mne_grid: tuple = (8, 6, 5, 4, 3)
     tune_grid: tuple = (("full", 0.5, 1, 10, 8, False), ("geometry", 0.2, 1, 0, 8, False),
                         ("geometry", 0.05, 2, 0, 8, False), ("geometry", 0.05, 2, 0, 6, False),
-                        ("geometry", 0.05, 2, 0, 5, False), ("geometry", 0.2, 2, 0, 6, False),
+                        ("geometry", 0.05, 2, 0, 5, False), ("geometry", 0.05, 2, 0, 4, False),
+                        ("geometry", 0.2, 2, 0, 6, False), ("geometry", 0.2, 2, 0, 4, False),
+                        ("full", 0.05, 2, 0, 6, False), ("full", 0.05, 2, 0, 4, False),
+                        ("full", 0.2, 1, 0, 5, False), ("full", 0.2, 2, 0, 4, False),
                         ("geometry", 0.05, 2, 0, 8, True), ("geometry", 0.05, 2, 0, 6, True),
                         ("geometry", 0.05, 2, 0, 5, True), ("geometry", 0.05, 1, 0, 5, True),
                         ("full", 0.05, 2, 10, 5, True), ("full", 0.05, 2, 10, 6, True))
@@ -175,7 +178,8 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
 
 
 # masked in the geometry model: x4 trail level, x5 best-tour membership
-# (x0-x3 and x6 -- length, rank, angle, length ratio, mutual rank -- stay)
+# (x0-x3, x6 and x7 -- length, rank, angle, length ratio, mutual rank,
+# alpha-nearness -- stay)
 COLONY_FEATURES = [4, 5]
 
 

@@ -34,11 +34,11 @@ def unpack(params: np.ndarray) -> dict:
 
 
 def init_params(seed: int = 0) -> np.ndarray:
-    """He-style initialisation (inputs 6, 7 zero)."""
+    """He-style initialisation."""
     rng = np.random.default_rng(seed)
     p = np.zeros(param_count(), np.float32)
     v = unpack(p)
-    v["w1"][:, :7] = rng.normal(0, np.sqrt(2 / 7), (HIDDEN, 7))
+    v["w1"][:] = rng.normal(0, np.sqrt(2 / IN), (HIDDEN, IN))
     v["w2"][:] = rng.normal(0, np.sqrt(2 / HIDDEN), (HIDDEN, HIDDEN))
     v["w3"][:] = rng.normal(0, np.sqrt(1 / HIDDEN), HIDDEN)
     v["b3"][:] = -2.0   # most candidate edges are not in the best tour

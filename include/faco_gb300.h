@@ -329,12 +329,13 @@ int faco_ant_diagnostic(const int32_t* xy, uint32_t n, const uint32_t* ls_rows, 
 
 /* ---- learned edge prior ----------------------------------------------------
  * No counterpart in the reference (its only candidate prior is an external
- * LKH export, python/gp_faco/candidate_prior.py:20-36).  A 6 -> 64 -> 64 -> 1
+ * LKH export, python/gp_faco/candidate_prior.py:20-36).  An 8 -> 64 -> 64 -> 1
  * MLP (ReLU, sigmoid output) scores every directed candidate edge from
  * [normalised distance, k-rank, angle to the nearest neighbour, ratio to the
- * k-th neighbour distance, normalised trail, in-global-best flag]; BF16
+ * k-th neighbour distance, normalised trail, in-global-best flag, mutual
+ * rank, alpha-nearness]; BF16
  * operands, FP32 accumulation on the tensor cores.  Parameters are one FP32
- * array of faco_mlp_param_count() values: w1[64][8] (inputs 6,7 unused),
+ * array of faco_mlp_param_count() values: w1[64][8],
  * b1[64], w2[64][64], b2[64], w3[64], b3, 3 padding.  Edge rows x are
  * [count][8] BF16 bit patterns. */
 int faco_mlp_param_count(void);

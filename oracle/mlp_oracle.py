@@ -34,7 +34,7 @@ def unpack(p: np.ndarray) -> dict:
 def forward(p: np.ndarray, x: np.ndarray):
     """x: [E, 8] float values (already BF16-representable)."""
     v = unpack(p)
-    w1 = bf16(v["w1"]); w1[:, 7:] = 0.0          # 7 features, slot 7 is padding
+    w1 = bf16(v["w1"])
     w2 = bf16(v["w2"])
     z1 = x @ w1.T + v["b1"]
     h1 = np.maximum(z1, 0.0)

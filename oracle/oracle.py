@@ -362,6 +362,48 @@ def departure_rows(primary, parent, trails, eta, prior_eta_rows) -> np.ndarray:
     return out
 
 
+def alpha_nearness(xy, primary, backup, ls) -> np.ndarray:
+    """Alpha-nearness of every primary candidate entry [n, k] (Helsgaun,
+    EJOR 126 (2000)): length minus the longest edge on the path between the
+    ends in a minimum spanning tree of the candidate graph (the union of the
+    primary, backup and LS rows); length where the ends lie in different
+    components.  The path maximum is the minimax (bottleneck) length, the same
+    for every minimum tree, found here by a walk over the tree from each node."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import minimum_spanning_tree
+    xy = np.asarray(xy, np.int64)
+    n = len(xy)
+    m = euc2d_matrix(xy).astype(np.int64)
+    rows = [np.asarray(r, np.int64) for r in (primary, backup, ls) if r is not None and np.asarray(r).size]
+    a = np.concatenate([np.repeat(np.arange(n), r.shape[1]) for r in rows])
+    c = np.concatenate([r.reshape(-1) for r in rows])
+    keep = a != c
+    pairs = np.unique(np.stack([np.minimum(a[keep], c[keep]), np.maximum(a[keep], c[keep])], axis=1), axis=0)
+    lo, hi = pairs[:, 0], pairs[:, 1]
+    # weights + 1: the tree routine drops explicit zeros (coincident points)
+    g = coo_matrix((m[lo, hi] + 1, (lo, hi)), shape=(n, n)).tocsr()
+    t = minimum_spanning_tree(g).tocoo()
+    adj = [[] for _ in range(n)]
+    for u, v, wt in zip(t.row, t.col, t.data):
+        adj[u].append((v, int(wt) - 1))
+        adj[v].append((u, int(wt) - 1))
+    primary = np.asarray(primary, np.int64)
+    out = np.zeros(primary.shape, np.float32)
+    for i in range(n):
+        best = np.full(n, -1, np.int64)
+        best[i] = 0
+        stack = [i]
+        while stack:
+            v = stack.pop()
+            for u, wt in adj[v]:
+                if best[u] < 0:
+                    best[u] = max(best[v], wt)
+                    stack.append(u)
+        for r, j in enumerate(primary[i]):
+            out[i, r] = m[i, j] - best[j] if best[j] >= 0 else m[i, j]
+    return out
+
+
 def prepare(xy, k, b, w, initial_ls_limit=100000):
     xy = np.ascontiguousarray(xy, dtype=np.int32)
     n = xy.shape[0]

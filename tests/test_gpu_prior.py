@@ -17,7 +17,7 @@ def prior(engine_lib):
 
 def _data(prior, rng, E):
     x = np.zeros((E, 8), np.float32)
-    x[:, :7] = rng.random((E, 7), dtype=np.float32)
+    x[:, :] = rng.random((E, 8), dtype=np.float32)
     x[:, 5] = (rng.random(E) < 0.2).astype(np.float32)
     bits = prior.to_bf16_bits(x)
     y = ((x[:, 0] < 0.3) ^ (x[:, 5] > 0.5)).astype(np.float32)
@@ -49,8 +49,6 @@ def test_gradient_matches_oracle(prior, E):
     ref = mlp_oracle.unpack(want)
     for name in ("w1", "b1", "w2", "b2", "w3", "b3"):
         g, r = view[name].astype(np.float64), ref[name]
-        if name == "w1":
-            g, r = g[:, :7], r[:, :7]
         scale = max(np.max(np.abs(r)), 1e-12)
         assert np.max(np.abs(g - r)) <= 1e-3 * scale, name
 
@@ -91,7 +89,14 @@ def test_edge_data_and_fallback(prior):
     assert x.shape == (3 * n * 16, 8) and y.shape == (3 * n * 16,)
     xf = prior.from_bf16_bits(x)
     assert np.array_equal(xf[:, 5], y)                       # in-best-tour flag == label at the same state
-    assert np.all((xf[:, :7] >= 0) & (xf[:, :7] <= 1))
+    assert np.all((xf >= 0) & (xf <= 1))
+    # x7: alpha-nearness over the mean nearest-neighbour length, clipped at 4, / 4
+    rows = engine.problem_rows(5)
+    alpha = oracle.alpha_nearness(xy, rows["primary"], rows["backup"], rows["ls"])
+    mean_nn = np.float32(max(1.0, float(np.mean(oracle.euc2d_matrix(xy)[np.arange(n), rows["ls"][:, 0]]))))
+    want7 = (np.minimum(alpha.astype(np.float32) / mean_nn, np.float32(4.0)) * np.float32(0.25)).astype(np.float32)
+    want7 = prior.from_bf16_bits(prior.to_bf16_bits(np.tile(want7.reshape(-1), 3)))
+    assert np.array_equal(xf[:, 7], want7)
     # x6: rank of i in j's candidate row / (k-1), 1 when absent (mutual nearness)
     primary = engine.problem_rows(5)["primary"].astype(np.int64)
     k = primary.shape[1]
