@@ -1,8 +1,8 @@
 """Generates tests/golden/ref_colony_lengths.json: final tour lengths of
 whole plain-FACO colony runs by the reference's own CPU core (oracle/_ref,
-compiled from the reference sources), 30 seeds per case, on seeded uniform
-instances with the EUC_2D integer metric.  The engine's 30-seed
-distributions are compared with these (mean and Mann-Whitney), since the
+compiled from the reference sources), 100 seeds per case, on seeded uniform
+instances with the EUC_2D integer metric.  The engine's distributions over
+the same seed count are compared with these (mean and Mann-Whitney), since the
 reference draws its randomness from std::mt19937_64 and the engine from
 Philox: only the distributions, not the tours, can agree.
 
@@ -23,7 +23,7 @@ from oracle import oracle  # noqa: E402
 
 # (n, instance seed, iterations): config 1's instance and uniform N=500/1000
 CASES = [(100, 1, 100), (500, 2, 100), (1000, 3, 100), (500, 2, 300), (1000, 3, 300)]
-SEEDS = list(range(1, 31))
+SEEDS = list(range(1, 101))
 PARAMS = dict(ants=32, k=16, b=64, w=20, mne=8, retention=0.98, p_best=0.1, epoch_source_probability=0.01)
 
 

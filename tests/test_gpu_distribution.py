@@ -1,8 +1,8 @@
-"""End to end against the reference's own CPU core: the engine's 30-seed
+"""End to end against the reference's own CPU core: the engine's
 final-length distributions on uniform N=100/500/1000 instances agree with
-the reference's (tests/golden/ref_colony_lengths.json): mean within 0.1% --
-or 2.5 standard errors where 30 seeds cannot resolve 0.1% -- and two-sided
-Mann-Whitney p > 0.05.  Runs through the C ABI (faco_evaluate)."""
+the reference's (tests/golden/ref_colony_lengths.json, 100 seeds per case):
+mean within 0.1% and two-sided Mann-Whitney p > 0.05.  Runs through the C
+ABI (faco_evaluate)."""
 import numpy as np
 import pytest
 

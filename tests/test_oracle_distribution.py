@@ -1,7 +1,6 @@
 """The oracle's whole colony runs (Philox draws) against the reference's own
-CPU core (std::mt19937_64 draws): 30-seed final-length distributions agree
-(mean within 0.1% -- or 2.5 standard errors where 30 seeds cannot resolve
-0.1% -- and two-sided Mann-Whitney p > 0.05)."""
+CPU core (std::mt19937_64 draws): final-length distributions over 100 seeds
+agree (mean within 0.1% and two-sided Mann-Whitney p > 0.05)."""
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
