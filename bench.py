@@ -52,15 +52,22 @@ L2_BYTES = 129 * 2**20
 CPU_COLONIES_PER_THREAD = 16
 STEADY_ITERATION = 400   # the converged-colony window of the throughput workload
 ITERATIONS_PER_STEP = 16  # a step: one replay of the engine's per-evaluation CUDA graph
-# DRAM traffic and issue figures of the default panel from ncu, filled in from
-# a capture of this panel (none yet: the line then reports null).
-# Reported for the default workload only.
+# DRAM traffic and issue figures of the default panel from one ncu capture at
+# iteration 160, the middle of the timed window (gplsaco_gb300.profile_ant:
+# one unchained launch of the ant kernel and of the colony update over every
+# colony): dram__bytes_read.sum + dram__bytes_write.sum of the two kernels,
+# 21.48 MB + 34.20 MB per iteration, x 16 iterations per step; the ant
+# kernel's smsp__issue_active and smsp__inst_executed (341.6 M over 8,192
+# ant-tours).  Reported for the default workload only.
 THROUGHPUT_CAPTURE = {
-    "traffic_bytes_per_step": None,
-    "traffic_source": None,
-    "ant_issue_active_pct": None,
-    "ant_warp_instructions_per_ant_tour": None,
-    "issue_source": None,
+    "traffic_bytes_per_step": 16 * (21_479_936 + 34_203_904),
+    "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of ant_kernel and colony_update_kernel, "
+                       "one unchained launch each over every colony at iteration 160 of this panel, x 16 "
+                       "iterations per step"),
+    "ant_issue_active_pct": 61.72,
+    "ant_warp_instructions_per_ant_tour": 341_637_677 / 8192,
+    "issue_source": ("ncu smsp__issue_active.avg.pct_of_peak_sustained_active and smsp__inst_executed.sum of "
+                     "the whole-panel ant launch at iteration 160 of this panel"),
 }
 
 

@@ -29,7 +29,7 @@ def test_bench_line_keeps_the_contract():
     assert e2e["h2d_bytes_per_step"] > 0 and e2e["d2h_bytes_per_step"] > 0
     roof = d["roofline"]
     assert roof["bound"] == "hbm" and roof["unit"] == "GB/s" and roof["peak"] > 0
-    assert abs(roof["frac"] - roof["achieved"] / roof["peak"]) < 1e-9
+    assert abs(roof["frac"] - roof["achieved"] / roof["peak"]) < 1e-9 and roof["traffic"] > 0
     # the roofline describes the timed window: its bytes over the timed step time
     assert abs(roof["achieved"] * 1e9 * d["ms_per_step"] / 1e3 - roof["bytes_per_step"]) < 1e-6 * roof["bytes_per_step"]
     assert 0 < roof["ant_kernel"]["share_of_unchained_time"] < 1
