@@ -399,3 +399,139 @@ def profile_prior_application(refreshes: int = 3, device: int = 0) -> None:
 
 if __name__ == "__main__":
     profile_prior_application()
+
+
+# ---------------------------------------------------------------------------
+# Large clustered batch with the learned prior and a per-instance plain
+# fallback: 16 instances with N ~ U[5000, 10000], 32-64 clusters in
+# [0, 10^7]^2, 5 seeds each (80 colonies), k=32, 64 ants, 2-opt window 32 +
+# Or-opt (segments <= 3), MNE 8, 1000 iterations.
+# ---------------------------------------------------------------------------
+@dataclass
+class LargeConfig:
+    instances: int = 16
+    seeds: int = 5
+    ants: int = 64
+    k: int = 32
+    ls_width: int = 32
+    retention: float = 0.98
+    mne: int = 8
+    iterations: int = 1000
+    chunk: int = 50                 # iterations between cost reads
+    warmup: int = 100               # iterations before the fallback decision
+    floor: float = 0.05
+    gamma: int = 2
+    train_pool: int = 16            # training instances: N ~ U[1000, 2000], same generator, seeds 700-715
+    train_snapshot: int = 25
+    train_iterations: int = 300
+    epochs: int = 12
+    batch: int = 8192
+    lr: float = 3e-3
+    follow: int = 0
+
+
+def _large_settings(cfg: LargeConfig) -> FixedFacoSettings:
+    return FixedFacoSettings(ants=cfg.ants, primary_width=cfg.k, backup_width=64, ls_width=cfg.ls_width,
+                             retention=cfg.retention, ls_mode=1, follow=cfg.follow)
+
+
+def large_training_data(cfg: LargeConfig, device: int = 0):
+    """Edge features and labels from plain runs of smaller instances of the
+    large workload's generator (same k, LS and Or-opt settings)."""
+    pool = []
+    for i in range(cfg.train_pool):
+        rng = np.random.default_rng(700 + i)
+        n = int(rng.integers(1000, 2001))
+        pool.append(inst.clustered(n, 700 + i, clusters=(32, 64), box=10**7))
+    engine = FacoBatchEngine(max(len(p) for p in pool), 2 * len(pool), _large_settings(cfg), device=device)
+    for i, xy in enumerate(pool):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    keys = np.repeat(np.arange(1, len(pool) + 1, dtype=np.uint64), 2)
+    engine.begin(keys, np.tile(np.array([11, 12], np.uint64), len(pool)), cfg.mne)
+    engine.step(cfg.train_snapshot)
+    x, _ = engine.edge_data(features=True, labels=False)
+    engine.step(cfg.train_iterations - cfg.train_snapshot)
+    _, y = engine.edge_data(features=False, labels=True)
+    engine.finish()
+    engine.close()
+    return x, y
+
+
+def _large_arm(cfg: LargeConfig, xys: list, params=None, plain_warm=None, device: int = 0):
+    """One arm on the large panel: rows (iteration, seconds, costs [instances,
+    seeds]) every `chunk` iterations, and the per-instance prior flags after
+    the warm-up (all ones for the plain arm)."""
+    count = len(xys) * cfg.seeds
+    engine = FacoBatchEngine(max(len(xy) for xy in xys), count, _large_settings(cfg), device=device)
+    for i, xy in enumerate(xys):
+        engine.register_problem(1 + i, xy.astype(np.float64))
+    keys = np.repeat(np.arange(1, len(xys) + 1, dtype=np.uint64), cfg.seeds)
+    seeds = np.tile(np.arange(1, cfg.seeds + 1, dtype=np.uint64), len(xys))
+    engine.begin(keys, seeds, cfg.mne)
+    costs, _ = engine.current_costs(count)
+    enabled = np.ones(len(xys), np.uint8)
+    t0 = time.perf_counter()
+    if params is not None:
+        engine.prior_set(params, np.ones(count, np.uint8), cfg.floor, cfg.gamma)
+    rows = [(0, 0.0, costs.reshape(len(xys), cfg.seeds).copy())]
+    done = 0
+    while done < cfg.iterations:
+        step = min(cfg.chunk, cfg.warmup - done) if done < cfg.warmup else cfg.chunk
+        engine.step(step)
+        done += step
+        costs, _ = engine.current_costs(count)
+        per = costs.reshape(len(xys), cfg.seeds)
+        if params is not None and done == cfg.warmup:
+            # the prior stays on an instance only where its seeds' mean length
+            # is not above the plain arm's at the same iteration
+            enabled = (per.mean(axis=1) <= plain_warm.mean(axis=1)).astype(np.uint8)
+            engine.prior_set(None, np.repeat(enabled, cfg.seeds), cfg.floor, cfg.gamma)
+        rows.append((done, time.perf_counter() - t0, per.copy()))
+    res = engine.finish()
+    engine.close()
+    work = {"construction_steps": res["construction_steps"] / float(cfg.ants * count * done),
+            "ls_evaluations": res["ls_evaluations"] / float(cfg.ants * count * done)}
+    return rows, enabled, work
+
+
+def large_prior(cfg: LargeConfig | None = None, device: int = 0, log=print) -> dict:
+    """Plain FACO against learned-prior FACO with the per-instance fallback on
+    the large clustered panel.  Gaps are taken against the best length either
+    arm reaches on the instance (all seeds, all iterations)."""
+    cfg = cfg or LargeConfig()
+    t_start = time.perf_counter()
+    x, y = large_training_data(cfg, device)
+    xg = x.copy()
+    xg[:, COLONY_FEATURES] = 0
+    params, losses = prior_mod.train(prior_mod.init_params(seed=1), xg, y, epochs=cfg.epochs, batch=cfg.batch,
+                                     lr=cfg.lr)
+    prior_mod.unpack(params)["w1"][:, COLONY_FEATURES] = 0.0
+    log(f"large-panel prior: {len(y)} training rows, losses {np.round(losses, 4).tolist()}")
+    xys = inst.large_clustered(cfg.instances)
+    plain, _, plain_work = _large_arm(cfg, xys, device=device)
+    warm = next(r for r in plain if r[0] == cfg.warmup)[2]
+    prior, enabled, prior_work = _large_arm(cfg, xys, params, warm, device)
+    best = np.minimum(np.min([r[2].min(axis=1) for r in plain], axis=0),
+                      np.min([r[2].min(axis=1) for r in prior], axis=0)).astype(np.float64)
+
+    def gap(per):
+        return float(np.mean((per.mean(axis=1) - best) / best))
+
+    final_plain, final_prior = plain[-1][2].mean(axis=1), prior[-1][2].mean(axis=1)
+    target = gap(plain[-1][2])
+    reach = next(((it, sec) for it, sec, per in prior if gap(per) <= target), (None, None))
+    return {
+        "instances": [{"n": len(xy), "prior_kept": bool(enabled[i]),
+                       "final_mean_plain": float(final_plain[i]), "final_mean_prior": float(final_prior[i])}
+                      for i, xy in enumerate(xys)],
+        "prior_kept": int(enabled.sum()),
+        "final_gap_plain": gap(plain[-1][2]), "final_gap_prior": gap(prior[-1][2]),
+        "seconds_plain": plain[-1][1], "seconds_prior": prior[-1][1],
+        "prior_reaches_plain_final_gap": {"iterations": reach[0], "seconds": reach[1],
+                                          "time_ratio": (reach[1] / plain[-1][1]) if reach[1] else None},
+        "gap_at": {str(p_[0]): [round(gap(p_[2]), 5), round(gap(q_[2]), 5)] for p_, q_ in zip(plain, prior)
+                   if p_[0] in (0, 100, 200, 500, 1000)},
+        "plain_work": plain_work, "prior_work": prior_work,
+        "training_rows": int(len(y)), "training_loss": [float(v) for v in losses],
+        "total_seconds": time.perf_counter() - t_start,
+    }
