@@ -1,0 +1,29 @@
+"""The ant kernel's own source run on the CPU (tests/emulation): engine-mode
+ants -- steps taken one at a time (ant_kernel<0>) and parent-following steps
+taken in batches (ant_kernel<5>) -- against the oracle's ant with the same
+Philox draws, bit for bit: final tour, construction and final lengths, step
+count.  The warp intrinsics are emulated with 32 threads that are delayed at
+random before every barrier, and the lanes' per-ant registers are compared
+after every step, so a warp race (lanes that read shared state while another
+lane writes it) fails the run instead of hiding behind lockstep execution.
+Each case runs in a child process (tests/emulation/run_ants.py).
+
+States: the prepared tour with plain heuristics (early walks) and an oracle
+colony after 100-150 iterations (converged trails: long walks along the
+parent tour, where the batches carry most steps)."""
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.mark.parametrize("kind,n,k,iterations", [("uniform", 60, 8, 0), ("clustered", 300, 20, 100),
+                                                  ("uniform", 800, 16, 150)])
+def test_emulated_kernel_ants_match_oracle(oracle, kind, n, k, iterations):
+    out = subprocess.run([sys.executable, str(ROOT / "tests" / "emulation" / "run_ants.py"), kind, str(n), str(k),
+                          str(iterations)], capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert out.returncode == 0, (out.stdout[-2000:], out.stderr[-3000:])
+    assert "equal the oracle" in out.stdout
