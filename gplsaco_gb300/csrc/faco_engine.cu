@@ -2034,14 +2034,24 @@ static cudaError_t prepare_tensor_kernels() {
     if (err == cudaSuccess)
         err = cudaFuncSetAttribute(faco::prior_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(faco::tc::kLaunchSmemBytes));
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(faco::mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(faco::tc::kGradSmemBytes));
     return err;
 }
 static std::uint32_t tensor_grid(std::uint64_t tiles) {
     return static_cast<std::uint32_t>(std::max<std::uint64_t>(1, std::min<std::uint64_t>(tiles, 152u * faco::tc::kCtasPerSm)));
 }
 
-static std::uint32_t mlp_blocks(std::uint64_t chunks) {
-    return static_cast<std::uint32_t>(std::max<std::uint64_t>(1, std::min<std::uint64_t>(chunks, 152ull * 8)));
+// Gradient CTAs for `rows` rows: one per 128-row tile, at most
+// tc::kGradCtasPerSm per SM (every CTA gets at least one tile).
+static std::uint32_t grad_blocks(std::uint64_t rows) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 152;
+    const std::uint64_t tiles = (rows + faco::tc::kRows - 1) / faco::tc::kRows;
+    return static_cast<std::uint32_t>(
+        std::max<std::uint64_t>(1, std::min<std::uint64_t>(tiles, static_cast<std::uint64_t>(sms) * faco::tc::kGradCtasPerSm)));
 }
 
 int faco_mlp_forward(const float* params, const uint16_t* x, uint32_t count, float* prob) {
@@ -2083,17 +2093,23 @@ int faco_mlp_gradient(const float* params, const uint16_t* x, const float* y, ui
         dy.upload(y, count, s);
         G.resize(1);
         cuda_check(cudaMemsetAsync(dl.get(), 0, sizeof(float), s), "memset");
-        const std::uint32_t blocks = mlp_blocks((count + 63) / 64);
+        cuda_check(prepare_tensor_kernels(), "tcgen05 kernel attributes");
+        const std::uint32_t blocks = grad_blocks(count);
         DeviceBuffer<faco::MlpParams> partials(blocks);
         DeviceBuffer<float> loss_partials(blocks);
-        faco::mlp_grad_kernel<<<blocks, 128, 0, s>>>(P.get(), O.get(), dx.get(), dy.get(), count, 1.0f / count,
-                                                     partials.get(), loss_partials.get());
+        DeviceBuffer<unsigned> derr(1);
+        cuda_check(cudaMemsetAsync(derr.get(), 0, sizeof(unsigned), s), "memset");
+        faco::mlp_grad_kernel<<<blocks, 128, faco::tc::kGradSmemBytes, s>>>(
+            P.get(), O.get(), dx.get(), dy.get(), count, 1.0f / count, partials.get(), loss_partials.get(), derr.get());
         faco::mlp_grad_reduce_kernel<<<20, 256, 0, s>>>(partials.get(), loss_partials.get(), blocks, G.get(),
                                                         dl.get());
         cuda_check(cudaGetLastError(), "mlp gradient");
+        unsigned err = 0;
         G.download(reinterpret_cast<faco::MlpParams*>(grad), 1, s);
         dl.download(loss, 1, s);
+        derr.download(&err, 1, s);
         cuda_check(cudaStreamSynchronize(s), "mlp gradient");
+        if (err) throw Error(FACO_EDEVICE, "device error word " + std::to_string(err) + " in the MLP gradient");
     });
 }
 
@@ -2115,17 +2131,20 @@ int faco_mlp_train(float* params, const uint16_t* x, const float* y, uint32_t co
         cuda_check(cudaMemsetAsync(dl.get(), 0, sizeof(float) * epochs, s), "memset");
         const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
         std::uint64_t step = 0;
-        const std::uint32_t max_blocks = mlp_blocks((std::min(batch, count) + 63) / 64);
+        cuda_check(prepare_tensor_kernels(), "tcgen05 kernel attributes");
+        const std::uint32_t max_blocks = grad_blocks(std::min(batch, count));
         DeviceBuffer<faco::MlpParams> partials(max_blocks);
         DeviceBuffer<float> loss_partials(max_blocks);
+        DeviceBuffer<unsigned> derr(1);
+        cuda_check(cudaMemsetAsync(derr.get(), 0, sizeof(unsigned), s), "memset");
         for (std::uint32_t ep = 0; ep < epochs; ++ep) {
             for (std::uint32_t first = 0; first < count; first += batch) {
                 const std::uint32_t size = std::min(batch, count - first);
-                const std::uint32_t blocks = mlp_blocks((size + 63) / 64);
+                const std::uint32_t blocks = grad_blocks(size);
                 ++step;
-                faco::mlp_grad_kernel<<<blocks, 128, 0, s>>>(
+                faco::mlp_grad_kernel<<<blocks, 128, faco::tc::kGradSmemBytes, s>>>(
                     P.get(), O.get(), dx.get() + static_cast<std::size_t>(first) * faco::kMlpIn, dy.get() + first,
-                    size, 1.0f / size, partials.get(), loss_partials.get());
+                    size, 1.0f / size, partials.get(), loss_partials.get(), derr.get());
                 faco::mlp_grad_reduce_kernel<<<20, 256, 0, s>>>(partials.get(), loss_partials.get(), blocks, G.get(),
                                                                 dl.get() + ep);
                 const float b1 = 1.0f - std::pow(beta1, static_cast<float>(step));
@@ -2135,9 +2154,13 @@ int faco_mlp_train(float* params, const uint16_t* x, const float* y, uint32_t co
                 cuda_check(cudaGetLastError(), "training step");
             }
         }
-        P.download(reinterpret_cast<faco::MlpParams*>(params), 1, s);
         std::vector<float> losses(epochs);
         dl.download(losses.data(), epochs, s);
+        unsigned err = 0;
+        derr.download(&err, 1, s);
+        cuda_check(cudaStreamSynchronize(s), "mlp training");
+        if (err) throw Error(FACO_EDEVICE, "device error word " + std::to_string(err) + " in the MLP gradient");
+        P.download(reinterpret_cast<faco::MlpParams*>(params), 1, s);
         cuda_check(cudaStreamSynchronize(s), "mlp training");
         if (epoch_losses)
             for (std::uint32_t ep = 0; ep < epochs; ++ep) epoch_losses[ep] = losses[ep] / count;

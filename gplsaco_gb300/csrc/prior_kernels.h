@@ -9,12 +9,14 @@
 
 namespace faco {
 
-// tcgen05 kernels (prior_mlp_tc.cuh): 128 threads, dynamic shared memory
-// tc::kLaunchSmemBytes, at most tc::kCtasPerSm CTAs per SM.
+// tcgen05 kernels (prior_mlp_tc.cuh), 128 threads: the forward pass with
+// tc::kLaunchSmemBytes of dynamic shared memory (at most tc::kCtasPerSm CTAs
+// per SM), the gradient with tc::kGradSmemBytes (tc::kGradCtasPerSm).
 __global__ void mlp_forward_kernel(const MlpParams* P, const MlpOperands* O, const __nv_bfloat16* x, std::uint32_t E,
                                    float* prob, unsigned* error);
 __global__ void mlp_grad_kernel(const MlpParams* P, const MlpOperands* O, const __nv_bfloat16* x, const float* y,
-                                std::uint32_t E, float inv_count, MlpParams* partials, float* loss_partials);
+                                std::uint32_t E, float inv_count, MlpParams* partials, float* loss_partials,
+                                unsigned* error);
 __global__ void mlp_grad_reduce_kernel(const MlpParams* partials, const float* loss_partials, std::uint32_t blocks,
                                        MlpParams* grad, float* loss);
 __global__ void adam_kernel(MlpParams* P, const MlpParams* grad, MlpParams* m, MlpParams* v, float lr, float beta1,
