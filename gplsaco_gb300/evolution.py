@@ -15,13 +15,28 @@ engine (FacoBatchEngine.evaluate_population_evaluations).
 Programs are IR dicts of feature spec 3 (the engine's compact controller)
 or, with EvolutionSettings(feature_spec_id=2), of the reference's 12-feature
 controller.
+
+State and checkpoints follow the reference's rules
+(python/gp_faco/evolution.py:250-388, python/gp_faco/checkpoint.py:12-69):
+a state holds every individual's program, whether it is scored, its score
+(a failed program's +inf written as null) and the panel that scored it;
+restoring checks the state against the generation protocol (scores only
+from the current panel, the archived winner equal to the population's best,
+programs valid and inside the limits) and refuses it otherwise; checkpoint
+files are written atomically (a temporary file in the same directory,
+fsync, rename).  DEAP is not available here, so its operators are restated
+on the postfix IR rather than called: runs follow the reference's protocol,
+operator order and probabilities, not its random draws bit for bit.
 """
 from __future__ import annotations
 
+import json
 import math
+import os
 import random
 import struct
 from dataclasses import asdict, dataclass
+from pathlib import Path
 
 import numpy as np
 
@@ -291,27 +306,179 @@ class Evolution:
         return tuple(unique[k] for k in sorted(unique))
 
     def state_dict(self) -> dict:
+        """JSON-ready state (no NaN or infinity: a failed program's score is
+        written as null beside valid=True)."""
+        population = []
+        for tree, f in zip(self.population, self.fitness):
+            population.append({"program": to_ir(tree, self.settings.extended, self.settings.feature_spec_id),
+                               "valid": f is not None,
+                               "fitness": f if f is not None and math.isfinite(f) else None,
+                               "evaluated_panel": self.panel_id if f is not None else None})
         return {"version": 1, "settings": asdict(self.settings), "generation": self.generation,
                 "panel_id": self.panel_id, "winners": [dict(w) for w in self.winners],
                 "rng_state": self.rng.getstate(), "variation_counts": dict(self.variation_counts),
-                "population": [{"program": p, "fitness": f, "program_id": i}
-                               for p, f, i in zip(self.programs(), self.fitness, self.program_ids)]}
+                "population": population}
+
+    def _check_program(self, program) -> list:
+        """The program as a tree, or ValueError: the IR of this run's grammar
+        and feature spec, one tree, inside the depth and size limits."""
+        s = self.settings
+        keys = {"ir_version", "numeric_spec_id", "feature_spec_id", "opcode", "operand", "constant_bits"}
+        if type(program) is not dict or set(program) != keys:
+            raise ValueError("malformed program")
+        if (program["ir_version"] != 1 or program["numeric_spec_id"] != (2 if s.extended else 1)
+                or program["feature_spec_id"] != s.feature_spec_id):
+            raise ValueError("the program belongs to another grammar or feature spec")
+        opcode, operand, bits = program["opcode"], program["operand"], program["constant_bits"]
+        if (type(opcode) is not list or type(operand) is not list or type(bits) is not list
+                or len(opcode) != len(operand) or not opcode):
+            raise ValueError("malformed program")
+        depth, constants = 0, 0
+        for op, arg in zip(opcode, operand):
+            if type(op) is not int or type(arg) is not int:
+                raise ValueError("malformed program")
+            if op == 0:
+                if not 0 <= arg < FEATURES[s.feature_spec_id]:
+                    raise ValueError("feature operand out of range")
+                depth += 1
+            elif op == 1:
+                if arg != constants:
+                    raise ValueError("constants out of order")
+                constants += 1
+                depth += 1
+            elif op in self.ops:
+                if depth < self.ops[op]:
+                    raise ValueError("operator without operands")
+                depth += 1 - self.ops[op]
+            else:
+                raise ValueError("unknown opcode")
+        if depth != 1 or constants != len(bits) or any(type(b) is not int or not 0 <= b < 2**32 for b in bits):
+            raise ValueError("malformed program")
+        tree = from_ir(program)
+        if any(op == 1 and not math.isfinite(c) for op, c in tree):
+            raise ValueError("non-finite constant")
+        if self._over_limit(tree):
+            raise ValueError("the program exceeds the tree limits")
+        return tree
 
     @classmethod
     def from_state_dict(cls, state: dict) -> "Evolution":
-        if state.get("version") != 1:
-            raise ValueError("unknown evolution state version")
+        """Restores a state, refusing one that the generation protocol could
+        not have produced (the reference's checks,
+        python/gp_faco/evolution.py:274-385)."""
+        expected = {"version", "settings", "generation", "panel_id", "winners", "rng_state", "variation_counts",
+                    "population"}
+        if type(state) is not dict or set(state) != expected or state["version"] != 1:
+            raise ValueError("unknown evolution state structure")
         evo = cls(EvolutionSettings(**state["settings"]), 0)
-        evo.generation = state["generation"]
-        evo.panel_id = state["panel_id"]
-        evo.winners = [dict(w) for w in state["winners"]]
-        rng_state = state["rng_state"]
-        evo.rng.setstate((rng_state[0], tuple(rng_state[1]), rng_state[2]))
-        evo.variation_counts = dict(state["variation_counts"])
-        evo.population = [from_ir(item["program"]) for item in state["population"]]
-        evo.fitness = [item["fitness"] for item in state["population"]]
-        evo.program_ids = [item["program_id"] for item in state["population"]]
+        s = evo.settings
+        generation = state["generation"]
+        if type(generation) is not int or not 0 <= generation < s.generations:
+            raise ValueError("generation out of range")
+        evo.generation = generation
+        panel = state["panel_id"]
+        if panel is not None and (type(panel) is not str or not panel):
+            raise ValueError("invalid panel identity")
+        evo.panel_id = panel
+        items = state["population"]
+        if type(items) is not list or len(items) != s.population:
+            raise ValueError("population size differs from the settings")
+        for item in items:
+            if type(item) is not dict or set(item) != {"program", "valid", "fitness", "evaluated_panel"} \
+                    or type(item["valid"]) is not bool:
+                raise ValueError("malformed individual")
+            tree = evo._check_program(item["program"])
+            value = item["fitness"]
+            if item["valid"]:
+                if panel is None or item["evaluated_panel"] != panel:
+                    raise ValueError("a score from another panel")
+                if value is not None and (type(value) not in (int, float) or not math.isfinite(value)):
+                    raise ValueError("a score is finite or null (a failed program)")
+                fitness = math.inf if value is None else float(value)
+            else:
+                if value is not None or item["evaluated_panel"] is not None:
+                    raise ValueError("an unscored individual carries a score or a panel")
+                fitness = None
+            evo.population.append(tree)
+            evo.fitness.append(fitness)
+        evo.program_ids = [f"g{generation + 1:03d}-i{i + 1:03d}" for i in range(s.population)]
+        winners = state["winners"]
+        if type(winners) is not list or len(winners) not in (generation, generation + 1):
+            raise ValueError("winner count does not match the generation")
+        for index, w in enumerate(winners):
+            if (type(w) is not dict or set(w) != {"generation", "panel_id", "program", "fitness"}
+                    or w["generation"] != index or type(w["panel_id"]) is not str or not w["panel_id"]
+                    or (w["fitness"] is not None
+                        and (type(w["fitness"]) not in (int, float) or not math.isfinite(w["fitness"])))):
+                raise ValueError("malformed winner record")
+            evo._check_program(w["program"])
+        if len(winners) == generation + 1:
+            if panel is None or any(f is None for f in evo.fitness):
+                raise ValueError("a winner archived before the whole generation was scored")
+            best = min(range(s.population), key=evo._rank)
+            best_fitness = evo.fitness[best]
+            if (winners[-1]["panel_id"] != panel
+                    or _key(from_ir(winners[-1]["program"])) != _key(evo.population[best])
+                    or winners[-1]["fitness"] != (best_fitness if math.isfinite(best_fitness) else None)):
+                raise ValueError("the current winner is not the population's best")
+        evo.winners = [dict(w) for w in winners]
+        counts = state["variation_counts"]
+        if (type(counts) is not dict or set(counts) != set(evo.variation_counts)
+                or any(type(v) is not int or v < 0 for v in counts.values())):
+            raise ValueError("invalid variation counts")
+        evo.variation_counts = dict(counts)
+        evo.rng.setstate(_tuples(state["rng_state"]))
         return evo
+
+
+def _tuples(value):
+    return tuple(_tuples(v) for v in value) if isinstance(value, (list, tuple)) else value
+
+
+def _unique_pairs(pairs):
+    out = {}
+    for key, item in pairs:
+        if key in out:
+            raise ValueError("duplicate key in the checkpoint")
+        out[key] = item
+    return out
+
+
+def save_checkpoint(path, state: dict) -> None:
+    """Writes {"checkpoint_version": 2, "state": state} as JSON, atomically:
+    a temporary file in the target's directory, flushed and fsynced, renamed
+    over the target, then the directory fsynced.  A failure leaves the old
+    file as it was and no temporary file behind."""
+    if type(state) is not dict:
+        raise ValueError("a checkpoint state is a JSON object")
+    normalized = json.loads(json.dumps(state, allow_nan=False), object_pairs_hook=_unique_pairs)
+    payload = json.dumps({"checkpoint_version": 2, "state": normalized}, sort_keys=True, separators=(",", ":"),
+                         allow_nan=False) + "\n"
+    target = Path(path).resolve()
+    target.parent.mkdir(parents=True, exist_ok=True)
+    temporary = target.with_name(f".{target.name}.{os.getpid()}.{os.urandom(8).hex()}.partial")
+    try:
+        with temporary.open("x", encoding="utf-8") as stream:
+            stream.write(payload)
+            stream.flush()
+            os.fsync(stream.fileno())
+        os.replace(temporary, target)
+        directory = os.open(target.parent, os.O_RDONLY | os.O_DIRECTORY)
+        try:
+            os.fsync(directory)
+        finally:
+            os.close(directory)
+    finally:
+        temporary.unlink(missing_ok=True)
+
+
+def load_checkpoint(path) -> dict:
+    """The state of a checkpoint file written by save_checkpoint."""
+    envelope = json.loads(Path(path).read_text(encoding="utf-8"), object_pairs_hook=_unique_pairs)
+    if (type(envelope) is not dict or set(envelope) != {"checkpoint_version", "state"}
+            or envelope["checkpoint_version"] != 2 or type(envelope["state"]) is not dict):
+        raise ValueError("unknown checkpoint structure")
+    return envelope["state"]
 
 
 def panel_fitness(result: dict, references: np.ndarray) -> float:
