@@ -8,7 +8,9 @@ Pipeline (all GPU work through the engine's C ABI):
  3. on the evaluation instances: a long plain run's best as the reference
     length per instance; then plain FACO and learned-prior FACO are each run
     in chunks of iterations, recording the mean gap over instances against
-    wall-clock; the prior is disabled per instance (plain fallback) when,
+    wall-clock (the first iteration at or below a target is taken exactly
+    from the per-iteration trace, its time interpolated within its chunk);
+    the prior is disabled per instance (plain fallback) when,
     after the warm-up, it trails the plain colony at the same iteration.
     The plain warm-up iterations the fallback decision needs are charged to
     the prior method's clock.
@@ -33,7 +35,7 @@ class GapConfig:
     retention: float = 0.98
     mne: int = 8
     follow: int = 0                 # parent-following steps in batches: 0 auto, 1 off, 2 on
-    chunk: int = 10                 # iterations between cost reads
+    chunk: int = 10                 # iterations between cost and clock reads
     iterations: int = 400           # budget of the validation (tuning) runs
     budget: int = 2000              # budget of the evaluation runs, per method
     reference_iterations: int = 3000
@@ -66,6 +68,8 @@ class GapConfig:
                         ("geometry", 0.05, 2, 0, 5, True), ("geometry", 0.05, 1, 0, 5, True),
                         ("full", 0.05, 2, 10, 5, True), ("full", 0.05, 2, 10, 6, True))
     train_pool: int = 32
+    train_n: tuple = (500, 1000)    # training instance sizes, uniform in this range
+    train_colonies: int = 2         # colonies (seeds) per training instance, each a labelled copy of its rows
     train_snapshot: int = 25
     train_iterations: int = 300
     epochs: int = 12
@@ -99,14 +103,15 @@ def collect_training_data(cfg: GapConfig, device: int = 0):
     pool = []
     for i in range(cfg.train_pool):
         rng = np.random.default_rng(500 + i)
-        n = int(rng.integers(500, 1001))
+        n = int(rng.integers(cfg.train_n[0], cfg.train_n[1] + 1))
         pool.append(_xy("clustered" if i % 4 else "uniform", n, 500 + i))
     dim = max(len(p) for p in pool)
-    engine = FacoBatchEngine(dim, 2 * len(pool), _settings(cfg), device=device)
+    copies = cfg.train_colonies
+    engine = FacoBatchEngine(dim, copies * len(pool), _settings(cfg), device=device)
     for i, xy in enumerate(pool):
         engine.register_problem(1 + i, xy.astype(np.float64))
-    keys = np.repeat(np.arange(1, len(pool) + 1, dtype=np.uint64), 2)
-    seeds = np.tile(np.array([11, 12], np.uint64), len(pool))
+    keys = np.repeat(np.arange(1, len(pool) + 1, dtype=np.uint64), copies)
+    seeds = np.tile(np.arange(11, 11 + copies, dtype=np.uint64), len(pool))
     engine.begin(keys, seeds, cfg.mne)
     engine.step(cfg.train_snapshot)
     x, _ = engine.edge_data(features=True, labels=False)
@@ -147,14 +152,14 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     seeds = np.ones(len(xys), np.uint64)
     rows = []
     enabled = np.ones(len(xys), np.uint8)
-    engine.begin(keys, seeds, cfg.mne if mne is None else mne)
+    budget = cfg.iterations if iterations is None else iterations
+    engine.begin(keys, seeds, cfg.mne if mne is None else mne, trace_iterations=budget)
     costs, _ = engine.current_costs(len(xys))
     t0 = time.perf_counter()
     if params is not None:
         engine.prior_set(params, enabled, floor, gamma, departures)
     rows.append((0, 0.0, float(np.mean((costs - refs) / refs)), costs.copy()))
     done = 0
-    budget = cfg.iterations if iterations is None else iterations
     while done < budget:
         step = min(chunk, cfg.warmup - done) if done < cfg.warmup else chunk
         engine.step(step)
@@ -174,7 +179,7 @@ def gap_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, plain_warm
     work = {"construction_steps": res["construction_steps"] / ant_iterations,
             "ls_evaluations": res["ls_evaluations"] / ant_iterations,
             "ms_per_iteration": 1e3 * rows[-1][1] / done}
-    return rows, enabled, work
+    return Rows(rows, per_iteration_gaps(res["trace"]["global_cost"], refs)), enabled, work
 
 
 # masked in the geometry model: x4 trail level, x5 best-tour membership
@@ -214,7 +219,8 @@ def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: i
     keys = np.repeat(np.arange(1, len(xys) + 1, dtype=np.uint64), 2)
     seeds = np.tile(np.array([1, 2], np.uint64), len(xys))
     plain_mne = cfg.mne if mne is None else mne
-    engine.begin(keys, seeds, plain_mne)
+    budget = cfg.iterations if iterations is None else iterations
+    engine.begin(keys, seeds, plain_mne, trace_iterations=budget)
     if params is not None and prior_mne is not None and prior_mne != plain_mne:
         engine.set_mne_targets(np.tile(np.array([plain_mne, prior_mne], np.uint32), len(xys)))
     costs, _ = engine.current_costs(count)
@@ -229,7 +235,6 @@ def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: i
     rows = [row(0, costs)]
     rows[0] = (0, 0.0) + rows[0][2:]
     done = 0
-    budget = cfg.iterations if iterations is None else iterations
     while done < budget:
         engine.step(chunk)
         done += chunk
@@ -243,10 +248,45 @@ def pair_run(cfg: GapConfig, xys: list, refs: np.ndarray, params=None, device: i
     work = {"construction_steps": res["construction_steps"] / ant_iterations,
             "ls_evaluations": res["ls_evaluations"] / ant_iterations,
             "ms_per_iteration": 1e3 * rows[-1][1] / done}
-    return rows, work
+    best = res["trace"]["global_cost"].reshape(-1, len(xys), 2).min(axis=2)
+    return Rows(rows, per_iteration_gaps(best, refs)), work
+
+
+class Rows(list):
+    """The rows (iteration, seconds, mean gap, costs) read every chunk of
+    iterations, with the mean gap after every single iteration (`gaps[i]`
+    after i + 1 iterations, from the colonies' per-iteration trace)."""
+
+    def __init__(self, rows, gaps):
+        super().__init__(rows)
+        self.gaps = gaps
+
+
+def per_iteration_gaps(best_costs, refs) -> np.ndarray:
+    """Mean gap over instances after each iteration; best_costs[i, j] is
+    instance j's best length after i + 1 iterations."""
+    best = np.asarray(best_costs, np.float64)
+    return np.mean((best - refs[None, :]) / refs[None, :], axis=1)
 
 
 def first_time_below(rows, target: float, extra_seconds: float = 0.0):
+    """Seconds and iterations to the first iteration whose mean gap is at
+    or below the target.  The iteration is exact (the per-iteration
+    trace); its time is interpolated linearly between the clock readings
+    of the chunk it falls in, the iterations of one chunk being alike.
+    Without a trace, the first chunk reading at or below the target."""
+    gaps = getattr(rows, "gaps", None)
+    if gaps is not None:
+        if rows[0][2] <= target:
+            return rows[0][1] + extra_seconds, 0
+        hit = np.nonzero(gaps <= target)[0]
+        if hit.size == 0:
+            return None, None
+        it = int(hit[0]) + 1
+        for (i0, t0, _, _), (i1, t1, _, _) in zip(rows, rows[1:]):
+            if i0 < it <= i1:
+                return t0 + (t1 - t0) * (it - i0) / (i1 - i0) + extra_seconds, it
+        return None, None
     for it, sec, gap, _ in rows:
         if gap <= target:
             return sec + extra_seconds, it
@@ -374,6 +414,8 @@ def summary(res: dict) -> dict:
         "instances": res["instances"], "budget_iterations": res.get("budget_iterations"),
         "prior_setting": res["prior_setting"], "plain_setting": res["plain_setting"],
         "gap_at": pair["gap_at"], "total_seconds": res["total_seconds"],
+        "crossing": "the first iteration at or below the target gap, exact from the colonies' per-iteration "
+                    "trace; its time interpolated between the clock readings around it (every 10 iterations)",
     }
 
 
