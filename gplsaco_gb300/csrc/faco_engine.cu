@@ -35,6 +35,11 @@ thread_local std::string g_error;
 // Iterations captured per CUDA graph (replayed until the budget is spent).
 constexpr std::uint32_t kGraphIterations = 16;
 // Automatic chain count: one chain per kColoniesPerChain colonies, at most kMaxChains.
+// Trail updates of more than 2 x kTrailCellsPerBlock entries per colony run in
+// colony_trails_kernel, one block per kTrailCellsPerBlock entries (at most
+// kMaxTrailBlocks per colony).
+constexpr std::uint64_t kTrailCellsPerBlock = 16384;
+constexpr std::uint64_t kMaxTrailBlocks = 64;
 constexpr std::uint32_t kColoniesPerChain = 16;
 constexpr std::uint32_t kMaxChains = 8;
 
@@ -614,6 +619,9 @@ void enqueue_update(faco_engine* e, cudaStream_t st, const std::uint32_t* list, 
     faco::colony_update_kernel<<<colonies, 256, 0, st>>>(e->d_instances.get(), e->colonies.get(), e->states.get(),
                                                           v.P, v.trace_cap ? e->trace.get() : nullptr, list,
                                                           v.count, v.trace_cap);
+    if (v.P.trail_blocks > 1)
+        faco::colony_trails_kernel<<<dim3(v.P.trail_blocks, colonies), 256, 0, st>>>(
+            e->d_instances.get(), e->colonies.get(), e->states.get(), v.P, list);
     cuda_check(cudaGetLastError(), "update launch");
 }
 
@@ -1084,6 +1092,17 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
                                             e->decision_actions.get()};
     }
     v.P.p_root = std::pow(e->settings.p_best, 1.0 / static_cast<double>(k_common));
+    // large candidate matrices: the trail update in a kernel of its own with
+    // one block per kTrailCellsPerBlock entries of the largest colony (the
+    // controllers read the updated trails inside the colony update, so
+    // controlled evaluations keep it there)
+    {
+        const std::uint64_t cells = static_cast<std::uint64_t>(n_max) * k_common;
+        v.P.trail_blocks = !v.P.controlled && !v.P.ref_control && cells >= 2 * kTrailCellsPerBlock
+                               ? static_cast<std::uint32_t>(std::min<std::uint64_t>(
+                                     kMaxTrailBlocks, (cells + kTrailCellsPerBlock - 1) / kTrailCellsPerBlock))
+                               : 0u;
+    }
     v.L = faco::AntLaunch{};
     v.L.instances = e->d_instances.get();
     v.L.colonies = e->colonies.get();
@@ -1552,7 +1571,7 @@ int faco_get_launch_plan(faco_engine* e, faco_launch_plan* plan) {
         std::unique_lock<std::mutex> lock(e->busy, std::try_to_lock);
         if (!lock.owns_lock()) throw Error(FACO_EBUSY, "engine is busy with another call");
         const auto& v = e->eval;
-        const std::uint32_t per_update = v.P.ref_control ? 2u : 1u;   // fingerprints + update
+        const std::uint32_t per_update = (v.P.ref_control ? 2u : 1u) + (v.P.trail_blocks > 1 ? 1u : 0u);   // fingerprints + update + trails
         const auto chains = static_cast<std::uint32_t>(v.chains.size());
         plan->size_classes = static_cast<std::uint32_t>(v.classes.size());
         plan->chains = chains;

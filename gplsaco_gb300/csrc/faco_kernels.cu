@@ -534,9 +534,9 @@ __device__ __forceinline__ void trail_update(std::uint32_t n, std::uint32_t k, c
 // plain ant does, and the prior only decides where it goes.  Rows over
 // [first, n) with the given stride; trails are already updated.
 __device__ __forceinline__ void departure_rows(const InstanceView& in, const ColonyView& cv, std::uint32_t first,
-                                               std::uint32_t stride) {
-    const std::uint32_t n = in.n, k = in.k;
-    for (std::uint32_t i = first; i < n; i += stride) {
+                                               std::uint32_t stride, std::uint32_t end) {
+    const std::uint32_t k = in.k;
+    for (std::uint32_t i = first; i < end; i += stride) {
         const std::uint32_t nb = cv.parent_nbr[i], succ = nb & 0xffffu, pred = nb >> 16;
         const std::size_t row = (std::size_t)i * k;
         float plain = 0.0f, prior = 0.0f;
@@ -1275,7 +1275,8 @@ __global__ void __launch_bounds__(256) prior_rows_kernel(const InstanceView* ins
     const std::uint32_t c = blockIdx.x;
     if (!modes[c]) return;
     const ColonyView cv = colonies[c];
-    departure_rows(instances[cv.instance], cv, threadIdx.x, blockDim.x);
+    const InstanceView in = instances[cv.instance];
+    departure_rows(in, cv, threadIdx.x, blockDim.x, in.n);
 }
 
 // Fingerprints (and node-0 positions) of every ant's tour of a batch, one
@@ -1476,11 +1477,13 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
         cv.parent_nbr[cv.parent[i]] = (std::uint32_t)cv.parent[i + 1 == n ? 0 : i + 1] |
                                       ((std::uint32_t)cv.parent[i == 0 ? n - 1 : i - 1] << 16);
     __syncthreads();
-    trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, cv.eta, cv.trails,
-                 cv.products, threadIdx.x, blockDim.x);
-    if (P.prior_rows && P.prior_rows[c]) {
-        __syncthreads();
-        departure_rows(in, cv, threadIdx.x, blockDim.x);
+    if (P.trail_blocks <= 1) {
+        trail_update(n, k, in.primary, cv.parent_nbr, P.retention_f, s_tmin, s_tmax, s_inc, cv.eta, cv.trails,
+                     cv.products, threadIdx.x, blockDim.x);
+        if (P.prior_rows && P.prior_rows[c]) {
+            __syncthreads();
+            departure_rows(in, cv, threadIdx.x, blockDim.x, n);
+        }
     }
     std::int32_t action = -1;
     if (P.ref_control) {
@@ -1574,6 +1577,35 @@ __global__ void __launch_bounds__(256) colony_update_kernel(const InstanceView* 
             write_trace(trace[(size_t)st.iteration * colony_count + c], st, s_used_mne, action, s_steps, s_evals);
         ++st.iteration;
         states[c] = st;
+    }
+}
+
+// The trail update of large candidate matrices, after the colony update has
+// chosen the parent and the trail limits (it leaves the trails alone when
+// P.trail_blocks > 1): block (x, y) updates rows [n x / X, n (x+1) / X) of
+// colony y of the launch (of `list`, or all when null) -- evaporation,
+// deposit on the parent's edges, bounds and products exactly as the colony
+// update would -- then, for a colony whose prior re-ranks departures, those
+// rows' products.  One block per colony streams a large matrix at a small
+// fraction of the memory bandwidth; X blocks per colony fill the GPU.
+__global__ void __launch_bounds__(256) colony_trails_kernel(const InstanceView* instances,
+                                                            const ColonyView* colonies, const ColonyState* states,
+                                                            ColonyParams P, const std::uint32_t* list) {
+    const std::uint32_t c = list ? list[blockIdx.y] : blockIdx.y;
+    const ColonyView cv = colonies[c];
+    const InstanceView in = instances[cv.instance];
+    const std::uint32_t n = in.n, k = in.k;
+    const std::uint32_t r0 = (std::uint32_t)((unsigned long long)n * blockIdx.x / gridDim.x);
+    const std::uint32_t r1 = (std::uint32_t)((unsigned long long)n * (blockIdx.x + 1) / gridDim.x);
+    if (r0 >= r1) return;
+    const ColonyState& st = states[c];
+    const float tmin = st.tau_min, tmax = st.tau_max, inc = (float)(1.0 / (double)st.parent_cost);
+    const std::size_t off = (std::size_t)r0 * k;
+    trail_update(r1 - r0, k, in.primary + off, cv.parent_nbr + r0, P.retention_f, tmin, tmax, inc, cv.eta + off,
+                 cv.trails + off, cv.products + off, threadIdx.x, blockDim.x);
+    if (P.prior_rows && P.prior_rows[c]) {
+        __syncthreads();
+        departure_rows(in, cv, r0 + threadIdx.x, blockDim.x, r1);
     }
 }
 

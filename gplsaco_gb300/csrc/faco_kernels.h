@@ -29,6 +29,8 @@ struct ColonyParams {
     unsigned long long ls_limit;     // LS evaluation budget per ant (LS-work feedback)
     DecisionCapture capture;         // decisions to record (count 0: none)
     const std::uint32_t* prior_rows; // per colony: 1 = the prior re-ranks departures only (device; may be null)
+    std::uint32_t trail_blocks;      // > 1: colony_trails_kernel updates the trails with this many blocks per
+                                     // colony, after the colony update (uncontrolled evaluations only)
 };
 
 // Candidate rows of registration on the GPU (faco_knn.cu): per node its
@@ -54,6 +56,8 @@ __global__ void colony_update_kernel(const InstanceView* instances, const Colony
                                      ColonyState* states, ColonyParams P, TraceRow* trace,
                                      const std::uint32_t* list, std::uint32_t colony_count,
                                      std::uint32_t trace_cap);
+__global__ void colony_trails_kernel(const InstanceView* instances, const ColonyView* colonies,
+                                     const ColonyState* states, ColonyParams P, const std::uint32_t* list);
 __global__ void pheromone_step_kernel(std::uint32_t n, std::uint32_t k, const node_t* primary,
                                       const std::uint32_t* parent_nbr, float ret, float tmin, float tmax, float inc,
                                       const float* eta, float* trails, float* products);

@@ -149,7 +149,8 @@ def _settings(api, ants, k=16, b=64, w=20, retention=0.98, epoch=0.01, ls_limit=
     (7, 4, 8, 0, 0, 0), (17, 8, 8, 1, 0, 0), (100, 32, 20, 2, 0, 0), (500, 16, 6, 3, 0, 0), (1000, 32, 4, 0, 0, 0),
     (17, 8, 8, 1, 1, 0), (100, 32, 20, 2, 1, 0), (1000, 32, 4, 0, 1, 0),
     (7, 4, 8, 0, 0, 2), (100, 32, 20, 2, 0, 2), (500, 16, 6, 3, 1, 2), (1000, 32, 4, 0, 0, 2),
-    (1000, 16, 40, 3, 0, 0), (2600, 8, 3, 3, 0, 0), (2600, 8, 3, 1, 1, 2)])
+    (1000, 16, 40, 3, 0, 0), (2600, 8, 3, 3, 0, 0), (2600, 8, 3, 1, 1, 2), (2600, 8, 4, 0, 0, 0),
+    (2600, 8, 4, 2, 1, 2)])
 @pytest.mark.parametrize("follow", [1, 2])
 def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls_mode, workspace, follow):
     """Whole plain-FACO runs: registration rows and initial tour, every
@@ -157,8 +158,10 @@ def test_engine_run_matches_oracle(api, oracle, n, ants, iterations, variant, ls
     tour and the FP32 trails agree bit-for-bit with the oracle -- with the
     ants' tours in shared memory and in the global-memory workspace, and
     with the relocations deferred into runs (long walks once trails
-    converge; every relocation above 2048 nodes), and with the steps along
-    the parent tour taken one at a time and in batches (follow 1 / 2)."""
+    converge; every relocation above 2048 nodes), with the steps along
+    the parent tour taken one at a time and in batches (follow 1 / 2), and
+    with the trail update of a large matrix (N=2600, k=16) spread over
+    several blocks per colony."""
     k = 2 if variant % 2 else 16
     b = 1 if variant % 2 else 64
     retention = (0.25, 0.5, 0.75, 0.98)[variant]

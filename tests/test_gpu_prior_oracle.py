@@ -96,12 +96,15 @@ def test_prior_rows_match_oracle(api, oracle, gamma, floor, departures):
 
 
 @pytest.mark.parametrize("n,gamma,floor,departures,ls_mode", [(200, 2, 0.05, False, 0), (200, 1, 0.5, True, 0),
-                                                               (537, 2, 0.05, False, 1), (1000, 2, 0.2, True, 0)])
+                                                               (537, 2, 0.05, False, 1), (1000, 2, 0.2, True, 0),
+                                                               (2300, 2, 0.05, True, 0)])
 def test_prior_colony_runs_match_oracle(api, oracle, n, gamma, floor, departures, ls_mode):
     """Whole prior-enabled colony runs: the colonies with the prior (and the
     one without, in the same evaluation) give the oracle's tours, lengths
     and every iteration's trace row bit for bit; so does a run whose prior
-    is refreshed mid-run and then disabled by the per-instance fallback."""
+    is refreshed mid-run and then disabled by the per-instance fallback.
+    At N=2300 the trail update and departure rows run in several blocks
+    per colony."""
     g, prior = api
     k, ants, iterations = 16, 8, 14
     xy = _cases.uniform_instance(n, seed=40 + n)
