@@ -10,9 +10,11 @@
 namespace faco {
 
 // Ants (warps) per block of the ant kernel, and the resident blocks per SM the
-// register budget is sized for (6 x 4 warps x 85 registers fills the file).
+// register budget is sized for (6 x 4 warps x 85 registers fills the file;
+// the variants use 72-80 registers without spills, where 8 blocks per SM
+// forced 64 registers and spills, and ran slower on every workload).
 constexpr std::uint32_t kMaxWarpsPerBlock = 4;
-constexpr std::uint32_t kAntBlocksPerSM = 8;
+constexpr std::uint32_t kAntBlocksPerSM = 6;
 
 struct ColonyParams {
     std::uint32_t ants;
