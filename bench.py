@@ -63,12 +63,12 @@ ITERATIONS_PER_STEP = 16  # a step: one replay of the engine's per-evaluation CU
 # kernel's smsp__issue_active and smsp__inst_executed (341.6 M over 8,192
 # ant-tours).  Reported for the default workload only.
 THROUGHPUT_CAPTURE = {
-    "traffic_bytes_per_step": 16 * (21_479_936 + 34_203_904),
+    "traffic_bytes_per_step": 16 * (21_403_136 + 30_208 + 34_198_528 + 22_528),
     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of ant_kernel and colony_update_kernel, "
                        "one unchained launch each over every colony at iteration 160 of this panel, x 16 "
                        "iterations per step"),
-    "ant_issue_active_pct": 61.72,
-    "ant_warp_instructions_per_ant_tour": 341_637_677 / 8192,
+    "ant_issue_active_pct": 61.36,
+    "ant_warp_instructions_per_ant_tour": 335_252_667 / 8192,
     "issue_source": ("ncu smsp__issue_active.avg.pct_of_peak_sustained_active and smsp__inst_executed.sum of "
                      "the whole-panel ant launch at iteration 160 of this panel"),
 }
