@@ -358,7 +358,7 @@ __device__ inline std::uint32_t follow_batch(const AntSmem& s, const int2* xy, c
     // caller's layout, which it reuses afterwards)
     const std::uint32_t base = r.steps + 1;
     if (base != draw_base) {
-        const uint4v rb = philox4x32(base + lane, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
+        const uint4v rb = philox4x32_rolled(base + lane, ant, batch, 0, (std::uint32_t)key, (std::uint32_t)(key >> 32));
         draw_base = base;
         draw_hi = rb.x;
         draw_lo = rb.y;
@@ -482,11 +482,26 @@ __device__ inline std::uint32_t follow_batch(const AntSmem& s, const int2* xy, c
         // six-edge delta of CpuTour::relocate for this lane's step, its
         // positions and tour neighbours read through the run with m = mr
         const std::uint32_t tpos = v.current_pos(), npos = v.source_pos(D);
-        const std::uint32_t target_after = v.read(s, tpos + 1 == n ? 0 : tpos + 1);
-        const std::uint32_t previous = v.read(s, npos == 0 ? n - 1 : npos - 1);
-        const std::uint32_t after = v.read(s, npos + 1 == n ? 0 : npos + 1);
-        d = (long long)euc2d(xy[previous], xy[after]) + euc2d(xy[cur], xy[sel]) + euc2d(xy[sel], xy[target_after]) -
-            euc2d(xy[previous], xy[sel]) - euc2d(xy[sel], xy[after]) - euc2d(xy[cur], xy[target_after]);
+        std::uint32_t target_after = n, previous = n, after = n;
+#pragma unroll 1
+        for (int t = 0; t < 3; ++t) {   // one copy of the run's read in the code
+            const std::uint32_t at = t == 0 ? (tpos + 1 == n ? 0 : tpos + 1)
+                                   : t == 1 ? (npos == 0 ? n - 1 : npos - 1) : (npos + 1 == n ? 0 : npos + 1);
+            const std::uint32_t x = v.read(s, at);
+            if (t == 0) target_after = x;
+            else if (t == 1) previous = x;
+            else after = x;
+        }
+        // added (previous,after) (cur,sel) (sel,target_after), removed
+        // (previous,sel) (sel,after) (cur,target_after): one loop, so that
+        // the batch's code holds one copy of the distance
+#pragma unroll 1
+        for (int t = 0; t < 6; ++t) {
+            const std::uint32_t ea = t == 0 || t == 3 ? previous : t == 2 || t == 4 ? sel : cur;
+            const std::uint32_t eb = t == 0 || t == 4 ? after : t == 1 || t == 3 ? sel : target_after;
+            const int dd = euc2d(xy[ea], xy[eb]);
+            d += t < 3 ? dd : -dd;
+        }
         moved = tpos < npos ? npos - tpos : tpos - npos + 1;
     }
     if (taken) atomicOr(&s.visited[sel >> 5], 1u << (sel & 31u));

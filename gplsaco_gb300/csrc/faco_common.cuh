@@ -64,6 +64,20 @@ __device__ __forceinline__ uint4v philox4x32(std::uint32_t c0, std::uint32_t c1,
     return {c0, c1, c2, c3};
 }
 
+// The same generator with its rounds in a loop: fewer instructions in the
+// code, for call sites where code size matters more than the loop overhead.
+__device__ __forceinline__ uint4v philox4x32_rolled(std::uint32_t c0, std::uint32_t c1, std::uint32_t c2,
+                                                    std::uint32_t c3, std::uint32_t k0, std::uint32_t k1) {
+#pragma unroll 1
+    for (int round = 0; round < 10; ++round) {
+        const std::uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const std::uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        c0 = hi1 ^ c1 ^ k0; c1 = lo1; c2 = hi0 ^ c3 ^ k1; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    return {c0, c1, c2, c3};
+}
+
 __device__ __forceinline__ double u53(std::uint32_t hi, std::uint32_t lo) {
     return (double)(((((unsigned long long)hi) << 32) | lo) >> 11) * 0x1.0p-53;
 }

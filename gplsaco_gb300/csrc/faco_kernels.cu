@@ -318,8 +318,20 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
                     if (target_after == selected) run_dir = 0;
                 }
                 if (run_dir) {
-                    previous = run.read(s, npos == 0 ? n - 1 : npos - 1);
-                    after = run.read(s, npos + 1 == n ? 0 : npos + 1);
+                    if constexpr (kFollow) {
+                        // the batched-step variants are bound by instruction
+                        // fetch: one copy of the run's read in their code
+#pragma unroll 1
+                        for (int t = 0; t < 2; ++t) {
+                            const std::uint32_t x = run.read(s, t == 0 ? (npos == 0 ? n - 1 : npos - 1)
+                                                                       : (npos + 1 == n ? 0 : npos + 1));
+                            if (t == 0) previous = x;
+                            else after = x;
+                        }
+                    } else {
+                        previous = run.read(s, npos == 0 ? n - 1 : npos - 1);
+                        after = run.read(s, npos + 1 == n ? 0 : npos + 1);
+                    }
                 } else {
                     run.apply(s, lane, current);
                     npos = s.pos[selected];
