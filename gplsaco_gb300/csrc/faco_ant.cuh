@@ -577,6 +577,9 @@ __device__ __forceinline__ LsRow pop_with_row(const AntSmem& s, Checklist& q, st
 
 // Checklist 2-opt, best gain per popped node, reference tie/cap rules
 // (cpp/src/faco_cpu.cpp:148-217; cuda/faco_device.cuh:295-478).
+// kCompact (the batched-step variants, bound by instruction fetch): the four
+// pushes of a move through one copy of push_absent.
+template <bool kCompact = false>
 __device__ __forceinline__ void checklist_two_opt(const AntSmem& s, const int2* xy, const InstanceView& in,
                                                   std::uint32_t n, std::uint32_t lane, Checklist& q,
                                                   unsigned long long cap, AntResult& r, long long& gain_sum,
@@ -635,10 +638,17 @@ __device__ __forceinline__ void checklist_two_opt(const AntSmem& s, const int2* 
             if (kind == 0) { m0 = an; m1 = nbj; m2 = a; m3 = bj; }
             else { m0 = a; m1 = bj; m2 = ap; m3 = nbj; }
             r.moved += flip(s, n, lane, m0, m1);
-            r.reactivations += push_absent(s, q, n, m0, lane, log, log_cap);
-            r.reactivations += push_absent(s, q, n, m1, lane, log, log_cap);
-            r.reactivations += push_absent(s, q, n, m2, lane, log, log_cap);
-            r.reactivations += push_absent(s, q, n, m3, lane, log, log_cap);
+            if constexpr (kCompact) {
+#pragma unroll 1
+                for (int t = 0; t < 4; ++t)
+                    r.reactivations += push_absent(s, q, n, t == 0 ? m0 : t == 1 ? m1 : t == 2 ? m2 : m3, lane, log,
+                                                   log_cap);
+            } else {
+                r.reactivations += push_absent(s, q, n, m0, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, m1, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, m2, lane, log, log_cap);
+                r.reactivations += push_absent(s, q, n, m3, lane, log, log_cap);
+            }
             ++r.accepted;
             gain_sum -= best;
         }

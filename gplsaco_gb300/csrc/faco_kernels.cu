@@ -382,9 +382,15 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
             const bool new_edge = (pnbr & 0xffffu) != selected && (pnbr >> 16) != selected;
             if (new_edge) {
                 ++r.mne;
-                push_absent(s, q, n, current, lane, log, log_cap);
-                push_absent(s, q, n, selected, lane, log, log_cap);
-                push_absent(s, q, n, previous, lane, log, log_cap);
+                if constexpr (kFollow) {
+#pragma unroll 1
+                    for (int t = 0; t < 3; ++t)
+                        push_absent(s, q, n, t == 0 ? current : t == 1 ? selected : previous, lane, log, log_cap);
+                } else {
+                    push_absent(s, q, n, current, lane, log, log_cap);
+                    push_absent(s, q, n, selected, lane, log, log_cap);
+                    push_absent(s, q, n, previous, lane, log, log_cap);
+                }
             }
             current = selected;
             __syncwarp();
@@ -398,7 +404,7 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
     // ---------------- local search ----------------
     long long gain_sum = 0;
     if (L.ls_mode == 1) checklist_ls_first(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
-    else checklist_two_opt(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
+    else checklist_two_opt<kFollow>(s, xy, in, n, lane, q, L.ls_limit, r, gain_sum, log, log_cap);
     r.final_cost = cost + gain_sum;
     r.checklist = q.pushed;
     if (log && q.pushed > log_cap && lane == 0) atomicOr(L.error, kErrQueueOverflow);
