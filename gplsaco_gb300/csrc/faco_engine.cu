@@ -34,6 +34,16 @@ thread_local std::string g_error;
 
 // Iterations captured per CUDA graph (replayed until the budget is spent).
 constexpr std::uint32_t kGraphIterations = 16;
+// Batched steps chosen per stretch of iterations (FACO_FOLLOW_AUTO on panels
+// beyond one wave of ant warps): every kAdaptIterations iterations the
+// colonies' step counters are read back, and the following replays take the
+// batched-step graph once the stretch averaged at least kBatchOnSteps
+// construction steps per ant and iteration, the one-step graph again below
+// kBatchOffSteps.  Measured on the N=1000 throughput panel: batches lose up
+// to 1.9x on the short walks of early iterations (11-30 steps), break even
+// near 70 and win 19-26 % from 110 steps on.
+constexpr std::uint32_t kAdaptIterations = 64;
+constexpr double kBatchOnSteps = 72.0, kBatchOffSteps = 60.0;
 // Automatic chain count: one chain per kColoniesPerChain colonies, at most kMaxChains.
 // Trail updates of more than 2 x kTrailCellsPerBlock entries per colony run in
 // colony_trails_kernel, one block per kTrailCellsPerBlock entries (at most
@@ -324,6 +334,15 @@ struct faco_engine {
         faco::AntLaunch L{};
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
+        // batched steps chosen per stretch of iterations: the batched-step
+        // graph beside the one-step one, the variant of the next replays and
+        // the step counters at the last reading
+        bool adaptive = false, batched = false;
+        cudaGraph_t graph_batched = nullptr;
+        cudaGraphExec_t exec_batched = nullptr;
+        unsigned long long steps_seen = 0;
+        std::uint32_t done_seen = 0;
+        bool rebase = false;                    // the next reading only sets the baseline (restored runs)
     } eval;
     std::vector<cudaStream_t> branch_streams;
     std::vector<cudaEvent_t> branch_events;   // [0] fork, [1 + i] join of branch i
@@ -334,6 +353,8 @@ struct faco_engine {
     ~faco_engine() {
         if (eval.exec) cudaGraphExecDestroy(eval.exec);
         if (eval.graph) cudaGraphDestroy(eval.graph);
+        if (eval.exec_batched) cudaGraphExecDestroy(eval.exec_batched);
+        if (eval.graph_batched) cudaGraphDestroy(eval.graph_batched);
         for (auto st : branch_streams) cudaStreamDestroy(st);
         for (auto ev : branch_events) cudaEventDestroy(ev);
         if (stream) {
@@ -586,8 +607,12 @@ namespace {
 void destroy_graph(faco_engine* e) {
     if (e->eval.exec) cudaGraphExecDestroy(e->eval.exec);
     if (e->eval.graph) cudaGraphDestroy(e->eval.graph);
+    if (e->eval.exec_batched) cudaGraphExecDestroy(e->eval.exec_batched);
+    if (e->eval.graph_batched) cudaGraphDestroy(e->eval.graph_batched);
     e->eval.exec = nullptr;
     e->eval.graph = nullptr;
+    e->eval.exec_batched = nullptr;
+    e->eval.graph_batched = nullptr;
 }
 
 // All ant launches of one iteration: class 0 on `st`, the others on branch
@@ -680,9 +705,7 @@ void enqueue_iterations(faco_engine* e, cudaStream_t st, std::uint32_t iteration
 // The evaluation's graph: kGraphIterations iterations, replayed.  A failed
 // enqueue ends the capture (discarding the partial graph) before the error
 // propagates, so the stream is usable again.
-void capture_graph(faco_engine* e, cudaStream_t st) {
-    auto& v = e->eval;
-    destroy_graph(e);
+void capture_one(faco_engine* e, cudaStream_t st, cudaGraph_t& graph, cudaGraphExec_t& exec) {
     cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
     try {
         enqueue_iterations(e, st, kGraphIterations);
@@ -692,10 +715,36 @@ void capture_graph(faco_engine* e, cudaStream_t st) {
         cudaGetLastError();
         throw;
     }
-    cuda_check(cudaStreamEndCapture(st, &v.graph), "end capture");
-    cuda_check(cudaGraphInstantiate(&v.exec, v.graph, 0), "graph instantiate");
+    cuda_check(cudaStreamEndCapture(st, &graph), "end capture");
+    cuda_check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
     // upload now, so that the first replay costs what every other one does
-    cuda_check(cudaGraphUpload(v.exec, st), "graph upload");
+    cuda_check(cudaGraphUpload(exec, st), "graph upload");
+}
+
+void capture_graph(faco_engine* e, cudaStream_t st) {
+    auto& v = e->eval;
+    destroy_graph(e);
+    capture_one(e, st, v.graph, v.exec);
+    if (v.adaptive) {
+        // the same iterations with every class's batched-step variant
+        std::vector<int> modes;
+        for (auto& cl : v.classes) {
+            modes.push_back(cl.mode);
+            cl.mode = faco::with_follow(cl.mode);
+        }
+        try {
+            capture_one(e, st, v.graph_batched, v.exec_batched);
+        } catch (...) {
+            for (std::size_t i = 0; i < modes.size(); ++i) v.classes[i].mode = modes[i];
+            throw;
+        }
+        for (std::size_t i = 0; i < modes.size(); ++i) v.classes[i].mode = modes[i];
+    }
+    // a fresh evaluation starts with every counter at zero
+    v.batched = false;
+    v.steps_seen = 0;
+    v.done_seen = 0;
+    v.rebase = false;
 }
 
 // Kernel variant of a size class: the global-memory workspace (tour and
@@ -851,8 +900,14 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
     // batched parent-following steps (the same results): on request, or
     // when every ant warp of the evaluation fits in one wave of the GPU
     const std::uint64_t ant_warps = static_cast<std::uint64_t>(v.count) * A;
-    v.follow = c.follow == FACO_FOLLOW_ON ||
-               (c.follow == FACO_FOLLOW_AUTO && ant_warps <= 32ull * static_cast<std::uint64_t>(e->sm_count));
+    const bool one_wave = ant_warps <= 32ull * static_cast<std::uint64_t>(e->sm_count);
+    v.follow = c.follow == FACO_FOLLOW_ON || (c.follow == FACO_FOLLOW_AUTO && one_wave);
+    // beyond one wave the automatic choice is made per stretch of iterations
+    // from the walk length (step_evaluation); only for shared-memory ant
+    // workspaces, the variant the crossover was measured on
+    bool shared_only = true;
+    for (const auto& cl : v.classes) shared_only = shared_only && !faco::global_mode(cl.mode);
+    v.adaptive = c.follow == FACO_FOLLOW_AUTO && !one_wave && shared_only;
     if (v.follow)
         for (auto& cl : v.classes) cl.mode = faco::with_follow(cl.mode);
     // the dynamic shared-memory limit is a property of each kernel variant,
@@ -864,8 +919,11 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
         m = std::max(m, cl.smem);
     }
     for (auto& ch : v.chains) ch.L = launch_of(ch.first_job, v.classes[ch.cls].warps, v.classes[ch.cls].n_max);
-    for (const auto& [mode, smem] : smem_max)
+    for (const auto& [mode, smem] : smem_max) {
         if (smem) cuda_check(faco::prepare_ant_kernel(mode, smem), "cudaFuncSetAttribute");
+        if (smem && v.adaptive)
+            cuda_check(faco::prepare_ant_kernel(faco::with_follow(mode), smem), "cudaFuncSetAttribute");
+    }
 }
 
 // Controller programs of a GP-controlled evaluation (null: plain FACO).
@@ -1123,16 +1181,40 @@ void begin_evaluation(faco_engine* e, const uint64_t* keys, const uint64_t* seed
     v.active = true;
 }
 
+// The batched or one-step graph for the next replays, from the average
+// construction steps per ant and iteration since the last reading (the
+// colonies' counters, read after the stream drains: one synchronisation per
+// kAdaptIterations iterations).  Results do not depend on the choice.
+void choose_variant(faco_engine* e) {
+    auto& v = e->eval;
+    std::vector<faco::ColonyState> states(v.count);
+    e->states.download(states.data(), v.count, e->stream);
+    cuda_check(cudaStreamSynchronize(e->stream), "step counters");
+    unsigned long long steps = 0;
+    for (const auto& st : states) steps += st.construction_steps;
+    if (!v.rebase && v.done > v.done_seen && steps >= v.steps_seen) {
+        const double per_ant = static_cast<double>(steps - v.steps_seen) /
+                               (static_cast<double>(v.done - v.done_seen) * v.count * std::max(1u, v.L.ants));
+        if (!v.batched && per_ant >= kBatchOnSteps) v.batched = true;
+        else if (v.batched && per_ant < kBatchOffSteps) v.batched = false;
+    }
+    v.steps_seen = steps;
+    v.done_seen = v.done;
+    v.rebase = false;
+}
+
 void step_evaluation(faco_engine* e, std::uint32_t iterations) {
     auto& v = e->eval;
     require(v.active, "no active evaluation");
     std::uint32_t left = iterations;
     while (left >= kGraphIterations) {
-        cuda_check(cudaGraphLaunch(v.exec, e->stream), "graph launch");
+        if (v.adaptive && (v.rebase || v.done >= v.done_seen + kAdaptIterations)) choose_variant(e);
+        cuda_check(cudaGraphLaunch(v.adaptive && v.batched ? v.exec_batched : v.exec, e->stream), "graph launch");
         left -= kGraphIterations;
+        v.done += kGraphIterations;
     }
     if (left) enqueue_iterations(e, e->stream, left);
-    v.done += iterations;
+    v.done += left;
 }
 
 void finish_evaluation(faco_engine* e, faco_outputs* out, std::uint32_t dimension) {
@@ -1504,6 +1586,8 @@ int faco_restore(faco_engine* e, const void* buffer, uint64_t bytes, uint32_t tr
             }
             cuda_check(cudaStreamSynchronize(s), "snapshot upload");
             v.done = h.done;
+            v.done_seen = v.done;   // the restored counters run from iteration 0: rebase first
+            v.rebase = true;
         } catch (...) {
             v.active = false;
             destroy_graph(e);
@@ -1577,7 +1661,7 @@ int faco_get_launch_plan(faco_engine* e, faco_launch_plan* plan) {
         plan->chains = chains;
         plan->graph_iterations = kGraphIterations;
         plan->launches_per_iteration = chains ? chains * (1 + per_update) : plan->size_classes + per_update;
-        plan->follow = v.follow ? 1u : 0u;
+        plan->follow = v.adaptive ? 2u : v.follow ? 1u : 0u;
     });
 }
 

@@ -62,10 +62,13 @@ typedef struct faco_settings {
                         time, one lane per step; results do not depend on it */
 } faco_settings;
 
-/* Batched parent-following steps: AUTO uses them when the evaluation's ant
- * warps fit in one wave of the GPU (at most 32 per SM), where an iteration
- * lasts as long as its longest walk; they cost more instructions than they
- * save when the GPU is full. */
+/* Batched parent-following steps: AUTO uses them always when the
+ * evaluation's ant warps fit in one wave of the GPU (at most 32 per SM),
+ * where an iteration lasts as long as its longest walk.  On fuller panels
+ * (shared-memory ant workspaces) AUTO chooses every 64 iterations from the
+ * walk length of the last 64: batches from 72 construction steps per ant
+ * and iteration on, steps one at a time again below 60; short walks take
+ * more instructions in batches than one at a time. */
 enum { FACO_FOLLOW_AUTO = 0, FACO_FOLLOW_OFF = 1, FACO_FOLLOW_ON = 2 };
 
 void faco_default_settings(faco_settings* s);
@@ -249,7 +252,8 @@ typedef struct faco_launch_plan {
     uint32_t chains;
     uint32_t graph_iterations;
     uint32_t launches_per_iteration;
-    uint32_t follow; /* 1: the ant launches take parent-following steps in batches */
+    uint32_t follow; /* 1: the ant launches take parent-following steps in batches; 2: chosen
+                        every 64 iterations from the walk length */
 } faco_launch_plan;
 int faco_get_launch_plan(faco_engine* engine, faco_launch_plan* plan);
 /* The engine's cudaStream_t (for events recorded by the caller). */

@@ -755,3 +755,51 @@ def test_follow_batches_change_nothing(api):
     assert np.array_equal(a["colony_work"], b["colony_work"])
     late = a["trace"][-16:]
     assert float(late["construction_steps"].sum()) / (16 * 4 * ants) > 30   # walks several times the MNE target
+
+
+def test_adaptive_batches_change_nothing(api):
+    """A panel beyond one wave of ant warps (160 colonies x 32 ants, N=1000)
+    with the automatic setting: the engine reads the walk length every 64
+    iterations and switches to the batched-step graph once walks are long.
+    The run equals the one that takes every step one at a time -- tours,
+    lengths, every trace row -- and by its end the walks are long enough for
+    the switch; a run restored from a snapshot in the middle goes on equal
+    too."""
+    n, ants, colonies, iterations = 1000, 32, 160, 320
+    xys = [_cases.uniform_instance(n, seed=500 + i) for i in range(4)]
+    keys = np.repeat(np.arange(10, 14, dtype=np.uint64), colonies // 4)
+    seeds = np.tile(np.arange(colonies // 4, dtype=np.uint64), 4)
+
+    def engine(follow):
+        e = api.FacoBatchEngine(n, colonies, _settings(api, ants, follow=follow))
+        for i, xy in enumerate(xys):
+            e.register_problem(10 + i, xy.astype(np.float64))
+        return e
+
+    out = {}
+    for follow in (0, 1):
+        e = engine(follow)
+        e.begin(keys, seeds, 8, trace_iterations=iterations)
+        assert e.launch_plan()["follow"] == (2 if follow == 0 else 0)
+        e.step(iterations)
+        out[follow] = e.finish()
+        e.close()
+    a, b = out[0], out[1]
+    assert np.array_equal(a["costs"], b["costs"])
+    assert all(np.array_equal(x, y) for x, y in zip(a["tours"], b["tours"]))
+    assert np.array_equal(a["trace"], b["trace"])
+    late = a["trace"][-64:]["construction_steps"].astype(np.float64).sum() / (64 * colonies * ants)
+    assert late >= 72                     # the last stretches ran with batches
+    # snapshot at 160, continued on a fresh engine with the automatic setting
+    e = engine(0)
+    e.begin(keys, seeds, 8)
+    e.step(160)
+    state = e.capture_state()
+    e.finish()
+    e.close()
+    e = engine(0)
+    e.restore_state(state)
+    e.step(iterations - 160)
+    res = e.finish()
+    e.close()
+    assert np.array_equal(res["costs"], a["costs"])
