@@ -42,8 +42,12 @@ constexpr std::uint32_t kGraphIterations = 16;
 // kBatchOffSteps.  Measured on the N=1000 throughput panel: batches lose up
 // to 1.9x on the short walks of early iterations (11-30 steps), break even
 // near 70 and win 19-26 % from 110 steps on.
+// With the global-memory ant workspace (large instances) the crossover is
+// later: on the large clustered panel (N 5,750-9,650) batches lose up to 17 %
+// below 50 steps and win 6-11 % from 150 on.
 constexpr std::uint32_t kAdaptIterations = 64;
 constexpr double kBatchOnSteps = 72.0, kBatchOffSteps = 60.0;
+constexpr double kBatchOnStepsGlobal = 96.0, kBatchOffStepsGlobal = 80.0;
 // Automatic chain count: one chain per kColoniesPerChain colonies, at most kMaxChains.
 // Trail updates of more than 2 x kTrailCellsPerBlock entries per colony run in
 // colony_trails_kernel, one block per kTrailCellsPerBlock entries (at most
@@ -338,6 +342,7 @@ struct faco_engine {
         // graph beside the one-step one, the variant of the next replays and
         // the step counters at the last reading
         bool adaptive = false, batched = false;
+        double batch_on = kBatchOnSteps, batch_off = kBatchOffSteps;
         cudaGraph_t graph_batched = nullptr;
         cudaGraphExec_t exec_batched = nullptr;
         unsigned long long steps_seen = 0;
@@ -903,11 +908,13 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
     const bool one_wave = ant_warps <= 32ull * static_cast<std::uint64_t>(e->sm_count);
     v.follow = c.follow == FACO_FOLLOW_ON || (c.follow == FACO_FOLLOW_AUTO && one_wave);
     // beyond one wave the automatic choice is made per stretch of iterations
-    // from the walk length (step_evaluation); only for shared-memory ant
-    // workspaces, the variant the crossover was measured on
-    bool shared_only = true;
-    for (const auto& cl : v.classes) shared_only = shared_only && !faco::global_mode(cl.mode);
-    v.adaptive = c.follow == FACO_FOLLOW_AUTO && !one_wave && shared_only;
+    // from the walk length (step_evaluation), with the later crossover of
+    // the global-memory workspace when a class uses it
+    bool any_global = false;
+    for (const auto& cl : v.classes) any_global = any_global || faco::global_mode(cl.mode);
+    v.adaptive = c.follow == FACO_FOLLOW_AUTO && !one_wave;
+    v.batch_on = any_global ? kBatchOnStepsGlobal : kBatchOnSteps;
+    v.batch_off = any_global ? kBatchOffStepsGlobal : kBatchOffSteps;
     if (v.follow)
         for (auto& cl : v.classes) cl.mode = faco::with_follow(cl.mode);
     // the dynamic shared-memory limit is a property of each kernel variant,
@@ -1195,8 +1202,8 @@ void choose_variant(faco_engine* e) {
     if (!v.rebase && v.done > v.done_seen && steps >= v.steps_seen) {
         const double per_ant = static_cast<double>(steps - v.steps_seen) /
                                (static_cast<double>(v.done - v.done_seen) * v.count * std::max(1u, v.L.ants));
-        if (!v.batched && per_ant >= kBatchOnSteps) v.batched = true;
-        else if (v.batched && per_ant < kBatchOffSteps) v.batched = false;
+        if (!v.batched && per_ant >= v.batch_on) v.batched = true;
+        else if (v.batched && per_ant < v.batch_off) v.batched = false;
     }
     v.steps_seen = steps;
     v.done_seen = v.done;

@@ -65,10 +65,11 @@ typedef struct faco_settings {
 /* Batched parent-following steps: AUTO uses them always when the
  * evaluation's ant warps fit in one wave of the GPU (at most 32 per SM),
  * where an iteration lasts as long as its longest walk.  On fuller panels
- * (shared-memory ant workspaces) AUTO chooses every 64 iterations from the
- * walk length of the last 64: batches from 72 construction steps per ant
- * and iteration on, steps one at a time again below 60; short walks take
- * more instructions in batches than one at a time. */
+ * AUTO chooses every 64 iterations from the walk length of the last 64:
+ * batches from 72 construction steps per ant and iteration on, steps one at
+ * a time again below 60 (96 and 80 with the global-memory ant workspace of
+ * large instances); short walks take more instructions in batches than one
+ * at a time. */
 enum { FACO_FOLLOW_AUTO = 0, FACO_FOLLOW_OFF = 1, FACO_FOLLOW_ON = 2 };
 
 void faco_default_settings(faco_settings* s);

@@ -757,9 +757,11 @@ def test_follow_batches_change_nothing(api):
     assert float(late["construction_steps"].sum()) / (16 * 4 * ants) > 30   # walks several times the MNE target
 
 
-def test_adaptive_batches_change_nothing(api):
+@pytest.mark.parametrize("workspace", [0, 2])
+def test_adaptive_batches_change_nothing(api, workspace):
     """A panel beyond one wave of ant warps (160 colonies x 32 ants, N=1000)
-    with the automatic setting: the engine reads the walk length every 64
+    with the automatic setting, the ants' tours in shared memory and in the
+    global-memory workspace: the engine reads the walk length every 64
     iterations and switches to the batched-step graph once walks are long.
     The run equals the one that takes every step one at a time -- tours,
     lengths, every trace row -- and by its end the walks are long enough for
@@ -771,7 +773,7 @@ def test_adaptive_batches_change_nothing(api):
     seeds = np.tile(np.arange(colonies // 4, dtype=np.uint64), 4)
 
     def engine(follow):
-        e = api.FacoBatchEngine(n, colonies, _settings(api, ants, follow=follow))
+        e = api.FacoBatchEngine(n, colonies, _settings(api, ants, workspace=workspace, follow=follow))
         for i, xy in enumerate(xys):
             e.register_problem(10 + i, xy.astype(np.float64))
         return e
@@ -789,7 +791,7 @@ def test_adaptive_batches_change_nothing(api):
     assert all(np.array_equal(x, y) for x, y in zip(a["tours"], b["tours"]))
     assert np.array_equal(a["trace"], b["trace"])
     late = a["trace"][-64:]["construction_steps"].astype(np.float64).sum() / (64 * colonies * ants)
-    assert late >= 72                     # the last stretches ran with batches
+    assert late >= (72 if workspace == 0 else 96)   # the last stretches ran with batches
     # snapshot at 160, continued on a fresh engine with the automatic setting
     e = engine(0)
     e.begin(keys, seeds, 8)
