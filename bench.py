@@ -16,8 +16,11 @@ baseline and the reference arm run.  Default workload (throughput): 16
 instances of N=1000 integer coordinates uniform in [0,10^6]^2 x 16 seeds =
 256 colonies, 32 ants each, k=16, backup 64, LS width 20, MNE 8, 2-opt,
 retention 0.98; its line also carries the converged window (iteration 400
-on) and the learned prior's time to a 1% gap against plain FACO (the
-learned-prior workload: 64 instances, N in {1000, 2000}, 32 ants, k=20).
+on), the learned prior's time to a 1% gap against plain FACO (the
+learned-prior workload: 64 instances, N in {1000, 2000}, 32 ants, k=20), and
+`other_workloads`: the uneven, large and GP-population lines of the same run
+(device and end-to-end values, each from a child run without its CPU
+baseline).
 Other workloads:
   uneven         256 clustered instances, N ~ U[200,1000], 16 ants, k=16
                  (one colony each; size-class launches in one CUDA graph);
@@ -482,7 +485,40 @@ def run_gb300(args, rank: int, world: int) -> None:
         line["steady_state"] = steady
     if wl.name == "throughput" and args.time_to_gap and world == 1:
         line["time_to_gap"] = time_to_gap_block(local, args.follow)
+    if wl.name == "throughput" and args.other_workloads and world == 1 and not args.window_only:
+        line["other_workloads"] = other_workloads_block(args)
     print(json.dumps(line), flush=True)
+
+
+OTHER_WORKLOADS = (("uneven", []), ("large", []), ("gp-population", []), ("gp-population", ["--controller", "2"]))
+
+
+def other_workloads_block(args) -> dict:
+    """The other throughput workloads in the same run, each as a child bench
+    process (its own device context and memory) without its CPU baseline:
+    device and end-to-end value, the workload, its kernel choice and the
+    clocks seen while it ran."""
+    out = {}
+    for name, extra in OTHER_WORKLOADS:
+        label = name + ("-controller-2" if extra else "")
+        cmd = [sys.executable, str(Path(__file__).resolve()), "--workload", name, "--no-cpu-baseline",
+               "--steps", str(args.steps), "--warmup", str(args.warmup), "--follow", str(args.follow), *extra]
+        try:
+            proc = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            lines = [ln for ln in proc.stdout.splitlines() if ln.startswith("{")]
+            if proc.returncode != 0 or not lines:
+                out[label] = {"error": (proc.stderr or proc.stdout)[-300:]}
+                continue
+            d = json.loads(lines[-1])
+        except subprocess.TimeoutExpired:
+            out[label] = {"error": "timed out"}
+            continue
+        cfg = d.get("config", {})
+        out[label] = {"metric": d.get("metric"), "value": d.get("value"), "unit": d.get("unit"),
+                      "ms_per_step": d.get("ms_per_step"), "e2e": (d.get("e2e") or {}).get("value"),
+                      "workload": cfg.get("workload"), "timed_iterations": cfg.get("timed_iterations"),
+                      "follow_batches": cfg.get("follow_batches"), "clocks": d.get("clocks")}
+    return out
 
 
 def time_to_gap_block(device: int = 0, follow: int = 0) -> dict:
@@ -680,6 +716,8 @@ def main():
                     help="parent-following construction steps in batches: 0 auto (always when every ant warp "
                          "fits in one wave of the GPU, else chosen every 64 iterations from the walk length), "
                          "1 off, 2 on")
+    ap.add_argument("--no-other-workloads", dest="other_workloads", action="store_false",
+                    help="leave the uneven, large and GP-population blocks out of the throughput line")
     ap.add_argument("--window-only", action="store_true",
                     help="registration, warm-up and the timed window only (for kernel profiles): no unchained "
                          "replay, converged window, end-to-end call, CPU baseline or time-to-gap")

@@ -14,7 +14,7 @@ ROOT = Path(__file__).resolve().parents[1]
 @pytest.mark.gpu
 def test_bench_line_keeps_the_contract():
     out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--steps", "1", "--warmup", "3",
-                          "--no-cpu-baseline", "--no-time-to-gap"], capture_output=True, text=True, timeout=900,
+                          "--no-cpu-baseline", "--no-time-to-gap", "--no-other-workloads"], capture_output=True, text=True, timeout=900,
                          cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [line for line in out.stdout.splitlines() if line.strip()]
