@@ -697,7 +697,7 @@ def run_large_prior(args) -> None:
             "config": {"workload": "16 clustered instances, N ~ U[5000,10000], 32-64 clusters in [0,10^7]^2, 5 seeds "
                                    "each (80 colonies), 64 ants, k=32, 2-opt window 32 + Or-opt (<= 3), MNE 8, "
                                    "retention 0.98, 1000 iterations; prior trained on 16 smaller instances of the "
-                                   "same generator (N 1000-2000); fallback at iteration 100; gaps against the best "
+                                   "same generator (N 1000-2000); fallback at iteration 96; gaps against the best "
                                    "length either arm reaches"},
             "large_prior": res}
     print(json.dumps(line), flush=True)

@@ -35,7 +35,7 @@ class GapConfig:
     retention: float = 0.98
     mne: int = 8
     follow: int = 0                 # parent-following steps in batches: 0 auto, 1 off, 2 on
-    chunk: int = 10                 # iterations between cost and clock reads
+    chunk: int = 16                 # iterations between cost and clock reads (one graph replay)
     iterations: int = 400           # budget of the validation (tuning) runs
     budget: int = 2000              # budget of the evaluation runs, per method
     reference_iterations: int = 3000
@@ -415,7 +415,8 @@ def summary(res: dict) -> dict:
         "prior_setting": res["prior_setting"], "plain_setting": res["plain_setting"],
         "gap_at": pair["gap_at"], "total_seconds": res["total_seconds"],
         "crossing": "the first iteration at or below the target gap, exact from the colonies' per-iteration "
-                    "trace; its time interpolated between the clock readings around it (every 10 iterations)",
+                    "trace; its time interpolated between the clock readings around it (every 16 iterations, "
+                    "one graph replay)",
     }
 
 
@@ -459,8 +460,8 @@ class LargeConfig:
     retention: float = 0.98
     mne: int = 8
     iterations: int = 1000
-    chunk: int = 50                 # iterations between cost reads
-    warmup: int = 100               # iterations before the fallback decision
+    chunk: int = 48                 # iterations between cost reads (three graph replays)
+    warmup: int = 96                # iterations before the fallback decision
     floor: float = 0.05
     gamma: int = 2
     train_pool: int = 16            # training instances: N ~ U[1000, 2000], same generator, seeds 700-715
@@ -518,7 +519,7 @@ def _large_arm(cfg: LargeConfig, xys: list, params=None, plain_warm=None, device
     rows = [(0, 0.0, costs.reshape(len(xys), cfg.seeds).copy())]
     done = 0
     while done < cfg.iterations:
-        step = min(cfg.chunk, cfg.warmup - done) if done < cfg.warmup else cfg.chunk
+        step = min(cfg.chunk, cfg.warmup - done) if done < cfg.warmup else min(cfg.chunk, cfg.iterations - done)
         engine.step(step)
         done += step
         costs, _ = engine.current_costs(count)
