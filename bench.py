@@ -469,7 +469,7 @@ def run_gb300(args, rank: int, world: int) -> None:
                    "iterations_per_step": per_step,
                    "timed_iterations": [0, window],
                    "warmup": "W steps of a separate evaluation; the timed one starts from the initial tours",
-                   "colony_chains": plan["chains"], "follow_batches": {0: "off", 1: "on", 2: "every 64 iterations from the walk length"}[plan["follow"]],
+                   "colony_chains": plan["chains"], "follow_batches": {0: "off", 1: "on", 2: "every 32 iterations from the walk length"}[plan["follow"]],
                    "registration_seconds": registration_s, "size_classes": classes},
         "e2e": {"value": e2e_value, "unit": "ant-tours+LS/s", "h2d_bytes_per_step": h2d * per_step / e2e_iters,
                 "d2h_bytes_per_step": d2h * per_step / e2e_iters, "iterations": e2e_iters,
@@ -714,7 +714,7 @@ def main():
                     help="leave the learned prior's time-to-gap block out of the throughput line")
     ap.add_argument("--follow", type=int, default=0, choices=[0, 1, 2],
                     help="parent-following construction steps in batches: 0 auto (always when every ant warp "
-                         "fits in one wave of the GPU, else chosen every 64 iterations from the walk length), "
+                         "fits in one wave of the GPU, else chosen every 32 iterations from the walk length), "
                          "1 off, 2 on")
     ap.add_argument("--no-other-workloads", dest="other_workloads", action="store_false",
                     help="leave the uneven, large and GP-population blocks out of the throughput line")

@@ -45,7 +45,7 @@ constexpr std::uint32_t kGraphIterations = 16;
 // With the global-memory ant workspace (large instances) the crossover is
 // later: on the large clustered panel (N 5,750-9,650) batches lose up to 17 %
 // below 50 steps and win 6-11 % from 150 on.
-constexpr std::uint32_t kAdaptIterations = 64;
+constexpr std::uint32_t kAdaptIterations = 32;   // 64 switched one stretch later: 3 % slower on iterations 0-320
 constexpr double kBatchOnSteps = 72.0, kBatchOffSteps = 60.0;
 constexpr double kBatchOnStepsGlobal = 96.0, kBatchOffStepsGlobal = 80.0;
 // Automatic chain count: one chain per kColoniesPerChain colonies, at most kMaxChains.

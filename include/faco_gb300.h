@@ -65,7 +65,7 @@ typedef struct faco_settings {
 /* Batched parent-following steps: AUTO uses them always when the
  * evaluation's ant warps fit in one wave of the GPU (at most 32 per SM),
  * where an iteration lasts as long as its longest walk.  On fuller panels
- * AUTO chooses every 64 iterations from the walk length of the last 64:
+ * AUTO chooses every 32 iterations from the walk length of the last 32:
  * batches from 72 construction steps per ant and iteration on, steps one at
  * a time again below 60 (96 and 80 with the global-memory ant workspace of
  * large instances); short walks take more instructions in batches than one
@@ -254,7 +254,7 @@ typedef struct faco_launch_plan {
     uint32_t graph_iterations;
     uint32_t launches_per_iteration;
     uint32_t follow; /* 1: the ant launches take parent-following steps in batches; 2: chosen
-                        every 64 iterations from the walk length */
+                        every 32 iterations from the walk length */
 } faco_launch_plan;
 int faco_get_launch_plan(faco_engine* engine, faco_launch_plan* plan);
 /* The engine's cudaStream_t (for events recorded by the caller). */

@@ -761,7 +761,7 @@ def test_follow_batches_change_nothing(api):
 def test_adaptive_batches_change_nothing(api, workspace):
     """A panel beyond one wave of ant warps (160 colonies x 32 ants, N=1000)
     with the automatic setting, the ants' tours in shared memory and in the
-    global-memory workspace: the engine reads the walk length every 64
+    global-memory workspace: the engine reads the walk length every 32
     iterations and switches to the batched-step graph once walks are long.
     The run equals the one that takes every step one at a time -- tours,
     lengths, every trace row -- and by its end the walks are long enough for
