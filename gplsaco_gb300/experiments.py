@@ -45,7 +45,7 @@ class GapConfig:
     gamma: int = 1
     target_gap: float = 0.01
     extra_targets: tuple = (0.0075, 0.005)   # reported beside the headline target
-    # Both arms are tuned on validation instances (seeds 200-215) by wall-clock
+    # Both arms are tuned on validation instances (seeds 200-231) by wall-clock
     # time to the target gap: plain FACO over MNE targets, the prior over
     # (model, floor, gamma, refresh, MNE, departures).  "full" sees all eight features;
     # "geometry" only the geometric ones (trail level and best-tour membership
@@ -76,9 +76,9 @@ class GapConfig:
     batch: int = 8192
     lr: float = 3e-3
     # the learned-prior workload: N in {1000, 2000}, uniform and clustered,
-    # instance seeds 100-163 (evaluation) and 200-215 (validation)
+    # instance seeds 100-163 (evaluation) and 200-231 (validation)
     eval_instances: list = field(default_factory=lambda: gap_instances(range(100, 164)))
-    validation_instances: list = field(default_factory=lambda: gap_instances(range(200, 216)))
+    validation_instances: list = field(default_factory=lambda: gap_instances(range(200, 232)))
 
 
 def gap_instances(seeds) -> list:
