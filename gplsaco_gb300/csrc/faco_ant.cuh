@@ -42,21 +42,31 @@ enum AntMode : int {
                             // coordinates read from global (large instances)
     kModeEngineFollow = 5,        // kModeEngine with batched parent-following steps (follow_batch)
     kModeEngineGlobalFollow = 6,  // kModeEngineGlobal with batched parent-following steps
+    // kModeEngineFollow compiled for panels beyond one wave of the GPU: the
+    // same arithmetic, the batch's roulette loops unrolled by two (72
+    // registers against 79: one more block per SM) where mode 5 favours one
+    // ant's latency.  The global-workspace variant has no such build: the
+    // same unrolling leaves it at 80 registers.
+    kModeEngineFollowDense = 7,
 };
 
 __host__ __device__ constexpr bool engine_mode(int mode) {
     return mode == kModeEngine || mode == kModeEngineGlobal || mode == kModeEngineFollow ||
-           mode == kModeEngineGlobalFollow;
+           mode == kModeEngineGlobalFollow || mode == kModeEngineFollowDense;
 }
 __host__ __device__ constexpr bool global_mode(int mode) {
     return mode == kModeEngineGlobal || mode == kModeEngineGlobalFollow;
 }
+__host__ __device__ constexpr bool dense_mode(int mode) { return mode == kModeEngineFollowDense; }
 __host__ __device__ constexpr bool follow_mode(int mode) {
-    return mode == kModeEngineFollow || mode == kModeEngineGlobalFollow;
+    return mode == kModeEngineFollow || mode == kModeEngineGlobalFollow || mode == kModeEngineFollowDense;
 }
-// The batched variant of an engine mode.
-__host__ __device__ constexpr int with_follow(int mode) {
-    return mode == kModeEngineGlobal ? kModeEngineGlobalFollow : mode == kModeEngine ? kModeEngineFollow : mode;
+// The batched variant of an engine mode (`dense`: the build for panels
+// beyond one wave, where there is one).
+__host__ __device__ constexpr int with_follow(int mode, bool dense = false) {
+    return mode == kModeEngineGlobal ? kModeEngineGlobalFollow
+           : mode == kModeEngine     ? (dense ? kModeEngineFollowDense : kModeEngineFollow)
+                                     : mode;
 }
 
 struct AntLaunch {
@@ -344,6 +354,85 @@ struct RelocationRun {
 // every lane of the chosen hypothesis was taken (the walk may go on).
 __device__ __forceinline__ bool on_segment(int lo, int hi, int q) { return q >= lo && q <= hi; }
 
+// The roulette of one lane's step in follow_batch: the candidates of `row`
+// still open to the walk (unvisited, and for a relocation run not on the
+// run's segment), their FP32 weights summed serially in candidate order,
+// and the first prefix at or above uf * total; -1 when that prefix lies
+// within the decision margin (the one-step path decides) or no candidate is
+// open.  The dense variants unroll both loops by two; the others leave them
+// to the compiler.  The loops are written out twice because any rewrite of
+// the shared body (a lambda, a helper per candidate) changed the compiler's
+// code for the latency-tuned variants.  Both run the same sums in the same
+// order.
+template <bool kDense>
+__device__ __forceinline__ int follow_roulette(const AntSmem& s, const node_t* row, const float* prow,
+                                               std::uint32_t n, std::uint32_t k, std::uint32_t rel, std::uint32_t t0,
+                                               bool identity, int lo, int hi, float uf) {
+    unsigned avail = 0;
+    float tot = 0.0f;
+    if constexpr (kDense) {
+#pragma unroll 2
+        for (std::uint32_t j = 0; j < k; ++j) {
+            const std::uint32_t x = __ldg(row + j);
+            const float w = __ldg(prow + j);
+            bool a = x < n && !test_bit(s.visited, x);
+            if (a && rel) {
+                const std::uint32_t px = s.pos[x];
+                const std::uint32_t dx = px >= t0 ? px - t0 : px + n - t0;   // tour positions after the start
+                a = identity ? !(dx >= 1 && dx <= rel) : !on_segment(lo, hi, (int)px);
+            }
+            if (a) {
+                avail |= 1u << j;
+                tot += w;
+            }
+        }
+    } else {
+        for (std::uint32_t j = 0; j < k; ++j) {
+            const std::uint32_t x = __ldg(row + j);
+            const float w = __ldg(prow + j);
+            bool a = x < n && !test_bit(s.visited, x);
+            if (a && rel) {
+                const std::uint32_t px = s.pos[x];
+                const std::uint32_t dx = px >= t0 ? px - t0 : px + n - t0;   // tour positions after the start
+                a = identity ? !(dx >= 1 && dx <= rel) : !on_segment(lo, hi, (int)px);
+            }
+            if (a) {
+                avail |= 1u << j;
+                tot += w;
+            }
+        }
+    }
+    int choice = -1;
+    if (avail && tot >= 0x1p-100f) {
+        const float thr = uf * tot, delta = tot * 0x1p-17f;
+        float prefix = 0.0f;
+        if constexpr (kDense) {
+#pragma unroll 2
+            for (std::uint32_t j = 0; j < k; ++j) {
+                if (!((avail >> j) & 1u)) continue;
+                prefix += __ldg(prow + j);
+                const float diff = prefix - thr;
+                if (diff >= -delta) {
+                    if (diff > delta) choice = (int)j;
+                    break;
+                }
+            }
+        } else {
+            for (std::uint32_t j = 0; j < k; ++j) {
+                if (!((avail >> j) & 1u)) continue;
+                prefix += __ldg(prow + j);
+                const float diff = prefix - thr;
+                if (diff >= -delta) {
+                    if (diff > delta) choice = (int)j;
+                    break;
+                }
+            }
+        }
+    }
+    return choice;
+}
+
+template <bool kDense>
 __device__ inline std::uint32_t follow_batch(const AntSmem& s, const int2* xy, const InstanceView& in,
                                              const float* products, const std::uint32_t* parent_nbr, std::uint32_t n,
                                              std::uint32_t lane, unsigned long long key, std::uint32_t batch,
@@ -427,36 +516,7 @@ __device__ inline std::uint32_t follow_batch(const AntSmem& s, const int2* xy, c
     if (ok) {
         const node_t* row = in.primary + (size_t)cur * k;
         const float* prow = products + (size_t)cur * k;
-        unsigned avail = 0;
-        float tot = 0.0f;
-        for (std::uint32_t j = 0; j < k; ++j) {
-            const std::uint32_t x = __ldg(row + j);
-            const float w = __ldg(prow + j);
-            bool a = x < n && !test_bit(s.visited, x);
-            if (a && rel) {
-                const std::uint32_t px = s.pos[x];
-                const std::uint32_t dx = px >= t0 ? px - t0 : px + n - t0;   // tour positions after the start
-                a = identity ? !(dx >= 1 && dx <= rel) : !on_segment(lo, hi, (int)px);
-            }
-            if (a) {
-                avail |= 1u << j;
-                tot += w;
-            }
-        }
-        int choice = -1;
-        if (avail && tot >= 0x1p-100f) {
-            const float thr = uf * tot, delta = tot * 0x1p-17f;
-            float prefix = 0.0f;
-            for (std::uint32_t j = 0; j < k; ++j) {
-                if (!((avail >> j) & 1u)) continue;
-                prefix += __ldg(prow + j);
-                const float diff = prefix - thr;
-                if (diff >= -delta) {
-                    if (diff > delta) choice = (int)j;
-                    break;
-                }
-            }
-        }
+        const int choice = follow_roulette<kDense>(s, row, prow, n, k, rel, t0, identity, lo, hi, uf);
         ok = choice >= 0 && __ldg(row + choice) == sel;
     }
     // the leading run of taken steps

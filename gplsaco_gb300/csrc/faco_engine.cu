@@ -307,7 +307,8 @@ struct faco_engine {
     // instance, and the classes run as parallel branches of each iteration.
     struct AntClass {
         std::uint32_t n_max = 0, warps = 1, smem = 0, blocks = 0, first_job = 0;
-        int mode = faco::kModeEngine;   // or kModeEngineGlobal (tour/inverse in global memory)
+        int mode = faco::kModeEngine;   // or kModeEngineGlobal (tour/inverse in global memory), or
+                                        // either's batched-step variant
         faco::AntLaunch L{};
     };
     // A chain: a subset of the colonies of one size class, whose iterations
@@ -731,11 +732,12 @@ void capture_graph(faco_engine* e, cudaStream_t st) {
     destroy_graph(e);
     capture_one(e, st, v.graph, v.exec);
     if (v.adaptive) {
-        // the same iterations with every class's batched-step variant
+        // the same iterations with every class's batched-step variant (the
+        // one compiled for panels beyond one wave)
         std::vector<int> modes;
         for (auto& cl : v.classes) {
             modes.push_back(cl.mode);
-            cl.mode = faco::with_follow(cl.mode);
+            cl.mode = faco::with_follow(cl.mode, true);
         }
         try {
             capture_one(e, st, v.graph_batched, v.exec_batched);
@@ -915,8 +917,10 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
     v.adaptive = c.follow == FACO_FOLLOW_AUTO && !one_wave;
     v.batch_on = any_global ? kBatchOnStepsGlobal : kBatchOnSteps;
     v.batch_off = any_global ? kBatchOffStepsGlobal : kBatchOffSteps;
+    // (beyond one wave, the batched build that favours throughput over one
+    // ant's latency)
     if (v.follow)
-        for (auto& cl : v.classes) cl.mode = faco::with_follow(cl.mode);
+        for (auto& cl : v.classes) cl.mode = faco::with_follow(cl.mode, !one_wave);
     // the dynamic shared-memory limit is a property of each kernel variant,
     // shared by every class that uses it: it must admit the largest one
     std::map<int, std::uint32_t> smem_max;
@@ -929,7 +933,7 @@ void build_work_tables(faco_engine* e, const std::vector<std::vector<std::uint32
     for (const auto& [mode, smem] : smem_max) {
         if (smem) cuda_check(faco::prepare_ant_kernel(mode, smem), "cudaFuncSetAttribute");
         if (smem && v.adaptive)
-            cuda_check(faco::prepare_ant_kernel(faco::with_follow(mode), smem), "cudaFuncSetAttribute");
+            cuda_check(faco::prepare_ant_kernel(faco::with_follow(mode, true), smem), "cudaFuncSetAttribute");
     }
 }
 

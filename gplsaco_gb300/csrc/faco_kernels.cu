@@ -50,7 +50,8 @@ __device__ __forceinline__ void load_parent(const AntSmem& s, const node_t* pare
 
 template <int MODE>
 __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_kernel(const AntLaunch L) {
-    constexpr bool kEngine = engine_mode(MODE), kGlobalWs = global_mode(MODE), kFollow = follow_mode(MODE);
+    constexpr bool kEngine = engine_mode(MODE), kGlobalWs = global_mode(MODE), kFollow = follow_mode(MODE),
+                   kDense = dense_mode(MODE);
     extern __shared__ __align__(16) unsigned char smem[];
     const std::uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     std::uint32_t colony = 0, ant = 0, task = 0;
@@ -167,8 +168,9 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, kAntBlocksPerSM) ant_k
             if (++guard > loop_cap) { if (lane == 0) atomicOr(L.error, kErrLoopCap); break; }
             if (kFollow && follow) {
                 bool full = false;
-                const std::uint32_t f = follow_batch(s, xy, in, products, parent_nbr, n, lane, key, batch, ant,
-                                                     current, r, cost, run, draw_base, draw_hi, draw_lo, full);
+                const std::uint32_t f = follow_batch<kDense>(s, xy, in, products, parent_nbr, n, lane, key, batch,
+                                                             ant, current, r, cost, run, draw_base, draw_hi, draw_lo,
+                                                             full);
                 follow = full;
                 if (f) continue;
             }
@@ -471,6 +473,7 @@ cudaError_t prepare_ant_kernel(int mode, std::uint32_t smem) {
         case kModeEngineGlobal: return prepare_mode<kModeEngineGlobal>(smem);
         case kModeEngineFollow: return prepare_mode<kModeEngineFollow>(smem);
         case kModeEngineGlobalFollow: return prepare_mode<kModeEngineGlobalFollow>(smem);
+        case kModeEngineFollowDense: return prepare_mode<kModeEngineFollowDense>(smem);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -486,6 +489,7 @@ cudaError_t launch_ant_kernel(int mode, const AntLaunch& L, std::uint32_t blocks
         case kModeEngineGlobal: ant_kernel<kModeEngineGlobal><<<grid, block, smem, stream>>>(L); break;
         case kModeEngineFollow: ant_kernel<kModeEngineFollow><<<grid, block, smem, stream>>>(L); break;
         case kModeEngineGlobalFollow: ant_kernel<kModeEngineGlobalFollow><<<grid, block, smem, stream>>>(L); break;
+        case kModeEngineFollowDense: ant_kernel<kModeEngineFollowDense><<<grid, block, smem, stream>>>(L); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

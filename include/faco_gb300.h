@@ -69,7 +69,9 @@ typedef struct faco_settings {
  * batches from 72 construction steps per ant and iteration on, steps one at
  * a time again below 60 (96 and 80 with the global-memory ant workspace of
  * large instances); short walks take more instructions in batches than one
- * at a time. */
+ * at a time.  Beyond one wave the batches run a build of the same steps
+ * tuned for throughput (fewer registers per thread, more warps per SM)
+ * rather than for one ant's latency. */
 enum { FACO_FOLLOW_AUTO = 0, FACO_FOLLOW_OFF = 1, FACO_FOLLOW_ON = 2 };
 
 void faco_default_settings(faco_settings* s);

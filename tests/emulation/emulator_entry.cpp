@@ -1,6 +1,7 @@
 
 // One engine-mode ant on the host: 32 lane threads run the kernel body
-// (follow != 0: the variant with batched parent-following steps).  Inputs are
+// (follow 1: the variant with batched parent-following steps, 2: its dense
+// build for panels beyond one wave).  Inputs are
 // the instance rows, the colony's parent tour with its packed neighbours and
 // products, the Philox key, batch and ant index; outputs the ant's final
 // tour, its construction and final lengths, and its step / LS / moved counts.
@@ -49,7 +50,8 @@ extern "C" int emu_ant(std::uint32_t follow, std::uint32_t n, std::uint32_t k, s
         th.emplace_back([&, l] {
             tl_warp = &warp;
             tl_lane = l;
-            if (follow) ant_kernel_emu<kModeEngineFollow>(L, sm);
+            if (follow == 2) ant_kernel_emu<kModeEngineFollowDense>(L, sm);
+            else if (follow) ant_kernel_emu<kModeEngineFollow>(L, sm);
             else ant_kernel_emu<kModeEngine>(L, sm);
         });
     for (auto& t : th) t.join();
