@@ -32,9 +32,11 @@ def generate() -> Path:
     (BUILD / "faco_ant.cuh").write_text((CSRC / "faco_ant.cuh").read_text())
     src = (CSRC / "faco_kernels.cu").read_text()
     body = src[src.index("__device__ __forceinline__ void load_parent("):src.index("namespace {\n// The dynamic shared")]
-    body = body.replace("template <int MODE>\n__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, "
-                        "kAntBlocksPerSM) ant_kernel(const AntLaunch L) {",
-                        "template <int MODE>\nvoid ant_kernel_emu(const AntLaunch L, unsigned char* smem) {")
+    signature = ("template <int MODE>\n__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32, "
+                 "kAntBlocksPerSM) ant_kernel(const AntLaunch L) {")
+    if signature not in body:
+        raise SystemExit("kernel source changed: cannot find the ant kernel's signature")
+    body = body.replace(signature, "template <int MODE>\nvoid ant_kernel_emu(const AntLaunch L, unsigned char* smem) {")
     body = body.replace("    extern __shared__ __align__(16) unsigned char smem[];\n", "")
     body = body.replace("threadIdx.x", "tl_lane").replace("blockIdx.x", "0u").replace("blockDim.x", "32u")
     body = body.replace("__syncthreads()", "__syncwarp()")
