@@ -727,25 +727,36 @@ void capture_one(faco_engine* e, cudaStream_t st, cudaGraph_t& graph, cudaGraphE
     cuda_check(cudaGraphUpload(exec, st), "graph upload");
 }
 
+// While alive, every class of an adaptive evaluation launches its
+// batched-step variant (the build for panels beyond one wave); the
+// one-step modes come back when it ends, an exception included.
+class BatchedModes {
+  public:
+    explicit BatchedModes(faco_engine::EvalState& v) : v_(v) {
+        for (auto& cl : v_.classes) {
+            modes_.push_back(cl.mode);
+            cl.mode = faco::with_follow(cl.mode, true);
+        }
+    }
+    ~BatchedModes() {
+        for (std::size_t i = 0; i < modes_.size(); ++i) v_.classes[i].mode = modes_[i];
+    }
+    BatchedModes(const BatchedModes&) = delete;
+    BatchedModes& operator=(const BatchedModes&) = delete;
+
+  private:
+    faco_engine::EvalState& v_;
+    std::vector<int> modes_;
+};
+
 void capture_graph(faco_engine* e, cudaStream_t st) {
     auto& v = e->eval;
     destroy_graph(e);
     capture_one(e, st, v.graph, v.exec);
     if (v.adaptive) {
-        // the same iterations with every class's batched-step variant (the
-        // one compiled for panels beyond one wave)
-        std::vector<int> modes;
-        for (auto& cl : v.classes) {
-            modes.push_back(cl.mode);
-            cl.mode = faco::with_follow(cl.mode, true);
-        }
-        try {
-            capture_one(e, st, v.graph_batched, v.exec_batched);
-        } catch (...) {
-            for (std::size_t i = 0; i < modes.size(); ++i) v.classes[i].mode = modes[i];
-            throw;
-        }
-        for (std::size_t i = 0; i < modes.size(); ++i) v.classes[i].mode = modes[i];
+        // the same iterations with every class's batched-step variant
+        BatchedModes batched(v);
+        capture_one(e, st, v.graph_batched, v.exec_batched);
     }
     // a fresh evaluation starts with every counter at zero
     v.batched = false;
@@ -1217,14 +1228,26 @@ void choose_variant(faco_engine* e) {
 void step_evaluation(faco_engine* e, std::uint32_t iterations) {
     auto& v = e->eval;
     require(v.active, "no active evaluation");
+    const auto adapt = [&] {
+        if (v.adaptive && (v.rebase || v.done >= v.done_seen + kAdaptIterations)) choose_variant(e);
+    };
     std::uint32_t left = iterations;
     while (left >= kGraphIterations) {
-        if (v.adaptive && (v.rebase || v.done >= v.done_seen + kAdaptIterations)) choose_variant(e);
+        adapt();
         cuda_check(cudaGraphLaunch(v.adaptive && v.batched ? v.exec_batched : v.exec, e->stream), "graph launch");
         left -= kGraphIterations;
         v.done += kGraphIterations;
     }
-    if (left) enqueue_iterations(e, e->stream, left);
+    // the rest as direct launches, of the same variant the graphs would run
+    if (left) {
+        adapt();
+        if (v.adaptive && v.batched) {
+            BatchedModes batched(v);
+            enqueue_iterations(e, e->stream, left);
+        } else {
+            enqueue_iterations(e, e->stream, left);
+        }
+    }
     v.done += left;
 }
 

@@ -766,7 +766,8 @@ def test_adaptive_batches_change_nothing(api, workspace):
     The run equals the one that takes every step one at a time -- tours,
     lengths, every trace row -- and by its end the walks are long enough for
     the switch; a run restored from a snapshot in the middle goes on equal
-    too."""
+    too, and so does a run stepped in pieces that are not whole graph
+    replays (the remainders launched directly, in the variant chosen)."""
     n, ants, colonies, iterations = 1000, 32, 160, 320
     xys = [_cases.uniform_instance(n, seed=500 + i) for i in range(4)]
     keys = np.repeat(np.arange(10, 14, dtype=np.uint64), colonies // 4)
@@ -805,3 +806,16 @@ def test_adaptive_batches_change_nothing(api, workspace):
     res = e.finish()
     e.close()
     assert np.array_equal(res["costs"], a["costs"])
+    # stepped in pieces of 5, 27, 11 and 9 iterations (then 8)
+    e = engine(0)
+    e.begin(keys, seeds, 8, trace_iterations=iterations)
+    done = 0
+    for piece in [5, 27, 11, 9] * 6 + [8]:
+        e.step(piece)
+        done += piece
+    assert done == iterations
+    res = e.finish()
+    e.close()
+    assert np.array_equal(res["costs"], b["costs"])
+    assert all(np.array_equal(x, y) for x, y in zip(res["tours"], b["tours"]))
+    assert np.array_equal(res["trace"], b["trace"])
