@@ -17,6 +17,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <optional>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -1661,11 +1662,17 @@ int faco_step_timed(faco_engine* e, uint32_t iterations, double* ant_ms, double*
         std::vector<cudaEvent_t> ev(3 * iterations);
         for (auto& x : ev) cuda_check(cudaEventCreate(&x), "event");
         for (std::uint32_t i = 0; i < iterations; ++i) {
+            // the variant step_evaluation would run (its check falls between
+            // iterations, outside the timed kernels)
+            if (v.adaptive && (v.rebase || v.done >= v.done_seen + kAdaptIterations)) choose_variant(e);
+            std::optional<BatchedModes> batched;
+            if (v.adaptive && v.batched) batched.emplace(v);
             cuda_check(cudaEventRecord(ev[3 * i], s), "event");
             enqueue_ants(e, s);
             cuda_check(cudaEventRecord(ev[3 * i + 1], s), "event");
             enqueue_update(e, s);
             cuda_check(cudaEventRecord(ev[3 * i + 2], s), "event");
+            v.done += 1;
         }
         cuda_check(cudaStreamSynchronize(s), "timed step");
         double a = 0, u = 0;
@@ -1677,7 +1684,6 @@ int faco_step_timed(faco_engine* e, uint32_t iterations, double* ant_ms, double*
             u += y;
         }
         for (auto& x : ev) cudaEventDestroy(x);
-        v.done += iterations;
         *ant_ms = a;
         *update_ms = u;
     });

@@ -235,9 +235,10 @@ int faco_score_controllers(const struct faco_program* trees, const uint32_t* kin
 /* The same evaluation in explicit steps (the reference's per-batch loop,
  * cuda/batch_engine.cu:875-1135, driven by the caller): faco_begin uploads the
  * panel and resets every colony; faco_step enqueues `iterations` ant batches
- * on the engine's stream (asynchronous); faco_step_timed runs them with a CUDA
- * event around every kernel and returns the summed device milliseconds of
- * the ant kernel and of the colony update (synchronous); faco_finish waits
+ * on the engine's stream (asynchronous); faco_step_timed runs them, with the
+ * kernel variants faco_step would run, as single launches with a CUDA event
+ * around every kernel and returns the summed device milliseconds of the ant
+ * kernel and of the colony update (synchronous); faco_finish waits
  * and fills tours, costs, counters and up to trace_iterations trace rows. */
 int faco_begin(faco_engine* engine, const uint64_t* instance_keys, const uint64_t* seeds, uint32_t count,
                uint32_t mne_target, uint32_t trace_iterations);

@@ -767,7 +767,8 @@ def test_adaptive_batches_change_nothing(api, workspace):
     lengths, every trace row -- and by its end the walks are long enough for
     the switch; a run restored from a snapshot in the middle goes on equal
     too, and so does a run stepped in pieces that are not whole graph
-    replays (the remainders launched directly, in the variant chosen)."""
+    replays (the remainders launched directly, in the variant chosen), or
+    timed kernel by kernel."""
     n, ants, colonies, iterations = 1000, 32, 160, 320
     xys = [_cases.uniform_instance(n, seed=500 + i) for i in range(4)]
     keys = np.repeat(np.arange(10, 14, dtype=np.uint64), colonies // 4)
@@ -818,4 +819,13 @@ def test_adaptive_batches_change_nothing(api, workspace):
     e.close()
     assert np.array_equal(res["costs"], b["costs"])
     assert all(np.array_equal(x, y) for x, y in zip(res["tours"], b["tours"]))
+    assert np.array_equal(res["trace"], b["trace"])
+    # the unchained timing path, which runs the variants step() would run
+    e = engine(0)
+    e.begin(keys, seeds, 8, trace_iterations=iterations)
+    ant_ms, update_ms = e.step_timed(iterations)
+    res = e.finish()
+    e.close()
+    assert ant_ms > 0 and update_ms > 0
+    assert np.array_equal(res["costs"], b["costs"])
     assert np.array_equal(res["trace"], b["trace"])
