@@ -13,7 +13,8 @@ runs L iterations with every kernel launched alone (unchained), printing the
 device milliseconds of the ant kernel and of the colony update.  Under a
 profiler the L ant launches of the second form are the only ant-kernel
 launches of their variant after registration: `ant_kernel<0>` (steps one at
-a time, F=1) or `ant_kernel<5>` (parent-following steps in batches, F=2).
+a time, F=1) or `ant_kernel<7>` (parent-following steps in batches, F=2: the
+batched build for panels beyond one wave, which this panel is).
 """
 from __future__ import annotations
 
