@@ -1,11 +1,14 @@
 
-// One engine-mode ant on the host: 32 lane threads run the kernel body
-// (follow 1: the variant with batched parent-following steps, 2: its dense
-// build for panels beyond one wave).  Inputs are
-// the instance rows, the colony's parent tour with its packed neighbours and
-// products, the Philox key, batch and ant index; outputs the ant's final
-// tour, its construction and final lengths, and its step / LS / moved counts.
-extern "C" int emu_ant(std::uint32_t follow, std::uint32_t n, std::uint32_t k, std::uint32_t b, std::uint32_t w,
+// One engine-mode ant on the host: 32 lane threads run the kernel body of
+// variant `mode` (kModeEngine, kModeEngineGlobal, kModeEngineFollow,
+// kModeEngineGlobalFollow or kModeEngineFollowDense; the global-workspace
+// variants keep the ant's tour and inverse in a host buffer standing for
+// the engine's workspace).  Inputs are the instance rows, the colony's
+// parent tour with its packed neighbours and products, the Philox key,
+// batch and ant index; outputs the ant's final tour, its construction and
+// final lengths, and its step / LS / moved counts.  Returns -1 for a mode
+// it does not run.
+extern "C" int emu_ant(std::uint32_t mode, std::uint32_t n, std::uint32_t k, std::uint32_t b, std::uint32_t w,
                        const int* xy, const std::uint16_t* primary, const std::uint16_t* backup,
                        const std::uint16_t* ls, const int* ls_dist, const std::uint16_t* parent,
                        const std::uint32_t* parent_nbr, const float* products, unsigned long long key,
@@ -13,6 +16,9 @@ extern "C" int emu_ant(std::uint32_t follow, std::uint32_t n, std::uint32_t k, s
                        std::uint32_t ls_mode, std::uint16_t* out_tour, long long* out_costs, unsigned* out_counts,
                        unsigned* error) {
     using namespace faco;
+    if (mode != kModeEngine && mode != kModeEngineGlobal && mode != kModeEngineFollow &&
+        mode != kModeEngineGlobalFollow && mode != kModeEngineFollowDense)
+        return -1;
     const std::uint32_t n_pad = pad8(n);
     InstanceView in{};
     in.n = n; in.k = k; in.b = b; in.w = w;
@@ -40,6 +46,13 @@ extern "C" int emu_ant(std::uint32_t follow, std::uint32_t n, std::uint32_t k, s
     AntLaunch L{};
     L.instances = &in; L.colonies = &cv; L.states = &st; L.work = &job; L.ants = ant + 1; L.warps = 1;
     L.n_max = n; L.ls_limit = 100000; L.ls_mode = ls_mode; L.error = error;
+    // the global-memory workspace: tour and inverse of every ant of the
+    // colony, indexed like ant_tours (garbage at first, as on the device)
+    std::vector<node_t> workspace(2 * static_cast<std::size_t>(ant + 1) * n_pad + 16, 0xABAB);
+    node_t* ws = workspace.data();
+    while (reinterpret_cast<std::uintptr_t>(ws) & 15) ++ws;
+    L.workspace = ws;
+    L.ant_tours_base = tours;
     // shared memory starts with garbage, as on the device
     std::vector<unsigned char> smem(block_smem_bytes(n, 1) + 64, 0xAB);
     unsigned char* sm = smem.data();
@@ -50,9 +63,14 @@ extern "C" int emu_ant(std::uint32_t follow, std::uint32_t n, std::uint32_t k, s
         th.emplace_back([&, l] {
             tl_warp = &warp;
             tl_lane = l;
-            if (follow == 2) ant_kernel_emu<kModeEngineFollowDense>(L, sm);
-            else if (follow) ant_kernel_emu<kModeEngineFollow>(L, sm);
-            else ant_kernel_emu<kModeEngine>(L, sm);
+            switch (mode) {
+                case kModeEngine: ant_kernel_emu<kModeEngine>(L, sm); break;
+                case kModeEngineGlobal: ant_kernel_emu<kModeEngineGlobal>(L, sm); break;
+                case kModeEngineFollow: ant_kernel_emu<kModeEngineFollow>(L, sm); break;
+                case kModeEngineGlobalFollow: ant_kernel_emu<kModeEngineGlobalFollow>(L, sm); break;
+                case kModeEngineFollowDense: ant_kernel_emu<kModeEngineFollowDense>(L, sm); break;
+                default: break;
+            }
         });
     for (auto& t : th) t.join();
     std::memcpy(out_tour, tours + static_cast<std::size_t>(ant) * n_pad, n * sizeof(node_t));

@@ -29,7 +29,7 @@ def _state(xy, k, b, w, iterations, seed):
     return prep, key, prep["initial"].astype(np.uint32), oracle.heuristic(xy, prep["primary"]) * np.float32(1e-6)
 
 
-def _ant(emu, follow, xy, prep, key, parent, products, k, b, w, batch, ant):
+def _ant(emu, mode, ls_mode, xy, prep, key, parent, products, k, b, w, batch, ant):
     n = len(xy)
     m = oracle.euc2d_matrix(xy)
     pos = np.empty(n, np.int64)
@@ -42,20 +42,30 @@ def _ant(emu, follow, xy, prep, key, parent, products, k, b, w, batch, ant):
                   parent=np.ascontiguousarray(parent, np.uint16))
     tour, costs, counts, err = np.zeros(n, np.uint16), np.zeros(2, np.int64), np.zeros(3, np.uint32), np.zeros(1, np.uint32)
     cost = int(np.sum(m[parent, np.roll(parent, -1)]))
-    emu.emu_ant(follow, n, k, b, w, *(arrays[x].ctypes.data for x in ("xy", "primary", "backup", "ls", "ls_dist",
-                                                                       "parent")),
-                nbr.ctypes.data, products.ctypes.data, key, batch, ant, 8, cost, 0, tour.ctypes.data,
-                costs.ctypes.data, counts.ctypes.data, err.ctypes.data)
+    rc = emu.emu_ant(mode, n, k, b, w, *(arrays[x].ctypes.data for x in ("xy", "primary", "backup", "ls",
+                                                                          "ls_dist", "parent")),
+                     nbr.ctypes.data, products.ctypes.data, key, batch, ant, 8, cost, ls_mode, tour.ctypes.data,
+                     costs.ctypes.data, counts.ctypes.data, err.ctypes.data)
+    assert rc == 0, mode
     uni = np.array([0.0] + [oracle.lib().orc_uniform(key, batch, ant, s) for s in range(1, n)])
     ref = oracle.ant(parent, prep["ls"], 8, 100000, xy=xy, uniforms=uni,
                      start=oracle.lib().orc_start_node(key, batch, ant, n), primary=prep["primary"],
-                     products32=products, backup=prep["backup"] if b else None)
-    assert err[0] == 0
-    assert np.array_equal(tour.astype(np.uint32), ref["tour"]), (follow, batch, ant)
-    assert (int(costs[0]), int(costs[1])) == (ref["construction_cost"], ref["final_cost"]), (follow, batch, ant)
-    assert int(counts[0]) == ref["steps"], (follow, batch, ant)
+                     products32=products, backup=prep["backup"] if b else None, ls_mode=ls_mode)
+    ctx = (mode, ls_mode, batch, ant)
+    assert err[0] == 0, ctx
+    assert np.array_equal(tour.astype(np.uint32), ref["tour"]), ctx
+    assert (int(costs[0]), int(costs[1])) == (ref["construction_cost"], ref["final_cost"]), ctx
+    assert int(counts[0]) == ref["steps"], ctx
     return int(counts[0])
 
+
+
+# (kernel variant, LS mode): steps one at a time (0), in batches (5), the
+# batched build for full panels (7), the global-workspace variants (4, 6),
+# and the 2-opt + Or-opt local search; the first three with every ant
+ANTS = ((3, 0), (3, 1), (7, 2), (11, 5))
+MAIN_VARIANTS = ((0, 0), (5, 0), (7, 0))
+VARIANTS = MAIN_VARIANTS + ((4, 0), (6, 0), (0, 1), (6, 1))
 
 
 def main() -> None:
@@ -67,12 +77,15 @@ def main() -> None:
     xy = instances.uniform(n, 500 + n) if kind == "uniform" else instances.clustered(n, 500 + n)
     b, w = min(64, n - 1 - k), min(20, n - 1)
     prep, key, parent, products = _state(xy, k, b, w, iterations, seed=3)
-    steps = 0
-    for follow in (0, 1, 2):
-        for batch, ant in ((3, 0), (3, 1), (7, 2), (11, 5)):
-            steps += _ant(emu, follow, xy, prep, key, parent, products, k, b, w, batch, ant)
+    steps = runs = 0
+    for mode, ls_mode in VARIANTS:
+        ants = ANTS if (mode, ls_mode) in MAIN_VARIANTS else ANTS[::2]
+        for batch, ant in ants:
+            steps += _ant(emu, mode, ls_mode, xy, prep, key, parent, products, k, b, w, batch, ant)
+            runs += 1
     assert steps > 0
-    print(f"{kind} n={n} k={k} it={iterations}: 8 ants x 3 variants equal the oracle ({steps} construction steps)")
+    print(f"{kind} n={n} k={k} it={iterations}: {runs} ants over {len(VARIANTS)} variants equal the oracle "
+          f"({steps} construction steps)")
 
 
 if __name__ == "__main__":

@@ -1,9 +1,10 @@
 """The ant kernel's own source run on the CPU (tests/emulation): engine-mode
 ants -- steps taken one at a time (ant_kernel<0>) and parent-following steps
 taken in batches (ant_kernel<5>, and ant_kernel<7>, the build of the same
-steps for panels beyond one wave) -- against the oracle's ant with the same
-Philox draws, bit for bit: final tour, construction and final lengths, step
-count.  The warp intrinsics are emulated with 32 threads that are delayed at
+steps for panels beyond one wave), the global-memory-workspace variants
+(ant_kernel<4>, <6>) and the 2-opt + Or-opt local search -- against the
+oracle's ant with the same Philox draws, bit for bit: final tour,
+construction and final lengths, step count.  The warp intrinsics are emulated with 32 threads that are delayed at
 random before every barrier, and the lanes' per-ant registers are compared
 after every step, so a warp race (lanes that read shared state while another
 lane writes it) fails the run instead of hiding behind lockstep execution.
