@@ -3,7 +3,10 @@ against the oracle's ant with the same Philox draws; exits non-zero on the
 first difference.  A warp race or an intrinsic reached by some lanes only
 aborts the emulation itself.  Test infrastructure only.
 
-    python tests/emulation/run_ants.py KIND N K ITERATIONS
+    python tests/emulation/run_ants.py KIND N K ITERATIONS [MODE:LS,...]
+
+The optional last argument limits the run to those (kernel variant, LS
+mode) pairs, e.g. 4:0,6:0.
 """
 import ctypes as C
 import sys
@@ -77,14 +80,17 @@ def main() -> None:
     xy = instances.uniform(n, 500 + n) if kind == "uniform" else instances.clustered(n, 500 + n)
     b, w = min(64, n - 1 - k), min(20, n - 1)
     prep, key, parent, products = _state(xy, k, b, w, iterations, seed=3)
+    variants = VARIANTS
+    if len(sys.argv) > 5:
+        variants = tuple(tuple(int(x) for x in v.split(":")) for v in sys.argv[5].split(","))
     steps = runs = 0
-    for mode, ls_mode in VARIANTS:
+    for mode, ls_mode in variants:
         ants = ANTS if (mode, ls_mode) in MAIN_VARIANTS else ANTS[::2]
         for batch, ant in ants:
             steps += _ant(emu, mode, ls_mode, xy, prep, key, parent, products, k, b, w, batch, ant)
             runs += 1
     assert steps > 0
-    print(f"{kind} n={n} k={k} it={iterations}: {runs} ants over {len(VARIANTS)} variants equal the oracle "
+    print(f"{kind} n={n} k={k} it={iterations}: {runs} ants over {len(variants)} variants equal the oracle "
           f"({steps} construction steps)")
 
 

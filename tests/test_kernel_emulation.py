@@ -22,10 +22,16 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 
 
-@pytest.mark.parametrize("kind,n,k,iterations", [("uniform", 60, 8, 0), ("clustered", 300, 20, 100),
-                                                  ("uniform", 800, 16, 150)])
-def test_emulated_kernel_ants_match_oracle(oracle, kind, n, k, iterations):
-    out = subprocess.run([sys.executable, str(ROOT / "tests" / "emulation" / "run_ants.py"), kind, str(n), str(k),
-                          str(iterations)], capture_output=True, text=True, timeout=900, cwd=ROOT)
+# the last case is above 2048 nodes, where every relocation is deferred into
+# a run, with the variants the engine runs there (global-memory workspace)
+# and the shared-memory one
+@pytest.mark.parametrize("kind,n,k,iterations,variants", [("uniform", 60, 8, 0, None),
+                                                           ("clustered", 300, 20, 100, None),
+                                                           ("uniform", 800, 16, 150, None),
+                                                           ("clustered", 2500, 16, 20, "4:0,6:0,0:0")])
+def test_emulated_kernel_ants_match_oracle(oracle, kind, n, k, iterations, variants):
+    args = [kind, str(n), str(k), str(iterations)] + ([variants] if variants else [])
+    out = subprocess.run([sys.executable, str(ROOT / "tests" / "emulation" / "run_ants.py")] + args,
+                         capture_output=True, text=True, timeout=900, cwd=ROOT)
     assert out.returncode == 0, (out.stdout[-2000:], out.stderr[-3000:])
     assert "equal the oracle" in out.stdout
